@@ -1,0 +1,229 @@
+"""ctypes wrapper of the FP64 CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Used by tests/, by ``__graft_entry__.smoke()`` as the checker and by
+``bench.py``'s CPU-baseline leg; the product never imports it.  The oracle
+restates the jswhit/gfs-dycore time step (src/shtns.f90, src/dyn_run.f90,
+src/run.f90, src/semimp_data.f90, src/pressure_data.f90,
+src/phy_run_hs.f90) in C++ (gd_oracle.cpp).
+
+Arrays use the reference layouts: spectral ``complex128[nlev, nlm]``
+(Fortran ``complex(ndimspec,nlevs)``), grid ``float64[nlev, nlat, nlon]``.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+
+def build():
+    """Compile the oracle with its Makefile (g++, OpenMP)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+class OraConfig(ctypes.Structure):
+    _fields_ = [
+        ("ntrunc", ctypes.c_int), ("nlon", ctypes.c_int), ("nlat", ctypes.c_int),
+        ("nlev", ctypes.c_int), ("ntrac", ctypes.c_int), ("dt", ctypes.c_double),
+        ("explicit_", ctypes.c_int), ("adiabatic", ctypes.c_int),
+        ("heldsuarez", ctypes.c_int), ("massfix", ctypes.c_int), ("dry", ctypes.c_int),
+        ("ndiss", ctypes.c_int), ("efold", ctypes.c_double), ("hdif_fac", ctypes.c_double),
+        ("hdif_fac2", ctypes.c_double), ("fshk", ctypes.c_double),
+        ("taustratdamp", ctypes.c_double), ("pdryini", ctypes.c_double),
+        ("nthreads", ctypes.c_int),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        vp = ctypes.c_void_p
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.ora_create.restype = vp
+        L.ora_create.argtypes = [ctypes.POINTER(OraConfig), dp, dp]
+        L.ora_destroy.argtypes = [vp]
+        L.ora_nlm.argtypes = [vp]
+        L.ora_nlm.restype = ctypes.c_int
+        L.ora_get_grid.restype = ctypes.c_int
+        for name in ["ora_set_state", "ora_get_state", "ora_spectogrd", "ora_grdtospec",
+                     "ora_getuv", "ora_getvrtdivspec", "ora_getgrad", "ora_getdyntend",
+                     "ora_grid_info", "ora_legendre", "ora_semimp", "ora_damp", "ora_diag",
+                     "ora_getphytend", "ora_get_grid"]:
+            getattr(L, name).restype = getattr(L, name).restype or None
+        L.ora_advance.argtypes = [vp, ctypes.c_double, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Oracle:
+    """FP64 CPU dycore; mirrors init_dyn / getdyntend / advance."""
+
+    def __init__(self, ntrunc, nlon, nlat, nlev, ak, bk, ntrac=0, dt=1200.0,
+                 explicit=False, adiabatic=False, heldsuarez=True, massfix=True,
+                 dry=True, nthreads=0, pdryini=0.0, **kw):
+        L = lib()
+        c = OraConfig()
+        L.ora_default_config(ctypes.byref(c))
+        c.ntrunc, c.nlon, c.nlat, c.nlev, c.ntrac = ntrunc, nlon, nlat, nlev, ntrac
+        c.dt = dt
+        c.explicit_ = int(explicit)
+        c.adiabatic = int(adiabatic)
+        c.heldsuarez = int(heldsuarez)
+        c.massfix = int(massfix)
+        c.dry = int(dry)
+        c.nthreads = nthreads
+        c.pdryini = pdryini
+        for k, v in kw.items():
+            setattr(c, k, v)
+        self.cfg = c
+        self.ak = np.ascontiguousarray(ak, dtype=np.float64)
+        self.bk = np.ascontiguousarray(bk, dtype=np.float64)
+        self.h = L.ora_create(ctypes.byref(c), self.ak.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                              self.bk.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        self.nlm = L.ora_nlm(self.h)
+        self.ntrunc, self.nlon, self.nlat, self.nlev, self.ntrac = ntrunc, nlon, nlat, nlev, ntrac
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ora_destroy(self.h)
+            self.h = None
+
+    # ---- state ----
+    def set_state(self, vrt, div, tv, lnps, trc=None, topo=None):
+        c128 = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.complex128)
+        self._keep = [c128(x) for x in (vrt, div, tv, trc, lnps, topo)]
+        lib().ora_set_state(self.h, *[_p(x) for x in self._keep])
+
+    def get_state(self):
+        L, n = self.nlev, self.nlm
+        vrt = np.zeros((L, n), np.complex128)
+        div = np.zeros_like(vrt)
+        tv = np.zeros_like(vrt)
+        trc = np.zeros((max(self.ntrac, 1), L, n), np.complex128)
+        lnps = np.zeros(n, np.complex128)
+        lib().ora_get_state(self.h, _p(vrt), _p(div), _p(tv), _p(trc), _p(lnps))
+        return dict(vrt=vrt, div=div, tv=tv, trc=trc[: self.ntrac], lnps=lnps)
+
+    # ---- transforms (batched over leading axis) ----
+    def _gshape(self, nb):
+        return (nb, self.nlat, self.nlon)
+
+    def spectogrd(self, spec):
+        spec = np.ascontiguousarray(np.atleast_2d(spec), np.complex128)
+        g = np.zeros(self._gshape(spec.shape[0]))
+        lib().ora_spectogrd(self.h, spec.shape[0], _p(spec), _p(g))
+        return g
+
+    def grdtospec(self, grid):
+        grid = np.ascontiguousarray(grid, np.float64).reshape(-1, self.nlat, self.nlon)
+        s = np.zeros((grid.shape[0], self.nlm), np.complex128)
+        lib().ora_grdtospec(self.h, grid.shape[0], _p(grid), _p(s))
+        return s
+
+    def getuv(self, vrt, div):
+        vrt = np.ascontiguousarray(np.atleast_2d(vrt), np.complex128)
+        div = np.ascontiguousarray(np.atleast_2d(div), np.complex128)
+        u = np.zeros(self._gshape(vrt.shape[0]))
+        v = np.zeros_like(u)
+        lib().ora_getuv(self.h, vrt.shape[0], _p(vrt), _p(div), _p(u), _p(v))
+        return u, v
+
+    def getvrtdivspec(self, u, v):
+        u = np.ascontiguousarray(u, np.float64).reshape(-1, self.nlat, self.nlon)
+        v = np.ascontiguousarray(v, np.float64).reshape(-1, self.nlat, self.nlon)
+        vrt = np.zeros((u.shape[0], self.nlm), np.complex128)
+        div = np.zeros_like(vrt)
+        lib().ora_getvrtdivspec(self.h, u.shape[0], _p(u), _p(v), _p(vrt), _p(div))
+        return vrt, div
+
+    def getgrad(self, spec):
+        spec = np.ascontiguousarray(np.atleast_2d(spec), np.complex128)
+        gx = np.zeros(self._gshape(spec.shape[0]))
+        gy = np.zeros_like(gx)
+        lib().ora_getgrad(self.h, spec.shape[0], _p(spec), _p(gx), _p(gy))
+        return gx, gy
+
+    # ---- dynamics ----
+    def getdyntend(self, rkstage=1, inverse_only=False):
+        L, n = self.nlev, self.nlm
+        d = [np.zeros((L, n), np.complex128) for _ in range(3)]
+        dtrc = np.zeros((max(self.ntrac, 1), L, n), np.complex128)
+        dl = np.zeros(n, np.complex128)
+        lib().ora_getdyntend(self.h, rkstage, int(inverse_only), _p(d[0]), _p(d[1]), _p(d[2]),
+                             _p(dtrc), _p(dl))
+        return dict(dvrt=d[0], ddiv=d[1], dtv=d[2], dtrc=dtrc[: self.ntrac], dlnps=dl)
+
+    def getphytend(self):
+        L, n = self.nlev, self.nlm
+        d = [np.zeros((L, n), np.complex128) for _ in range(3)]
+        lib().ora_getphytend(self.h, _p(d[0]), _p(d[1]), _p(d[2]))
+        return dict(dvrt=d[0], ddiv=d[1], dtv=d[2])
+
+    def advance(self, nsteps=1, t=0.0):
+        lib().ora_advance(self.h, ctypes.c_double(t), nsteps)
+
+    def get_grid(self, name):
+        L = self.nlev
+        shapes = dict(ug=L, vg=L, vrtg=L, divg=L, tvg=L, dlnpdtg=L, prs=L, etadot=L + 1,
+                      trcg=max(self.ntrac, 1) * L, lnpsg=1, psg=1, dlnpsdt=1, dphisdx=1, dphisdy=1)
+        out = np.zeros((shapes[name], self.nlat, self.nlon))
+        rc = lib().ora_get_grid(self.h, name.encode(), _p(out))
+        assert rc == 0
+        return out
+
+    def grid_info(self):
+        lats = np.zeros(self.nlat)
+        gw = np.zeros(self.nlat)
+        aw = np.zeros(self.nlat)
+        deg = np.zeros(self.nlm, np.int32)
+        order = np.zeros(self.nlm, np.int32)
+        lap = np.zeros(self.nlm)
+        ilap = np.zeros(self.nlm)
+        lib().ora_grid_info(self.h, _p(lats), _p(gw), _p(aw), _p(deg), _p(order), _p(lap), _p(ilap))
+        return dict(lats=lats, gauwts=gw, areawts=aw, degree=deg, order=order, lap=lap, invlap=ilap)
+
+    def legendre(self, m):
+        K = self.ntrunc - m + 1
+        P = np.zeros((self.nlat // 2, K))
+        H = np.zeros_like(P)
+        lib().ora_legendre(self.h, m, _p(P), _p(H))
+        return P, H
+
+    def semimp(self):
+        L, T = self.nlev, self.ntrunc
+        a = np.zeros((L, L))
+        b = np.zeros((L, L))
+        sv = np.zeros(L)
+        tor = np.zeros(L)
+        d = np.zeros((3, T + 1, L, L))
+        ym = np.zeros((L, L))
+        lib().ora_semimp(self.h, _p(a), _p(b), _p(sv), _p(tor), _p(d), _p(ym))
+        return dict(amhyb=a, bmhyb=b, svhyb=sv, tor_hyb=tor, d_hyb_m=d, ym=ym)
+
+    def damp(self):
+        dis = np.zeros(self.nlm)
+        dp = np.zeros(self.nlev)
+        mp = np.zeros(self.nlev)
+        lib().ora_damp(self.h, _p(dis), _p(dp), _p(mp))
+        return dict(disspec=dis, diff_prof=dp, dmp_prof=mp)
+
+    def diag(self):
+        o = np.zeros(5)
+        lib().ora_diag(self.h, _p(o))
+        return dict(spdmax=o[0], psmin=o[1], psmax=o[2], pstend=o[3], pdryini=o[4])

@@ -1,0 +1,162 @@
+"""Pins the FP64 CPU oracle's transforms (the role SHTns plays for
+src/shtns.f90) against scipy / numpy and analytic known answers.
+
+The reference ships no golden vectors for this path; these known-answer
+tests fix the convention of src/shtns.f90:110 (orthonormal, no
+Condon-Shortley phase) and the physical contract of getuv / getvrtdivspec /
+getgrad (src/shtns.f90:233-352).
+"""
+import numpy as np
+import pytest
+from scipy.special import gammaln, lpmv, roots_legendre
+
+from gdpy import inputs
+from sht_numpy import ShtNumpy
+
+A = inputs.RERTH
+
+
+def make(oracle_mod, T=21, nlon=64, nlat=32, nlev=2):
+    ak, bk = inputs.hybrid_coords(nlev)
+    return oracle_mod.Oracle(T, nlon, nlat, nlev, ak, bk, dt=1200.0)
+
+
+def rand_spec(T, nb, seed=1):
+    rng = np.random.default_rng(seed)
+    deg, order = inputs.degree_order(T)
+    a = rng.standard_normal((nb, deg.size)) + 1j * rng.standard_normal((nb, deg.size))
+    a[:, order == 0] = a[:, order == 0].real
+    return a
+
+
+@pytest.mark.parametrize("nlat,nlon", [(32, 64), (64, 128), (190, 384), (576, 1152)])
+def test_gauss_nodes_weights_vs_scipy(oracle_mod, nlat, nlon):
+    o = make(oracle_mod, T=21, nlon=nlon, nlat=nlat)
+    gi = o.grid_info()
+    x, w = roots_legendre(nlat)
+    np.testing.assert_allclose(np.sin(gi["lats"]), x[::-1], rtol=0, atol=2e-15)
+    # scipy's polar weights carry up to ~2e-9 relative error at n = 576 (its
+    # n > 150 branch is asymptotic); the oracle's are checked against
+    # mpmath below and are ~1e-11 or better.
+    np.testing.assert_allclose(gi["gauwts"], w[::-1], rtol=5e-9 if nlat > 150 else 2e-12)
+    np.testing.assert_allclose(gi["gauwts"].sum(), 2.0, rtol=1e-14)
+    np.testing.assert_allclose(gi["areawts"].sum() * o.nlon, 1.0, rtol=1e-14)
+
+
+@pytest.mark.parametrize("N,nlon,tol", [(32, 64, 1e-13), (576, 1152, 2e-11)])
+def test_polar_gauss_weight_vs_mpmath(oracle_mod, N, nlon, tol):
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 50
+    o = make(oracle_mod, T=21, nlon=nlon, nlat=N)
+    gi = o.grid_info()
+
+    def pn(t):
+        p0, p1 = mp.mpf(1), t
+        for k in range(1, N):
+            p0, p1 = p1, ((2 * k + 1) * t * p1 - k * p0) / (k + 1)
+        return p0, p1
+
+    for j in (0, 1, 5):
+        r = mp.mpf(np.sin(gi["lats"][j]))
+        for _ in range(8):
+            pm1, p = pn(r)
+            r = r - p / (N * (r * p - pm1) / (r * r - 1))
+        pm1, p = pn(r)
+        dp = N * (r * p - pm1) / (r * r - 1)
+        wr = float(2 / ((1 - r ** 2) * dp ** 2))
+        assert abs(gi["gauwts"][j] - wr) / wr < tol
+        assert abs(float(np.sin(gi["lats"][j]) - r)) < 1e-16
+
+
+def test_legendre_tables_vs_scipy(oracle_mod):
+    T, nlat = 42, 64
+    o = make(oracle_mod, T=T, nlon=128, nlat=nlat)
+    mu = np.sin(o.grid_info()["lats"][: nlat // 2])
+    for m in [0, 1, 2, 7, 20, 42]:
+        P, H = o.legendre(m)
+        for n in range(m, T + 1):
+            norm = np.sqrt((2 * n + 1) / (4 * np.pi) * np.exp(gammaln(n - m + 1) - gammaln(n + m + 1)))
+            ref = norm * (-1.0) ** m * lpmv(m, n, mu)
+            np.testing.assert_allclose(P[:, n - m], ref, rtol=1e-10, atol=1e-13)
+
+
+def test_orthonormality_under_gauss_quadrature(oracle_mod):
+    T, nlat = 42, 64
+    o = make(oracle_mod, T=T, nlon=128, nlat=nlat)
+    w = o.grid_info()["gauwts"][: nlat // 2]
+    for m in [0, 3, 17, 42]:
+        P, _ = o.legendre(m)
+        # both hemispheres: parity (-1)^(n-m)
+        n = np.arange(m, T + 1)
+        sgn = (-1.0) ** (n - m)
+        G = 2 * np.pi * (P.T * w) @ P + 2 * np.pi * ((P * sgn).T * w) @ (P * sgn)
+        np.testing.assert_allclose(G, np.eye(T - m + 1), atol=1e-13)
+
+
+@pytest.mark.parametrize("T,nlon,nlat", [(21, 64, 32), (42, 128, 64), (62, 192, 94)])
+def test_round_trip(oracle_mod, T, nlon, nlat):
+    o = make(oracle_mod, T=T, nlon=nlon, nlat=nlat)
+    a = rand_spec(T, 3)
+    g = o.spectogrd(a)
+    b = o.grdtospec(g)
+    np.testing.assert_allclose(b, a, atol=1e-12 * np.abs(a).max())
+    vrt, div = rand_spec(T, 2, 5), rand_spec(T, 2, 6)
+    vrt[:, 0] = 0
+    div[:, 0] = 0
+    u, v = o.getuv(vrt, div)
+    vrt2, div2 = o.getvrtdivspec(u, v)
+    np.testing.assert_allclose(vrt2, vrt, atol=1e-12 * np.abs(vrt).max())
+    np.testing.assert_allclose(div2, div, atol=1e-12 * np.abs(div).max())
+
+
+def test_cpp_oracle_matches_numpy_oracle(oracle_mod):
+    T, nlon, nlat = 21, 64, 32
+    o = make(oracle_mod, T=T, nlon=nlon, nlat=nlat)
+    s = ShtNumpy(T, nlon, nlat, A)
+    a, b = rand_spec(T, 1, 11)[0], rand_spec(T, 1, 12)[0]
+    g = o.spectogrd(a)[0]
+    np.testing.assert_allclose(g, s.spectogrd(a), atol=1e-12 * np.abs(g).max())
+    np.testing.assert_allclose(o.grdtospec(g)[0], s.grdtospec(g), atol=1e-12 * np.abs(a).max())
+    u, v = o.getuv(a, b)
+    us, vs = s.getuv(a, b)
+    np.testing.assert_allclose(u[0], us, atol=1e-12 * np.abs(us).max())
+    np.testing.assert_allclose(v[0], vs, atol=1e-12 * np.abs(vs).max())
+    gx, gy = o.getgrad(a)
+    gxs, gys = s.getgrad(a)
+    np.testing.assert_allclose(gx[0], gxs, atol=1e-12 * np.abs(gxs).max())
+    np.testing.assert_allclose(gy[0], gys, atol=1e-12 * np.abs(gys).max())
+    rng = np.random.default_rng(3)
+    ug, vg = rng.standard_normal((nlat, nlon)), rng.standard_normal((nlat, nlon))
+    vr, dv = o.getvrtdivspec(ug, vg)
+    vrs, dvs = s.getvrtdivspec(ug, vg)
+    np.testing.assert_allclose(vr[0], vrs, atol=1e-12 * np.abs(vrs).max())
+    np.testing.assert_allclose(dv[0], dvs, atol=1e-12 * np.abs(dvs).max())
+
+
+def test_solid_body_rotation_and_gradients(oracle_mod):
+    T, nlon, nlat = 21, 64, 32
+    o = make(oracle_mod, T=T, nlon=nlon, nlat=nlat)
+    gi = o.grid_info()
+    phi = gi["lats"][:, None] * np.ones(nlon)
+    lam = 2 * np.pi * np.arange(nlon)[None, :] / nlon * np.ones((nlat, 1))
+    U0 = 20.0
+    # u = U0 cos(phi), v = 0  <=>  vrt = 2 U0 sin(phi) / a, i.e. n=1,m=0 coefficient
+    vrt = np.zeros(o.nlm, np.complex128)
+    vrt[1] = 2 * U0 / A * np.sqrt(4 * np.pi / 3)
+    u, v = o.getuv(vrt, np.zeros_like(vrt))
+    np.testing.assert_allclose(u[0], U0 * np.cos(phi), atol=1e-12 * U0)
+    np.testing.assert_allclose(v[0], 0.0, atol=1e-12 * U0)
+    vr, dv = o.getvrtdivspec(U0 * np.cos(phi), 0 * phi)
+    np.testing.assert_allclose(vr[0], vrt, atol=1e-13 * abs(vrt[1]))
+    np.testing.assert_allclose(dv[0], 0, atol=1e-13 * abs(vrt[1]))
+    # f = cos(phi) cos(lambda): grad = (-sin(lambda)/a, -sin(phi) cos(lambda)/a)
+    f = np.cos(phi) * np.cos(lam)
+    fs = o.grdtospec(f)[0]
+    gx, gy = o.getgrad(fs)
+    np.testing.assert_allclose(gx[0], -np.sin(lam) / A, atol=1e-12 / A)
+    np.testing.assert_allclose(gy[0], -np.sin(phi) * np.cos(lam) / A, atol=1e-12 / A)
+    # no Condon-Shortley phase: Y_1^1 coefficient of cos(phi)cos(lambda) is positive
+    k11 = T + 1  # m=1, n=1
+    assert fs[k11].real > 0
+    # Laplacian eigenvalues (lap = -n(n+1))
+    np.testing.assert_array_equal(gi["lap"], -gi["degree"] * (gi["degree"] + 1.0))

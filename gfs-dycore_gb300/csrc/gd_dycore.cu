@@ -1,0 +1,1145 @@
+// gd_dycore.cu -- host orchestration of the GB300 spectral dycore step and
+// the C ABI of include/gd_api.h.
+//
+// Mirrors the reference's dynamics interface: init_dyn
+// (src/dyn_init.f90:37-91), getdyntend (src/dyn_run.f90:33-305), advance
+// (src/run.f90:194-565), getphytend for Held-Suarez (src/phy_run_hs.f90:22),
+// finalize_dyn (src/dyn_finalize.f90:19-28), and the transform facade of
+// src/shtns.f90.  All state lives on one GPU; one context owns one stream,
+// and every step is one CUDA graph replay.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "../../include/gd_api.h"
+#include "gd_grid.cuh"
+#include "gd_kernels.h"
+#include "gd_spec.cuh"
+
+namespace gd {
+
+// Lorenz 3-cycle + trapezoidal IMEX tableau (src/semimp_data.f90:74-88),
+// single-precision literals as in the reference.
+struct Tableau {
+  double a21 = GD_FLIT(1.f / 3.f), a31 = GD_FLIT(1.f / 6.f), a32 = GD_FLIT(1.f / 2.f);
+  double aa21 = GD_FLIT(1.f / 6.f), aa22 = GD_FLIT(1.f / 6.f), aa31 = GD_FLIT(1.f / 3.f), aa32 = 0.0,
+         aa33 = GD_FLIT(1.f / 3.f);
+  double b1 = GD_FLIT(1.f / 2.f), b2 = GD_FLIT(-1.f / 2.f), b3 = 1.0;
+  double bb1 = GD_FLIT(3.f / 8.f), bb2 = 0.0, bb3 = GD_FLIT(3.f / 8.f), bb4 = GD_FLIT(1.f / 4.f);
+};
+
+class DycoreBase {
+ public:
+  virtual ~DycoreBase() {}
+  virtual void set_state(const double*, const double*, const double*, const double*, const double*,
+                         const double*) = 0;
+  virtual void get_state(double*, double*, double*, double*, double*) = 0;
+  virtual void getdyntend(int, int, double*, double*, double*, double*, double*) = 0;
+  virtual void getphytend(double*, double*, double*, double*, double*) = 0;
+  virtual void advance(int nsteps) = 0;
+  virtual void spectogrd(int, const double*, double*) = 0;
+  virtual void grdtospec(int, const double*, double*) = 0;
+  virtual void getuv(int, const double*, const double*, double*, double*) = 0;
+  virtual void getvrtdivspec(int, const double*, const double*, double*, double*) = 0;
+  virtual void getgrad(int, const double*, double*, double*) = 0;
+  virtual void grid_info(double*, double*, double*, int*, int*, double*, double*) = 0;
+  virtual int get_grid(const char*, double*) = 0;
+  virtual void diag(double*) = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = true;
+  std::string err;
+};
+
+template <typename R>
+class Dycore : public DycoreBase {
+ public:
+  typedef typename C2<R>::T V;
+  gd_config c;
+  int T, nlon, nlat, nh, L, nt, nlm, M;
+  long ng;
+  std::vector<void*> allocs;
+  // grid and tables
+  double *mu = nullptr, *w = nullptr;
+  long *moff = nullptr, *toff = nullptr;
+  R *P = nullptr, *H = nullptr, *rcos = nullptr, *wn = nullptr, *sinlat = nullptr, *coslat = nullptr;
+  V *twM = nullptr, *twN = nullptr;
+  ShtDev<R> sd;
+  std::vector<double> h_mu, h_w, h_lat;
+  std::vector<int> h_deg, h_ord;
+  std::vector<double> h_lap;
+  // vertical coordinate, damping, semi-implicit matrices
+  R *ak = nullptr, *bk = nullptr, *dbk = nullptr, *ck = nullptr;
+  R *lapv = nullptr, *disspec = nullptr, *diff_prof = nullptr, *dmp_prof = nullptr;
+  R *amhyb = nullptr, *bmhyb = nullptr, *svhyb = nullptr, *tor = nullptr, *dhyb = nullptr;
+  // state and work buffers
+  R *S = nullptr, *S0 = nullptr, *TD[3] = {nullptr, nullptr, nullptr}, *AP = nullptr, *AH = nullptr;
+  R *FPb = nullptr, *FHb = nullptr, *gS = nullptr, *gA = nullptr;
+  R *psg = nullptr, *dlnpsdt = nullptr, *dlnpdtg = nullptr, *etadot = nullptr, *prs = nullptr;
+  R *dphisdx = nullptr, *dphisdy = nullptr;
+  double *pdryini = nullptr, *pmean = nullptr, *rowsum = nullptr, *diagbuf = nullptr, *diagout = nullptr;
+  int4* stage_items = nullptr;
+  int nstage_items = 0;
+  SpecCols sc;
+  TendCols tc;
+  APCols ap;
+  AHCols ah;
+  SynthRows sr;
+  AnalRows ar;
+  long ldS, ldTD, ldAP, ldAH, ldFP, ldFH, ldGP, ldGH;
+  GemmPlan synP, synH, anaP, anaH, anaPhys;
+  FftPlan c2rFull, c2rInv, r2cDyn, r2cPhys;
+  Tableau tb;
+  bool state_set = false;
+  cudaGraphExec_t gexec = nullptr;
+  int steps_done = 0;
+  long long launches_per_step = 0;
+  std::map<int, GemmPlan> synth_cache, anal_cache;
+
+  template <typename X>
+  X* dalloc(size_t n) {
+    X* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(X));
+    if (e != cudaSuccess) throw CudaError(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    allocs.push_back(p);
+    return p;
+  }
+  template <typename X>
+  X* upload(const std::vector<X>& h) {
+    X* p = dalloc<X>(h.size());
+    GD_CUDA(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(X), cudaMemcpyHostToDevice, stream));
+    return p;
+  }
+  std::vector<R> toR(const std::vector<double>& v) {
+    std::vector<R> r(v.size());
+    for (size_t i = 0; i < v.size(); ++i) r[i] = (R)v[i];
+    return r;
+  }
+  static long pad2(long ncol) { return 2 * ((ncol + 1) / 2 * 2); }  // reals, even complex count
+
+  Dycore(const gd_config& cfg, const double* ak_, const double* bk_) : c(cfg) {
+    T = c.ntrunc;
+    nlon = c.nlon;
+    nlat = c.nlat;
+    nh = nlat / 2;
+    L = c.nlev;
+    nt = c.ntrac;
+    nlm = (T + 1) * (T + 2) / 2;
+    M = nlon / 2;
+    ng = (long)nlon * nlat;
+    GD_CUDA(cudaSetDevice(c.device));
+    GD_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    init_grid();
+    init_vertical(ak_, bk_);
+    init_buffers();
+    init_plans();
+    GD_CUDA(cudaStreamSynchronize(stream));
+  }
+  ~Dycore() override {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    free_plan(synP);
+    free_plan(synH);
+    free_plan(anaP);
+    free_plan(anaH);
+    free_plan(anaPhys);
+    for (auto& kv : synth_cache) free_plan(kv.second);
+    for (auto& kv : anal_cache) free_plan(kv.second);
+    free_fft_plan(c2rFull);
+    free_fft_plan(c2rInv);
+    free_fft_plan(r2cDyn);
+    free_fft_plan(r2cPhys);
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* p : allocs) cudaFree(p);
+    if (stream && own_stream) cudaStreamDestroy(stream);
+  }
+
+  // --- shtns_init (shtns.f90:90-156): nodes, weights, tables, all FP64 ---
+  void init_grid() {
+    std::vector<long> hm(T + 2), ht(T + 2);
+    hm[0] = ht[0] = 0;
+    for (int m = 0; m <= T; ++m) {
+      hm[m + 1] = hm[m] + (T - m + 1);
+      ht[m + 1] = ht[m] + (long)(T - m + 1) * nh;
+    }
+    moff = upload(hm);
+    toff = upload(ht);
+    mu = dalloc<double>(nlat);
+    w = dalloc<double>(nlat);
+    launch_gauss(nlat, mu, w, stream);
+    double* P64 = dalloc<double>(ht[T + 1]);
+    double* H64 = dalloc<double>(ht[T + 1]);
+    launch_legendre_tables(T, nh, mu, toff, P64, H64, stream);
+    if (sizeof(R) == 8) {
+      P = reinterpret_cast<R*>(P64);
+      H = reinterpret_cast<R*>(H64);
+    } else {
+      P = dalloc<R>(ht[T + 1]);
+      H = dalloc<R>(ht[T + 1]);
+      launch_convert<R>(P64, P, ht[T + 1], stream);
+      launch_convert<R>(H64, H, ht[T + 1], stream);
+    }
+    h_mu.resize(nlat);
+    h_w.resize(nlat);
+    GD_CUDA(cudaMemcpyAsync(h_mu.data(), mu, nlat * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    GD_CUDA(cudaMemcpyAsync(h_w.data(), w, nlat * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    GD_CUDA(cudaStreamSynchronize(stream));
+    if (sizeof(R) != 8) {  // FP64 copies are no longer needed
+      cudaFree(P64);
+      cudaFree(H64);
+      allocs.erase(std::remove(allocs.begin(), allocs.end(), (void*)P64), allocs.end());
+      allocs.erase(std::remove(allocs.begin(), allocs.end(), (void*)H64), allocs.end());
+    }
+    std::vector<double> rc(nlat), wnv(nlat), sl(nlat), cl(nlat);
+    h_lat.resize(nlat);
+    for (int j = 0; j < nlat; ++j) {
+      h_lat[j] = asin(h_mu[j]);
+      rc[j] = 1.0 / sqrt((1.0 - h_mu[j]) * (1.0 + h_mu[j]));
+      wnv[j] = 2.0 * M_PI * h_w[j] / nlon;
+      sl[j] = sin(h_lat[j]);
+      cl[j] = cos(h_lat[j]);
+    }
+    rcos = upload(toR(rc));
+    wn = upload(toR(wnv));
+    sinlat = upload(toR(sl));
+    coslat = upload(toR(cl));
+    twM = dalloc<V>(M);
+    twN = dalloc<V>(M + 1);
+    fft_init_tables<R>(nlon, twM, twN, stream);
+    h_deg.resize(nlm);
+    h_ord.resize(nlm);
+    h_lap.resize(nlm);
+    for (int m = 0, k = 0; m <= T; ++m)
+      for (int n = m; n <= T; ++n, ++k) {
+        h_deg[k] = n;
+        h_ord[k] = m;
+        h_lap[k] = -(double)n * (n + 1.0);
+      }
+    lapv = upload(toR(h_lap));
+    sd.T = T;
+    sd.nlon = nlon;
+    sd.nlat = nlat;
+    sd.nh = nh;
+    sd.nlm = nlm;
+    sd.M = M;
+    sd.moff = moff;
+    sd.toff = toff;
+    sd.P = P;
+    sd.H = H;
+    sd.rcos = rcos;
+    sd.wn = wn;
+    sd.twM = twM;
+    sd.twN = twN;
+    fft_radix_plan(M, &sd.nrad, sd.rad);
+  }
+
+  // --- pressure_data / setdampspec / init_semimpdata ---
+  void init_vertical(const double* ak_, const double* bk_) {
+    std::vector<double> a(ak_, ak_ + L + 1), b(bk_, bk_ + L + 1), db(L), ckv(L), si(L + 1), slv(L);
+    for (int k = 0; k < L; ++k) {  // dyn_init.f90:57-61
+      db[k] = b[k + 1] - b[k];
+      ckv[k] = a[k + 1] * b[k] - a[k] * b[k + 1];
+    }
+    ak = upload(toR(a));
+    bk = upload(toR(b));
+    dbk = upload(toR(db));
+    ck = upload(toR(ckv));
+    for (int k = 0; k <= L; ++k) si[L - k] = a[k] / 101300.0 + b[k];  // pressure_data.f90:65-67
+    for (int k = 0; k < L; ++k) slv[k] = 0.5 * (si[k] + si[k + 1]);
+    // setdampspec (dyn_init.f90:450-494)
+    int ndiss = c.ndiss == 0 ? 8 : c.ndiss;
+    double efold = c.efold, fshk = c.fshk;
+    const double RE = Phys::rerth;
+    if (efold <= 0) {
+      if (T > 170) {
+        float x = (float)T / 170.f;
+        float x4 = (x * x) * (x * x);
+        efold = 3600. / (c.hdif_fac2 * (double)x4 * GD_FLIT(1.1f));
+      } else if (T == 126 || T == 170) {
+        efold = 1. / (c.hdif_fac2 * GD_FLIT(12.E15f) / pow(RE, 4) * 41990400.0);
+      } else {
+        efold = 1. / (c.hdif_fac2 * GD_FLIT(3.E15f) / pow(RE, 4) * 41990400.0);
+      }
+      efold = 2. * efold;
+    }
+    if (fshk <= 0) {
+      fshk = 1.0 * c.hdif_fac;
+      if (T > 170) fshk = GD_FLIT(2.2f) * c.hdif_fac;
+      if (T == 126) fshk = GD_FLIT(1.5f) * c.hdif_fac;
+    }
+    const double slrd0 = GD_FLIT(0.002f), dmp1 = 1. / c.taustratdamp;
+    std::vector<double> dp(L), mp(L, 0.0), dis(nlm);
+    for (int k = 0; k < L; ++k) {
+      dp[k] = pow(slv[k], log(1. / fshk));
+      if (slv[k] < slrd0) mp[k] = dmp1 * log(slrd0 / slv[k]);
+    }
+    double minlap = *std::min_element(h_lap.begin(), h_lap.end());
+    for (int k = 0; k < nlm; ++k) {
+      double r = h_lap[k] / minlap, rp = 1.0;
+      for (int q = 0; q < ndiss / 2; ++q) rp *= r;
+      dis[k] = -(1. / efold) * rp;
+    }
+    diff_prof = upload(toR(dp));
+    dmp_prof = upload(toR(mp));
+    disspec = upload(toR(dis));
+    // semi-implicit reference-state operators (semimp_data.f90:174-234)
+    const double RD = Phys::rd, KAPPA = Phys::rd / Phys::cp, TREF = 300.0, PREF = 800.e2;
+    std::vector<double> pkref(L + 1), dpkref(L), alfaref(L), yecm((long)L * L, 0), tecm((long)L * L, 0), vecm(L);
+    for (int k = 0; k <= L; ++k) pkref[k] = a[k] + b[k] * PREF;
+    for (int k = 0; k < L; ++k) dpkref[k] = pkref[k + 1] - pkref[k];
+    alfaref[0] = GD_FLIT(logf(2.f));
+    for (int k = 1; k < L; ++k) alfaref[k] = 1. - (pkref[k] / dpkref[k]) * log(pkref[k + 1] / pkref[k]);
+    for (int i = 0; i < L; ++i) {
+      yecm[(long)i * L + i] = alfaref[i] * RD;
+      for (int j = i + 1; j < L; ++j) yecm[(long)i * L + j] = RD * log(pkref[j + 1] / pkref[j]);
+      tecm[(long)i * L + i] = KAPPA * TREF * alfaref[i];
+      for (int j = 0; j < i; ++j)
+        tecm[(long)i * L + j] = (KAPPA * TREF * dpkref[j] / dpkref[i]) * log(pkref[i + 1] / pkref[i]);
+    }
+    for (int k = 0; k < L; ++k) vecm[k] = dpkref[k] / PREF;
+    std::vector<double> am((long)L * L), bm((long)L * L), sv(L), to(L);
+    for (int j = 0; j < L; ++j) {
+      sv[j] = vecm[L - 1 - j];
+      for (int k = 0; k < L; ++k) {
+        am[(long)k * L + j] = yecm[(long)(L - 1 - k) * L + (L - 1 - j)];
+        bm[(long)k * L + j] = tecm[(long)(L - 1 - k) * L + (L - 1 - j)];
+      }
+    }
+    for (auto& x : am) x /= RE * RE;
+    for (int k = 0; k < L; ++k) to[k] = RD * TREF / (RE * RE);
+    // the state arithmetic uses these in r_kind; ym is formed in FP64 from
+    // the r_kind values (semimp_data.f90:130,216-234)
+    for (auto* v : {&am, &bm, &sv, &to})
+      for (auto& x : *v) x = (double)(R)x;
+    amhyb = upload(toR(am));
+    bmhyb = upload(toR(bm));
+    svhyb = upload(toR(sv));
+    tor = upload(toR(to));
+    std::vector<double> ym((long)L * L);
+    for (int i = 0; i < L; ++i) {
+      for (int j = 0; j < L; ++j) ym[(long)i * L + j] = to[i] * sv[j];
+      for (int k = 0; k < L; ++k)
+        for (int j = 0; j < L; ++j) ym[(long)i * L + j] += am[(long)i * L + k] * bm[(long)k * L + j];
+    }
+    const double consts[3] = {tb.aa22, tb.aa33, tb.bb4};
+    std::vector<double> Y((long)3 * (T + 1) * L * L);
+    for (int s = 0; s < 3; ++s)
+      for (int n = 0; n <= T; ++n) {
+        double f = (consts[s] * c.dt) * (consts[s] * c.dt) * ((double)n * (n + 1));
+        double* y = &Y[((long)s * (T + 1) + n) * L * L];
+        for (int i = 0; i < L; ++i)
+          for (int j = 0; j < L; ++j) y[(long)i * L + j] = (i == j ? 1.0 : 0.0) + f * ym[(long)i * L + j];
+      }
+    double* dY = dalloc<double>(Y.size());
+    GD_CUDA(cudaMemcpyAsync(dY, Y.data(), Y.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    launch_batched_inverse(dY, 3 * (T + 1), L, stream);  // FP64 on the GPU
+    if (sizeof(R) == 8) {
+      dhyb = reinterpret_cast<R*>(dY);
+    } else {
+      dhyb = dalloc<R>(Y.size());
+      launch_convert<R>(dY, dhyb, (long)Y.size(), stream);
+    }
+    GD_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  void init_buffers() {
+    sc.vrt = 0;
+    sc.div = L;
+    sc.tv = 2 * L;
+    sc.trc = 3 * L;
+    sc.s = (3 + nt) * L;
+    sc.c = (4 + nt) * L;
+    sc.lnps = (5 + nt) * L;
+    sc.ncol = (5 + nt) * L + 1;
+    tc.dvrt = 0;
+    tc.ddiv = L;
+    tc.dtv = 2 * L;
+    tc.dtrc = 3 * L;
+    tc.dlnps = (3 + nt) * L;
+    tc.ddl = (3 + nt) * L + 1;
+    tc.dtl = (4 + nt) * L + 1;
+    tc.dpl = (5 + nt) * L + 1;
+    tc.ncol = (5 + nt) * L + 2;
+    ap.ttend = 0;
+    ap.ke = L;
+    ap.qtend = 2 * L;
+    ap.dlnps = (2 + nt) * L;
+    ap.imfv = (2 + nt) * L + 1;
+    ap.imfu = (3 + nt) * L + 1;
+    ap.ncol = (4 + nt) * L + 1;
+    ah.fu = 0;
+    ah.mfv = L;
+    ah.ncol = 2 * L;
+    sr.vrt = 0;
+    sr.div = L;
+    sr.tv = 2 * L;
+    sr.trc = 3 * L;
+    sr.u = (3 + nt) * L;
+    sr.v = (4 + nt) * L;
+    sr.dtvdx = (5 + nt) * L;
+    sr.dtvdy = (6 + nt) * L;
+    sr.dqdx = (7 + nt) * L;
+    sr.dqdy = (7 + 2 * nt) * L;
+    sr.lnps = (7 + 3 * nt) * L;
+    sr.dlnpsdx = sr.lnps + 1;
+    sr.dlnpsdy = sr.lnps + 2;
+    sr.total = sr.lnps + 3;
+    ar.ttend = 0;
+    ar.ke = L;
+    ar.qtend = 2 * L;
+    ar.dlnps = (2 + nt) * L;
+    ar.fu = (2 + nt) * L + 1;
+    ar.fv = (3 + nt) * L + 1;
+    ar.total = (4 + nt) * L + 1;
+    ldS = pad2(sc.ncol);
+    ldTD = pad2(tc.ncol);
+    ldAP = pad2(ap.ncol);
+    ldAH = pad2(ah.ncol);
+    ldFP = pad2(sc.ncol);
+    ldFH = pad2(sc.ncol - 2 * L);
+    ldGP = pad2(ap.ncol);
+    ldGH = pad2(ah.ncol);
+    S = dalloc<R>((size_t)nlm * ldS);
+    S0 = dalloc<R>((size_t)nlm * ldS);
+    GD_CUDA(cudaMemsetAsync(S, 0, sizeof(R) * nlm * ldS, stream));
+    for (int i = 0; i < 3; ++i) TD[i] = dalloc<R>((size_t)nlm * ldTD);
+    AP = dalloc<R>((size_t)nlm * ldAP);
+    AH = dalloc<R>((size_t)nlm * ldAH);
+    const long nf = (long)(T + 1) * nlat;
+    FPb = dalloc<R>((size_t)nf * std::max(std::max(ldFP, ldGP), ldS));
+    // the transform API writes both Fourier buffers with the S row pitch
+    FHb = dalloc<R>((size_t)nf * std::max(std::max(ldFH, ldGH), ldS));
+    gS = dalloc<R>((size_t)sr.total * ng);
+    gA = dalloc<R>((size_t)ar.total * ng);
+    psg = dalloc<R>(ng);
+    dlnpsdt = dalloc<R>(ng);
+    dlnpdtg = dalloc<R>((size_t)L * ng);
+    etadot = dalloc<R>((size_t)(L + 1) * ng);
+    prs = dalloc<R>((size_t)L * ng);
+    dphisdx = dalloc<R>(ng);
+    dphisdy = dalloc<R>(ng);
+    GD_CUDA(cudaMemsetAsync(dphisdx, 0, sizeof(R) * ng, stream));
+    GD_CUDA(cudaMemsetAsync(dphisdy, 0, sizeof(R) * ng, stream));
+    pdryini = dalloc<double>(1);
+    pmean = dalloc<double>(1);
+    rowsum = dalloc<double>(nlat);
+    diagbuf = dalloc<double>(4 * nlat);
+    diagout = dalloc<double>(8);
+    GD_CUDA(cudaMemcpyAsync(pdryini, &c.pdryini, sizeof(double), cudaMemcpyHostToDevice, stream));
+    auto items = make_stage_items(T, 16);
+    nstage_items = (int)items.size();
+    stage_items = upload(items);
+  }
+
+  void init_plans() {
+    synP = make_synth_plan(T, nh, 2 * sc.ncol, stream);
+    synH = make_synth_plan(T, nh, 2 * (sc.ncol - 2 * L), stream);
+    anaP = make_anal_plan(T, 2 * ap.ncol, stream);
+    anaH = make_anal_plan(T, 2 * ah.ncol, stream);
+    anaPhys = make_anal_plan(T, 2 * (3 * L + 1), stream);
+    const double ai = 1.0 / Phys::rerth;
+    const int h0 = 2 * L;  // FH column = S column - 2L
+    std::vector<SynthDesc> full = {
+        {L, sr.vrt, 0, sc.vrt, -1, 0, 1.0, 0.0},
+        {L, sr.div, 0, sc.div, -1, 0, 1.0, 0.0},
+        {L, sr.tv, 0, sc.tv, -1, 0, 1.0, 0.0},
+        {L, sr.u, 1, sc.s - h0, 0, sc.c, -1.0, 1.0},
+        {L, sr.v, 1, sc.c - h0, 0, sc.s, 1.0, 1.0},
+        {L, sr.dtvdx, -1, 0, 0, sc.tv, 0.0, ai},
+        {L, sr.dtvdy, 1, sc.tv - h0, -1, 0, ai, 0.0},
+        {1, sr.lnps, 0, sc.lnps, -1, 0, 1.0, 0.0},
+        {1, sr.dlnpsdx, -1, 0, 0, sc.lnps, 0.0, ai},
+        {1, sr.dlnpsdy, 1, sc.lnps - h0, -1, 0, ai, 0.0},
+    };
+    if (nt > 0) {
+      full.push_back({nt * L, sr.trc, 0, sc.trc, -1, 0, 1.0, 0.0});
+      full.push_back({nt * L, sr.dqdx, -1, 0, 0, sc.trc, 0.0, ai});
+      full.push_back({nt * L, sr.dqdy, 1, sc.trc - h0, -1, 0, ai, 0.0});
+    }
+    c2rFull = make_c2r_plan<R>(full.data(), (int)full.size(), stream);
+    std::vector<SynthDesc> inv = {
+        full[0], full[1], full[2], full[3], full[4], full[7], full[8], full[9],
+    };
+    if (nt > 0) inv.push_back(full[10]);
+    c2rInv = make_c2r_plan<R>(inv.data(), (int)inv.size(), stream);
+    std::vector<AnalDesc> an = {
+        {L, ar.ttend, ap.ttend, 0, -1, 1.0, 0.0},
+        {L, ar.ke, ap.ke, 0, -1, 1.0, 0.0},
+        {1, ar.dlnps, ap.dlnps, 0, -1, 1.0, 0.0},
+        {L, ar.fu, ap.imfu, 1, ah.fu, 1.0, 1.0},
+        {L, ar.fv, ap.imfv, 1, ah.mfv, 1.0, -1.0},
+    };
+    if (nt > 0) an.push_back({nt * L, ar.qtend, ap.qtend, 0, -1, 1.0, 0.0});
+    r2cDyn = make_r2c_plan<R>(an.data(), (int)an.size(), stream);
+    AnalDesc ph = {3 * L + 1, 0, 0, 0, -1, 1.0, 0.0};
+    r2cPhys = make_r2c_plan<R>(&ph, 1, stream);
+  }
+
+  // ------------------------------------------------------------ passes --
+  void synthesis(const FftPlan& plan) {
+    launch_synth<R>(sd, false, synP, S, ldS, 2 * sc.ncol, FPb, ldFP, stream);
+    launch_synth<R>(sd, true, synH, S + 2 * (2 * L), ldS, 2 * (sc.ncol - 2 * L), FHb, ldFH, stream);
+    launch_c2r<R>(sd, plan, FPb, ldFP, FHb, ldFH, gS, stream);
+  }
+  ColumnArgs<R> column_args(bool want_extra) {
+    ColumnArgs<R> a;
+    a.L = L;
+    a.nt = nt;
+    a.nlon = nlon;
+    a.nlat = nlat;
+    a.dry = c.dry;
+    a.ak = ak;
+    a.bk = bk;
+    a.dbk = dbk;
+    a.ck = ck;
+    a.sinlat = sinlat;
+    a.coslat = coslat;
+    a.gS = gS;
+    a.s = sr;
+    a.dphisdx = dphisdx;
+    a.dphisdy = dphisdy;
+    a.gA = gA;
+    a.a = ar;
+    a.psg = psg;
+    a.dlnpsdt = dlnpsdt;
+    a.dlnpdtg = want_extra ? dlnpdtg : nullptr;
+    a.etadot = want_extra ? etadot : nullptr;
+    a.prs = want_extra ? prs : nullptr;
+    a.kappa = (R)(Phys::rd / Phys::cp);
+    a.rd = (R)Phys::rd;
+    a.cvap_cp = (R)(Phys::cvap / Phys::cp - 1.0);
+    a.omega2 = (R)(2.0 * Phys::omega);
+    a.log2sp = (R)GD_FLIT(logf(2.f));
+    a.rlnp_top = (R)GD_FLIT(99999.99f);
+    return a;
+  }
+  // getdyntend: transforms to the grid, column physics, transforms back
+  void dyn_pass(int stage, bool want_extra) {
+    synthesis(c2rFull);
+    launch_dyn_columns<R>(column_args(want_extra), false, stream);
+    if (stage == 0) {  // pdry on stage 1 (dyn_run.f90:135-153); dry runs only
+      launch_area_mean_ps<R>(psg, w, nlat, nlon, rowsum, pmean, stream);
+      launch_pdry_init(pmean, pdryini, stream);
+    }
+    launch_r2c<R>(sd, r2cDyn, gA, FPb, ldGP, FHb, ldGH, stream);
+    launch_anal<R>(sd, false, anaP, FPb, ldGP, 2 * ap.ncol, AP, ldAP, stream);
+    launch_anal<R>(sd, true, anaH, FHb, ldGH, 2 * ah.ncol, AH, ldAH, stream);
+  }
+  void inverse_pass(bool want_extra) {
+    synthesis(c2rInv);
+    launch_dyn_columns<R>(column_args(want_extra), true, stream);
+  }
+  StageArgs<R> stage_args(int s) {
+    StageArgs<R> a;
+    a.L = L;
+    a.nt = nt;
+    a.T = T;
+    a.stage = s;
+    a.explicit_ = c.explicit_;
+    a.final_ = (s == 2);
+    a.items = stage_items;
+    a.nitems = nstage_items;
+    a.moff = moff;
+    a.S = S;
+    a.S0 = S0;
+    a.ldS = ldS;
+    a.AP = AP;
+    a.ldAP = ldAP;
+    a.AH = AH;
+    a.ldAH = ldAH;
+    a.TD0 = TD[0];
+    a.TD1 = TD[1];
+    a.TD2 = TD[2];
+    a.ldTD = ldTD;
+    a.amhyb = amhyb;
+    a.bmhyb = bmhyb;
+    a.svhyb = svhyb;
+    a.tor = tor;
+    a.dhyb = dhyb;
+    a.disspec = disspec;
+    a.diff_prof = diff_prof;
+    a.dmp_prof = dmp_prof;
+    a.dt = (R)c.dt;
+    a.ainv = (R)(1.0 / Phys::rerth);
+    a.ainv2 = (R)(1.0 / (Phys::rerth * Phys::rerth));
+    a.rerth = (R)Phys::rerth;
+    double ce[3][3] = {{tb.a21, 0, 0}, {tb.a31, tb.a32, 0}, {tb.b1, tb.b2, tb.b3}};
+    double ci[3][3] = {{tb.aa21, 0, 0}, {tb.aa31, tb.aa32, 0}, {tb.bb1, tb.bb2, tb.bb3}};
+    double cimp[3] = {tb.aa22, tb.aa33, fabs(tb.bb4) > 1.e-5 ? tb.bb4 : 0.0};
+    for (int r = 0; r < 3; ++r) {
+      a.ce[r] = (R)ce[s][r];
+      a.ci[r] = c.explicit_ ? R(0) : (R)ci[s][r];
+    }
+    a.cimp = c.explicit_ ? R(0) : (R)cimp[s];
+    a.sc = sc;
+    a.tc = tc;
+    a.ap = ap;
+    a.ah = ah;
+    return a;
+  }
+  HsArgs<R> hs_args() {
+    HsArgs<R> h;
+    h.L = L;
+    h.nlon = nlon;
+    h.nlat = nlat;
+    h.ak = ak;
+    h.bk = bk;
+    h.sinlat = sinlat;
+    h.coslat = coslat;
+    h.gS = gS;
+    h.s = sr;
+    h.gA = gA;
+    h.kappa = (R)(Phys::rd / Phys::cp);
+    h.sigbot = (R)GD_FLIT(0.7f);  // phy_run_hs.f90:42-49
+    h.kdrag = (R)GD_FLIT(1.f / (1.f * 86400.f));
+    h.krada = (R)GD_FLIT(1.f / (40.f * 86400.f));
+    h.kradb = (R)GD_FLIT(1.f / (4.f * 86400.f));
+    h.expo = (R)GD_FLIT(2.f / 7.f);
+    return h;
+  }
+  void phys_pass() {
+    inverse_pass(false);
+    if (c.heldsuarez) launch_hs_forcing<R>(hs_args(), stream);
+    if (c.massfix) {
+      launch_area_mean_ps<R>(psg, w, nlat, nlon, rowsum, pmean, stream);
+      launch_massfix_grid<R>(psg, pdryini, pmean, (int)ng, gA + (long)3 * L * ng, stream);
+    }
+    if (c.heldsuarez || c.massfix) {
+      launch_r2c<R>(sd, r2cPhys, gA, FPb, ldGP, FHb, ldGH, stream);
+      launch_anal<R>(sd, false, anaPhys, FPb, ldGP, 2 * (3 * L + 1), AP, ldAP, stream);
+      launch_phys_update<R>(S, ldS, sc, L, nt, nlm, AP, ldAP, c.massfix, c.heldsuarez, (R)c.dt, lapv,
+                            (R)Phys::rerth, stream);
+    }
+  }
+  // advance (run.f90:194-565)
+  void step() {
+    GD_CUDA(cudaMemcpyAsync(S0, S, sizeof(R) * nlm * ldS, cudaMemcpyDeviceToDevice, stream));
+    for (int s = 0; s < 3; ++s) {
+      dyn_pass(s, false);
+      launch_stage<R>(stage_args(s), stream);
+    }
+    if (!c.adiabatic) phys_pass();
+  }
+  void advance(int nsteps) override {
+    if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
+    for (int i = 0; i < nsteps; ++i) {
+      if (steps_done == 0 || gexec == nullptr) {
+        if (steps_done == 0) {  // first step eagerly (sets kernel attributes)
+          long long l0 = g_launches;
+          step();
+          launches_per_step = g_launches - l0;
+        } else {
+          cudaGraph_t g;
+          GD_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+          step();
+          GD_CUDA(cudaStreamEndCapture(stream, &g));
+          GD_CUDA(cudaGraphInstantiate(&gexec, g, 0));
+          GD_CUDA(cudaGraphDestroy(g));
+          g_launches -= launches_per_step;  // counted once per replay below
+          GD_CUDA(cudaGraphLaunch(gexec, stream));
+          g_launches += launches_per_step;
+        }
+      } else {
+        GD_CUDA(cudaGraphLaunch(gexec, stream));
+        g_launches += launches_per_step;
+      }
+      ++steps_done;
+    }
+  }
+
+  // ------------------------------------------------------------ state --
+  void set_state(const double* vrt, const double* div, const double* tv, const double* trc, const double* lnps,
+                 const double* topo) override {
+    const long NS = (long)L * nlm;
+    double* tmp = dalloc<double>(2 * NS * std::max(1, nt));
+    auto put = [&](const double* h, int nb, int col) {
+      GD_CUDA(cudaMemcpyAsync(tmp, h, sizeof(double) * 2 * (long)nb * nlm, cudaMemcpyHostToDevice, stream));
+      launch_ref2int<R>(tmp, nb, nlm, S, ldS, col, stream);
+    };
+    put(vrt, L, sc.vrt);
+    put(div, L, sc.div);
+    put(tv, L, sc.tv);
+    if (nt > 0) {
+      if (!trc) throw std::invalid_argument("trc is NULL but ntrac > 0");
+      put(trc, nt * L, sc.trc);
+    }
+    put(lnps, 1, sc.lnps);
+    launch_sc<R>(S, ldS, sc, L, nlm, lapv, (R)Phys::rerth, stream);
+    // grad(grav*topo) (dyn_init.f90:84)
+    if (topo) {
+      std::vector<double> gt(2 * (size_t)nlm);
+      for (long q = 0; q < 2L * nlm; ++q) gt[q] = Phys::grav * topo[q];
+      std::vector<double> gx(ng), gy(ng);
+      getgrad(1, gt.data(), gx.data(), gy.data());
+      std::vector<R> rx(gx.begin(), gx.end()), ry(gy.begin(), gy.end());
+      GD_CUDA(cudaMemcpyAsync(dphisdx, rx.data(), sizeof(R) * ng, cudaMemcpyHostToDevice, stream));
+      GD_CUDA(cudaMemcpyAsync(dphisdy, ry.data(), sizeof(R) * ng, cudaMemcpyHostToDevice, stream));
+    } else {
+      GD_CUDA(cudaMemsetAsync(dphisdx, 0, sizeof(R) * ng, stream));
+      GD_CUDA(cudaMemsetAsync(dphisdy, 0, sizeof(R) * ng, stream));
+    }
+    GD_CUDA(cudaStreamSynchronize(stream));
+    release(tmp);
+    state_set = true;
+  }
+  void release(void* p) {
+    cudaFree(p);
+    allocs.erase(std::remove(allocs.begin(), allocs.end(), p), allocs.end());
+  }
+  void get_state(double* vrt, double* div, double* tv, double* trc, double* lnps) override {
+    const long NS = (long)L * nlm;
+    double* tmp = dalloc<double>(2 * NS * std::max(1, nt));
+    auto get = [&](double* h, int nb, int col) {
+      if (!h) return;
+      launch_int2ref<R>(S, ldS, col, nb, nlm, tmp, stream);
+      GD_CUDA(cudaMemcpyAsync(h, tmp, sizeof(double) * 2 * (long)nb * nlm, cudaMemcpyDeviceToHost, stream));
+      GD_CUDA(cudaStreamSynchronize(stream));
+    };
+    get(vrt, L, sc.vrt);
+    get(div, L, sc.div);
+    get(tv, L, sc.tv);
+    if (nt > 0) get(trc, nt * L, sc.trc);
+    get(lnps, 1, sc.lnps);
+    release(tmp);
+  }
+  void spec_out(const R* src, long ld, int col, int nb, double* h, double* tmp) {
+    if (!h) return;
+    launch_int2ref<R>(src, ld, col, nb, nlm, tmp, stream);
+    GD_CUDA(cudaMemcpyAsync(h, tmp, sizeof(double) * 2 * (long)nb * nlm, cudaMemcpyDeviceToHost, stream));
+    GD_CUDA(cudaStreamSynchronize(stream));
+  }
+  void getdyntend(int rkstage, int inverse_only, double* dvrt, double* ddiv, double* dtv, double* dtrc,
+                  double* dlnps) override {
+    if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
+    if (inverse_only) {
+      inverse_pass(true);
+      GD_CUDA(cudaStreamSynchronize(stream));
+      return;
+    }
+    dyn_pass(rkstage == 1 ? 0 : 1, true);
+    StageArgs<R> a = stage_args(0);
+    launch_assemble<R>(a, TD[0], stream);
+    double* tmp = dalloc<double>(2L * nlm * L * std::max(1, nt));
+    spec_out(TD[0], ldTD, tc.dvrt, L, dvrt, tmp);
+    spec_out(TD[0], ldTD, tc.ddiv, L, ddiv, tmp);
+    spec_out(TD[0], ldTD, tc.dtv, L, dtv, tmp);
+    if (nt > 0) spec_out(TD[0], ldTD, tc.dtrc, nt * L, dtrc, tmp);
+    spec_out(TD[0], ldTD, tc.dlnps, 1, dlnps, tmp);
+    release(tmp);
+  }
+  void getphytend(double* dvrt, double* ddiv, double* dtv, double* dtrc, double* dlnps) override {
+    if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
+    launch_hs_forcing<R>(hs_args(), stream);
+    launch_r2c<R>(sd, r2cPhys, gA, FPb, ldGP, FHb, ldGH, stream);
+    launch_anal<R>(sd, false, anaPhys, FPb, ldGP, 2 * (3 * L + 1), AP, ldAP, stream);
+    double* tmp = dalloc<double>(2L * nlm * L);
+    spec_out(AP, ldAP, 0, L, dtv, tmp);
+    spec_out(AP, ldAP, L, L, dvrt, tmp);
+    spec_out(AP, ldAP, 2 * L, L, ddiv, tmp);
+    release(tmp);
+    if (dtrc) memset(dtrc, 0, sizeof(double) * 2 * (size_t)nt * L * nlm);
+    if (dlnps) memset(dlnps, 0, sizeof(double) * 2 * (size_t)nlm);
+  }
+
+  // ------------------------------------------------------ transform API --
+  const GemmPlan& synth_plan(int ncr) {
+    auto it = synth_cache.find(ncr);
+    if (it != synth_cache.end()) return it->second;
+    return synth_cache[ncr] = make_synth_plan(T, nh, ncr, stream);
+  }
+  const GemmPlan& anal_plan(int ncr) {
+    auto it = anal_cache.find(ncr);
+    if (it != anal_cache.end()) return it->second;
+    return anal_cache[ncr] = make_anal_plan(T, ncr, stream);
+  }
+  int chunk_cols() const { return std::max(1, std::min(sc.ncol / 2, ar.total / 2)); }
+  // synthesis of ncs complex columns X[nlm][ldS] with descriptors -> host grids
+  void api_synth(const R* X, int ncs, bool needH, const std::vector<SynthDesc>& ds, int nrows, double* out) {
+    launch_synth<R>(sd, false, synth_plan(2 * ncs), X, ldS, 2 * ncs, FPb, ldS, stream);
+    if (needH) launch_synth<R>(sd, true, synth_plan(2 * ncs), X, ldS, 2 * ncs, FHb, ldS, stream);
+    FftPlan p = make_c2r_plan<R>(ds.data(), (int)ds.size(), stream);
+    launch_c2r<R>(sd, p, FPb, ldS, FHb, ldS, gS, stream);
+    grid_out(gS, nrows, out);
+    free_fft_plan(p);
+  }
+  void grid_out(const R* g, int nrows, double* out) {
+    long n = (long)nrows * ng;
+    if (sizeof(R) == 8) {
+      GD_CUDA(cudaMemcpyAsync(out, g, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+    } else {
+      double* tmp = dalloc<double>(n);
+      launch_to_double<R>(g, tmp, n, stream);
+      GD_CUDA(cudaMemcpyAsync(out, tmp, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+      GD_CUDA(cudaStreamSynchronize(stream));
+      release(tmp);
+    }
+    GD_CUDA(cudaStreamSynchronize(stream));
+  }
+  void grid_in(const double* in, int nrows, R* g) {
+    long n = (long)nrows * ng;
+    double* tmp = dalloc<double>(n);
+    GD_CUDA(cudaMemcpyAsync(tmp, in, sizeof(double) * n, cudaMemcpyHostToDevice, stream));
+    launch_convert<R>(tmp, g, n, stream);
+    GD_CUDA(cudaStreamSynchronize(stream));
+    release(tmp);
+  }
+  R* X_ = nullptr;
+  R* scratchX() {
+    if (!X_) X_ = dalloc<R>((size_t)nlm * ldS);
+    return X_;
+  }
+  void spec_in(const double* h, int nb, R* X, int col) {
+    double* tmp = dalloc<double>(2L * nb * nlm);
+    GD_CUDA(cudaMemcpyAsync(tmp, h, sizeof(double) * 2 * (long)nb * nlm, cudaMemcpyHostToDevice, stream));
+    launch_ref2int<R>(tmp, nb, nlm, X, ldS, col, stream);
+    GD_CUDA(cudaStreamSynchronize(stream));
+    release(tmp);
+  }
+  void spectogrd(int nb, const double* spec, double* grid) override {
+    R* X = scratchX();
+    for (int b0 = 0; b0 < nb; b0 += chunk_cols()) {
+      int k = std::min(chunk_cols(), nb - b0);
+      spec_in(spec + 2L * b0 * nlm, k, X, 0);
+      std::vector<SynthDesc> ds = {{k, 0, 0, 0, -1, 0, 1.0, 0.0}};
+      api_synth(X, k, false, ds, k, grid + (long)b0 * ng);
+    }
+  }
+  void getuv(int nb, const double* vrt, const double* div, double* u, double* v) override {
+    R* X = scratchX();
+    const int ch = chunk_cols();
+    for (int b0 = 0; b0 < nb; b0 += ch) {
+      int k = std::min(ch, nb - b0);
+      spec_in(vrt + 2L * b0 * nlm, k, X, 0);
+      spec_in(div + 2L * b0 * nlm, k, X, k);
+      // s = a invlap vrt, c = a invlap div (shtns.f90:259-260)
+      launch_scale_cols<R>(X, ldS, 0, 2 * k, nlm, invlap_a(), R(1), stream);
+      std::vector<SynthDesc> ds = {{k, 0, 1, 0, 0, k, -1.0, 1.0}, {k, k, 1, k, 0, 0, 1.0, 1.0}};
+      std::vector<double> out(2L * k * ng);
+      api_synth(X, 2 * k, true, ds, 2 * k, out.data());
+      memcpy(u + (long)b0 * ng, out.data(), sizeof(double) * k * ng);
+      memcpy(v + (long)b0 * ng, out.data() + (long)k * ng, sizeof(double) * k * ng);
+    }
+  }
+  R* invlap_ = nullptr;
+  const R* invlap_a() {  // rerth * invlap, 0 for n = 0
+    if (!invlap_) {
+      std::vector<double> il(nlm);
+      for (int q = 0; q < nlm; ++q) il[q] = (q == 0) ? 0.0 : Phys::rerth / h_lap[q];
+      invlap_ = upload(toR(il));
+    }
+    return invlap_;
+  }
+  void getgrad(int nb, const double* spec, double* gx, double* gy) override {
+    R* X = scratchX();
+    const double ai = 1.0 / Phys::rerth;
+    const int ch = chunk_cols();
+    for (int b0 = 0; b0 < nb; b0 += ch) {
+      int k = std::min(ch, nb - b0);
+      spec_in(spec + 2L * b0 * nlm, k, X, 0);
+      std::vector<SynthDesc> ds = {{k, 0, -1, 0, 0, 0, 0.0, ai}, {k, k, 1, 0, -1, 0, ai, 0.0}};
+      std::vector<double> out(2L * k * ng);
+      api_synth(X, k, true, ds, 2 * k, out.data());
+      memcpy(gx + (long)b0 * ng, out.data(), sizeof(double) * k * ng);
+      memcpy(gy + (long)b0 * ng, out.data() + (long)k * ng, sizeof(double) * k * ng);
+    }
+  }
+  void api_anal(const std::vector<AnalDesc>& ds, int ncP, int ncH) {
+    FftPlan p = make_r2c_plan<R>(ds.data(), (int)ds.size(), stream);
+    launch_r2c<R>(sd, p, gA, FPb, ldS, FHb, ldS, stream);
+    launch_anal<R>(sd, false, anal_plan(2 * ncP), FPb, ldS, 2 * ncP, AP, ldAP, stream);
+    if (ncH > 0) launch_anal<R>(sd, true, anal_plan(2 * ncH), FHb, ldS, 2 * ncH, AH, ldAH, stream);
+    free_fft_plan(p);
+  }
+  int achunk() const { return std::max(1, std::min(ap.ncol / 2, ar.total / 2)); }
+  void grdtospec(int nb, const double* grid, double* spec) override {
+    const int ch = achunk();
+    double* tmp = dalloc<double>(2L * ch * nlm);
+    for (int b0 = 0; b0 < nb; b0 += ch) {
+      int k = std::min(ch, nb - b0);
+      grid_in(grid + (long)b0 * ng, k, gA);
+      api_anal({{k, 0, 0, 0, -1, 1.0, 0.0}}, k, 0);
+      launch_int2ref<R>(AP, ldAP, 0, k, nlm, tmp, stream);
+      GD_CUDA(cudaMemcpyAsync(spec + 2L * b0 * nlm, tmp, sizeof(double) * 2 * (long)k * nlm, cudaMemcpyDeviceToHost,
+                              stream));
+      GD_CUDA(cudaStreamSynchronize(stream));
+    }
+    release(tmp);
+  }
+  void getvrtdivspec(int nb, const double* u, const double* v, double* vrt, double* div) override {
+    const int ch = std::max(1, std::min(ah.ncol / 2, achunk()));
+    double* tmp = dalloc<double>(2L * ch * nlm);
+    const R ai = (R)(1.0 / Phys::rerth);
+    for (int b0 = 0; b0 < nb; b0 += ch) {
+      int k = std::min(ch, nb - b0);
+      grid_in(u + (long)b0 * ng, k, gA);
+      grid_in(v + (long)b0 * ng, k, gA + (long)k * ng);
+      // GP: [i m/cos V | i m/cos U], GH: [U | -V]
+      std::vector<AnalDesc> ds = {{k, 0, k, 1, 0, 1.0, 1.0}, {k, k, 0, 1, k, 1.0, -1.0}};
+      api_anal(ds, 2 * k, 2 * k);
+      // vrt = (AP[0:k] + AH[0:k]) / a, div = (AP[k:2k] + AH[k:2k]) / a
+      launch_combine<R>(AP, ldAP, 0, AH, ldAH, 0, AP, ldAP, 0, 2 * k, nlm, ai, stream);
+      launch_int2ref<R>(AP, ldAP, 0, k, nlm, tmp, stream);
+      GD_CUDA(cudaMemcpyAsync(vrt + 2L * b0 * nlm, tmp, sizeof(double) * 2 * (long)k * nlm, cudaMemcpyDeviceToHost,
+                              stream));
+      GD_CUDA(cudaStreamSynchronize(stream));
+      launch_int2ref<R>(AP, ldAP, k, k, nlm, tmp, stream);
+      GD_CUDA(cudaMemcpyAsync(div + 2L * b0 * nlm, tmp, sizeof(double) * 2 * (long)k * nlm, cudaMemcpyDeviceToHost,
+                              stream));
+      GD_CUDA(cudaStreamSynchronize(stream));
+    }
+    release(tmp);
+  }
+
+  void grid_info(double* lats, double* gauwts, double* areawts, int* degree, int* order, double* lap,
+                 double* invlap) override {
+    for (int j = 0; j < nlat; ++j) {
+      if (lats) lats[j] = h_lat[j];
+      if (gauwts) gauwts[j] = h_w[j];
+      if (areawts) areawts[j] = h_w[j] / (2.0 * nlon);
+    }
+    for (int q = 0; q < nlm; ++q) {
+      if (degree) degree[q] = h_deg[q];
+      if (order) order[q] = h_ord[q];
+      if (lap) lap[q] = h_lap[q];
+      if (invlap) invlap[q] = q == 0 ? 0.0 : 1.0 / h_lap[q];
+    }
+  }
+  int get_grid(const char* name, double* out) override {
+    std::string n(name);
+    const R* src = nullptr;
+    int rows = 0;
+    if (n == "ug") src = gS + (long)sr.u * ng, rows = L;
+    else if (n == "vg") src = gS + (long)sr.v * ng, rows = L;
+    else if (n == "vrtg") src = gS + (long)sr.vrt * ng, rows = L;
+    else if (n == "divg") src = gS + (long)sr.div * ng, rows = L;
+    else if (n == "tvg") src = gS + (long)sr.tv * ng, rows = L;
+    else if (n == "trcg") src = gS + (long)sr.trc * ng, rows = nt * L;
+    else if (n == "lnpsg") src = gS + (long)sr.lnps * ng, rows = 1;
+    else if (n == "dlnpdtg") src = dlnpdtg, rows = L;
+    else if (n == "etadot") src = etadot, rows = L + 1;
+    else if (n == "psg") src = psg, rows = 1;
+    else if (n == "dlnpsdt") src = dlnpsdt, rows = 1;
+    else if (n == "prs") src = prs, rows = L;
+    else if (n == "dphisdx") src = dphisdx, rows = 1;
+    else if (n == "dphisdy") src = dphisdy, rows = 1;
+    if (!src || rows == 0) return GD_ERR_ARG;
+    grid_out(src, rows, out);
+    return GD_OK;
+  }
+  void diag(double* out) override {
+    launch_diag<R>(gS + (long)sr.u * ng, gS + (long)sr.v * ng, L, psg, dlnpsdt, w, nlat, nlon, diagbuf, diagout,
+                   stream);
+    double h[5];
+    GD_CUDA(cudaMemcpyAsync(h, diagout, 4 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    GD_CUDA(cudaMemcpyAsync(h + 4, pdryini, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    GD_CUDA(cudaStreamSynchronize(stream));
+    memcpy(out, h, sizeof(h));
+  }
+};
+
+}  // namespace gd
+
+// ====================================================================== ABI
+struct gd_ctx {
+  std::unique_ptr<gd::DycoreBase> d;
+  gd_config cfg;
+  std::string err;
+};
+
+static std::string g_init_error;
+
+template <typename F>
+static int guarded(gd_ctx* ctx, F f) {
+  if (!ctx || !ctx->d) return GD_ERR_ARG;
+  try {
+    f();
+    return GD_OK;
+  } catch (const gd::CudaError& e) {
+    ctx->err = e.what();
+    return GD_ERR_CUDA;
+  } catch (const std::invalid_argument& e) {
+    ctx->err = e.what();
+    return GD_ERR_ARG;
+  } catch (const std::runtime_error& e) {
+    ctx->err = e.what();
+    return GD_ERR_STATE;
+  } catch (const std::exception& e) {
+    ctx->err = e.what();
+    return GD_ERR_CUDA;
+  }
+}
+
+static bool is_2a3b(int n) {
+  if (n <= 0) return false;
+  while (n % 2 == 0) n /= 2;
+  while (n % 3 == 0) n /= 3;
+  return n == 1;
+}
+
+extern "C" {
+
+int gd_default_config(gd_config* c) {
+  if (!c) return GD_ERR_ARG;
+  memset(c, 0, sizeof(*c));
+  c->ntrunc = 42;
+  c->nlon = 128;
+  c->nlat = 64;
+  c->nlev = 20;
+  c->ntrac = 0;
+  c->dt = 1200.0;
+  c->precision = GD_PREC_FP64;
+  c->explicit_ = 0;
+  c->adiabatic = 0;
+  c->heldsuarez = 1;
+  c->massfix = 1;
+  c->dry = 1;
+  c->ndiss = 0;
+  c->efold = 0.0;
+  c->hdif_fac = 1.0;
+  c->hdif_fac2 = 1.0;
+  c->fshk = 0.0;
+  c->taustratdamp = 5.0 * 86400.0;
+  c->pdryini = 0.0;
+  c->device = 0;
+  return GD_OK;
+}
+
+int gd_init(const gd_config* cfg, const double* ak, const double* bk, gd_ctx** out) {
+  if (!cfg || !ak || !bk || !out) {
+    g_init_error = "gd_init: null argument";
+    return GD_ERR_ARG;
+  }
+  *out = nullptr;
+  const gd_config& c = *cfg;
+  std::string why;
+  if (!is_2a3b(c.nlon) || c.nlon % 2) why = "nlon must be an even 2^a 3^b";
+  else if (c.nlat < 4 || c.nlat % 2) why = "nlat must be even and >= 4";
+  else if (c.ntrunc < 1 || c.ntrunc >= c.nlon / 2 || c.ntrunc >= c.nlat) why = "ntrunc must satisfy 1 <= T < nlon/2 and T < nlat";
+  else if (c.nlev < 3 || c.nlev > 126) why = "nlev must be in [3, 126]";
+  else if (c.ntrac < 0) why = "ntrac must be >= 0";
+  else if (!(c.dt > 0)) why = "dt must be positive";
+  else if (c.precision < GD_PREC_FP64 || c.precision > GD_PREC_BF16X3) why = "unknown precision";
+  else if (!c.dry && c.ntrac > 0) why = "moist mass bookkeeping (dry = 0 with tracers) is not supported";
+  if (!why.empty()) {
+    g_init_error = "gd_init: " + why;
+    return (why.find("not supported") != std::string::npos) ? GD_ERR_UNSUPPORTED : GD_ERR_ARG;
+  }
+  if (c.precision == GD_PREC_TF32X3 || c.precision == GD_PREC_BF16X3) {
+    g_init_error = "gd_init: split-precision Legendre GEMMs are not built in this library version";
+    return GD_ERR_UNSUPPORTED;
+  }
+  gd_ctx* ctx = new gd_ctx();
+  ctx->cfg = c;
+  try {
+    if (c.precision == GD_PREC_FP64)
+      ctx->d.reset(new gd::Dycore<double>(c, ak, bk));
+    else
+      ctx->d.reset(new gd::Dycore<float>(c, ak, bk));
+  } catch (const gd::CudaError& e) {
+    g_init_error = e.what();
+    delete ctx;
+    return std::string(e.what()).find("cudaMalloc") != std::string::npos ? GD_ERR_NOMEM : GD_ERR_CUDA;
+  } catch (const std::exception& e) {
+    g_init_error = e.what();
+    delete ctx;
+    return GD_ERR_CUDA;
+  }
+  *out = ctx;
+  return GD_OK;
+}
+
+int gd_finalize(gd_ctx* ctx) {
+  if (!ctx) return GD_ERR_ARG;
+  delete ctx;
+  return GD_OK;
+}
+
+int gd_set_state(gd_ctx* ctx, const double* vrt, const double* div, const double* tv, const double* trc,
+                 const double* lnps, const double* topo) {
+  if (!vrt || !div || !tv || !lnps) {
+    if (ctx) ctx->err = "gd_set_state: null state array";
+    return GD_ERR_ARG;
+  }
+  return guarded(ctx, [&] { ctx->d->set_state(vrt, div, tv, trc, lnps, topo); });
+}
+int gd_get_state(gd_ctx* ctx, double* vrt, double* div, double* tv, double* trc, double* lnps) {
+  return guarded(ctx, [&] { ctx->d->get_state(vrt, div, tv, trc, lnps); });
+}
+int gd_getdyntend(gd_ctx* ctx, int rkstage, int inverse_only, double* dvrt, double* ddiv, double* dtv, double* dtrc,
+                  double* dlnps) {
+  if (rkstage < 1 || rkstage > 3) {
+    if (ctx) ctx->err = "gd_getdyntend: rkstage must be 1, 2 or 3";
+    return GD_ERR_ARG;
+  }
+  if (!inverse_only && (!dvrt || !ddiv || !dtv || !dlnps)) {
+    if (ctx) ctx->err = "gd_getdyntend: null tendency array";
+    return GD_ERR_ARG;
+  }
+  return guarded(ctx, [&] { ctx->d->getdyntend(rkstage, inverse_only, dvrt, ddiv, dtv, dtrc, dlnps); });
+}
+int gd_getphytend(gd_ctx* ctx, double* dvrt, double* ddiv, double* dtv, double* dtrc, double* dlnps) {
+  return guarded(ctx, [&] { ctx->d->getphytend(dvrt, ddiv, dtv, dtrc, dlnps); });
+}
+int gd_advance(gd_ctx* ctx, double t, int nsteps) {
+  (void)t;
+  if (nsteps < 0) {
+    if (ctx) ctx->err = "gd_advance: nsteps < 0";
+    return GD_ERR_ARG;
+  }
+  return guarded(ctx, [&] { ctx->d->advance(nsteps); });
+}
+int gd_spectogrd(gd_ctx* ctx, int nb, const double* spec, double* grid) {
+  if (nb < 0 || (nb > 0 && (!spec || !grid))) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->spectogrd(nb, spec, grid); });
+}
+int gd_grdtospec(gd_ctx* ctx, int nb, const double* grid, double* spec) {
+  if (nb < 0 || (nb > 0 && (!spec || !grid))) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->grdtospec(nb, grid, spec); });
+}
+int gd_getuv(gd_ctx* ctx, int nb, const double* vrt, const double* div, double* u, double* v) {
+  if (nb < 0 || (nb > 0 && (!vrt || !div || !u || !v))) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->getuv(nb, vrt, div, u, v); });
+}
+int gd_getvrtdivspec(gd_ctx* ctx, int nb, const double* u, const double* v, double* vrt, double* div) {
+  if (nb < 0 || (nb > 0 && (!vrt || !div || !u || !v))) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->getvrtdivspec(nb, u, v, vrt, div); });
+}
+int gd_getgrad(gd_ctx* ctx, int nb, const double* spec, double* gx, double* gy) {
+  if (nb < 0 || (nb > 0 && (!spec || !gx || !gy))) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->getgrad(nb, spec, gx, gy); });
+}
+int gd_grid_info(gd_ctx* ctx, double* lats, double* gauwts, double* areawts, int* degree, int* order, double* lap,
+                 double* invlap) {
+  return guarded(ctx, [&] { ctx->d->grid_info(lats, gauwts, areawts, degree, order, lap, invlap); });
+}
+int gd_get_grid(gd_ctx* ctx, const char* name, double* out) {
+  if (!name || !out) return GD_ERR_ARG;
+  int rc = GD_OK;
+  int g = guarded(ctx, [&] { rc = ctx->d->get_grid(name, out); });
+  return g != GD_OK ? g : rc;
+}
+int gd_diag(gd_ctx* ctx, double* out5) {
+  if (!out5) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->diag(out5); });
+}
+int gd_set_stream(gd_ctx* ctx, void* stream) {
+  return guarded(ctx, [&] {
+    GD_CUDA(cudaStreamSynchronize(ctx->d->stream));
+    if (ctx->d->own_stream) cudaStreamDestroy(ctx->d->stream);
+    ctx->d->stream = (cudaStream_t)stream;
+    ctx->d->own_stream = false;
+  });
+}
+int gd_sync(gd_ctx* ctx) {
+  return guarded(ctx, [&] { GD_CUDA(cudaStreamSynchronize(ctx->d->stream)); });
+}
+long long gd_launch_count(gd_ctx* ctx) {
+  (void)ctx;
+  return gd::g_launches;
+}
+const char* gd_last_error(gd_ctx* ctx) {
+  if (!ctx) return g_init_error.c_str();
+  return ctx->err.c_str();
+}
+
+}  // extern "C"

@@ -1,0 +1,679 @@
+// gd_sht.cu -- Gaussian-grid spherical harmonic transform kernels for
+// sm_103a: FP64 grid/table construction, per-order Legendre GEMMs with the
+// even/odd hemispheric split, and shared-memory Stockham FFTs along longitude.
+//
+// These take over the roles SHTns (+FFTW) plays behind src/shtns.f90 of
+// jswhit/gfs-dycore: shtns_cos_array / shtns_gauss_wts (shtns.f90:125-126),
+// the SHT_GAUSS_FLY Legendre recurrences, shtns_sh_to_spat /
+// shtns_spat_to_sh (shtns.f90:195,199,225,229) and the vector forms
+// (shtns.f90:261,270,303,308,341,348).  Convention: orthonormal harmonics
+// without Condon-Shortley phase (shtns.f90:110), latitudes north to south.
+#include <vector>
+
+#include "gd_kernels.h"
+
+namespace gd {
+
+long long g_launches = 0;
+
+// ------------------------------------------------------------------ init --
+// Gauss-Legendre nodes (north to south) and weights by Newton iteration on
+// P_nlat, FP64.  One thread per northern node.
+__global__ void k_gauss(int N, double* mu, double* w) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= N / 2) return;
+  double x = cos(3.14159265358979323846 * (j + 0.75) / (N + 0.5));
+  double dp = 0.0;
+  for (int it = 0; it < 100; ++it) {
+    double p0 = 1.0, p1 = x;
+    for (int k = 1; k < N; ++k) {
+      double p2 = ((2 * k + 1) * x * p1 - k * p0) / (k + 1);
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = N * (x * p1 - p0) / (x * x - 1.0);
+    double dx = p1 / dp;
+    x -= dx;
+    if (fabs(dx) <= 1e-16) break;
+  }
+  double p0 = 1.0, p1 = x;
+  for (int k = 1; k < N; ++k) {
+    double p2 = ((2 * k + 1) * x * p1 - k * p0) / (k + 1);
+    p0 = p1;
+    p1 = p2;
+  }
+  dp = N * (x * p1 - p0) / (x * x - 1.0);
+  double wj = 2.0 / ((1.0 - x) * (1.0 + x) * dp * dp);
+  mu[j] = x;
+  mu[N - 1 - j] = -x;
+  w[j] = wj;
+  w[N - 1 - j] = wj;
+}
+
+void launch_gauss(int nlat, double* mu, double* w, cudaStream_t s) {
+  k_gauss<<<ceil_div(nlat / 2, 64), 64, 0, s>>>(nlat, mu, w);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+
+// Orthonormal associated Legendre functions P_n^m(mu_j)/sqrt(2 pi) and their
+// latitude derivative, by the three-term recurrence in n with exact binary
+// rescaling (ldexp) so high orders near the poles neither underflow nor lose
+// the recurrence.  FP64; one thread per (m, j).
+__global__ void k_legendre(int T, int nh, const double* mu, const long* toff, double* P, double* H) {
+  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)(T + 1) * nh) return;
+  const int m = (int)(t / nh), j = (int)(t % nh);
+  const int K = T - m + 1;
+  const double x = mu[j];
+  const double s = sqrt((1.0 - x) * (1.0 + x));
+  const double inv_s2pi = 0.39894228040143267794;  // 1/sqrt(2 pi)
+  const int SC = 600;
+  double v = 0.70710678118654752440;
+  int c = 0;
+  for (int k = 1; k <= m; ++k) {
+    v *= sqrt((2.0 * k + 1.0) / (2.0 * k)) * s;
+    if (fabs(v) < ldexp(1.0, -SC)) {
+      v = ldexp(v, SC);
+      ++c;
+    }
+  }
+  double pm1 = 0.0, p = v;
+  double* Pr = P + toff[m] + (long)j * K;
+  double* Hr = H + toff[m] + (long)j * K;
+  for (int n = m; n <= T; ++n) {
+    if (n == m + 1) {
+      double pn = sqrt(2.0 * m + 3.0) * x * p;
+      pm1 = p;
+      p = pn;
+    } else if (n > m + 1) {
+      double a = sqrt((4.0 * n * n - 1.0) / ((double)n * n - (double)m * m));
+      double b = sqrt(((n - 1.0) * (n - 1.0) - (double)m * m) / (4.0 * (n - 1.0) * (n - 1.0) - 1.0));
+      double pn = a * (x * p - b * pm1);
+      pm1 = p;
+      p = pn;
+    }
+    if (c > 0 && fabs(p) > ldexp(1.0, 300)) {
+      p = ldexp(p, -SC);
+      pm1 = ldexp(pm1, -SC);
+      --c;
+    }
+    double cnm = (n > m) ? sqrt(((double)n * n - (double)m * m) * (2.0 * n + 1.0) / (2.0 * n - 1.0)) : 0.0;
+    double h = (-n * x * p + cnm * pm1) / s;
+    double pv = (c == 0) ? p : ldexp(p, -SC * c);
+    double hv = (c == 0) ? h : ldexp(h, -SC * c);
+    Pr[n - m] = pv * inv_s2pi;
+    Hr[n - m] = hv * inv_s2pi;
+  }
+}
+
+void launch_legendre_tables(int T, int nh, const double* mu, const long* toff, double* P64, double* H64,
+                            cudaStream_t s) {
+  long n = (long)(T + 1) * nh;
+  k_legendre<<<ceil_div(n, 128), 128, 0, s>>>(T, nh, mu, toff, P64, H64);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+
+template <typename R>
+__global__ void k_convert(const double* src, R* dst, long n) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    dst[i] = (R)src[i];
+}
+template <typename R>
+void launch_convert(const double* src, R* dst, long n, cudaStream_t s) {
+  int blocks = (int)std::min<long>(ceil_div(n, 256), 152L * 16);
+  k_convert<R><<<blocks, 256, 0, s>>>(src, dst, n);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template void launch_convert<double>(const double*, double*, long, cudaStream_t);
+template void launch_convert<float>(const double*, float*, long, cudaStream_t);
+
+// --------------------------------------------------------- Legendre GEMMs --
+// Tiles: synthesis 32 latitude pairs x 64 real columns, analysis 32 degrees
+// x 64 real columns; 256 threads, each 2 rows x 4 columns (columns strided
+// by 16 for conflict-free shared reads and coalesced stores).
+constexpr int GT_R = 32, GT_C = 64, GT_K = 16;
+
+GemmPlan make_synth_plan(int T, int nh, int ncols_real, cudaStream_t s) {
+  std::vector<int4> it;
+  int tj = ceil_div(nh, GT_R), tc = ceil_div(ncols_real, GT_C);
+  for (int m = 0; m <= T; ++m)  // longest K first for load balance
+    for (int a = 0; a < tj; ++a)
+      for (int b = 0; b < tc; ++b) it.push_back(make_int4(m, a, b, 0));
+  GemmPlan p;
+  p.nitems = (int)it.size();
+  GD_CUDA(cudaMalloc(&p.items, sizeof(int4) * it.size()));
+  GD_CUDA(cudaMemcpyAsync(p.items, it.data(), sizeof(int4) * it.size(), cudaMemcpyHostToDevice, s));
+  GD_CUDA(cudaStreamSynchronize(s));
+  return p;
+}
+
+GemmPlan make_anal_plan(int T, int ncols_real, cudaStream_t s) {
+  std::vector<int4> it;
+  int tc = ceil_div(ncols_real, GT_C);
+  for (int m = 0; m <= T; ++m)
+    for (int a = 0; a < ceil_div(T - m + 1, GT_R); ++a)
+      for (int b = 0; b < tc; ++b) it.push_back(make_int4(m, a, b, 0));
+  GemmPlan p;
+  p.nitems = (int)it.size();
+  GD_CUDA(cudaMalloc(&p.items, sizeof(int4) * it.size()));
+  GD_CUDA(cudaMemcpyAsync(p.items, it.data(), sizeof(int4) * it.size(), cudaMemcpyHostToDevice, s));
+  GD_CUDA(cudaStreamSynchronize(s));
+  return p;
+}
+
+void free_plan(GemmPlan& p) {
+  if (p.items) cudaFree(p.items);
+  p.items = nullptr;
+  p.nitems = 0;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_synth(const int4* __restrict__ items, int T, int nh, int nlat,
+                                               const long* __restrict__ moff, const long* __restrict__ toff,
+                                               const R* __restrict__ tab, const R* __restrict__ B, long ldB,
+                                               int ncols, R* __restrict__ F, long ldF, int parityH) {
+  __shared__ R sA[GT_K][GT_R];
+  __shared__ R sB[GT_K][GT_C];
+  const int4 it = items[blockIdx.x];
+  const int m = it.x, j0 = it.y * GT_R, c0 = it.z * GT_C;
+  const int K = T - m + 1;
+  const R* A = tab + toff[m];
+  const R* Bm = B + moff[m] * ldB;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  R ae[2][4], ao[2][4];
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) ae[r][i] = ao[r][i] = R(0);
+  for (int q0 = 0; q0 < K; q0 += GT_K) {
+    for (int e = threadIdx.x; e < GT_R * GT_K; e += 256) {
+      int jj = e / GT_K, qq = e % GT_K;
+      int j = j0 + jj, q = q0 + qq;
+      sA[qq][jj] = (j < nh && q < K) ? A[(long)j * K + q] : R(0);
+    }
+    for (int e = threadIdx.x; e < GT_K * GT_C; e += 256) {
+      int qq = e / GT_C, cc = e % GT_C;
+      int q = q0 + qq, c = c0 + cc;
+      sB[qq][cc] = (q < K && c < ncols) ? Bm[(long)q * ldB + c] : R(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int qq = 0; qq < GT_K; qq += 2) {
+      R a0 = sA[qq][2 * ty], a1 = sA[qq][2 * ty + 1];
+      R b0 = sA[qq + 1][2 * ty], b1 = sA[qq + 1][2 * ty + 1];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        R be = sB[qq][tx + 16 * i], bo = sB[qq + 1][tx + 16 * i];
+        ae[0][i] += a0 * be;
+        ae[1][i] += a1 * be;
+        ao[0][i] += b0 * bo;
+        ao[1][i] += b1 * bo;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    int j = j0 + 2 * ty + r;
+    if (j >= nh) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      int c = c0 + tx + 16 * i;
+      if (c >= ncols) continue;
+      R E = ae[r][i], O = ao[r][i];
+      F[((long)m * nlat + j) * ldF + c] = E + O;
+      F[((long)m * nlat + (nlat - 1 - j)) * ldF + c] = parityH ? (O - E) : (E - O);
+    }
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_anal(const int4* __restrict__ items, int T, int nh, int nlat,
+                                              const long* __restrict__ moff, const long* __restrict__ toff,
+                                              const R* __restrict__ tab, const R* __restrict__ G, long ldG,
+                                              int ncols, R* __restrict__ A, long ldA, int parityH) {
+  __shared__ R sT[GT_K][GT_R];
+  __shared__ R sE[GT_K][GT_C];
+  __shared__ R sO[GT_K][GT_C];
+  const int4 it = items[blockIdx.x];
+  const int m = it.x, q0 = it.y * GT_R, c0 = it.z * GT_C;
+  const int K = T - m + 1;
+  const R* Tm = tab + toff[m];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  R acc[2][4];
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc[r][i] = R(0);
+  for (int jb = 0; jb < nh; jb += GT_K) {
+    for (int e = threadIdx.x; e < GT_K * GT_R; e += 256) {
+      int jl = e / GT_R, ql = e % GT_R;
+      int j = jb + jl, q = q0 + ql;
+      sT[jl][ql] = (j < nh && q < K) ? Tm[(long)j * K + q] : R(0);
+    }
+    for (int e = threadIdx.x; e < GT_K * GT_C; e += 256) {
+      int jl = e / GT_C, cc = e % GT_C;
+      int j = jb + jl, c = c0 + cc;
+      R gn = R(0), gs = R(0);
+      if (j < nh && c < ncols) {
+        gn = G[((long)m * nlat + j) * ldG + c];
+        gs = G[((long)m * nlat + (nlat - 1 - j)) * ldG + c];
+      }
+      // n-m even rows pair with (gn+gs) for P and (gn-gs) for dP/dphi
+      sE[jl][cc] = parityH ? gn - gs : gn + gs;
+      sO[jl][cc] = parityH ? gn + gs : gn - gs;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int jl = 0; jl < GT_K; ++jl) {
+      R t0 = sT[jl][2 * ty], t1 = sT[jl][2 * ty + 1];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        acc[0][i] += t0 * sE[jl][tx + 16 * i];
+        acc[1][i] += t1 * sO[jl][tx + 16 * i];
+      }
+    }
+    __syncthreads();
+  }
+  const long base = moff[m];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    int q = q0 + 2 * ty + r;
+    if (q >= K) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      int c = c0 + tx + 16 * i;
+      if (c < ncols) A[(base + q) * ldA + c] = acc[r][i];
+    }
+  }
+}
+
+template <typename R>
+void launch_synth(const ShtDev<R>& d, bool useH, const GemmPlan& plan, const R* B, long ldB, int ncols_real,
+                  R* F, long ldF, cudaStream_t s) {
+  if (plan.nitems == 0) return;
+  k_synth<R><<<plan.nitems, 256, 0, s>>>(plan.items, d.T, d.nh, d.nlat, d.moff, d.toff, useH ? d.H : d.P, B, ldB,
+                                         ncols_real, F, ldF, useH ? 1 : 0);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template <typename R>
+void launch_anal(const ShtDev<R>& d, bool useH, const GemmPlan& plan, const R* G, long ldG, int ncols_real, R* A,
+                 long ldA, cudaStream_t s) {
+  if (plan.nitems == 0) return;
+  k_anal<R><<<plan.nitems, 256, 0, s>>>(plan.items, d.T, d.nh, d.nlat, d.moff, d.toff, useH ? d.H : d.P, G, ldG,
+                                        ncols_real, A, ldA, useH ? 1 : 0);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template void launch_synth<double>(const ShtDev<double>&, bool, const GemmPlan&, const double*, long, int, double*,
+                                   long, cudaStream_t);
+template void launch_synth<float>(const ShtDev<float>&, bool, const GemmPlan&, const float*, long, int, float*,
+                                  long, cudaStream_t);
+template void launch_anal<double>(const ShtDev<double>&, bool, const GemmPlan&, const double*, long, int, double*,
+                                  long, cudaStream_t);
+template void launch_anal<float>(const ShtDev<float>&, bool, const GemmPlan&, const float*, long, int, float*,
+                                 long, cudaStream_t);
+
+// -------------------------------------------------------------- FFTs ------
+// Real transforms of length nlon = 2M through one complex Stockham FFT of
+// length M per row, several rows per CTA, ping-pong buffers in shared memory.
+void fft_radix_plan(int M, int* nrad, int* rad) {
+  int n = 0, r = M;
+  while (r % 4 == 0) {
+    rad[n++] = 4;
+    r /= 4;
+  }
+  while (r % 2 == 0) {
+    rad[n++] = 2;
+    r /= 2;
+  }
+  while (r % 3 == 0) {
+    rad[n++] = 3;
+    r /= 3;
+  }
+  if (r != 1) throw std::runtime_error("nlon/2 must be 2^a 3^b");
+  *nrad = n;
+}
+
+template <typename R>
+__global__ void k_fft_tables(int M, typename C2<R>::T* twM, typename C2<R>::T* twN) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < M) {
+    double sn, cs;
+    sincospi(-2.0 * k / M, &sn, &cs);
+    twM[k] = mk2<R>((R)cs, (R)sn);
+  }
+  if (k <= M) {
+    double sn, cs;
+    sincospi(-1.0 * k / M, &sn, &cs);  // exp(-2 pi i k / (2M))
+    twN[k] = mk2<R>((R)cs, (R)sn);
+  }
+}
+template <typename R>
+void fft_init_tables(int nlon, typename C2<R>::T* twM, typename C2<R>::T* twN, cudaStream_t s) {
+  int M = nlon / 2;
+  k_fft_tables<R><<<ceil_div(M + 1, 128), 128, 0, s>>>(M, twM, twN);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template void fft_init_tables<double>(int, double2*, double2*, cudaStream_t);
+template void fft_init_tables<float>(int, float2*, float2*, cudaStream_t);
+
+template <typename V>
+__device__ __forceinline__ V cmul(V a, V b) {
+  V r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename V>
+__device__ __forceinline__ V cadd(V a, V b) {
+  a.x += b.x;
+  a.y += b.y;
+  return a;
+}
+template <typename V>
+__device__ __forceinline__ V csub(V a, V b) {
+  a.x -= b.x;
+  a.y -= b.y;
+  return a;
+}
+template <typename V>
+__device__ __forceinline__ V cconj(V a) {
+  a.y = -a.y;
+  return a;
+}
+
+// In-shared-memory Stockham FFT of nr rows of length M; sign -1 forward,
+// +1 inverse (unnormalised).  Returns the buffer holding the result.
+template <typename R>
+__device__ typename C2<R>::T* fft_rows(typename C2<R>::T* a, typename C2<R>::T* b, int M, int nr,
+                                       const typename C2<R>::T* __restrict__ tw, int nrad, const int* rad,
+                                       int sign) {
+  typedef typename C2<R>::T V;
+  int Ns = 1;
+  for (int st = 0; st < nrad; ++st) {
+    const int p = rad[st];
+    const int nb = M / p;
+    const int tstep = M / (Ns * p);
+    for (int e = threadIdx.x; e < nr * nb; e += blockDim.x) {
+      const int r = e / nb, jj = e - r * nb;
+      const V* in = a + (long)r * M;
+      V* out = b + (long)r * M;
+      const int k = jj % Ns;
+      V v[4];
+      for (int q = 0; q < p; ++q) {
+        V x = in[jj + q * nb];
+        if (q > 0 && k > 0) {
+          V w = tw[k * q * tstep];
+          if (sign > 0) w = cconj(w);
+          x = cmul(x, w);
+        }
+        v[q] = x;
+      }
+      if (p == 2) {
+        V t = v[0];
+        v[0] = cadd(t, v[1]);
+        v[1] = csub(t, v[1]);
+      } else if (p == 4) {
+        V s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+        V s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+        V id13;  // sign * i * d13
+        id13.x = -sign * d13.y;
+        id13.y = sign * d13.x;
+        v[0] = cadd(s02, s13);
+        v[2] = csub(s02, s13);
+        v[1] = cadd(d02, id13);
+        v[3] = csub(d02, id13);
+      } else {  // p == 3
+        const R c3 = R(-0.5), s3 = R(0.86602540378443864676) * R(sign);
+        V t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
+        V y0 = cadd(v[0], t1);
+        V m1;
+        m1.x = v[0].x + c3 * t1.x;
+        m1.y = v[0].y + c3 * t1.y;
+        V m2;  // i s3 t2
+        m2.x = -s3 * t2.y;
+        m2.y = s3 * t2.x;
+        v[0] = y0;
+        v[1] = cadd(m1, m2);
+        v[2] = csub(m1, m2);
+      }
+      const int od = (jj / Ns) * Ns * p + k;
+      for (int q = 0; q < p; ++q) out[od + q * Ns] = v[q];
+    }
+    __syncthreads();
+    V* t = a;
+    a = b;
+    b = t;
+    Ns *= p;
+  }
+  return a;
+}
+
+template <typename R>
+int fft_rows_per_cta() {
+  return sizeof(R) == 8 ? 8 : 16;
+}
+template int fft_rows_per_cta<double>();
+template int fft_rows_per_cta<float>();
+
+struct FftArgs {
+  int nrad;
+  int rad[12];
+};
+
+// Fourier -> grid for runs of rows described by SynthDesc.
+template <typename R>
+__global__ void __launch_bounds__(256) k_c2r(const int2* __restrict__ jobs, const SynthDesc* __restrict__ descs,
+                                             ShtDev<R> d, FftArgs fa, const R* __restrict__ FP, long ldP,
+                                             const R* __restrict__ FH, long ldH, R* __restrict__ grid) {
+  typedef typename C2<R>::T V;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int NR = sizeof(R) == 8 ? 8 : 16;
+  const int M = d.M, T = d.T, nlat = d.nlat, nlon = d.nlon;
+  V* b0 = reinterpret_cast<V*>(smraw);
+  V* b1 = b0 + (long)NR * M;
+  const int2 jb = jobs[blockIdx.x];
+  const SynthDesc ds = descs[jb.x];
+  const int j = blockIdx.y;
+  const int r0 = jb.y;
+  const int nr = min(NR, ds.count - r0);
+  const R rc = d.rcos[j];
+  const R alpha = (R)ds.alpha, beta = (R)ds.beta;
+  // gather X[r][k] = alpha A + beta (i k / cos) B, zero above T
+  for (int e = threadIdx.x; e < nr * M; e += blockDim.x) {
+    const int k = e / nr, r = e - k * nr;
+    V x = mk2<R>(R(0), R(0));
+    if (k <= T) {
+      if (ds.srcA >= 0) {
+        const R* src = ds.srcA == 0 ? FP : FH;
+        const long ld = ds.srcA == 0 ? ldP : ldH;
+        V a = *reinterpret_cast<const V*>(src + ((long)k * nlat + j) * ld + 2 * (ds.colA + r0 + r));
+        x.x = alpha * a.x;
+        x.y = alpha * a.y;
+      }
+      if (ds.srcB >= 0) {
+        const R* src = ds.srcB == 0 ? FP : FH;
+        const long ld = ds.srcB == 0 ? ldP : ldH;
+        V bb = *reinterpret_cast<const V*>(src + ((long)k * nlat + j) * ld + 2 * (ds.colB + r0 + r));
+        const R f = beta * (R)k * rc;  // i f bb
+        x.x -= f * bb.y;
+        x.y += f * bb.x;
+      }
+      if (k == 0) x.y = R(0);
+    }
+    b1[(long)r * M + k] = x;
+  }
+  __syncthreads();
+  // Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) exp(+2 pi i k / nlon)
+  for (int e = threadIdx.x; e < nr * M; e += blockDim.x) {
+    const int r = e / M, k = e - r * M;
+    V xk = b1[(long)r * M + k];
+    V xm = (k == 0) ? mk2<R>(R(0), R(0)) : cconj(b1[(long)r * M + (M - k)]);
+    V A = cadd(xk, xm), B = csub(xk, xm);
+    V w = cconj(d.twN[k]);
+    V Bw = cmul(B, w);
+    V z;
+    z.x = A.x - Bw.y;
+    z.y = A.y + Bw.x;
+    b0[(long)r * M + k] = z;
+  }
+  __syncthreads();
+  V* res = fft_rows<R>(b0, b1, M, nr, d.twM, fa.nrad, fa.rad, +1);
+  for (int e = threadIdx.x; e < nr * M; e += blockDim.x) {
+    const int r = e / M, n = e - r * M;
+    *reinterpret_cast<V*>(grid + ((long)(ds.dst + r0 + r) * nlat + j) * nlon + 2 * n) = res[(long)r * M + n];
+  }
+}
+
+// grid -> Fourier (scaled by the quadrature weight 2 pi w_j / nlon) for runs
+// of rows described by AnalDesc.
+template <typename R>
+__global__ void __launch_bounds__(256) k_r2c(const int2* __restrict__ jobs, const AnalDesc* __restrict__ descs,
+                                             ShtDev<R> d, FftArgs fa, const R* __restrict__ grid,
+                                             R* __restrict__ GP, long ldP, R* __restrict__ GH, long ldH) {
+  typedef typename C2<R>::T V;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int NR = sizeof(R) == 8 ? 8 : 16;
+  const int M = d.M, T = d.T, nlat = d.nlat, nlon = d.nlon;
+  V* b0 = reinterpret_cast<V*>(smraw);
+  V* b1 = b0 + (long)NR * M;
+  const int2 jb = jobs[blockIdx.x];
+  const AnalDesc ds = descs[jb.x];
+  const int j = blockIdx.y;
+  const int r0 = jb.y;
+  const int nr = min(NR, ds.count - r0);
+  for (int e = threadIdx.x; e < nr * M; e += blockDim.x) {
+    const int r = e / M, n = e - r * M;
+    b0[(long)r * M + n] = *reinterpret_cast<const V*>(grid + ((long)(ds.src + r0 + r) * nlat + j) * nlon + 2 * n);
+  }
+  __syncthreads();
+  V* Z = fft_rows<R>(b0, b1, M, nr, d.twM, fa.nrad, fa.rad, -1);
+  const R wn = d.wn[j], rc = d.rcos[j];
+  const R half = R(0.5);
+  for (int e = threadIdx.x; e < nr * (T + 1); e += blockDim.x) {
+    const int k = e / nr, r = e - k * nr;
+    V zk = Z[(long)r * M + k];
+    V zm = cconj(Z[(long)r * M + ((M - k) % M)]);
+    V E = cadd(zk, zm), O = csub(zk, zm);  // 2E, 2iO
+    // X = E + exp(-2 pi i k/nlon) O,  O = -i/2 (Z[k] - conj Z[M-k])
+    V Oi;
+    Oi.x = O.y;
+    Oi.y = -O.x;
+    V X = cadd(E, cmul(d.twN[k], Oi));
+    X.x *= half * wn;
+    X.y *= half * wn;
+    const int col = r0 + r;
+    if (ds.dstP >= 0) {
+      V y = X;
+      if (ds.imcosP) {
+        const R f = (R)k * rc;
+        y.x = -f * X.y;
+        y.y = f * X.x;
+      }
+      y.x *= (R)ds.scaleP;
+      y.y *= (R)ds.scaleP;
+      *reinterpret_cast<V*>(GP + ((long)k * nlat + j) * ldP + 2 * (ds.dstP + col)) = y;
+    }
+    if (ds.dstH >= 0) {
+      V y = X;
+      y.x *= (R)ds.scaleH;
+      y.y *= (R)ds.scaleH;
+      *reinterpret_cast<V*>(GH + ((long)k * nlat + j) * ldH + 2 * (ds.dstH + col)) = y;
+    }
+  }
+}
+
+template <typename R, typename D>
+static FftPlan make_plan(const D* descs, int ndesc, cudaStream_t s) {
+  const int NR = fft_rows_per_cta<R>();
+  std::vector<int2> jobs;
+  for (int i = 0; i < ndesc; ++i)
+    for (int r = 0; r < descs[i].count; r += NR) jobs.push_back(make_int2(i, r));
+  FftPlan p;
+  p.njobs = (int)jobs.size();
+  if (p.njobs == 0) return p;
+  GD_CUDA(cudaMalloc(&p.jobs, sizeof(int2) * jobs.size()));
+  GD_CUDA(cudaMalloc(&p.descs, sizeof(D) * ndesc));
+  GD_CUDA(cudaMemcpyAsync(p.jobs, jobs.data(), sizeof(int2) * jobs.size(), cudaMemcpyHostToDevice, s));
+  GD_CUDA(cudaMemcpyAsync(p.descs, descs, sizeof(D) * ndesc, cudaMemcpyHostToDevice, s));
+  GD_CUDA(cudaStreamSynchronize(s));
+  return p;
+}
+template <typename R>
+FftPlan make_c2r_plan(const SynthDesc* descs, int ndesc, cudaStream_t s) {
+  return make_plan<R>(descs, ndesc, s);
+}
+template <typename R>
+FftPlan make_r2c_plan(const AnalDesc* descs, int ndesc, cudaStream_t s) {
+  return make_plan<R>(descs, ndesc, s);
+}
+template FftPlan make_c2r_plan<double>(const SynthDesc*, int, cudaStream_t);
+template FftPlan make_c2r_plan<float>(const SynthDesc*, int, cudaStream_t);
+template FftPlan make_r2c_plan<double>(const AnalDesc*, int, cudaStream_t);
+template FftPlan make_r2c_plan<float>(const AnalDesc*, int, cudaStream_t);
+
+void free_fft_plan(FftPlan& p) {
+  if (p.jobs) cudaFree(p.jobs);
+  if (p.descs) cudaFree(p.descs);
+  p.jobs = nullptr;
+  p.descs = nullptr;
+  p.njobs = 0;
+}
+
+template <typename R>
+static size_t fft_smem(int M) {
+  return 2 * (size_t)fft_rows_per_cta<R>() * M * sizeof(typename C2<R>::T);
+}
+
+template <typename R>
+void launch_c2r(const ShtDev<R>& d, const FftPlan& plan, const R* FP, long ldP, const R* FH, long ldH, R* grid,
+                cudaStream_t s) {
+  if (plan.njobs == 0) return;
+  FftArgs fa;
+  fa.nrad = d.nrad;
+  for (int i = 0; i < 12; ++i) fa.rad[i] = d.rad[i];
+  size_t sm = fft_smem<R>(d.M);
+  static bool attr = false;
+  if (!attr) {
+    GD_CUDA(cudaFuncSetAttribute(k_c2r<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  dim3 grd(plan.njobs, d.nlat);
+  k_c2r<R><<<grd, 256, sm, s>>>(plan.jobs, (const SynthDesc*)plan.descs, d, fa, FP, ldP, FH, ldH, grid);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template <typename R>
+void launch_r2c(const ShtDev<R>& d, const FftPlan& plan, const R* grid, R* GP, long ldP, R* GH, long ldH,
+                cudaStream_t s) {
+  if (plan.njobs == 0) return;
+  FftArgs fa;
+  fa.nrad = d.nrad;
+  for (int i = 0; i < 12; ++i) fa.rad[i] = d.rad[i];
+  size_t sm = fft_smem<R>(d.M);
+  static bool attr = false;
+  if (!attr) {
+    GD_CUDA(cudaFuncSetAttribute(k_r2c<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  dim3 grd(plan.njobs, d.nlat);
+  k_r2c<R><<<grd, 256, sm, s>>>(plan.jobs, (const AnalDesc*)plan.descs, d, fa, grid, GP, ldP, GH, ldH);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template void launch_c2r<double>(const ShtDev<double>&, const FftPlan&, const double*, long, const double*, long,
+                                 double*, cudaStream_t);
+template void launch_c2r<float>(const ShtDev<float>&, const FftPlan&, const float*, long, const float*, long,
+                                float*, cudaStream_t);
+template void launch_r2c<double>(const ShtDev<double>&, const FftPlan&, const double*, double*, long, double*,
+                                 long, cudaStream_t);
+template void launch_r2c<float>(const ShtDev<float>&, const FftPlan&, const float*, float*, long, float*, long,
+                                cudaStream_t);
+
+}  // namespace gd

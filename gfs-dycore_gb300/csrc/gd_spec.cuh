@@ -1,0 +1,94 @@
+// gd_spec.cuh -- spectral-space kernels (declarations).
+#pragma once
+#include "gd_common.cuh"
+
+namespace gd {
+
+// Complex-column layout of the spectral state buffer S[nlm][ncol]:
+// vrt | div | tv | trc (ntrac*L) | s = a invlap vrt | c = a invlap div | lnps
+struct SpecCols {
+  int vrt, div, tv, trc, s, c, lnps, ncol;
+};
+// Per-stage tendency buffer TD[nlm][ncol]: nonlinear tendencies (after the
+// linear gravity-wave terms are removed) and the linear terms themselves.
+struct TendCols {
+  int dvrt, ddiv, dtv, dtrc, dlnps, ddl, dtl, dpl, ncol;
+};
+// Analysis outputs: AP = P^T-analysis columns, AH = dP/dphi^T-analysis.
+struct APCols {
+  int ttend, ke, qtend, dlnps, imfv, imfu, ncol;
+};
+struct AHCols {
+  int fu, mfv, ncol;
+};
+
+template <typename R>
+struct StageArgs {
+  int L, nt, T, stage, explicit_, final_;
+  const int4* items;  // (n, m0, count)
+  int nitems;
+  const long* moff;
+  R* S;
+  const R* S0;
+  long ldS;  // reals per spectral row
+  const R* AP;
+  long ldAP;
+  const R* AH;
+  long ldAH;
+  R* TD0;
+  R* TD1;
+  R* TD2;
+  long ldTD;
+  const R* amhyb;  // [L][L] row-major (row = output level)
+  const R* bmhyb;
+  const R* svhyb;  // [L]
+  const R* tor;    // [L]
+  const R* dhyb;   // [3][T+1][L][L]
+  const R* disspec;
+  const R* diff_prof;
+  const R* dmp_prof;
+  R dt, ainv, ainv2, rerth;
+  R ce[3], ci[3], cimp;
+  SpecCols sc;
+  TendCols tc;
+  APCols ap;
+  AHCols ah;
+};
+std::vector<int4> make_stage_items(int T, int qc);
+template <typename R>
+void launch_stage(const StageArgs<R>& a, cudaStream_t s);
+
+// Tendencies of getdyntend (no linear terms removed) into TD columns.
+template <typename R>
+void launch_assemble(const StageArgs<R>& a, R* TD, cudaStream_t s);
+
+// Physics adjustment (run.f90:526-538): state += dt * HS tendencies in AP
+// columns [0,L) tv, [L,2L) vrt, [2L,3L) div; lnps from the dry-mass fixer
+// analysis in AP column 3L (or unchanged); recomputes s, c.
+template <typename R>
+void launch_phys_update(R* S, long ldS, const SpecCols& sc, int L, int nt, int nlm, const R* AP, long ldAP,
+                        int massfix, int heldsuarez, R dt, const R* lapv, R rerth, cudaStream_t s);
+
+// s = a invlap vrt, c = a invlap div for all coefficients.
+template <typename R>
+void launch_sc(R* S, long ldS, const SpecCols& sc, int L, int nlm, const R* lapv, R rerth, cudaStream_t s);
+
+// Layout conversion: ref [nb][nlm] complex double <-> internal [nlm][ld] R.
+template <typename R>
+void launch_ref2int(const double* ref, int nb, int nlm, R* dst, long ld, int col0, cudaStream_t s);
+template <typename R>
+void launch_int2ref(const R* src, long ld, int col0, int nb, int nlm, double* ref, cudaStream_t s);
+// out[c] = scale * (X[c] + Y[c]) on [nlm][nb] complex columns
+template <typename R>
+void launch_combine(const R* X, long ldX, int cx, const R* Y, long ldY, int cy, R* O, long ldO, int co, int nb,
+                    int nlm, R scale, cudaStream_t s);
+// columns c0..c0+nb of X scaled by f[idx] * scale
+template <typename R>
+void launch_scale_cols(R* X, long ldX, int c0, int nb, int nlm, const R* f, R scale, cudaStream_t s);
+template <typename R>
+void launch_to_double(const R* src, double* dst, long n, cudaStream_t s);
+
+// FP64 batched inversion of nmat LxL row-major matrices (in place).
+void launch_batched_inverse(double* mats, int nmat, int L, cudaStream_t s);
+
+}  // namespace gd

@@ -1,0 +1,236 @@
+"""ctypes binding of libgdcore.so (include/gd_api.h).
+
+``Dycore`` mirrors the reference's dynamics interface -- init_dyn,
+getdyntend, getphytend, advance, finalize_dyn (src/dyn_init.f90,
+src/dyn_run.f90, src/phy_run_hs.f90, src/run.f90) -- and the shtns.f90
+transform facade, with the reference's array layouts:
+spectral ``complex128[nlev, nlm]`` and grid ``float64[nlev, nlat, nlon]``.
+
+Errors raise ``GdError`` carrying the library status and message; there is
+no fallback path: if the CUDA library cannot be loaded or the device cannot
+be initialised the call fails.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+GD_OK = 0
+GD_ERR_ARG = -1
+GD_ERR_CUDA = -2
+GD_ERR_STATE = -3
+GD_ERR_NOMEM = -4
+GD_ERR_UNSUPPORTED = -5
+GD_ERR_NUMERIC = -6
+
+PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3}
+
+API_FUNCTIONS = [
+    "gd_default_config", "gd_init", "gd_finalize", "gd_set_state", "gd_get_state",
+    "gd_getdyntend", "gd_getphytend", "gd_advance", "gd_spectogrd", "gd_grdtospec",
+    "gd_getuv", "gd_getvrtdivspec", "gd_getgrad", "gd_grid_info", "gd_get_grid", "gd_diag",
+    "gd_set_stream", "gd_sync", "gd_launch_count", "gd_last_error",
+]
+
+
+class GdConfig(ctypes.Structure):
+    _fields_ = [
+        ("ntrunc", ctypes.c_int), ("nlon", ctypes.c_int), ("nlat", ctypes.c_int),
+        ("nlev", ctypes.c_int), ("ntrac", ctypes.c_int), ("dt", ctypes.c_double),
+        ("precision", ctypes.c_int), ("explicit_", ctypes.c_int), ("adiabatic", ctypes.c_int),
+        ("heldsuarez", ctypes.c_int), ("massfix", ctypes.c_int), ("dry", ctypes.c_int),
+        ("ndiss", ctypes.c_int), ("efold", ctypes.c_double), ("hdif_fac", ctypes.c_double),
+        ("hdif_fac2", ctypes.c_double), ("fshk", ctypes.c_double),
+        ("taustratdamp", ctypes.c_double), ("pdryini", ctypes.c_double), ("device", ctypes.c_int),
+    ]
+
+
+class GdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gd error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(build_if_missing=True):
+    """Load the in-tree libgdcore.so (building it first if absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB):
+        if not build_if_missing:
+            raise OSError(f"{_build.LIB} is not built")
+        _build.build()
+    L = ctypes.CDLL(_build.LIB)
+    vp = ctypes.c_void_p
+    L.gd_init.argtypes = [ctypes.POINTER(GdConfig), vp, vp, ctypes.POINTER(vp)]
+    L.gd_finalize.argtypes = [vp]
+    L.gd_last_error.restype = ctypes.c_char_p
+    L.gd_last_error.argtypes = [vp]
+    L.gd_launch_count.restype = ctypes.c_longlong
+    L.gd_launch_count.argtypes = [vp]
+    L.gd_advance.argtypes = [vp, ctypes.c_double, ctypes.c_int]
+    L.gd_set_stream.argtypes = [vp, vp]
+    for f in ["gd_set_state", "gd_get_state", "gd_getdyntend", "gd_getphytend", "gd_spectogrd",
+              "gd_grdtospec", "gd_getuv", "gd_getvrtdivspec", "gd_getgrad", "gd_grid_info",
+              "gd_get_grid", "gd_diag", "gd_sync"]:
+        getattr(L, f).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def default_config(**kw):
+    c = GdConfig()
+    load().gd_default_config(ctypes.byref(c))
+    for k, v in kw.items():
+        if k == "precision" and isinstance(v, str):
+            v = PREC[v]
+        setattr(c, k, v)
+    return c
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Dycore:
+    """One device context (gd_ctx) of the GB300 spectral dycore."""
+
+    def __init__(self, ntrunc, nlon, nlat, nlev, ak, bk, ntrac=0, dt=1200.0, precision="fp64",
+                 explicit=False, adiabatic=False, heldsuarez=True, massfix=True, dry=True,
+                 device=0, **kw):
+        L = load()
+        self.cfg = default_config(ntrunc=ntrunc, nlon=nlon, nlat=nlat, nlev=nlev, ntrac=ntrac,
+                                  dt=dt, precision=precision, explicit_=int(explicit),
+                                  adiabatic=int(adiabatic), heldsuarez=int(heldsuarez),
+                                  massfix=int(massfix), dry=int(dry), device=device, **kw)
+        self.ak = np.ascontiguousarray(ak, np.float64)
+        self.bk = np.ascontiguousarray(bk, np.float64)
+        h = ctypes.c_void_p()
+        rc = L.gd_init(ctypes.byref(self.cfg), _p(self.ak), _p(self.bk), ctypes.byref(h))
+        if rc != GD_OK:
+            raise GdError(rc, L.gd_last_error(None).decode())
+        self.h = h
+        self.ntrunc, self.nlon, self.nlat, self.nlev, self.ntrac = ntrunc, nlon, nlat, nlev, ntrac
+        self.nlm = (ntrunc + 1) * (ntrunc + 2) // 2
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().gd_finalize(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        if rc != GD_OK:
+            raise GdError(rc, load().gd_last_error(self.h).decode())
+
+    # ---- state ----
+    def set_state(self, vrt, div, tv, lnps, trc=None, topo=None):
+        c = lambda a: None if a is None else np.ascontiguousarray(a, np.complex128)
+        arr = [c(x) for x in (vrt, div, tv, trc, lnps, topo)]
+        self._chk(load().gd_set_state(self.h, *[_p(x) for x in arr]))
+
+    def get_state(self):
+        L, n = self.nlev, self.nlm
+        vrt = np.zeros((L, n), np.complex128)
+        div = np.zeros_like(vrt)
+        tv = np.zeros_like(vrt)
+        trc = np.zeros((max(self.ntrac, 1), L, n), np.complex128)
+        lnps = np.zeros(n, np.complex128)
+        self._chk(load().gd_get_state(self.h, _p(vrt), _p(div), _p(tv), _p(trc), _p(lnps)))
+        return dict(vrt=vrt, div=div, tv=tv, trc=trc[: self.ntrac], lnps=lnps)
+
+    # ---- dynamics ----
+    def getdyntend(self, rkstage=1, inverse_only=False):
+        L, n = self.nlev, self.nlm
+        d = [np.zeros((L, n), np.complex128) for _ in range(3)]
+        dtrc = np.zeros((max(self.ntrac, 1), L, n), np.complex128)
+        dl = np.zeros(n, np.complex128)
+        self._chk(load().gd_getdyntend(self.h, rkstage, int(inverse_only), _p(d[0]), _p(d[1]),
+                                       _p(d[2]), _p(dtrc), _p(dl)))
+        return dict(dvrt=d[0], ddiv=d[1], dtv=d[2], dtrc=dtrc[: self.ntrac], dlnps=dl)
+
+    def getphytend(self):
+        L, n = self.nlev, self.nlm
+        d = [np.zeros((L, n), np.complex128) for _ in range(3)]
+        self._chk(load().gd_getphytend(self.h, _p(d[0]), _p(d[1]), _p(d[2]), None, None))
+        return dict(dvrt=d[0], ddiv=d[1], dtv=d[2])
+
+    def advance(self, nsteps=1, t=0.0):
+        self._chk(load().gd_advance(self.h, ctypes.c_double(t), int(nsteps)))
+
+    def sync(self):
+        self._chk(load().gd_sync(self.h))
+
+    def set_stream(self, stream_handle):
+        self._chk(load().gd_set_stream(self.h, ctypes.c_void_p(stream_handle)))
+
+    def launch_count(self):
+        return load().gd_launch_count(self.h)
+
+    # ---- transforms ----
+    def _g(self, nb):
+        return np.zeros((nb, self.nlat, self.nlon))
+
+    def spectogrd(self, spec):
+        spec = np.ascontiguousarray(np.atleast_2d(spec), np.complex128)
+        g = self._g(spec.shape[0])
+        self._chk(load().gd_spectogrd(self.h, spec.shape[0], _p(spec), _p(g)))
+        return g
+
+    def grdtospec(self, grid):
+        grid = np.ascontiguousarray(grid, np.float64).reshape(-1, self.nlat, self.nlon)
+        s = np.zeros((grid.shape[0], self.nlm), np.complex128)
+        self._chk(load().gd_grdtospec(self.h, grid.shape[0], _p(grid), _p(s)))
+        return s
+
+    def getuv(self, vrt, div):
+        vrt = np.ascontiguousarray(np.atleast_2d(vrt), np.complex128)
+        div = np.ascontiguousarray(np.atleast_2d(div), np.complex128)
+        u, v = self._g(vrt.shape[0]), self._g(vrt.shape[0])
+        self._chk(load().gd_getuv(self.h, vrt.shape[0], _p(vrt), _p(div), _p(u), _p(v)))
+        return u, v
+
+    def getvrtdivspec(self, u, v):
+        u = np.ascontiguousarray(u, np.float64).reshape(-1, self.nlat, self.nlon)
+        v = np.ascontiguousarray(v, np.float64).reshape(-1, self.nlat, self.nlon)
+        vrt = np.zeros((u.shape[0], self.nlm), np.complex128)
+        div = np.zeros_like(vrt)
+        self._chk(load().gd_getvrtdivspec(self.h, u.shape[0], _p(u), _p(v), _p(vrt), _p(div)))
+        return vrt, div
+
+    def getgrad(self, spec):
+        spec = np.ascontiguousarray(np.atleast_2d(spec), np.complex128)
+        gx, gy = self._g(spec.shape[0]), self._g(spec.shape[0])
+        self._chk(load().gd_getgrad(self.h, spec.shape[0], _p(spec), _p(gx), _p(gy)))
+        return gx, gy
+
+    def grid_info(self):
+        lats, gw, aw = np.zeros(self.nlat), np.zeros(self.nlat), np.zeros(self.nlat)
+        deg, order = np.zeros(self.nlm, np.int32), np.zeros(self.nlm, np.int32)
+        lap, ilap = np.zeros(self.nlm), np.zeros(self.nlm)
+        self._chk(load().gd_grid_info(self.h, _p(lats), _p(gw), _p(aw), _p(deg), _p(order),
+                                      _p(lap), _p(ilap)))
+        return dict(lats=lats, gauwts=gw, areawts=aw, degree=deg, order=order, lap=lap, invlap=ilap)
+
+    def get_grid(self, name):
+        L = self.nlev
+        rows = dict(ug=L, vg=L, vrtg=L, divg=L, tvg=L, dlnpdtg=L, prs=L, etadot=L + 1,
+                    trcg=max(self.ntrac, 1) * L, lnpsg=1, psg=1, dlnpsdt=1, dphisdx=1, dphisdy=1)
+        out = np.zeros((rows[name], self.nlat, self.nlon))
+        self._chk(load().gd_get_grid(self.h, name.encode(), _p(out)))
+        return out
+
+    def diag(self):
+        o = np.zeros(5)
+        self._chk(load().gd_diag(self.h, _p(o)))
+        return dict(spdmax=o[0], psmin=o[1], psmax=o[2], pstend=o[3], pdryini=o[4])

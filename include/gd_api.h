@@ -1,0 +1,153 @@
+/*
+ * gd_api.h -- C ABI of the GB300 (sm_103a) GFS spectral dycore step.
+ *
+ * Drop-in boundary for the time-step path of jswhit/gfs-dycore: the Fortran
+ * host keeps init_dyn / getdyntend / advance / finalize_dyn and the shtns
+ * transform facade, and binds these entry points through ISO_C_BINDING.
+ *
+ * Conventions
+ *  - Every function returns an int status: GD_OK (0) or a negative GD_ERR_*.
+ *    Nothing aborts; gd_last_error() describes the last failure.
+ *  - Host arrays are caller-owned, read or written only during the call,
+ *    in the reference layouts:
+ *      spectral  double _Complex [nlev][nlm]  == Fortran complex(ndimspec,nlevs)
+ *                (interleaved re,im doubles; m-major triangular order,
+ *                 src/shtns.f90:149-150)
+ *      grid      double [nlev][nlat][nlon]     == Fortran real(nlons,nlats,nlevs)
+ *                (latitudes north to south, 3-D fields bottom to top,
+ *                 src/grid_data.f90:14)
+ *      tracers   double _Complex [ntrac][nlev][nlm]
+ *  - Spectral harmonics are orthonormal without Condon-Shortley phase
+ *    (src/shtns.f90:110); m > 0 coefficients stand for the (+m,-m) pair of a
+ *    real field.
+ *  - One context = one device state and one CUDA stream.  Calls on one
+ *    context must be serialised by the caller (src/dyn_run.f90 calls the
+ *    transforms from OpenMP threads; such callers use one context per
+ *    thread or a lock).
+ */
+#ifndef GD_API_H
+#define GD_API_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GD_OK 0
+#define GD_ERR_ARG (-1)         /* bad argument, shape or null pointer      */
+#define GD_ERR_CUDA (-2)        /* CUDA runtime error (message has detail)  */
+#define GD_ERR_STATE (-3)       /* call out of order (e.g. no state set)    */
+#define GD_ERR_NOMEM (-4)       /* device allocation failed                 */
+#define GD_ERR_UNSUPPORTED (-5) /* configuration not supported              */
+#define GD_ERR_NUMERIC (-6)     /* non-finite value detected in the state   */
+
+/* Arithmetic of the transforms and the state. */
+#define GD_PREC_FP64 0        /* everything FP64 (reference with default_real=2) */
+#define GD_PREC_FP32 1        /* FP32 state and SIMT FP32 Legendre GEMMs          */
+#define GD_PREC_TF32X3 2      /* FP32 state, Legendre as TF32x3 tcgen05 products  */
+#define GD_PREC_BF16X3 3      /* FP32 state, Legendre as BF16x3 tcgen05 products  */
+
+typedef struct gd_config {
+  int ntrunc;          /* triangular truncation T (params.f90 ntrunc)       */
+  int nlon, nlat;      /* Gaussian grid; nlon = 2^a 3^b, nlat even          */
+  int nlev;            /* levels (>= 3)                                     */
+  int ntrac;           /* tracers; tracer 1 is humidity in the energy term  */
+  double dt;           /* time step in seconds (params.f90 dt)              */
+  int precision;       /* GD_PREC_*                                         */
+  int explicit_;       /* params.f90 explicit (0 = semi-implicit IMEX RK3)  */
+  int adiabatic;       /* params.f90 adiabatic (1 = no physics)             */
+  int heldsuarez;      /* Held-Suarez physics plugin (phy_run_hs.f90)       */
+  int massfix;         /* params.f90 massfix (dry-mass fixer)               */
+  int dry;             /* params.f90 dry                                    */
+  int ndiss;           /* params.f90 ndiss (0 -> 8)                         */
+  double efold;        /* params.f90 efold (<= 0 -> GFS default)            */
+  double hdif_fac, hdif_fac2, fshk, taustratdamp; /* params.f90:76-86      */
+  double pdryini;      /* 0 -> set on the first stage-1 call               */
+  int device;          /* CUDA device ordinal                               */
+} gd_config;
+
+typedef struct gd_ctx gd_ctx;
+
+/* Fills the reference's namelist defaults (src/params.f90:39-86) for a
+   T42 128x64 L20 Held-Suarez run. */
+int gd_default_config(gd_config* cfg);
+
+/* Replaces init_dyn (src/dyn_init.f90:37-91) and shtns_init
+   (src/shtns.f90:90-156): Gaussian grid, Legendre tables, damping
+   (setdampspec, dyn_init.f90:450-494) and semi-implicit inverses
+   (init_semimpdata, semimp_data.f90:127-256), all computed on the GPU in
+   FP64.  ak, bk: nlev+1 interface coefficients, top to bottom
+   (dyn_init.f90:52-56). */
+int gd_init(const gd_config* cfg, const double* ak, const double* bk, gd_ctx** ctx);
+
+/* Replaces finalize_dyn (src/dyn_finalize.f90:19-28). */
+int gd_finalize(gd_ctx* ctx);
+
+/* Sets / reads the prognostic spectral state (spectral_data.f90:11-21).
+   trc may be NULL when ntrac = 0; topo may be NULL (flat orography).
+   gd_set_state also derives phis and its gradient (dyn_init.f90:76-84). */
+int gd_set_state(gd_ctx* ctx, const double* vrt, const double* div, const double* tv,
+                 const double* trc, const double* lnps, const double* topo);
+int gd_get_state(gd_ctx* ctx, double* vrt, double* div, double* tv, double* trc,
+                 double* lnps);
+
+/* Replaces getdyntend (src/dyn_run.f90:33-305) on the current state.
+   inverse_only != 0 is the just_do_inverse_transform form (grid fields,
+   pressure data and getomega only; no tendencies are written). */
+int gd_getdyntend(gd_ctx* ctx, int rkstage, int inverse_only, double* dvrt, double* ddiv,
+                  double* dtv, double* dtrc, double* dlnps);
+
+/* Replaces the physics plugin contract getphytend(dvrtspecdt, ddivspecdt,
+   dvirtempspecdt, dtracerspecdt, dlnpsspecdt, t, dt) for the Held-Suarez
+   forcing (src/phy_run_hs.f90:22-84), evaluated on the grid fields of the
+   last gd_getdyntend call.  dtrc (may be NULL) is set to 0. */
+int gd_getphytend(gd_ctx* ctx, double* dvrt, double* ddiv, double* dtv, double* dtrc,
+                  double* dlnps);
+
+/* Replaces nsteps calls of advance(t) (src/run.f90:194-565): IMEX RK3 with
+   the semi-implicit solve, implicit hyperdiffusion, time-split Held-Suarez
+   physics and the dry-mass fixer.  Runs asynchronously on the context
+   stream; the state stays on the device. */
+int gd_advance(gd_ctx* ctx, double t, int nsteps);
+
+/* Transform facade of src/shtns.f90, batched over nb 2-D fields
+   (spectral [nb][nlm], grid [nb][nlat][nlon]); rsphere = 6.3712e6 m.
+   gd_spectogrd    <- spectogrd     (shtns.f90:203-231)
+   gd_grdtospec    <- grdtospec     (shtns.f90:171-201)
+   gd_getuv        <- getuv         (shtns.f90:233-273)
+   gd_getvrtdivspec<- getvrtdivspec (shtns.f90:275-311)
+   gd_getgrad      <- getgrad       (shtns.f90:313-352) */
+int gd_spectogrd(gd_ctx* ctx, int nb, const double* spec, double* grid);
+int gd_grdtospec(gd_ctx* ctx, int nb, const double* grid, double* spec);
+int gd_getuv(gd_ctx* ctx, int nb, const double* vrt, const double* div, double* u, double* v);
+int gd_getvrtdivspec(gd_ctx* ctx, int nb, const double* u, const double* v, double* vrt,
+                     double* div);
+int gd_getgrad(gd_ctx* ctx, int nb, const double* spec, double* gx, double* gy);
+
+/* Module data of src/shtns.f90:58-60: lats (radians, nlat), gauwts (nlat),
+   areawts per latitude (nlat; sum over the grid is 1), degree, order (nlm),
+   lap, invlap (nlm).  Any pointer may be NULL. */
+int gd_grid_info(gd_ctx* ctx, double* lats, double* gauwts, double* areawts, int* degree,
+                 int* order, double* lap, double* invlap);
+
+/* Grid fields of the last getdyntend: "ug" "vg" "vrtg" "divg" "tvg" "trcg"
+   "dlnpdtg" "etadot" "lnpsg" "psg" "dlnpsdt" "prs" "dphisdx" "dphisdy". */
+int gd_get_grid(gd_ctx* ctx, const char* name, double* out);
+
+/* Step diagnostics of src/run.f90:159-161 after the last step:
+   out[0] spdmax (m/s), out[1] min ps (hPa), out[2] max ps (hPa),
+   out[3] ps tendency RMS (hPa/hr), out[4] pdryini (Pa). */
+int gd_diag(gd_ctx* ctx, double* out5);
+
+/* Runs the context on an external CUDA stream (cudaStream_t as void*). */
+int gd_set_stream(gd_ctx* ctx, void* stream);
+/* Waits for all work of the context. */
+int gd_sync(gd_ctx* ctx);
+/* Number of GPU kernel launches issued by the context so far. */
+long long gd_launch_count(gd_ctx* ctx);
+/* Text of the last error on ctx (or of the last failed gd_init if NULL). */
+const char* gd_last_error(gd_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GD_API_H */

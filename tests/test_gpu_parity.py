@@ -1,0 +1,182 @@
+"""GPU parity: the CUDA library (through its C ABI) against the FP64 CPU
+oracle on identical seeded inputs.
+
+FP64 tolerance: 1e-12 relative (max-norm) for single transforms, 1e-11 for
+tendencies and one step, 1e-9 for a one-day trajectory (72 steps).  FP32
+mode: 2e-5 relative for transforms, 1e-3 for tendencies.
+"""
+import numpy as np
+import pytest
+
+from gdpy import core, inputs
+from helpers import rand_spec, rel
+
+pytestmark = pytest.mark.gpu
+
+GRIDS = {21: (64, 32), 42: (128, 64), 62: (192, 94), 126: (384, 190)}
+
+
+def pair(oracle_mod, T, nlev, ntrac=0, precision="fp64", dt=1200.0, **kw):
+    nlon, nlat = GRIDS[T]
+    ak, bk = inputs.hybrid_coords(nlev)
+    g = core.Dycore(T, nlon, nlat, nlev, ak, bk, ntrac=ntrac, dt=dt, precision=precision, **kw)
+    o = oracle_mod.Oracle(T, nlon, nlat, nlev, ak, bk, ntrac=ntrac, dt=dt, **kw)
+    return g, o
+
+
+def set_both(g, o, st):
+    trc = st["trc"] if len(st["trc"]) else None
+    g.set_state(st["vrt"], st["div"], st["tv"], st["lnps"], trc=trc)
+    o.set_state(st["vrt"], st["div"], st["tv"], st["lnps"], trc=trc)
+
+
+@pytest.mark.parametrize("T", [21, 42, 126])
+def test_grid_info(oracle_mod, T):
+    g, o = pair(oracle_mod, T, 4)
+    a, b = g.grid_info(), o.grid_info()
+    for k in ("lats", "gauwts", "areawts", "lap", "invlap"):
+        assert rel(a[k], b[k]) < 1e-14, k
+    np.testing.assert_array_equal(a["degree"], b["degree"])
+    np.testing.assert_array_equal(a["order"], b["order"])
+
+
+@pytest.mark.parametrize("T", [21, 42, 62, 126])
+def test_transforms_fp64(oracle_mod, T):
+    g, o = pair(oracle_mod, T, 4)
+    a = rand_spec(T, 5, seed=T)
+    b = rand_spec(T, 5, seed=T + 1)
+    assert rel(g.spectogrd(a), o.spectogrd(a)) < 1e-12
+    grid = o.spectogrd(a)
+    assert rel(g.grdtospec(grid), o.grdtospec(grid)) < 1e-12
+    ug, vg = g.getuv(a, b)
+    uo, vo = o.getuv(a, b)
+    assert rel(ug, uo) < 1e-12 and rel(vg, vo) < 1e-12
+    vr, dv = g.getvrtdivspec(uo, vo)
+    vro, dvo = o.getvrtdivspec(uo, vo)
+    assert rel(vr, vro) < 1e-12 and rel(dv, dvo) < 1e-12
+    gx, gy = g.getgrad(a)
+    ox, oy = o.getgrad(a)
+    assert rel(gx, ox) < 1e-12 and rel(gy, oy) < 1e-12
+
+
+def test_transform_edge_cases(oracle_mod):
+    g, o = pair(oracle_mod, 21, 4)
+    z = np.zeros((1, g.nlm), np.complex128)
+    assert np.abs(g.spectogrd(z)).max() == 0
+    assert g.spectogrd(np.zeros((0, g.nlm), np.complex128)).shape == (0, 32, 64)
+    # many fields at once (chunked through the work buffers)
+    a = rand_spec(21, 37, seed=3)
+    assert rel(g.spectogrd(a), o.spectogrd(a)) < 1e-12
+    # round trip of a band-limited field
+    assert rel(g.grdtospec(g.spectogrd(a)), a) < 1e-12
+
+
+def test_transforms_fp32(oracle_mod):
+    g, o = pair(oracle_mod, 42, 4, precision="fp32")
+    a = rand_spec(42, 3, seed=9, slope=-1.0)
+    assert rel(g.spectogrd(a), o.spectogrd(a)) < 2e-5
+    u, v = o.getuv(a, a)
+    vr, dv = g.getvrtdivspec(u, v)
+    vro, dvo = o.getvrtdivspec(u, v)
+    assert rel(vr, vro) < 2e-5 and rel(dv, dvo) < 2e-5
+
+
+def check_tend(a, b, tol):
+    for k in ("dvrt", "ddiv", "dtv", "dlnps"):
+        assert rel(a[k], b[k]) < tol, (k, rel(a[k], b[k]))
+    if b["dtrc"].size:
+        assert rel(a["dtrc"], b["dtrc"]) < tol, ("dtrc", rel(a["dtrc"], b["dtrc"]))
+
+
+def test_getdyntend_hs_noise_fp64(oracle_mod):
+    g, o = pair(oracle_mod, 42, 20)
+    set_both(g, o, inputs.hs_rest_state(42, 20, seed=3))
+    check_tend(g.getdyntend(1), o.getdyntend(1), 1e-11)
+    for name in ("ug", "vg", "vrtg", "divg", "tvg", "psg", "dlnpsdt", "dlnpdtg", "etadot"):
+        assert rel(g.get_grid(name), o.get_grid(name)) < 1e-11, name
+
+
+def test_getdyntend_tracers_fp64(oracle_mod):
+    T, L = 21, 8
+    g, o = pair(oracle_mod, T, L, ntrac=3)
+    st = inputs.smooth_random_state(T, L, ntrac=3, seed=5)
+    set_both(g, o, st)
+    check_tend(g.getdyntend(1), o.getdyntend(1), 1e-11)
+
+
+def test_getdyntend_inverse_only_and_phytend(oracle_mod):
+    g, o = pair(oracle_mod, 42, 20)
+    set_both(g, o, inputs.hs_rest_state(42, 20, seed=4))
+    g.getdyntend(3, inverse_only=True)
+    o.getdyntend(3, inverse_only=True)
+    for name in ("ug", "vg", "psg", "prs", "dlnpsdt"):
+        assert rel(g.get_grid(name), o.get_grid(name)) < 1e-11, name
+    a, b = g.getphytend(), o.getphytend()
+    for k in ("dvrt", "ddiv", "dtv"):
+        assert rel(a[k], b[k]) < 1e-11, k
+
+
+@pytest.mark.parametrize("explicit", [False, True])
+def test_one_step_fp64(oracle_mod, explicit):
+    g, o = pair(oracle_mod, 42, 20, dt=600.0 if explicit else 1200.0, explicit=explicit)
+    set_both(g, o, inputs.hs_rest_state(42, 20, seed=11))
+    g.advance(1)
+    o.advance(1)
+    a, b = g.get_state(), o.get_state()
+    for k in ("vrt", "div", "tv", "lnps"):
+        assert rel(a[k], b[k]) < 1e-11, (k, rel(a[k], b[k]))
+    da, db = g.diag(), o.diag()
+    for k in da:
+        assert abs(da[k] - db[k]) <= 1e-10 * max(1.0, abs(db[k])), k
+
+
+def test_steps_with_tracers_fp64(oracle_mod):
+    T, L = 21, 8
+    g, o = pair(oracle_mod, T, L, ntrac=3, dt=900.0)
+    set_both(g, o, inputs.smooth_random_state(T, L, ntrac=3, seed=8))
+    g.advance(3)
+    o.advance(3)
+    a, b = g.get_state(), o.get_state()
+    for k in ("vrt", "div", "tv", "lnps", "trc"):
+        assert rel(a[k], b[k]) < 1e-10, (k, rel(a[k], b[k]))
+
+
+def test_one_day_trajectory_t42l20(oracle_mod):
+    g, o = pair(oracle_mod, 42, 20)
+    set_both(g, o, inputs.hs_rest_state(42, 20, seed=0))
+    g.advance(72)
+    o.advance(72)
+    a, b = g.get_state(), o.get_state()
+    for k in ("vrt", "div", "tv", "lnps"):
+        assert rel(a[k], b[k]) < 1e-9, (k, rel(a[k], b[k]))
+
+
+def test_step_fp32_close_to_fp64(oracle_mod):
+    g, o = pair(oracle_mod, 42, 20, precision="fp32")
+    set_both(g, o, inputs.hs_rest_state(42, 20, seed=2))
+    g.advance(2)
+    o.advance(2)
+    a, b = g.get_state(), o.get_state()
+    assert rel(a["tv"], b["tv"]) < 1e-5
+    assert rel(a["vrt"], b["vrt"]) < 1e-3
+    assert rel(a["lnps"], b["lnps"]) < 1e-5
+
+
+def test_launch_count_and_graph_replay(oracle_mod):
+    g, o = pair(oracle_mod, 21, 8)
+    set_both(g, o, inputs.hs_rest_state(21, 8, seed=1))
+    n0 = g.launch_count()
+    g.advance(4)  # first step eager, then one captured graph replayed
+    g.sync()
+    assert g.launch_count() > n0
+    o.advance(4)
+    assert rel(g.get_state()["vrt"], o.get_state()["vrt"]) < 1e-10
+
+
+def test_errors_are_reported_not_raised_by_device(oracle_mod):
+    g, _ = pair(oracle_mod, 21, 4)
+    with pytest.raises(core.GdError) as e:
+        g.advance(1)  # no state set yet
+    assert e.value.code == core.GD_ERR_STATE
+    with pytest.raises(core.GdError):
+        g.getdyntend(4)

@@ -1,0 +1,355 @@
+#!/usr/bin/env python3
+"""Benchmark of the GFS spectral dycore time step on GB300.
+
+Metric: simulated days per wall-clock day at T574L64 (1152x576 Gaussian
+grid, 64 levels, 7 prognostic 3-D fields = vrt, div, Tv + 4 tracers,
+dt = 150 s), balanced-jet initial state, Held-Suarez forcing.  ``value`` is
+the fast-precision GPU step with the state resident in HBM; the plain FP64
+GPU step is measured in the same run (``fp64_days_per_day``) together with
+the relative error of the fast step against it after the timed steps.
+
+``e2e`` times the same step through the C ABI with the state copied in from
+pinned host memory and out again every step (gd_set_state / gd_advance /
+gd_get_state).  ``--impl reference`` times the FP64 CPU restatement of the
+reference algorithm (the reference's Fortran + SHTns build cannot be made
+here) on the host cores.
+
+Multi-GPU: replicas only (independent members, one per rank, no exchange);
+``value`` is the aggregate member-days per day.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "gfs-dycore_gb300"))
+
+WORKLOADS = {
+    # name: (T, nlon, nlat, nlev, ntrac, dt)
+    "T574L64": (574, 1152, 576, 64, 4, 150.0),
+    "T126L64": (126, 384, 190, 64, 3, 600.0),
+    "T42L20": (42, 128, 64, 20, 0, 1200.0),
+}
+METRIC = "simulated days/day at T574L64: mixed-precision vs FP64 GPU at stated error"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return dict(hbm=d["hbm_gbs"], bf16=d["bf16_tflops"], bf16s=d["bf16_tflops_sustained"], src="measured")
+    return dict(hbm=6800.0, bf16=1900.0, bf16s=1700.0, src="fallback")
+
+
+def make_state(name, seed):
+    from gdpy import inputs
+
+    T, nlon, nlat, L, nt, dt = WORKLOADS[name]
+    if name == "T574L64":
+        return inputs.balanced_jet_state(T, nlat, L, seed=seed, ntrac=nt)
+    if name == "T126L64":
+        return inputs.smooth_random_state(T, L, ntrac=nt, seed=seed)
+    return inputs.hs_rest_state(T, L, seed=seed)
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.device = device
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+        self.f.flush()
+
+    def summary(self):
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return dict(sm_mhz=None, sm_max_mhz=None, reasons=["unavailable"], samples=0)
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return dict(sm_mhz=statistics.median(sm) if sm else None,
+                    sm_max_mhz=float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                    reasons=reasons, samples=len(rows))
+
+
+def work_counts(T, nlon, nlat, L, nt, rsize):
+    """Algorithmic work of one step of this implementation, per phase.
+
+    Legendre: 2*nlm*nlat flop per transformed complex column (a scalar
+    transform; 4 flop per complex x real multiply-add over nlat/2 latitude
+    pairs).  FFT/grid phases: bytes each row must move once.
+    """
+    nlm = (T + 1) * (T + 2) // 2
+    ncolS = (5 + nt) * L + 1
+    synth_cols = ncolS + (ncolS - 2 * L)
+    anal_cols = ((4 + nt) * L + 1) + 2 * L
+    cols = 3 * (synth_cols + anal_cols) + synth_cols + (3 * L + 1)
+    scalar_flop = 2.0 * nlm * nlat
+    ng = nlon * nlat
+    cbytes = 2 * rsize
+    c2r_rows = (7 + 3 * nt) * L + 3
+    inv_rows = 5 * L + 3 + nt * L
+    two_src = 2 * L + 0  # u, v read two Fourier columns
+    c2r_bytes = 3 * (c2r_rows * ng * rsize + (c2r_rows + two_src) * (T + 1) * nlat * cbytes) + \
+        (inv_rows * ng * rsize + (inv_rows + two_src) * (T + 1) * nlat * cbytes)
+    r2c_rows = (4 + nt) * L + 1
+    r2c_bytes = 3 * (r2c_rows * ng * rsize + (r2c_rows + 2 * L) * (T + 1) * nlat * cbytes) + \
+        ((3 * L + 1) * ng * rsize + (3 * L + 1) * (T + 1) * nlat * cbytes)
+    col_in = (7 + 3 * nt) * L + 3
+    col_bytes = 3 * (col_in + r2c_rows) * ng * rsize + (5 * L + 3) * ng * rsize
+    return dict(legendre_flop=cols * scalar_flop, legendre_cols=cols, c2r_bytes=c2r_bytes, r2c_bytes=r2c_bytes,
+                col_bytes=col_bytes, scalar_flop=scalar_flop)
+
+
+def gpu_arm(args):
+    import torch
+
+    from gdpy import core, inputs
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    name = args.workload
+    T, nlon, nlat, L, nt, dt = WORKLOADS[name]
+    ak, bk = inputs.hybrid_coords(L)
+    st = make_state(name, seed=rank)
+    trc = st["trc"] if nt else None
+    stream = torch.cuda.current_stream()
+
+    def ctx(prec):
+        g = core.Dycore(T, nlon, nlat, L, ak, bk, ntrac=nt, dt=dt, precision=prec, device=local)
+        g.set_stream(stream.cuda_stream)
+        g.set_state(st["vrt"], st["div"], st["tv"], st["lnps"], trc=trc)
+        return g
+
+    def barrier():
+        if dist:
+            tdist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(g, steps, warmup):
+        g.advance(warmup)
+        barrier()
+        n0 = g.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with Clocks(local) as ck:
+            e0.record(stream)
+            g.advance(steps)
+            e1.record(stream)
+            barrier()
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, g.launch_count() - n0, ck.summary()
+
+    # fast-precision step (the headline)
+    g = ctx(args.precision)
+    ms, launches, clocks = timed(g, args.steps, args.warmup)
+    ms_step = ms / args.steps
+    dpd = dt * 1e3 / ms_step  # simulated seconds per wall second == simulated days per day
+    value = dpd * world
+    phases = g.profile_step()
+    fast_state = g.get_state()
+    steps_done = args.warmup + args.steps + 1
+
+    # plain FP64 step, same initial state, for the ratio and the error
+    fp64 = None
+    if args.fp64_steps > 0 and args.precision != "fp64":
+        g64 = ctx("fp64")
+        ms64, _, _ = timed(g64, args.fp64_steps, 1)
+        dpd64 = (86400.0 * 1e3 / (ms64 / args.fp64_steps)) * dt / 86400.0
+        # bring FP64 to the same step count as the fast run, then compare
+        g64.advance(steps_done - (1 + args.fp64_steps))
+        ref = g64.get_state()
+        err = {k: float(np.abs(fast_state[k] - ref[k]).max() / max(np.abs(ref[k]).max(), 1e-300))
+               for k in ("vrt", "div", "tv", "lnps")}
+        if nt:
+            err["trc"] = float(np.abs(fast_state["trc"] - ref["trc"]).max() / np.abs(ref["trc"]).max())
+        fp64 = dict(days_per_day=dpd64 * world, ms_per_step=ms64 / args.fp64_steps, rel_err=err,
+                    steps_compared=steps_done)
+        g64.close()
+
+    # end to end through the C ABI with host buffers
+    pinned = {}
+    for k in ("vrt", "div", "tv", "lnps") + (("trc",) if nt else ()):
+        t = torch.empty(st[k].shape + (2,), dtype=torch.float64, pin_memory=True)
+        a = t.numpy().view(np.complex128).reshape(st[k].shape)
+        a[...] = st[k]
+        pinned[k] = a
+    lib = core.load()
+    import ctypes
+
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    h2d = sum(a.nbytes for a in pinned.values())
+    for _ in range(2):
+        g.set_state(pinned["vrt"], pinned["div"], pinned["tv"], pinned["lnps"], trc=pinned.get("trc"))
+        g.advance(1)
+    barrier()
+    e2e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        g._chk(lib.gd_set_state(g.h, P(pinned["vrt"]), P(pinned["div"]), P(pinned["tv"]),
+                                P(pinned["trc"]) if nt else None, P(pinned["lnps"]), None))
+        g.advance(1)
+        g._chk(lib.gd_get_state(g.h, P(pinned["vrt"]), P(pinned["div"]), P(pinned["tv"]),
+                                P(pinned["trc"]) if nt else None, P(pinned["lnps"])))
+    barrier()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = dict(value=(86400.0 * 1e3 / e2e_ms) * dt / 86400.0 * world, unit="simulated days/day",
+               h2d_bytes_per_step=h2d, d2h_bytes_per_step=h2d, ms_per_step=e2e_ms)
+
+    # roofline of the dominant phase
+    pk = peaks()
+    rsize = 8 if args.precision == "fp64" else 4
+    wc = work_counts(T, nlon, nlat, L, nt, rsize)
+    dom = max(phases, key=phases.get)
+    leg_ms = phases["legendre_synth"] + phases["legendre_anal"]
+    if dom in ("legendre_synth", "legendre_anal") or leg_ms >= max(phases.values()):
+        achieved = wc["legendre_flop"] / (leg_ms * 1e-3) / 1e12
+        roof = dict(kernel="legendre GEMMs (synthesis+analysis)", bound="tensor", achieved=achieved,
+                    peak=pk["bf16"], unit="TFLOP/s", frac=achieved / pk["bf16"], traffic=None,
+                    peak_source=pk["src"] + " bf16 burst",
+                    note="SIMT FMA path; tensor peak shown for scale" if args.precision in ("fp32", "fp64") else "")
+    else:
+        key = {"fft_synth": "c2r_bytes", "fft_anal": "r2c_bytes", "columns": "col_bytes"}.get(dom)
+        byt = wc[key] if key else None
+        achieved = byt / (phases[dom] * 1e-3) / 1e9 if byt else None
+        roof = dict(kernel=dom, bound="hbm", achieved=achieved, peak=pk["hbm"], unit="GB/s",
+                    frac=(achieved / pk["hbm"]) if achieved else None, traffic=None, peak_source=pk["src"])
+    out = {
+        "metric": METRIC, "value": value, "unit": "simulated days/day", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64", "fp32": "f32", "tf32x3": "f32+tf32x3",
+                                                         "bf16x3": "f32+bf16x3"}[args.precision],
+        "data": "synthetic (seeded balanced jet, Held-Suarez forcing)",
+        "config": {"workload": name, "ntrunc": T, "grid": f"{nlon}x{nlat}", "nlev": L, "ntrac": nt, "dt_s": dt,
+                   "precision": args.precision, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (resident state and grids are GBs)"},
+        "fp64": fp64, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
+        "phases_ms": phases, "clocks": clocks,
+    }
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(name, args.cpu_levels)
+        print(json.dumps(out))
+    g.close()
+    if dist:
+        tdist.destroy_process_group()
+
+
+def cpu_baseline(name, levels, nthreads=None):
+    """FP64 CPU restatement of the reference step on the host cores, timed
+    on a bounded sample: one step of the full horizontal grid with
+    ``levels`` of the workload's levels, scaled linearly to all levels."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    from gdpy import inputs
+
+    T, nlon, nlat, L, nt, dt = WORKLOADS[name]
+    Ls = min(levels, L)
+    nthreads = nthreads or os.cpu_count()
+    ak, bk = inputs.hybrid_coords(Ls)
+    st = make_state(name, seed=0) if Ls == L else None
+    if st is None:
+        full = make_state(name, seed=0)
+        st = {k: (v[:Ls] if k in ("vrt", "div", "tv") else (v[:, :Ls] if k == "trc" else v)) for k, v in full.items()}
+    o = oracle_py.Oracle(T, nlon, nlat, Ls, ak, bk, ntrac=nt, dt=dt, nthreads=nthreads)
+    o.set_state(st["vrt"], st["div"], st["tv"], st["lnps"], trc=st["trc"] if nt else None)
+    t0 = time.perf_counter()
+    o.advance(1)
+    sec = (time.perf_counter() - t0) * (L / Ls)
+    return dict(value=86400.0 / sec * dt / 86400.0, unit="simulated days/day", cores=nthreads, kind="port",
+                sample=f"1 step of {name} with {Ls} of {L} levels on {nthreads} threads, time scaled x{L / Ls:g}",
+                seconds_per_step=sec)
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    T, nlon, nlat, L, nt, dt = WORKLOADS[args.workload]
+    times = []
+    for _ in range(args.warmup + args.steps):
+        times.append(cpu_baseline(args.workload, args.cpu_levels))
+    vals = [t["value"] for t in times[args.warmup:]] or [times[-1]["value"]]
+    v = statistics.median(vals)
+    cb = dict(times[-1])
+    cb["value"] = v
+    print(json.dumps({
+        "metric": METRIC, "value": v, "unit": "simulated days/day", "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * times[-1]["seconds_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+        "data": "synthetic (seeded balanced jet, Held-Suarez forcing)",
+        "config": {"workload": args.workload, "ntrunc": T, "grid": f"{nlon}x{nlat}", "nlev": L, "ntrac": nt,
+                   "dt_s": dt, "precision": "fp64"},
+        "cpu_baseline": cb,
+        "e2e": {"value": v, "unit": "simulated days/day", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "FP64 C++ restatement of the reference algorithm; the reference's Fortran+SHTns build cannot be "
+                "made on this image (no Fortran compiler, no SHTns/FFTW)",
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gd", choices=["gd", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "tf32x3", "bf16x3"])
+    ap.add_argument("--workload", default="T574L64", choices=list(WORKLOADS))
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--cpu-levels", type=int, default=16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gd":
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

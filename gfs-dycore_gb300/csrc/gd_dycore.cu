@@ -47,6 +47,7 @@ class DycoreBase {
   virtual void grid_info(double*, double*, double*, int*, int*, double*, double*) = 0;
   virtual int get_grid(const char*, double*) = 0;
   virtual void diag(double*) = 0;
+  virtual void profile_step(double*, int) = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = true;
   std::string err;
@@ -91,6 +92,22 @@ class Dycore : public DycoreBase {
   GemmPlan synP, synH, anaP, anaH, anaPhys;
   FftPlan c2rFull, c2rInv, r2cDyn, r2cPhys;
   Tableau tb;
+  // per-phase CUDA-event profiling of one eager step (gd_profile_step)
+  enum { PH_LSYN, PH_FSYN, PH_COL, PH_FANA, PH_LANA, PH_SEMI, PH_PHYS, PH_OTHER, PH_N };
+  bool profiling = false;
+  std::vector<std::pair<int, cudaEvent_t>> marks;
+  std::vector<cudaEvent_t> evpool;
+  void mark(int ph) {
+    if (!profiling) return;
+    if (marks.size() >= evpool.size()) {
+      cudaEvent_t e;
+      GD_CUDA(cudaEventCreate(&e));
+      evpool.push_back(e);
+    }
+    cudaEvent_t e = evpool[marks.size()];
+    GD_CUDA(cudaEventRecord(e, stream));
+    marks.push_back({ph, e});
+  }
   bool state_set = false;
   cudaGraphExec_t gexec = nullptr;
   int steps_done = 0;
@@ -138,6 +155,7 @@ class Dycore : public DycoreBase {
   }
   ~Dycore() override {
     if (gexec) cudaGraphExecDestroy(gexec);
+    for (auto e : evpool) cudaEventDestroy(e);
     free_plan(synP);
     free_plan(synH);
     free_plan(anaP);
@@ -479,7 +497,9 @@ class Dycore : public DycoreBase {
   void synthesis(const FftPlan& plan) {
     launch_synth<R>(sd, false, synP, S, ldS, 2 * sc.ncol, FPb, ldFP, stream);
     launch_synth<R>(sd, true, synH, S + 2 * (2 * L), ldS, 2 * (sc.ncol - 2 * L), FHb, ldFH, stream);
+    mark(PH_LSYN);
     launch_c2r<R>(sd, plan, FPb, ldFP, FHb, ldFH, gS, stream);
+    mark(PH_FSYN);
   }
   ColumnArgs<R> column_args(bool want_extra) {
     ColumnArgs<R> a;
@@ -521,13 +541,17 @@ class Dycore : public DycoreBase {
       launch_area_mean_ps<R>(psg, w, nlat, nlon, rowsum, pmean, stream);
       launch_pdry_init(pmean, pdryini, stream);
     }
+    mark(PH_COL);
     launch_r2c<R>(sd, r2cDyn, gA, FPb, ldGP, FHb, ldGH, stream);
+    mark(PH_FANA);
     launch_anal<R>(sd, false, anaP, FPb, ldGP, 2 * ap.ncol, AP, ldAP, stream);
     launch_anal<R>(sd, true, anaH, FHb, ldGH, 2 * ah.ncol, AH, ldAH, stream);
+    mark(PH_LANA);
   }
   void inverse_pass(bool want_extra) {
     synthesis(c2rInv);
     launch_dyn_columns<R>(column_args(want_extra), true, stream);
+    mark(PH_COL);
   }
   StageArgs<R> stage_args(int s) {
     StageArgs<R> a;
@@ -604,21 +628,44 @@ class Dycore : public DycoreBase {
       launch_area_mean_ps<R>(psg, w, nlat, nlon, rowsum, pmean, stream);
       launch_massfix_grid<R>(psg, pdryini, pmean, (int)ng, gA + (long)3 * L * ng, stream);
     }
+    mark(PH_PHYS);
     if (c.heldsuarez || c.massfix) {
       launch_r2c<R>(sd, r2cPhys, gA, FPb, ldGP, FHb, ldGH, stream);
+      mark(PH_FANA);
       launch_anal<R>(sd, false, anaPhys, FPb, ldGP, 2 * (3 * L + 1), AP, ldAP, stream);
+      mark(PH_LANA);
       launch_phys_update<R>(S, ldS, sc, L, nt, nlm, AP, ldAP, c.massfix, c.heldsuarez, (R)c.dt, lapv,
                             (R)Phys::rerth, stream);
+      mark(PH_PHYS);
     }
   }
   // advance (run.f90:194-565)
   void step() {
+    mark(-1);
     GD_CUDA(cudaMemcpyAsync(S0, S, sizeof(R) * nlm * ldS, cudaMemcpyDeviceToDevice, stream));
+    mark(PH_OTHER);
     for (int s = 0; s < 3; ++s) {
       dyn_pass(s, false);
       launch_stage<R>(stage_args(s), stream);
+      mark(PH_SEMI);
     }
     if (!c.adiabatic) phys_pass();
+  }
+  // one eager step with CUDA events between phases; ms[ph] accumulates
+  void profile_step(double* ms, int n) override {
+    if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
+    for (int i = 0; i < n; ++i) ms[i] = 0;
+    marks.clear();
+    profiling = true;
+    step();
+    profiling = false;
+    GD_CUDA(cudaStreamSynchronize(stream));
+    for (size_t i = 1; i < marks.size(); ++i) {
+      float t = 0;
+      GD_CUDA(cudaEventElapsedTime(&t, marks[i - 1].second, marks[i].second));
+      if (marks[i].first >= 0 && marks[i].first < n) ms[marks[i].first] += t;
+    }
+    ++steps_done;
   }
   void advance(int nsteps) override {
     if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
@@ -648,59 +695,69 @@ class Dycore : public DycoreBase {
   }
 
   // ------------------------------------------------------------ state --
+  // Persistent FP64 staging area in the reference layout: one region per
+  // field, so host copies of all fields are in flight together.
+  double* staging_ = nullptr;
+  double* staging() {
+    if (!staging_) staging_ = dalloc<double>(2L * nlm * ((3 + nt) * (long)L + 1));
+    return staging_;
+  }
   void set_state(const double* vrt, const double* div, const double* tv, const double* trc, const double* lnps,
                  const double* topo) override {
-    const long NS = (long)L * nlm;
-    double* tmp = dalloc<double>(2 * NS * std::max(1, nt));
+    if (nt > 0 && !trc) throw std::invalid_argument("trc is NULL but ntrac > 0");
+    double* st = staging();
+    long off = 0;
     auto put = [&](const double* h, int nb, int col) {
-      GD_CUDA(cudaMemcpyAsync(tmp, h, sizeof(double) * 2 * (long)nb * nlm, cudaMemcpyHostToDevice, stream));
-      launch_ref2int<R>(tmp, nb, nlm, S, ldS, col, stream);
+      double* d = st + off;
+      GD_CUDA(cudaMemcpyAsync(d, h, sizeof(double) * 2 * (long)nb * nlm, cudaMemcpyHostToDevice, stream));
+      launch_ref2int<R>(d, nb, nlm, S, ldS, col, stream);
+      off += 2L * nb * nlm;
     };
     put(vrt, L, sc.vrt);
     put(div, L, sc.div);
     put(tv, L, sc.tv);
-    if (nt > 0) {
-      if (!trc) throw std::invalid_argument("trc is NULL but ntrac > 0");
-      put(trc, nt * L, sc.trc);
-    }
+    if (nt > 0) put(trc, nt * L, sc.trc);
     put(lnps, 1, sc.lnps);
     launch_sc<R>(S, ldS, sc, L, nlm, lapv, (R)Phys::rerth, stream);
-    // grad(grav*topo) (dyn_init.f90:84)
-    if (topo) {
-      std::vector<double> gt(2 * (size_t)nlm);
-      for (long q = 0; q < 2L * nlm; ++q) gt[q] = Phys::grav * topo[q];
-      std::vector<double> gx(ng), gy(ng);
-      getgrad(1, gt.data(), gx.data(), gy.data());
-      std::vector<R> rx(gx.begin(), gx.end()), ry(gy.begin(), gy.end());
-      GD_CUDA(cudaMemcpyAsync(dphisdx, rx.data(), sizeof(R) * ng, cudaMemcpyHostToDevice, stream));
-      GD_CUDA(cudaMemcpyAsync(dphisdy, ry.data(), sizeof(R) * ng, cudaMemcpyHostToDevice, stream));
-    } else {
-      GD_CUDA(cudaMemsetAsync(dphisdx, 0, sizeof(R) * ng, stream));
-      GD_CUDA(cudaMemsetAsync(dphisdy, 0, sizeof(R) * ng, stream));
+    if (topo != topo_seen_ || topo) {  // grad(grav*topo) (dyn_init.f90:84)
+      if (topo) {
+        std::vector<double> gt(2 * (size_t)nlm);
+        for (long q = 0; q < 2L * nlm; ++q) gt[q] = Phys::grav * topo[q];
+        std::vector<double> gx(ng), gy(ng);
+        getgrad(1, gt.data(), gx.data(), gy.data());
+        std::vector<R> rx(gx.begin(), gx.end()), ry(gy.begin(), gy.end());
+        GD_CUDA(cudaMemcpyAsync(dphisdx, rx.data(), sizeof(R) * ng, cudaMemcpyHostToDevice, stream));
+        GD_CUDA(cudaMemcpyAsync(dphisdy, ry.data(), sizeof(R) * ng, cudaMemcpyHostToDevice, stream));
+      } else {
+        GD_CUDA(cudaMemsetAsync(dphisdx, 0, sizeof(R) * ng, stream));
+        GD_CUDA(cudaMemsetAsync(dphisdy, 0, sizeof(R) * ng, stream));
+      }
+      topo_seen_ = topo;
     }
     GD_CUDA(cudaStreamSynchronize(stream));
-    release(tmp);
     state_set = true;
   }
+  const double* topo_seen_ = reinterpret_cast<const double*>(1);
   void release(void* p) {
     cudaFree(p);
     allocs.erase(std::remove(allocs.begin(), allocs.end(), p), allocs.end());
   }
   void get_state(double* vrt, double* div, double* tv, double* trc, double* lnps) override {
-    const long NS = (long)L * nlm;
-    double* tmp = dalloc<double>(2 * NS * std::max(1, nt));
+    double* st = staging();
+    long off = 0;
     auto get = [&](double* h, int nb, int col) {
+      double* d = st + off;
+      off += 2L * nb * nlm;
       if (!h) return;
-      launch_int2ref<R>(S, ldS, col, nb, nlm, tmp, stream);
-      GD_CUDA(cudaMemcpyAsync(h, tmp, sizeof(double) * 2 * (long)nb * nlm, cudaMemcpyDeviceToHost, stream));
-      GD_CUDA(cudaStreamSynchronize(stream));
+      launch_int2ref<R>(S, ldS, col, nb, nlm, d, stream);
+      GD_CUDA(cudaMemcpyAsync(h, d, sizeof(double) * 2 * (long)nb * nlm, cudaMemcpyDeviceToHost, stream));
     };
     get(vrt, L, sc.vrt);
     get(div, L, sc.div);
     get(tv, L, sc.tv);
     if (nt > 0) get(trc, nt * L, sc.trc);
     get(lnps, 1, sc.lnps);
-    release(tmp);
+    GD_CUDA(cudaStreamSynchronize(stream));
   }
   void spec_out(const R* src, long ld, int col, int nb, double* h, double* tmp) {
     if (!h) return;
@@ -1121,6 +1178,13 @@ int gd_get_grid(gd_ctx* ctx, const char* name, double* out) {
 int gd_diag(gd_ctx* ctx, double* out5) {
   if (!out5) return GD_ERR_ARG;
   return guarded(ctx, [&] { ctx->d->diag(out5); });
+}
+int gd_profile_step(gd_ctx* ctx, double* ms, int nphase) {
+  if (!ms || nphase < 8) {
+    if (ctx) ctx->err = "gd_profile_step: need room for 8 phases";
+    return GD_ERR_ARG;
+  }
+  return guarded(ctx, [&] { ctx->d->profile_step(ms, nphase); });
 }
 int gd_set_stream(gd_ctx* ctx, void* stream) {
   return guarded(ctx, [&] {

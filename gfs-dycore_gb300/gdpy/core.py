@@ -31,8 +31,10 @@ API_FUNCTIONS = [
     "gd_default_config", "gd_init", "gd_finalize", "gd_set_state", "gd_get_state",
     "gd_getdyntend", "gd_getphytend", "gd_advance", "gd_spectogrd", "gd_grdtospec",
     "gd_getuv", "gd_getvrtdivspec", "gd_getgrad", "gd_grid_info", "gd_get_grid", "gd_diag",
-    "gd_set_stream", "gd_sync", "gd_launch_count", "gd_last_error",
+    "gd_set_stream", "gd_sync", "gd_launch_count", "gd_last_error", "gd_profile_step",
 ]
+PHASES = ["legendre_synth", "fft_synth", "columns", "fft_anal", "legendre_anal", "semi_implicit",
+          "physics", "other"]
 
 
 class GdConfig(ctypes.Structure):
@@ -77,7 +79,7 @@ def load(build_if_missing=True):
     L.gd_set_stream.argtypes = [vp, vp]
     for f in ["gd_set_state", "gd_get_state", "gd_getdyntend", "gd_getphytend", "gd_spectogrd",
               "gd_grdtospec", "gd_getuv", "gd_getvrtdivspec", "gd_getgrad", "gd_grid_info",
-              "gd_get_grid", "gd_diag", "gd_sync"]:
+              "gd_get_grid", "gd_diag", "gd_sync", "gd_profile_step"]:
         getattr(L, f).restype = ctypes.c_int
     _lib = L
     return L
@@ -173,6 +175,12 @@ class Dycore:
 
     def set_stream(self, stream_handle):
         self._chk(load().gd_set_stream(self.h, ctypes.c_void_p(stream_handle)))
+
+    def profile_step(self):
+        """One eager step; returns {phase: milliseconds}."""
+        ms = np.zeros(len(PHASES))
+        self._chk(load().gd_profile_step(self.h, _p(ms), len(PHASES)))
+        return dict(zip(PHASES, ms.tolist()))
 
     def launch_count(self):
         return load().gd_launch_count(self.h)

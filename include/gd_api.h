@@ -138,6 +138,15 @@ int gd_get_grid(gd_ctx* ctx, const char* name, double* out);
    out[3] ps tendency RMS (hPa/hr), out[4] pdryini (Pa). */
 int gd_diag(gd_ctx* ctx, double* out5);
 
+/* Runs one time step eagerly with CUDA events between its phases (the
+   reference prints per-stage system_clock times, src/run.f90:311,361,427,
+   :506,:525).  ms[0..7] receive milliseconds spent in: 0 Legendre
+   synthesis, 1 longitude FFT synthesis, 2 grid-space column kernels,
+   3 longitude FFT analysis, 4 Legendre analysis, 5 semi-implicit / RK
+   stage updates, 6 physics grid work and update, 7 other.  The state
+   advances by one step.  nphase must be >= 8. */
+int gd_profile_step(gd_ctx* ctx, double* ms, int nphase);
+
 /* Runs the context on an external CUDA stream (cudaStream_t as void*). */
 int gd_set_stream(gd_ctx* ctx, void* stream);
 /* Waits for all work of the context. */

@@ -48,45 +48,103 @@ const double REF_TEMP = 300.0, REF_PRESS = 800.e2;  // semimp_data.f90:122-123
 const double LOG2_SP = FLIT(logf(2.f));             // log(2.) in single precision
 
 // ---------------------------------------------------------------------------
-// Complex mixed radix (2,3) FFT.  Role of FFTW inside SHTns (not vendored).
+// Complex Stockham FFT (radices 4, 2, 3) of length M, used through the
+// half-length trick for the real transforms of length nlon = 2M.  Role of
+// FFTW inside SHTns (not vendored).
 struct Fft {
-  int n = 0;
-  std::vector<cplx> tw;  // exp(-2 pi i k / n)
+  int n = 0;  // real length nlon
+  int M = 0;  // complex length nlon/2
+  std::vector<int> rad;
+  std::vector<cplx> twM;  // exp(-2 pi i k / M)
+  std::vector<cplx> twN;  // exp(-2 pi i k / nlon), k <= M
   void init(int n_) {
     n = n_;
-    tw.resize(n);
-    for (int k = 0; k < n; ++k) tw[k] = cplx(cos(2 * PI_D * k / n), -sin(2 * PI_D * k / n));
-    int r = n;
-    while (r % 3 == 0) r /= 3;
-    while (r % 2 == 0) r /= 2;
-    if (r != 1) {
-      fprintf(stderr, "oracle fft: nlon must be 2^a 3^b\n");
-    }
+    M = n / 2;
+    int r = M;
+    rad.clear();
+    while (r % 4 == 0) rad.push_back(4), r /= 4;
+    while (r % 2 == 0) rad.push_back(2), r /= 2;
+    while (r % 3 == 0) rad.push_back(3), r /= 3;
+    if (r != 1 || n % 2) fprintf(stderr, "oracle fft: nlon must be 2^a 3^b\n");
+    twM.resize(M);
+    for (int k = 0; k < M; ++k) twM[k] = cplx(cos(2 * PI_D * k / M), -sin(2 * PI_D * k / M));
+    twN.resize(M + 1);
+    for (int k = 0; k <= M; ++k) twN[k] = cplx(cos(2 * PI_D * k / n), -sin(2 * PI_D * k / n));
   }
-  void rec(const cplx* in, long istride, cplx* out, int len, long twstep, bool inv) const {
-    if (len == 1) {
-      out[0] = in[0];
-      return;
-    }
-    int p = (len % 3 == 0) ? 3 : 2;
-    int m = len / p;
-    for (int r = 0; r < p; ++r) rec(in + r * istride, istride * p, out + (long)r * m, m, twstep * p, inv);
-    cplx tmp[3];
-    for (int k = 0; k < m; ++k) {
-      for (int r = 0; r < p; ++r) tmp[r] = out[(long)r * m + k];
-      for (int q = 0; q < p; ++q) {
-        cplx s = 0;
-        for (int r = 0; r < p; ++r) {
-          long e = ((long)r * (k + (long)q * m) * twstep) % n;
-          cplx w = inv ? std::conj(tw[e]) : tw[e];
-          s += tmp[r] * w;
+  // in-place length-M transform, sign -1 forward, +1 inverse (unnormalised);
+  // b is scratch of length M
+  void cfft(cplx* a, cplx* b, int sign) const {
+    int Ns = 1;
+    cplx* x = a;
+    cplx* y = b;
+    for (int p : rad) {
+      const int nb = M / p, tstep = M / (Ns * p);
+      const cplx w3 = cplx(-0.5, sign * 0.86602540378443864676);
+      for (int jj = 0; jj < nb; ++jj) {
+        const int k = jj % Ns;
+        cplx v[4];
+        for (int q = 0; q < p; ++q) {
+          cplx t = x[jj + q * nb];
+          if (q > 0 && k > 0) {
+            cplx w = twM[k * q * tstep];
+            if (sign > 0) w = std::conj(w);
+            t *= w;
+          }
+          v[q] = t;
         }
-        out[k + (long)q * m] = s;
+        if (p == 2) {
+          cplx t = v[0];
+          v[0] = t + v[1];
+          v[1] = t - v[1];
+        } else if (p == 4) {
+          cplx s02 = v[0] + v[2], d02 = v[0] - v[2], s13 = v[1] + v[3], d13 = v[1] - v[3];
+          cplx id13 = cplx(-sign * d13.imag(), sign * d13.real());
+          v[0] = s02 + s13;
+          v[2] = s02 - s13;
+          v[1] = d02 + id13;
+          v[3] = d02 - id13;
+        } else {
+          cplx y0 = v[0] + v[1] + v[2];
+          cplx y1 = v[0] + w3 * v[1] + w3 * w3 * v[2];
+          cplx y2 = v[0] + w3 * w3 * v[1] + w3 * v[2];
+          v[0] = y0;
+          v[1] = y1;
+          v[2] = y2;
+        }
+        const int od = (jj / Ns) * Ns * p + k;
+        for (int q = 0; q < p; ++q) y[od + q * Ns] = v[q];
       }
+      std::swap(x, y);
+      Ns *= p;
+    }
+    if (x != a) std::copy(x, x + M, a);
+  }
+  // out[i] = Re X0 + 2 Re sum_{k=1..T} X[k] exp(+2 pi i k i / n)
+  void c2r(const cplx* X, int T, double* out, cplx* z, cplx* tmp) const {
+    for (int k = 0; k < M; ++k) {
+      cplx xk = (k <= T) ? X[k] : cplx(0, 0);
+      if (k == 0) xk = cplx(xk.real(), 0.0);
+      cplx xm = (k == 0 || M - k > T) ? cplx(0, 0) : std::conj(X[M - k]);
+      cplx A = xk + xm, B = xk - xm;
+      z[k] = A + cplx(0, 1) * B * std::conj(twN[k]);
+    }
+    cfft(z, tmp, +1);
+    for (int k = 0; k < M; ++k) {
+      out[2 * k] = z[k].real();
+      out[2 * k + 1] = z[k].imag();
     }
   }
-  // out[k] = sum_i in[i] exp(-/+ 2 pi i k i / n)
-  void transform(const cplx* in, cplx* out, bool inv) const { rec(in, 1, out, n, 1, inv); }
+  // X[k] = sum_i g[i] exp(-2 pi i k i / n), k = 0..T
+  void r2c(const double* g, int T, cplx* X, cplx* z, cplx* tmp) const {
+    for (int k = 0; k < M; ++k) z[k] = cplx(g[2 * k], g[2 * k + 1]);
+    cfft(z, tmp, -1);
+    for (int k = 0; k <= T; ++k) {
+      cplx zk = z[k], zm = std::conj(z[(M - k) % M]);
+      cplx E = zk + zm, O = zk - zm;
+      cplx Oi = cplx(O.imag(), -O.real());
+      X[k] = 0.5 * (E + twN[k] * Oi);
+    }
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -272,26 +330,18 @@ struct Sht {
   // ----- longitude stage -----
   // grid[j][i] = Re F_0 + 2 Re sum_{m=1..T} F_m exp(i m lambda_i)
   void f2g(const cplx* F, double* g) const {
-    std::vector<cplx> X(nlon), Y(nlon);
+    std::vector<cplx> X(T + 1), z(fft.M), tmp(fft.M);
     for (int j = 0; j < nlat; ++j) {
-      std::fill(X.begin(), X.end(), cplx(0, 0));
-      X[0] = cplx(F[j].real(), 0.0);
-      for (int m = 1; m <= T; ++m) {
-        cplx f = F[(long)m * nlat + j];
-        X[m] = f;
-        X[nlon - m] = std::conj(f);
-      }
-      fft.transform(X.data(), Y.data(), true);
-      for (int i = 0; i < nlon; ++i) g[(long)j * nlon + i] = Y[i].real();
+      for (int m = 0; m <= T; ++m) X[m] = F[(long)m * nlat + j];
+      fft.c2r(X.data(), T, g + (long)j * nlon, z.data(), tmp.data());
     }
   }
   // F_m(j) = (1/nlon) sum_i g[j][i] exp(-i m lambda_i)
   void g2f(const double* g, cplx* F) const {
-    std::vector<cplx> X(nlon), Y(nlon);
+    std::vector<cplx> X(T + 1), z(fft.M), tmp(fft.M);
     for (int j = 0; j < nlat; ++j) {
-      for (int i = 0; i < nlon; ++i) X[i] = cplx(g[(long)j * nlon + i], 0.0);
-      fft.transform(X.data(), Y.data(), false);
-      for (int m = 0; m <= T; ++m) F[(long)m * nlat + j] = Y[m] / (double)nlon;
+      fft.r2c(g + (long)j * nlon, T, X.data(), z.data(), tmp.data());
+      for (int m = 0; m <= T; ++m) F[(long)m * nlat + j] = X[m] / (double)nlon;
     }
   }
 

@@ -150,7 +150,7 @@ def gpu_arm(args):
     ak, bk = inputs.hybrid_coords(L)
     st = make_state(name, seed=rank)
     trc = st["trc"] if nt else None
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # a capturable stream shared with the library
 
     def ctx(prec):
         g = core.Dycore(T, nlon, nlat, L, ak, bk, ntrac=nt, dt=dt, precision=prec, device=local)

@@ -670,7 +670,11 @@ class Dycore : public DycoreBase {
   void advance(int nsteps) override {
     if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
     for (int i = 0; i < nsteps; ++i) {
-      if (steps_done == 0 || gexec == nullptr) {
+      // the legacy default stream cannot be captured: launch eagerly there
+      const bool capturable = stream != nullptr && stream != cudaStreamLegacy && stream != cudaStreamPerThread;
+      if (!capturable) {
+        step();
+      } else if (steps_done == 0 || gexec == nullptr) {
         if (steps_done == 0) {  // first step eagerly (sets kernel attributes)
           long long l0 = g_launches;
           step();

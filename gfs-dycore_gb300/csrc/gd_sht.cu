@@ -456,8 +456,12 @@ __device__ typename C2<R>::T* fft_rows(typename C2<R>::T* a, typename C2<R>::T* 
 }
 
 template <typename R>
+__host__ __device__ constexpr int nr_of() {
+  return sizeof(R) == 8 ? 2 : 4;
+}
+template <typename R>
 int fft_rows_per_cta() {
-  return sizeof(R) == 8 ? 8 : 16;
+  return nr_of<R>();
 }
 template int fft_rows_per_cta<double>();
 template int fft_rows_per_cta<float>();
@@ -474,7 +478,7 @@ __global__ void __launch_bounds__(256) k_c2r(const int2* __restrict__ jobs, cons
                                              const R* __restrict__ FH, long ldH, R* __restrict__ grid) {
   typedef typename C2<R>::T V;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int NR = sizeof(R) == 8 ? 8 : 16;
+  const int NR = nr_of<R>();
   const int M = d.M, T = d.T, nlat = d.nlat, nlon = d.nlon;
   V* b0 = reinterpret_cast<V*>(smraw);
   V* b1 = b0 + (long)NR * M;
@@ -539,7 +543,7 @@ __global__ void __launch_bounds__(256) k_r2c(const int2* __restrict__ jobs, cons
                                              R* __restrict__ GP, long ldP, R* __restrict__ GH, long ldH) {
   typedef typename C2<R>::T V;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int NR = sizeof(R) == 8 ? 8 : 16;
+  const int NR = nr_of<R>();
   const int M = d.M, T = d.T, nlat = d.nlat, nlon = d.nlon;
   V* b0 = reinterpret_cast<V*>(smraw);
   V* b1 = b0 + (long)NR * M;
@@ -589,6 +593,293 @@ __global__ void __launch_bounds__(256) k_r2c(const int2* __restrict__ jobs, cons
   }
 }
 
+// ---- compile-time-planned FFT kernels (common lengths) -------------------
+// One in-place shared-memory buffer per CTA (NR rows of M complex values);
+// each Stockham stage stages its butterflies through registers, so a CTA
+// needs NR*M*sizeof(complex) bytes and many CTAs fit on an SM.  Radix plan,
+// strides and divisions are compile-time constants.
+template <int M>
+struct FftPlanC {
+  static constexpr int count() {
+    int n = 0, r = M;
+    while (r % 4 == 0) r /= 4, ++n;
+    while (r % 2 == 0) r /= 2, ++n;
+    while (r % 3 == 0) r /= 3, ++n;
+    return n;
+  }
+  static constexpr int radix(int s) {
+    int r = M, i = 0;
+    while (r % 4 == 0) {
+      if (i == s) return 4;
+      r /= 4, ++i;
+    }
+    while (r % 2 == 0) {
+      if (i == s) return 2;
+      r /= 2, ++i;
+    }
+    while (r % 3 == 0) {
+      if (i == s) return 3;
+      r /= 3, ++i;
+    }
+    return 1;
+  }
+  static constexpr int ns(int s) {
+    int n = 1;
+    for (int i = 0; i < s; ++i) n *= radix(i);
+    return n;
+  }
+};
+
+template <typename R, int M, int NR, int NT, int S, int SIGN>
+__device__ __forceinline__ void stage_c(typename C2<R>::T* buf, const typename C2<R>::T* __restrict__ tw) {
+  typedef typename C2<R>::T V;
+  constexpr int p = FftPlanC<M>::radix(S), Ns = FftPlanC<M>::ns(S), nb = M / p, tstep = M / (Ns * p);
+  constexpr int NB = NR * nb, PER = (NB + NT - 1) / NT;
+  V v[PER][p];
+  int od[PER];
+#pragma unroll
+  for (int u = 0; u < PER; ++u) {
+    const int e = threadIdx.x + u * NT;
+    od[u] = -1;
+    if (e < NB) {
+      const int r = e / nb, jj = e - r * nb, k = jj % Ns;
+#pragma unroll
+      for (int q = 0; q < p; ++q) {
+        V x = buf[r * M + jj + q * nb];
+        if (q > 0 && k > 0) {
+          V w = tw[k * q * tstep];
+          if (SIGN > 0) w.y = -w.y;
+          x = cmul(x, w);
+        }
+        v[u][q] = x;
+      }
+      if (p == 2) {
+        V t = v[u][0];
+        v[u][0] = cadd(t, v[u][1]);
+        v[u][1] = csub(t, v[u][1]);
+      } else if (p == 4) {
+        V s02 = cadd(v[u][0], v[u][2]), d02 = csub(v[u][0], v[u][2]);
+        V s13 = cadd(v[u][1], v[u][3]), d13 = csub(v[u][1], v[u][3]);
+        V id13;
+        id13.x = -SIGN * d13.y;
+        id13.y = SIGN * d13.x;
+        v[u][0] = cadd(s02, s13);
+        v[u][2] = csub(s02, s13);
+        v[u][1] = cadd(d02, id13);
+        v[u][3] = csub(d02, id13);
+      } else if (p == 3) {
+        const R c3 = R(-0.5), s3 = R(0.86602540378443864676) * R(SIGN);
+        V t1 = cadd(v[u][1], v[u][2]), t2 = csub(v[u][1], v[u][2]);
+        V m1, m2;
+        m1.x = v[u][0].x + c3 * t1.x;
+        m1.y = v[u][0].y + c3 * t1.y;
+        m2.x = -s3 * t2.y;
+        m2.y = s3 * t2.x;
+        v[u][0] = cadd(v[u][0], t1);
+        v[u][1] = cadd(m1, m2);
+        v[u][2] = csub(m1, m2);
+      }
+      od[u] = r * M + (jj / Ns) * Ns * p + k;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < PER; ++u)
+    if (od[u] >= 0) {
+#pragma unroll
+      for (int q = 0; q < p; ++q) buf[od[u] + q * Ns] = v[u][q];
+    }
+  __syncthreads();
+}
+
+template <typename R, int M, int NR, int NT, int S, int SIGN>
+__device__ __forceinline__ void stages_c(typename C2<R>::T* buf, const typename C2<R>::T* __restrict__ tw) {
+  if constexpr (S < FftPlanC<M>::count()) {
+    stage_c<R, M, NR, NT, S, SIGN>(buf, tw);
+    stages_c<R, M, NR, NT, S + 1, SIGN>(buf, tw);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ typename C2<R>::T synth_coef(const SynthDesc& ds, int k, int T, int j, int nlat, int col,
+                                                      const R* __restrict__ FP, long ldP,
+                                                      const R* __restrict__ FH, long ldH, R rc, R alpha,
+                                                      R beta) {
+  typedef typename C2<R>::T V;
+  V x = mk2<R>(R(0), R(0));
+  if (k > T) return x;
+  if (ds.srcA >= 0) {
+    const R* src = ds.srcA == 0 ? FP : FH;
+    const long ld = ds.srcA == 0 ? ldP : ldH;
+    V a = *reinterpret_cast<const V*>(src + ((long)k * nlat + j) * ld + 2 * (ds.colA + col));
+    x.x = alpha * a.x;
+    x.y = alpha * a.y;
+  }
+  if (ds.srcB >= 0) {
+    const R* src = ds.srcB == 0 ? FP : FH;
+    const long ld = ds.srcB == 0 ? ldP : ldH;
+    V bb = *reinterpret_cast<const V*>(src + ((long)k * nlat + j) * ld + 2 * (ds.colB + col));
+    const R f = beta * (R)k * rc;
+    x.x -= f * bb.y;
+    x.y += f * bb.x;
+  }
+  if (k == 0) x.y = R(0);
+  return x;
+}
+
+template <typename R, int M>
+__global__ void __launch_bounds__(128) k_c2r_t(const int2* __restrict__ jobs, const SynthDesc* __restrict__ descs,
+                                               ShtDev<R> d, const R* __restrict__ FP, long ldP,
+                                               const R* __restrict__ FH, long ldH, R* __restrict__ grid) {
+  typedef typename C2<R>::T V;
+  constexpr int NR = nr_of<R>(), NT = 128;
+  __shared__ V buf[NR * M];
+  const int T = d.T, nlat = d.nlat, nlon = d.nlon;
+  const int2 jb = jobs[blockIdx.x];
+  const SynthDesc ds = descs[jb.x];
+  const int j = blockIdx.y, r0 = jb.y;
+  const int nr = min(NR, ds.count - r0);
+  const R rc = d.rcos[j], alpha = (R)ds.alpha, beta = (R)ds.beta;
+  // gather X[k], X[M-k] and form the half-length spectrum Z in place:
+  // Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) exp(2 pi i k / nlon)
+  for (int e = threadIdx.x; e < NR * (M / 2 + 1); e += NT) {
+    const int kk = e / NR, r = e - kk * NR;
+    V z1 = mk2<R>(R(0), R(0)), z2 = z1;
+    if (r < nr) {
+      const int k2 = M - kk;
+      const V x1 = synth_coef<R>(ds, kk, T, j, nlat, r0 + r, FP, ldP, FH, ldH, rc, alpha, beta);
+      const V x2 = (kk == 0) ? mk2<R>(R(0), R(0))
+                             : synth_coef<R>(ds, k2, T, j, nlat, r0 + r, FP, ldP, FH, ldH, rc, alpha, beta);
+      V A = cadd(x1, cconj(x2)), B = csub(x1, cconj(x2));
+      V Bw = cmul(B, cconj(d.twN[kk]));
+      z1.x = A.x - Bw.y;
+      z1.y = A.y + Bw.x;
+      if (kk > 0 && k2 != kk) {
+        V A2 = cadd(x2, cconj(x1)), B2 = csub(x2, cconj(x1));
+        V Bw2 = cmul(B2, cconj(d.twN[k2]));
+        z2.x = A2.x - Bw2.y;
+        z2.y = A2.y + Bw2.x;
+      }
+    }
+    buf[r * M + kk] = z1;
+    if (kk > 0 && M - kk != kk) buf[r * M + (M - kk)] = z2;
+  }
+  __syncthreads();
+  stages_c<R, M, NR, NT, 0, +1>(buf, d.twM);
+  for (int e = threadIdx.x; e < nr * M; e += NT) {
+    const int r = e / M, n = e - r * M;
+    *reinterpret_cast<V*>(grid + ((long)(ds.dst + r0 + r) * nlat + j) * nlon + 2 * n) = buf[r * M + n];
+  }
+}
+
+template <typename R, int M>
+__global__ void __launch_bounds__(128) k_r2c_t(const int2* __restrict__ jobs, const AnalDesc* __restrict__ descs,
+                                               ShtDev<R> d, const R* __restrict__ grid, R* __restrict__ GP,
+                                               long ldP, R* __restrict__ GH, long ldH) {
+  typedef typename C2<R>::T V;
+  constexpr int NR = nr_of<R>(), NT = 128;
+  __shared__ V buf[NR * M];
+  const int T = d.T, nlat = d.nlat, nlon = d.nlon;
+  const int2 jb = jobs[blockIdx.x];
+  const AnalDesc ds = descs[jb.x];
+  const int j = blockIdx.y, r0 = jb.y;
+  const int nr = min(NR, ds.count - r0);
+  for (int e = threadIdx.x; e < NR * M; e += NT) {
+    const int r = e / M, n = e - r * M;
+    V z = mk2<R>(R(0), R(0));
+    if (r < nr) z = *reinterpret_cast<const V*>(grid + ((long)(ds.src + r0 + r) * nlat + j) * nlon + 2 * n);
+    buf[e] = z;
+  }
+  __syncthreads();
+  stages_c<R, M, NR, NT, 0, -1>(buf, d.twM);
+  const R wn = d.wn[j] * R(0.5), rc = d.rcos[j];
+  for (int e = threadIdx.x; e < nr * (M / 2 + 1); e += NT) {
+    const int kk = e / nr, r = e - kk * nr;
+    const V Z1 = buf[r * M + kk], Z2 = buf[r * M + (M - kk) % M];
+    for (int h = 0; h < 2; ++h) {
+      const int k = h ? M - kk : kk;
+      if (k > T || (h && (kk == 0 || M - kk == kk))) continue;
+      const V za = h ? Z2 : Z1, zb = h ? Z1 : Z2;
+      V E = cadd(za, cconj(zb)), O = csub(za, cconj(zb));
+      V Oi;
+      Oi.x = O.y;
+      Oi.y = -O.x;
+      V X = cadd(E, cmul(d.twN[k], Oi));
+      X.x *= wn;
+      X.y *= wn;
+      const int col = r0 + r;
+      if (ds.dstP >= 0) {
+        V y = X;
+        if (ds.imcosP) {
+          const R f = (R)k * rc;
+          y.x = -f * X.y;
+          y.y = f * X.x;
+        }
+        y.x *= (R)ds.scaleP;
+        y.y *= (R)ds.scaleP;
+        *reinterpret_cast<V*>(GP + ((long)k * nlat + j) * ldP + 2 * (ds.dstP + col)) = y;
+      }
+      if (ds.dstH >= 0) {
+        V y = X;
+        y.x *= (R)ds.scaleH;
+        y.y *= (R)ds.scaleH;
+        *reinterpret_cast<V*>(GH + ((long)k * nlat + j) * ldH + 2 * (ds.dstH + col)) = y;
+      }
+    }
+  }
+}
+
+template <typename R>
+static bool launch_c2r_fixed(const ShtDev<R>& d, const FftPlan& plan, const R* FP, long ldP, const R* FH, long ldH,
+                             R* grid, cudaStream_t s) {
+  dim3 grd(plan.njobs, d.nlat);
+  const SynthDesc* ds = (const SynthDesc*)plan.descs;
+#define GD_C2R(MM)                                                                               \
+  case MM:                                                                                       \
+    k_c2r_t<R, MM><<<grd, 128, 0, s>>>(plan.jobs, ds, d, FP, ldP, FH, ldH, grid);                \
+    return true;
+  switch (d.M) {
+    GD_C2R(32)
+    GD_C2R(48)
+    GD_C2R(64)
+    GD_C2R(96)
+    GD_C2R(128)
+    GD_C2R(192)
+    GD_C2R(256)
+    GD_C2R(384)
+    GD_C2R(576)
+    GD_C2R(768)
+    default:
+      return false;
+  }
+#undef GD_C2R
+}
+template <typename R>
+static bool launch_r2c_fixed(const ShtDev<R>& d, const FftPlan& plan, const R* grid, R* GP, long ldP, R* GH,
+                             long ldH, cudaStream_t s) {
+  dim3 grd(plan.njobs, d.nlat);
+  const AnalDesc* ds = (const AnalDesc*)plan.descs;
+#define GD_R2C(MM)                                                                               \
+  case MM:                                                                                       \
+    k_r2c_t<R, MM><<<grd, 128, 0, s>>>(plan.jobs, ds, d, grid, GP, ldP, GH, ldH);                \
+    return true;
+  switch (d.M) {
+    GD_R2C(32)
+    GD_R2C(48)
+    GD_R2C(64)
+    GD_R2C(96)
+    GD_R2C(128)
+    GD_R2C(192)
+    GD_R2C(256)
+    GD_R2C(384)
+    GD_R2C(576)
+    GD_R2C(768)
+    default:
+      return false;
+  }
+#undef GD_R2C
+}
+
 template <typename R, typename D>
 static FftPlan make_plan(const D* descs, int ndesc, cudaStream_t s) {
   const int NR = fft_rows_per_cta<R>();
@@ -635,6 +926,11 @@ template <typename R>
 void launch_c2r(const ShtDev<R>& d, const FftPlan& plan, const R* FP, long ldP, const R* FH, long ldH, R* grid,
                 cudaStream_t s) {
   if (plan.njobs == 0) return;
+  if (launch_c2r_fixed<R>(d, plan, FP, ldP, FH, ldH, grid, s)) {
+    count_launch();
+    GD_LAUNCH_CHECK();
+    return;
+  }
   FftArgs fa;
   fa.nrad = d.nrad;
   for (int i = 0; i < 12; ++i) fa.rad[i] = d.rad[i];
@@ -653,6 +949,11 @@ template <typename R>
 void launch_r2c(const ShtDev<R>& d, const FftPlan& plan, const R* grid, R* GP, long ldP, R* GH, long ldH,
                 cudaStream_t s) {
   if (plan.njobs == 0) return;
+  if (launch_r2c_fixed<R>(d, plan, grid, GP, ldP, GH, ldH, s)) {
+    count_launch();
+    GD_LAUNCH_CHECK();
+    return;
+  }
   FftArgs fa;
   fa.nrad = d.nrad;
   for (int i = 0; i < 12; ++i) fa.rad[i] = d.rad[i];

@@ -17,6 +17,8 @@
 #include "gd_grid.cuh"
 #include "gd_kernels.h"
 #include "gd_spec.cuh"
+#include "gd_tc.cuh"
+#include <type_traits>
 
 namespace gd {
 
@@ -48,6 +50,7 @@ class DycoreBase {
   virtual int get_grid(const char*, double*) = 0;
   virtual void diag(double*) = 0;
   virtual void profile_step(double*, int) = 0;
+  virtual void check() = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = true;
   std::string err;
@@ -113,6 +116,33 @@ class Dycore : public DycoreBase {
   int steps_done = 0;
   long long launches_per_step = 0;
   std::map<int, GemmPlan> synth_cache, anal_cache;
+  // tensor-core split-precision Legendre path (FP32 state only)
+  std::unique_ptr<TcPlan> tcp;
+  double *P64keep = nullptr, *H64keep = nullptr;
+  bool split_mode() const { return c.precision == GD_PREC_TF32X3 || c.precision == GD_PREC_BF16X3; }
+  void do_synth(bool useH, const GemmPlan& plan, const R* B, long ldB, int ncr, R* F, long ldF) {
+    if constexpr (std::is_same<R, float>::value) {
+      if (tcp) {
+        tc_synth(*tcp, moff, useH, B, ldB, ncr, F, ldF, stream);
+        return;
+      }
+    }
+    launch_synth<R>(sd, useH, plan, B, ldB, ncr, F, ldF, stream);
+  }
+  void do_anal(bool useH, const GemmPlan& plan, const R* G, long ldG, int ncr, R* A, long ldA) {
+    if constexpr (std::is_same<R, float>::value) {
+      if (tcp) {
+        tc_anal(*tcp, moff, useH, G, ldG, ncr, A, ldA, stream);
+        return;
+      }
+    }
+    launch_anal<R>(sd, useH, plan, G, ldG, ncr, A, ldA, stream);
+  }
+  void check() override { tc_status(); }
+  void tc_status() {
+    if (tcp && tc_check(*tcp, stream))
+      throw CudaError("tensor-core Legendre pipeline: a bounded wait gave up (results invalid)");
+  }
 
   template <typename X>
   X* dalloc(size_t n) {
@@ -151,10 +181,22 @@ class Dycore : public DycoreBase {
     init_vertical(ak_, bk_);
     init_buffers();
     init_plans();
+    if (split_mode()) {
+      if constexpr (std::is_same<R, float>::value) {
+        tcp.reset(new TcPlan());
+        const int ncap = 2 * std::max(sc.ncol, ap.ncol);
+        tc_init(*tcp, c.precision == GD_PREC_TF32X3 ? TC_TF32 : TC_BF16, T, nh, nlat, ncap, toff, P64keep, H64keep,
+                stream);
+      }
+      release(P64keep);
+      release(H64keep);
+      P64keep = H64keep = nullptr;
+    }
     GD_CUDA(cudaStreamSynchronize(stream));
   }
   ~Dycore() override {
     if (gexec) cudaGraphExecDestroy(gexec);
+    if (tcp) tc_free(*tcp);
     for (auto e : evpool) cudaEventDestroy(e);
     free_plan(synP);
     free_plan(synH);
@@ -202,11 +244,14 @@ class Dycore : public DycoreBase {
     GD_CUDA(cudaMemcpyAsync(h_mu.data(), mu, nlat * sizeof(double), cudaMemcpyDeviceToHost, stream));
     GD_CUDA(cudaMemcpyAsync(h_w.data(), w, nlat * sizeof(double), cudaMemcpyDeviceToHost, stream));
     GD_CUDA(cudaStreamSynchronize(stream));
-    if (sizeof(R) != 8) {  // FP64 copies are no longer needed
-      cudaFree(P64);
-      cudaFree(H64);
-      allocs.erase(std::remove(allocs.begin(), allocs.end(), (void*)P64), allocs.end());
-      allocs.erase(std::remove(allocs.begin(), allocs.end(), (void*)H64), allocs.end());
+    if (sizeof(R) != 8) {  // FP64 copies: kept only to split for the tensor-core path
+      if (split_mode()) {
+        P64keep = P64;
+        H64keep = H64;
+      } else {
+        release(P64);
+        release(H64);
+      }
     }
     std::vector<double> rc(nlat), wnv(nlat), sl(nlat), cl(nlat);
     h_lat.resize(nlat);
@@ -495,8 +540,8 @@ class Dycore : public DycoreBase {
 
   // ------------------------------------------------------------ passes --
   void synthesis(const FftPlan& plan) {
-    launch_synth<R>(sd, false, synP, S, ldS, 2 * sc.ncol, FPb, ldFP, stream);
-    launch_synth<R>(sd, true, synH, S + 2 * (2 * L), ldS, 2 * (sc.ncol - 2 * L), FHb, ldFH, stream);
+    do_synth(false, synP, S, ldS, 2 * sc.ncol, FPb, ldFP);
+    do_synth(true, synH, S + 2 * (2 * L), ldS, 2 * (sc.ncol - 2 * L), FHb, ldFH);
     mark(PH_LSYN);
     launch_c2r<R>(sd, plan, FPb, ldFP, FHb, ldFH, gS, stream);
     mark(PH_FSYN);
@@ -544,8 +589,8 @@ class Dycore : public DycoreBase {
     mark(PH_COL);
     launch_r2c<R>(sd, r2cDyn, gA, FPb, ldGP, FHb, ldGH, stream);
     mark(PH_FANA);
-    launch_anal<R>(sd, false, anaP, FPb, ldGP, 2 * ap.ncol, AP, ldAP, stream);
-    launch_anal<R>(sd, true, anaH, FHb, ldGH, 2 * ah.ncol, AH, ldAH, stream);
+    do_anal(false, anaP, FPb, ldGP, 2 * ap.ncol, AP, ldAP);
+    do_anal(true, anaH, FHb, ldGH, 2 * ah.ncol, AH, ldAH);
     mark(PH_LANA);
   }
   void inverse_pass(bool want_extra) {
@@ -632,7 +677,7 @@ class Dycore : public DycoreBase {
     if (c.heldsuarez || c.massfix) {
       launch_r2c<R>(sd, r2cPhys, gA, FPb, ldGP, FHb, ldGH, stream);
       mark(PH_FANA);
-      launch_anal<R>(sd, false, anaPhys, FPb, ldGP, 2 * (3 * L + 1), AP, ldAP, stream);
+      do_anal(false, anaPhys, FPb, ldGP, 2 * (3 * L + 1), AP, ldAP);
       mark(PH_LANA);
       launch_phys_update<R>(S, ldS, sc, L, nt, nlm, AP, ldAP, c.massfix, c.heldsuarez, (R)c.dt, lapv,
                             (R)Phys::rerth, stream);
@@ -762,6 +807,7 @@ class Dycore : public DycoreBase {
     if (nt > 0) get(trc, nt * L, sc.trc);
     get(lnps, 1, sc.lnps);
     GD_CUDA(cudaStreamSynchronize(stream));
+    tc_status();
   }
   void spec_out(const R* src, long ld, int col, int nb, double* h, double* tmp) {
     if (!h) return;
@@ -792,7 +838,7 @@ class Dycore : public DycoreBase {
     if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
     launch_hs_forcing<R>(hs_args(), stream);
     launch_r2c<R>(sd, r2cPhys, gA, FPb, ldGP, FHb, ldGH, stream);
-    launch_anal<R>(sd, false, anaPhys, FPb, ldGP, 2 * (3 * L + 1), AP, ldAP, stream);
+    do_anal(false, anaPhys, FPb, ldGP, 2 * (3 * L + 1), AP, ldAP);
     double* tmp = dalloc<double>(2L * nlm * L);
     spec_out(AP, ldAP, 0, L, dtv, tmp);
     spec_out(AP, ldAP, L, L, dvrt, tmp);
@@ -816,8 +862,8 @@ class Dycore : public DycoreBase {
   int chunk_cols() const { return std::max(1, std::min(sc.ncol / 2, ar.total / 2)); }
   // synthesis of ncs complex columns X[nlm][ldS] with descriptors -> host grids
   void api_synth(const R* X, int ncs, bool needH, const std::vector<SynthDesc>& ds, int nrows, double* out) {
-    launch_synth<R>(sd, false, synth_plan(2 * ncs), X, ldS, 2 * ncs, FPb, ldS, stream);
-    if (needH) launch_synth<R>(sd, true, synth_plan(2 * ncs), X, ldS, 2 * ncs, FHb, ldS, stream);
+    do_synth(false, synth_plan(2 * ncs), X, ldS, 2 * ncs, FPb, ldS);
+    if (needH) do_synth(true, synth_plan(2 * ncs), X, ldS, 2 * ncs, FHb, ldS);
     FftPlan p = make_c2r_plan<R>(ds.data(), (int)ds.size(), stream);
     launch_c2r<R>(sd, p, FPb, ldS, FHb, ldS, gS, stream);
     grid_out(gS, nrows, out);
@@ -907,8 +953,8 @@ class Dycore : public DycoreBase {
   void api_anal(const std::vector<AnalDesc>& ds, int ncP, int ncH) {
     FftPlan p = make_r2c_plan<R>(ds.data(), (int)ds.size(), stream);
     launch_r2c<R>(sd, p, gA, FPb, ldS, FHb, ldS, stream);
-    launch_anal<R>(sd, false, anal_plan(2 * ncP), FPb, ldS, 2 * ncP, AP, ldAP, stream);
-    if (ncH > 0) launch_anal<R>(sd, true, anal_plan(2 * ncH), FHb, ldS, 2 * ncH, AH, ldAH, stream);
+    do_anal(false, anal_plan(2 * ncP), FPb, ldS, 2 * ncP, AP, ldAP);
+    if (ncH > 0) do_anal(true, anal_plan(2 * ncH), FHb, ldS, 2 * ncH, AH, ldAH);
     free_fft_plan(p);
   }
   int achunk() const { return std::max(1, std::min(ap.ncol / 2, ar.total / 2)); }
@@ -1085,10 +1131,6 @@ int gd_init(const gd_config* cfg, const double* ak, const double* bk, gd_ctx** o
     g_init_error = "gd_init: " + why;
     return (why.find("not supported") != std::string::npos) ? GD_ERR_UNSUPPORTED : GD_ERR_ARG;
   }
-  if (c.precision == GD_PREC_TF32X3 || c.precision == GD_PREC_BF16X3) {
-    g_init_error = "gd_init: split-precision Legendre GEMMs are not built in this library version";
-    return GD_ERR_UNSUPPORTED;
-  }
   gd_ctx* ctx = new gd_ctx();
   ctx->cfg = c;
   try {
@@ -1199,7 +1241,10 @@ int gd_set_stream(gd_ctx* ctx, void* stream) {
   });
 }
 int gd_sync(gd_ctx* ctx) {
-  return guarded(ctx, [&] { GD_CUDA(cudaStreamSynchronize(ctx->d->stream)); });
+  return guarded(ctx, [&] {
+    GD_CUDA(cudaStreamSynchronize(ctx->d->stream));
+    ctx->d->check();
+  });
 }
 long long gd_launch_count(gd_ctx* ctx) {
   (void)ctx;

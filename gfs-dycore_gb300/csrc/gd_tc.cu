@@ -1,0 +1,729 @@
+// gd_tc.cu -- split-precision Legendre GEMMs on the sm_103a tensor cores.
+//
+// The per-order Legendre contractions of the transforms (the work SHTns
+// does inside shtns_sh_to_spat / shtns_spat_to_sh and the vector forms
+// behind src/shtns.f90) as tcgen05 MMAs with FP32 accumulators in TMEM.
+// Each FP32 operand x is carried as hi + lo, hi = round(x) and
+// lo = round(x - hi) to TF32 (kind::tf32) or BF16 (kind::f16), and the
+// product is hi*hi + hi*lo + lo*hi ("x3").  The Legendre tables are split
+// from their FP64 values once at init; the data operands are split by
+// transpose kernels on the way in.
+//
+// GEMM orientation (both directions): D[c][n] with M = 128 real batch
+// columns c on the TMEM lanes (so every epilogue store of a warp is 128
+// contiguous bytes), N = latitudes (synthesis) or degrees of one parity
+// (analysis), K = degrees (synthesis) or latitudes (analysis).  Both
+// operands are K-major, staged by TMA with 128-byte swizzle.  The even/odd
+// hemispheric split is two TMEM accumulators over de-interleaved K ranges.
+// One CTA per (order m, column tile, N tile); a 3-stage TMA -> MMA
+// mbarrier ring; one elected thread issues TMA, one issues MMA; every wait
+// is bounded and reports through a device error flag.
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "gd_tc.cuh"
+
+namespace gd {
+
+constexpr int TC_NS = 3;          // pipeline stages
+constexpr int TC_M = 128;         // MMA M (batch columns per CTA)
+constexpr int TC_THREADS = 128;   // 4 warps
+constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // bounded waits: 2 s
+
+// ------------------------------------------------------------ PTX helpers --
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false (and the error flag set) if the phase does not
+// complete within TC_WAIT_NS
+__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer();
+  for (;;) {
+    for (int i = 0; i < 64; ++i)
+      if (mbar_try(bar, parity)) return true;
+    if (globaltimer() - t0 > TC_WAIT_NS) {
+      atomicCAS(err, 0, code);
+      return false;
+    }
+    __nanosleep(64);
+  }
+}
+__device__ __forceinline__ void tma_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tma_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(dst),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row
+// groups 1024 bytes apart (SBO), descriptor version 1 (sm_100 family)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;              // LBO (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;    // SBO
+  d |= (uint64_t)1 << 46;              // version
+  d |= (uint64_t)2 << 61;              // SWIZZLE_128B
+  return d;
+}
+template <int KIND>
+__device__ __forceinline__ void mma(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  if (KIND == TC_TF32)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+  else
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ------------------------------------------------------------ splitting --
+template <int KIND>
+struct Elem;
+template <>
+struct Elem<TC_TF32> {
+  typedef uint32_t T;  // tf32 bit pattern in a 32-bit word
+  __device__ static void split(double x, T& hi, T& lo) {
+    float f = (float)x;
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(f));
+    float r = (float)(x - (double)__uint_as_float(h));
+    uint32_t l;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(r));
+    hi = h;
+    lo = l;
+  }
+  __device__ static void splitf(float f, T& hi, T& lo) {
+    uint32_t h, l;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(f));
+    float r = f - __uint_as_float(h);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(r));
+    hi = h;
+    lo = l;
+  }
+};
+template <>
+struct Elem<TC_BF16> {
+  typedef __nv_bfloat16 T;
+  __device__ static void split(double x, T& hi, T& lo) {
+    float f = (float)x;
+    hi = __float2bfloat16_rn(f);
+    lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
+  }
+  __device__ static void splitf(float f, T& hi, T& lo) {
+    hi = __float2bfloat16_rn(f);
+    lo = __float2bfloat16_rn(f - __bfloat162float(hi));
+  }
+};
+
+// synthesis tables: [m][j][par*kepad + i] = tab[m][j][2i+par]
+template <int KIND>
+__global__ void k_tc_tab_syn(int T, int nh, int kepad, const long* toff, const double* tab,
+                             typename Elem<KIND>::T* hi, typename Elem<KIND>::T* lo) {
+  const long tot = (long)(T + 1) * nh * 2 * kepad;
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (long)gridDim.x * blockDim.x) {
+    const int k = (int)(e % (2 * kepad));
+    const long mj = e / (2 * kepad);
+    const int j = (int)(mj % nh), m = (int)(mj / nh);
+    const int par = k / kepad, i = k - par * kepad, q = 2 * i + par, K = T - m + 1;
+    const double v = (q < K) ? tab[toff[m] + (long)j * K + q] : 0.0;
+    Elem<KIND>::split(v, hi[e], lo[e]);
+  }
+}
+// analysis tables: [m][par*kirows + i][j] = tab[m][j][2i+par]
+template <int KIND>
+__global__ void k_tc_tab_ana(int T, int nh, int kirows, int nhpad, const long* toff, const double* tab,
+                             typename Elem<KIND>::T* hi, typename Elem<KIND>::T* lo) {
+  const long tot = (long)(T + 1) * 2 * kirows * nhpad;
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (long)gridDim.x * blockDim.x) {
+    const int j = (int)(e % nhpad);
+    const long mr = e / nhpad;
+    const int r = (int)(mr % (2 * kirows)), m = (int)(mr / (2 * kirows));
+    const int par = r / kirows, i = r - par * kirows, q = 2 * i + par, K = T - m + 1;
+    const double v = (q < K && j < nh) ? tab[toff[m] + (long)j * K + q] : 0.0;
+    Elem<KIND>::split(v, hi[e], lo[e]);
+  }
+}
+
+// X[c][x] = B[xmap[x]][c] split, x in [0, xlen), c in [0, ncols)
+template <int KIND>
+__global__ void __launch_bounds__(256) k_tc_split_x(const float* __restrict__ B, long ldB, int ncols,
+                                                    const int* __restrict__ xmap, long xlen,
+                                                    typename Elem<KIND>::T* __restrict__ hi,
+                                                    typename Elem<KIND>::T* __restrict__ lo) {
+  __shared__ float t[32][33];
+  const long x0 = (long)blockIdx.x * 32;
+  const int c0 = blockIdx.y * 32;
+  for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+    const long x = x0 + yy;
+    const int c = c0 + threadIdx.x;
+    float v = 0.f;
+    if (x < xlen && c < ncols) {
+      const int idx = xmap[x];
+      if (idx >= 0) v = B[(long)idx * ldB + c];
+    }
+    t[yy][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+    const int c = c0 + yy;
+    const long x = x0 + threadIdx.x;
+    if (c < ncols && x < xlen) {
+      typename Elem<KIND>::T h, l;
+      Elem<KIND>::splitf(t[threadIdx.x][yy], h, l);
+      hi[(long)c * xlen + x] = h;
+      lo[(long)c * xlen + x] = l;
+    }
+  }
+}
+
+// G+-[m][c][j] = G[m][j][c] +- G[m][nlat-1-j][c] split, j < nhpad (0 >= nh)
+template <int KIND>
+__global__ void __launch_bounds__(256) k_tc_split_g(const float* __restrict__ G, long ldG, int ncols, int nh,
+                                                    int nlat, int nhpad, int ncap, typename Elem<KIND>::T* __restrict__ ph,
+                                                    typename Elem<KIND>::T* __restrict__ pl,
+                                                    typename Elem<KIND>::T* __restrict__ mh,
+                                                    typename Elem<KIND>::T* __restrict__ ml) {
+  __shared__ float tp[32][33], tm[32][33];
+  const int j0 = blockIdx.x * 32, c0 = blockIdx.y * 32, m = blockIdx.z;
+  for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+    const int j = j0 + yy, c = c0 + threadIdx.x;
+    float a = 0.f, b = 0.f;
+    if (j < nh && c < ncols) {
+      a = G[((long)m * nlat + j) * ldG + c];
+      b = G[((long)m * nlat + (nlat - 1 - j)) * ldG + c];
+    }
+    tp[yy][threadIdx.x] = a + b;
+    tm[yy][threadIdx.x] = a - b;
+  }
+  __syncthreads();
+  for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+    const int c = c0 + yy, j = j0 + threadIdx.x;
+    if (c < ncols && j < nhpad) {
+      const long o = ((long)m * ncap + c) * nhpad + j;
+      typename Elem<KIND>::T h, l;
+      Elem<KIND>::splitf(tp[threadIdx.x][yy], h, l);
+      ph[o] = h;
+      pl[o] = l;
+      Elem<KIND>::splitf(tm[threadIdx.x][yy], h, l);
+      mh[o] = h;
+      ml[o] = l;
+    }
+  }
+}
+
+// ------------------------------------------------------------- the GEMM --
+struct TcArgs {
+  const int4* items;
+  int mode;  // 0 synthesis, 1 analysis
+  int T, nh, nlat, N, kc, kepad, kirows;
+  const long* xbase;
+  const long* moff;
+  int parityH;
+  int ncols;  // real columns of this GEMM
+  int coff;   // row offset of the first column in the synthesis staging
+  float* out;
+  long ldout;
+  int* err;
+  uint32_t idesc;
+  uint32_t tmem_cols;
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_tc_gemm(const __grid_constant__ CUtensorMap mA0h, const __grid_constant__ CUtensorMap mA0l,
+              const __grid_constant__ CUtensorMap mA1h, const __grid_constant__ CUtensorMap mA1l,
+              const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t)1023);
+  const int N = a.N;
+  const uint32_t bytesA = TC_M * 128, bytesB = (uint32_t)N * 128;
+  const uint32_t stage_bytes = 2 * bytesA + 2 * bytesB;
+  unsigned char* bar_area = sm + TC_NS * stage_bytes;
+  uint64_t* full = reinterpret_cast<uint64_t*>(bar_area);
+  uint64_t* empty = full + TC_NS;
+  uint64_t* done = empty + TC_NS;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  const int4 it = a.items[blockIdx.x];
+  const int m = it.x, c0 = it.y * TC_M, n0 = it.z * N;
+  const int K = a.T - m + 1;
+  int nk0, nk1;
+  long xb = 0;
+  int kp = 0;
+  if (a.mode == 0) {
+    const int ke = (K + 1) / 2, ko = K / 2;
+    kp = (ke + a.kc - 1) / a.kc * a.kc;
+    nk0 = (ke + a.kc - 1) / a.kc;
+    nk1 = (ko + a.kc - 1) / a.kc;
+    xb = a.xbase[m];
+  } else {
+    nk0 = nk1 = (a.nh + a.kc - 1) / a.kc;
+  }
+  const int total = nk0 + nk1;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(a.tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < TC_NS; ++s) {
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&empty[s]), 1);
+    }
+    mbar_init(smem_u32(done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+
+  if (tid == 0) {  // ---- TMA producer
+    int fills[TC_NS] = {0, 0, 0};
+    for (int i = 0; i < total; ++i) {
+      const int s = i % TC_NS, u = i / TC_NS;
+      if (u >= 1 && !mbar_wait(smem_u32(&empty[s]), (u - 1) & 1, a.err, 1)) break;
+      const int acc = (i < nk0) ? 0 : 1, kk = acc ? i - nk0 : i;
+      unsigned char* st = sm + s * stage_bytes;
+      const uint32_t fb = smem_u32(&full[s]);
+      mbar_expect_tx(fb, stage_bytes);
+      const CUtensorMap* ah = acc ? &mA1h : &mA0h;
+      const CUtensorMap* al = acc ? &mA1l : &mA0l;
+      if (a.mode == 0) {
+        const int x = (int)(xb + (long)acc * kp + (long)kk * a.kc);
+        tma_2d(smem_u32(st), ah, x, a.coff + c0, fb);
+        tma_2d(smem_u32(st + bytesA), al, x, a.coff + c0, fb);
+        const int xt = acc * a.kepad + kk * a.kc;
+        tma_3d(smem_u32(st + 2 * bytesA), &mBh, xt, n0, m, fb);
+        tma_3d(smem_u32(st + 2 * bytesA + bytesB), &mBl, xt, n0, m, fb);
+      } else {
+        const int x = kk * a.kc;
+        tma_3d(smem_u32(st), ah, x, c0, m, fb);
+        tma_3d(smem_u32(st + bytesA), al, x, c0, m, fb);
+        const int yt = acc * a.kirows + n0;
+        tma_3d(smem_u32(st + 2 * bytesA), &mBh, x, yt, m, fb);
+        tma_3d(smem_u32(st + 2 * bytesA + bytesB), &mBl, x, yt, m, fb);
+      }
+      ++fills[s];
+    }
+    // never leave with copies in flight into this CTA's shared memory
+    for (int s = 0; s < TC_NS; ++s)
+      if (fills[s] > 0) mbar_wait(smem_u32(&full[s]), (fills[s] - 1) & 1, a.err, 2);
+  } else if (tid == 32) {  // ---- MMA issuer
+    for (int i = 0; i < total; ++i) {
+      const int s = i % TC_NS, u = i / TC_NS;
+      if (!mbar_wait(smem_u32(&full[s]), u & 1, a.err, 3)) break;
+      tc_fence_after();
+      const int acc = (i < nk0) ? 0 : 1, kk = acc ? i - nk0 : i;
+      unsigned char* st = sm + s * stage_bytes;
+      const uint64_t dah = smem_desc(smem_u32(st)), dal = smem_desc(smem_u32(st + bytesA));
+      const uint64_t dbh = smem_desc(smem_u32(st + 2 * bytesA)), dbl = smem_desc(smem_u32(st + 2 * bytesA + bytesB));
+      const uint32_t d = tbase + (uint32_t)(acc * N);
+#pragma unroll
+      for (int k4 = 0; k4 < 4; ++k4) {  // 4 MMAs of K = 32 bytes per 128-byte row
+        const uint64_t o = (uint64_t)(2 * k4);
+        mma<KIND>(d, dah + o, dbh + o, a.idesc, (kk > 0 || k4 > 0) ? 1u : 0u);
+        mma<KIND>(d, dah + o, dbl + o, a.idesc, 1u);
+        mma<KIND>(d, dal + o, dbh + o, a.idesc, 1u);
+      }
+      mma_commit(smem_u32(&empty[s]));
+    }
+    mma_commit(smem_u32(done));  // all issued MMAs complete -> done
+  }
+  __syncwarp();
+  // ---- epilogue: warp w holds TMEM lanes 32w..32w+31 = columns c0+32w+lane
+  const bool ok = mbar_wait(smem_u32(done), 0, a.err, 4);
+  tc_fence_after();
+  // warp-uniform decision: tcgen05.ld is a .sync.aligned warp instruction
+  const bool go = __all_sync(0xffffffffu, ok && *(volatile int*)a.err == 0);
+  if (go) {
+    const int c = c0 + warp * 32 + lane;
+    const uint32_t tw = tbase + ((uint32_t)(warp * 32) << 16);
+    for (int g = 0; g < N; g += 16) {
+      float e[16], o[16];
+      tmem_ld16(tw + g, e);
+      if (nk1 > 0)
+        tmem_ld16(tw + N + g, o);
+      else
+#pragma unroll
+        for (int q = 0; q < 16; ++q) o[q] = 0.f;
+      if (c < a.ncols) {
+        if (a.mode == 0) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int j = n0 + g + q;
+            if (j < a.nh) {
+              a.out[((long)m * a.nlat + j) * a.ldout + c] = e[q] + o[q];
+              a.out[((long)m * a.nlat + (a.nlat - 1 - j)) * a.ldout + c] = a.parityH ? o[q] - e[q] : e[q] - o[q];
+            }
+          }
+        } else {
+          const long base = a.moff[m];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int qe = 2 * (n0 + g + q), qo = qe + 1;
+            if (qe < K) a.out[(base + qe) * a.ldout + c] = e[q];
+            if (qo < K) a.out[(base + qo) * a.ldout + c] = o[q];
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(a.tmem_cols));
+}
+
+// ------------------------------------------------------------ host side --
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    GD_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p) throw CudaError("cuTensorMapEncodeTiled unavailable");
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+static void make_map(CUtensorMap* m, void* base, int kind, int rank, const uint64_t* dims, int box_inner,
+                     int box_rows) {
+  const size_t es = kind == TC_TF32 ? 4 : 2;
+  cuuint64_t gd[3], gs[2];
+  cuuint32_t bx[3], estr[3] = {1, 1, 1};
+  for (int i = 0; i < rank; ++i) gd[i] = dims[i];
+  gs[0] = dims[0] * es;
+  if (rank == 3) gs[1] = dims[0] * dims[1] * es;
+  bx[0] = box_inner;
+  bx[1] = box_rows;
+  bx[2] = 1;
+  CUresult r = encode_fn()(m, kind == TC_TF32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                           rank, base, gd, gs, bx, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw CudaError("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+}
+
+static int round_up(int x, int a) { return (x + a - 1) / a * a; }
+// N tile: multiple of 16, at most 160 so that three stages of
+// (2 x 128 + 2 x N) rows of 128 bytes fit in 227 KB of shared memory
+static int tile_n(int n) {
+  int nt = (n + 159) / 160;
+  return round_up((n + nt - 1) / nt, 16);
+}
+
+static void* tc_alloc(TcPlan& p, size_t bytes) {
+  void* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, std::max<size_t>(bytes, 16));
+  if (e != cudaSuccess) throw CudaError(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  p.allocs.push_back(d);
+  return d;
+}
+
+void tc_init(TcPlan& p, int kind, int T, int nh, int nlat, int ncap, const long* d_toff, const double* P64,
+             const double* H64, cudaStream_t s) {
+  p.kind = kind;
+  p.T = T;
+  p.nh = nh;
+  p.nlat = nlat;
+  p.esize = kind == TC_TF32 ? 4 : 2;
+  p.kc = 128 / p.esize;
+  const int kemax = (T + 2) / 2;  // even-degree count of m = 0
+  p.kepad = round_up(kemax, p.kc);
+  p.nhpad = round_up(nh, p.kc);
+  p.nsyn = tile_n(nh);
+  p.nana = tile_n(kemax);
+  p.kirows = round_up(kemax, p.nana);
+  p.ncap = round_up(ncap, 32);
+  p.xbase.assign(T + 1, 0);
+  long x = 0;
+  std::vector<int> xmap;
+  for (int m = 0; m <= T; ++m) {
+    const int K = T - m + 1, ke = (K + 1) / 2, kp = round_up(ke, p.kc);
+    p.xbase[m] = x;
+    x += 2L * kp;
+  }
+  p.xlen = x;
+  const size_t es = p.esize;
+  // tables
+  const long nsyn = (long)(T + 1) * nh * 2 * p.kepad, nana = (long)(T + 1) * 2 * p.kirows * p.nhpad;
+  for (int t = 0; t < 2; ++t)
+    for (int h = 0; h < 2; ++h) {
+      p.tsyn[t][h] = tc_alloc(p, nsyn * es);
+      p.tana[t][h] = tc_alloc(p, nana * es);
+    }
+  for (int t = 0; t < 2; ++t) {
+    const double* tab = t ? H64 : P64;
+    if (kind == TC_TF32) {
+      k_tc_tab_syn<TC_TF32><<<2048, 256, 0, s>>>(T, nh, p.kepad, d_toff, tab, (uint32_t*)p.tsyn[t][0],
+                                                 (uint32_t*)p.tsyn[t][1]);
+      k_tc_tab_ana<TC_TF32><<<2048, 256, 0, s>>>(T, nh, p.kirows, p.nhpad, d_toff, tab, (uint32_t*)p.tana[t][0],
+                                                 (uint32_t*)p.tana[t][1]);
+    } else {
+      k_tc_tab_syn<TC_BF16><<<2048, 256, 0, s>>>(T, nh, p.kepad, d_toff, tab, (__nv_bfloat16*)p.tsyn[t][0],
+                                                 (__nv_bfloat16*)p.tsyn[t][1]);
+      k_tc_tab_ana<TC_BF16><<<2048, 256, 0, s>>>(T, nh, p.kirows, p.nhpad, d_toff, tab,
+                                                 (__nv_bfloat16*)p.tana[t][0], (__nv_bfloat16*)p.tana[t][1]);
+    }
+    count_launch(2);
+    GD_LAUNCH_CHECK();
+  }
+  // staging
+  for (int h = 0; h < 2; ++h) {
+    p.x[h] = tc_alloc(p, (size_t)p.ncap * p.xlen * es);
+    p.gp[h] = tc_alloc(p, (size_t)(T + 1) * p.ncap * p.nhpad * es);
+    p.gm[h] = tc_alloc(p, (size_t)(T + 1) * p.ncap * p.nhpad * es);
+    GD_CUDA(cudaMemsetAsync(p.x[h], 0, (size_t)p.ncap * p.xlen * es, s));
+  }
+  p.d_xbase = (long*)tc_alloc(p, sizeof(long) * (T + 1));
+  GD_CUDA(cudaMemcpyAsync(p.d_xbase, p.xbase.data(), sizeof(long) * (T + 1), cudaMemcpyHostToDevice, s));
+  p.d_err = (int*)tc_alloc(p, sizeof(int));
+  GD_CUDA(cudaMemsetAsync(p.d_err, 0, sizeof(int), s));
+  // tensor maps
+  for (int t = 0; t < 2; ++t)
+    for (int h = 0; h < 2; ++h) {
+      uint64_t ds[3] = {(uint64_t)2 * p.kepad, (uint64_t)nh, (uint64_t)T + 1};
+      make_map(&p.m_tsyn[t][h], p.tsyn[t][h], kind, 3, ds, p.kc, p.nsyn);
+      uint64_t da[3] = {(uint64_t)p.nhpad, (uint64_t)2 * p.kirows, (uint64_t)T + 1};
+      make_map(&p.m_tana[t][h], p.tana[t][h], kind, 3, da, p.kc, p.nana);
+    }
+  for (int h = 0; h < 2; ++h) {
+    uint64_t dx[2] = {(uint64_t)p.xlen, (uint64_t)p.ncap};
+    make_map(&p.m_x[h], p.x[h], kind, 2, dx, p.kc, TC_M);
+    uint64_t dg[3] = {(uint64_t)p.nhpad, (uint64_t)p.ncap, (uint64_t)T + 1};
+    make_map(&p.m_gp[h], p.gp[h], kind, 3, dg, p.kc, TC_M);
+    make_map(&p.m_gm[h], p.gm[h], kind, 3, dg, p.kc, TC_M);
+  }
+  GD_CUDA(cudaStreamSynchronize(s));
+}
+
+void tc_free(TcPlan& p) {
+  for (void* d : p.allocs) cudaFree(d);
+  p.allocs.clear();
+  p.item_cache.clear();
+  p.d_xmap = nullptr;
+}
+
+static uint32_t make_idesc(int kind, int N) {
+  const uint32_t fmt = kind == TC_TF32 ? 2u : 1u;  // TF32 (kind::tf32) or BF16 (kind::f16)
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+}
+
+static uint32_t tmem_cols_for(int N) {
+  uint32_t c = 32;
+  while (c < (uint32_t)(2 * N)) c <<= 1;
+  return c;
+}
+
+static size_t smem_for(int N) { return (size_t)TC_NS * (2 * TC_M * 128 + 2 * N * 128) + 1024 + 256; }
+
+template <int KIND>
+static void launch_gemm(const TcPlan& p, const CUtensorMap& a0h, const CUtensorMap& a0l, const CUtensorMap& a1h,
+                        const CUtensorMap& a1l, const CUtensorMap& bh, const CUtensorMap& bl, TcArgs& args,
+                        int nitems, cudaStream_t s) {
+  const size_t sm = smem_for(args.N);
+  if (sm > 227 * 1024 || args.N > 160 || args.N % 16) throw std::runtime_error("tc gemm: bad N tile");
+  static bool attr = false;
+  if (!attr) {
+    GD_CUDA(cudaFuncSetAttribute(k_tc_gemm<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    attr = true;
+  }
+  k_tc_gemm<KIND><<<nitems, TC_THREADS, sm, s>>>(a0h, a0l, a1h, a1l, bh, bl, args);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+
+static int4* cached_items(TcPlan& p, long key, const std::vector<int4>& it) {
+  for (auto& kv : p.item_cache)
+    if (kv.first == key) return kv.second;
+  int4* d = nullptr;
+  GD_CUDA(cudaMalloc(&d, sizeof(int4) * std::max<size_t>(it.size(), 1)));
+  GD_CUDA(cudaMemcpy(d, it.data(), sizeof(int4) * it.size(), cudaMemcpyHostToDevice));
+  p.item_cache.push_back({key, d});
+  p.allocs.push_back(d);
+  return d;
+}
+
+void tc_synth(TcPlan& p, const long* d_moff, bool useH, const float* B, long ldB, int ncols, float* F, long ldF,
+              cudaStream_t s) {
+  if (ncols > p.ncap) throw std::runtime_error("tc_synth: too many columns");
+  // 1) split the spectral columns into the padded K-major staging
+  if (!p.d_xmap) {
+    std::vector<long> hm(p.T + 2);
+    hm[0] = 0;
+    for (int m = 0; m <= p.T; ++m) hm[m + 1] = hm[m] + (p.T - m + 1);
+    std::vector<int> xm(p.xlen, -1);
+    for (int m = 0; m <= p.T; ++m) {
+      const int K = p.T - m + 1, ke = (K + 1) / 2, kp = round_up(ke, p.kc);
+      for (int par = 0; par < 2; ++par)
+        for (int i = 0; i < kp; ++i) {
+          const int q = 2 * i + par;
+          if (q < K) xm[p.xbase[m] + (long)par * kp + i] = (int)(hm[m] + q);
+        }
+    }
+    p.d_xmap = (int*)tc_alloc(p, sizeof(int) * p.xlen);
+    GD_CUDA(cudaMemcpy(p.d_xmap, xm.data(), sizeof(int) * p.xlen, cudaMemcpyHostToDevice));
+  }
+  dim3 g((unsigned)((p.xlen + 31) / 32), (unsigned)((ncols + 31) / 32)), b(32, 8);
+  if (p.kind == TC_TF32)
+    k_tc_split_x<TC_TF32><<<g, b, 0, s>>>(B, ldB, ncols, p.d_xmap, p.xlen, (uint32_t*)p.x[0], (uint32_t*)p.x[1]);
+  else
+    k_tc_split_x<TC_BF16><<<g, b, 0, s>>>(B, ldB, ncols, p.d_xmap, p.xlen, (__nv_bfloat16*)p.x[0],
+                                          (__nv_bfloat16*)p.x[1]);
+  count_launch();
+  GD_LAUNCH_CHECK();
+  // 2) GEMM
+  const int ct = (ncols + TC_M - 1) / TC_M, nt = (p.nh + p.nsyn - 1) / p.nsyn;
+  std::vector<int4> it;
+  for (int m = 0; m <= p.T; ++m)
+    for (int a = 0; a < ct; ++a)
+      for (int b2 = 0; b2 < nt; ++b2) it.push_back(make_int4(m, a, b2, 0));
+  int4* dit = cached_items(p, ((long)ncols << 2) | 0, it);
+  TcArgs args;
+  args.items = dit;
+  args.mode = 0;
+  args.T = p.T;
+  args.nh = p.nh;
+  args.nlat = p.nlat;
+  args.N = p.nsyn;
+  args.kc = p.kc;
+  args.kepad = p.kepad;
+  args.kirows = p.kirows;
+  args.xbase = p.d_xbase;
+  args.moff = d_moff;
+  args.parityH = useH ? 1 : 0;
+  args.ncols = ncols;
+  args.coff = 0;
+  args.out = F;
+  args.ldout = ldF;
+  args.err = p.d_err;
+  args.idesc = make_idesc(p.kind, p.nsyn);
+  args.tmem_cols = tmem_cols_for(p.nsyn);
+  const int t = useH ? 1 : 0;
+  if (p.kind == TC_TF32)
+    launch_gemm<TC_TF32>(p, p.m_x[0], p.m_x[1], p.m_x[0], p.m_x[1], p.m_tsyn[t][0], p.m_tsyn[t][1], args,
+                         (int)it.size(), s);
+  else
+    launch_gemm<TC_BF16>(p, p.m_x[0], p.m_x[1], p.m_x[0], p.m_x[1], p.m_tsyn[t][0], p.m_tsyn[t][1], args,
+                         (int)it.size(), s);
+}
+
+void tc_anal(TcPlan& p, const long* d_moff, bool useH, const float* G, long ldG, int ncols, float* A, long ldA,
+             cudaStream_t s) {
+  if (ncols > p.ncap) throw std::runtime_error("tc_anal: too many columns");
+  dim3 g((unsigned)((p.nhpad + 31) / 32), (unsigned)((ncols + 31) / 32), (unsigned)(p.T + 1)), b(32, 8);
+  if (p.kind == TC_TF32)
+    k_tc_split_g<TC_TF32><<<g, b, 0, s>>>(G, ldG, ncols, p.nh, p.nlat, p.nhpad, p.ncap, (uint32_t*)p.gp[0],
+                                          (uint32_t*)p.gp[1], (uint32_t*)p.gm[0], (uint32_t*)p.gm[1]);
+  else
+    k_tc_split_g<TC_BF16><<<g, b, 0, s>>>(G, ldG, ncols, p.nh, p.nlat, p.nhpad, p.ncap, (__nv_bfloat16*)p.gp[0],
+                                          (__nv_bfloat16*)p.gp[1], (__nv_bfloat16*)p.gm[0],
+                                          (__nv_bfloat16*)p.gm[1]);
+  count_launch();
+  GD_LAUNCH_CHECK();
+  const int ct = (ncols + TC_M - 1) / TC_M;
+  std::vector<int4> it;
+  for (int m = 0; m <= p.T; ++m) {
+    const int ke = (p.T - m + 2) / 2;
+    for (int a = 0; a < ct; ++a)
+      for (int b2 = 0; b2 < (ke + p.nana - 1) / p.nana; ++b2) it.push_back(make_int4(m, a, b2, 0));
+  }
+  int4* dit = cached_items(p, ((long)ncols << 2) | 1, it);
+  TcArgs args;
+  args.items = dit;
+  args.mode = 1;
+  args.T = p.T;
+  args.nh = p.nh;
+  args.nlat = p.nlat;
+  args.N = p.nana;
+  args.kc = p.kc;
+  args.kepad = p.kepad;
+  args.kirows = p.kirows;
+  args.xbase = p.d_xbase;
+  args.moff = d_moff;
+  args.parityH = useH ? 1 : 0;
+  args.ncols = ncols;
+  args.coff = 0;
+  args.out = A;
+  args.ldout = ldA;
+  args.err = p.d_err;
+  args.idesc = make_idesc(p.kind, p.nana);
+  args.tmem_cols = tmem_cols_for(p.nana);
+  const int t = useH ? 1 : 0;
+  // P: even degrees pair with G_N + G_S, odd with G_N - G_S; dP/dphi the reverse
+  const CUtensorMap* e0 = useH ? p.m_gm : p.m_gp;
+  const CUtensorMap* e1 = useH ? p.m_gp : p.m_gm;
+  if (p.kind == TC_TF32)
+    launch_gemm<TC_TF32>(p, e0[0], e0[1], e1[0], e1[1], p.m_tana[t][0], p.m_tana[t][1], args, (int)it.size(), s);
+  else
+    launch_gemm<TC_BF16>(p, e0[0], e0[1], e1[0], e1[1], p.m_tana[t][0], p.m_tana[t][1], args, (int)it.size(), s);
+}
+
+int tc_check(TcPlan& p, cudaStream_t s) {
+  int h = 0;
+  GD_CUDA(cudaMemcpyAsync(&h, p.d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GD_CUDA(cudaStreamSynchronize(s));
+  if (h) GD_CUDA(cudaMemsetAsync(p.d_err, 0, sizeof(int), s));
+  return h;
+}
+
+}  // namespace gd

@@ -1,0 +1,56 @@
+// gd_tc.cuh -- split-precision (TF32x3 / BF16x3) Legendre GEMMs on the
+// sm_103a tensor cores (tcgen05 + TMEM + TMA).  Declarations.
+#pragma once
+#include <cuda.h>
+
+#include "gd_kernels.h"
+
+namespace gd {
+
+enum TcKind { TC_TF32 = 0, TC_BF16 = 1 };
+
+// Tables and staging buffers of the tensor-core Legendre path for one grid.
+struct TcPlan {
+  int kind = TC_TF32;
+  int T = 0, nh = 0, nlat = 0;
+  int esize = 4;    // bytes per operand element (4 tf32, 2 bf16)
+  int kc = 32;      // K elements per 128-byte swizzle row
+  int kepad = 0;    // padded even/odd K extent of the synthesis tables
+  int nhpad = 0;    // padded latitude extent of the analysis operands
+  int nsyn = 0;     // N tile (latitudes) of the synthesis GEMM
+  int nana = 0;     // N tile (degrees per parity) of the analysis GEMM
+  int kirows = 0;   // rows per parity of the analysis tables
+  int ncap = 0;     // real-column capacity of the staging buffers
+  long xlen = 0;    // padded spectral length of the synthesis operand
+  std::vector<long> xbase;  // [T+1] start of order m in the padded layout
+  long* d_xbase = nullptr;
+  // tables: synthesis [m][j][2*kepad], analysis [m][2*kirows][nhpad]; hi/lo
+  void* tsyn[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [P/H][hi/lo]
+  void* tana[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  // staging: X [ncap][xlen] hi/lo; G+- [T+1][ncap][nhpad] hi/lo
+  void* x[2] = {nullptr, nullptr};
+  void* gp[2] = {nullptr, nullptr};
+  void* gm[2] = {nullptr, nullptr};
+  CUtensorMap m_tsyn[2][2], m_tana[2][2], m_x[2], m_gp[2], m_gm[2];
+  std::vector<std::pair<long, int4*>> item_cache;  // work lists by (ncols, direction)
+  int* d_xmap = nullptr;  // padded synthesis position -> spectral index (or -1)
+  int* d_err = nullptr;   // device error flag (bounded waits)
+  std::vector<void*> allocs;
+};
+
+// Builds tables (from the FP64 tables), staging buffers and tensor maps.
+void tc_init(TcPlan& p, int kind, int T, int nh, int nlat, int ncap, const long* d_toff, const double* P64,
+             const double* H64, cudaStream_t s);
+void tc_free(TcPlan& p);
+
+// F[m][j][c] (real columns c0.. of the GEMM) = Legendre synthesis of the
+// real columns [0, ncols) of B[idx][.] (row pitch ldB), tensor-core path.
+void tc_synth(TcPlan& p, const long* d_moff, bool useH, const float* B, long ldB, int ncols, float* F, long ldF,
+              cudaStream_t s);
+// A[idx][c] = Legendre analysis of G[m][j][c] (real columns [0, ncols)).
+void tc_anal(TcPlan& p, const long* d_moff, bool useH, const float* G, long ldG, int ncols, float* A, long ldA,
+             cudaStream_t s);
+// returns and clears the device error flag (nonzero: a bounded wait gave up)
+int tc_check(TcPlan& p, cudaStream_t s);
+
+}  // namespace gd

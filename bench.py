@@ -338,7 +338,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gd", choices=["gd", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "tf32x3", "bf16x3"])
+    ap.add_argument("--precision", default="tf32x3", choices=["fp64", "fp32", "tf32x3", "bf16x3"])
     ap.add_argument("--workload", default="T574L64", choices=list(WORKLOADS))
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-levels", type=int, default=16)

@@ -120,9 +120,13 @@ class Dycore : public DycoreBase {
   std::unique_ptr<TcPlan> tcp;
   double *P64keep = nullptr, *H64keep = nullptr;
   bool split_mode() const { return c.precision == GD_PREC_TF32X3 || c.precision == GD_PREC_BF16X3; }
+  std::map<int, GemmPlan> synth0_cache, anal0_cache;  // order-0-only SIMT work lists
   void do_synth(bool useH, const GemmPlan& plan, const R* B, long ldB, int ncr, R* F, long ldF) {
     if constexpr (std::is_same<R, float>::value) {
       if (tcp) {
+        auto it = synth0_cache.find(ncr);
+        if (it == synth0_cache.end()) it = synth0_cache.emplace(ncr, make_synth_plan(T, nh, ncr, stream, 0, 0)).first;
+        launch_synth<R>(sd, useH, it->second, B, ldB, ncr, F, ldF, stream);
         tc_synth(*tcp, moff, useH, B, ldB, ncr, F, ldF, stream);
         return;
       }
@@ -132,6 +136,9 @@ class Dycore : public DycoreBase {
   void do_anal(bool useH, const GemmPlan& plan, const R* G, long ldG, int ncr, R* A, long ldA) {
     if constexpr (std::is_same<R, float>::value) {
       if (tcp) {
+        auto it = anal0_cache.find(ncr);
+        if (it == anal0_cache.end()) it = anal0_cache.emplace(ncr, make_anal_plan(T, ncr, stream, 0, 0)).first;
+        launch_anal<R>(sd, useH, it->second, G, ldG, ncr, A, ldA, stream);
         tc_anal(*tcp, moff, useH, G, ldG, ncr, A, ldA, stream);
         return;
       }
@@ -205,6 +212,8 @@ class Dycore : public DycoreBase {
     free_plan(anaPhys);
     for (auto& kv : synth_cache) free_plan(kv.second);
     for (auto& kv : anal_cache) free_plan(kv.second);
+    for (auto& kv : synth0_cache) free_plan(kv.second);
+    for (auto& kv : anal0_cache) free_plan(kv.second);
     free_fft_plan(c2rFull);
     free_fft_plan(c2rInv);
     free_fft_plan(r2cDyn);

@@ -36,8 +36,9 @@ struct GemmPlan {
   int4* items = nullptr;  // device work list
   int nitems = 0;
 };
-GemmPlan make_synth_plan(int T, int nh, int ncols_real, cudaStream_t s);
-GemmPlan make_anal_plan(int T, int ncols_real, cudaStream_t s);
+// work lists over orders m in [m_lo, m_hi] (default: all orders)
+GemmPlan make_synth_plan(int T, int nh, int ncols_real, cudaStream_t s, int m_lo = 0, int m_hi = -1);
+GemmPlan make_anal_plan(int T, int ncols_real, cudaStream_t s, int m_lo = 0, int m_hi = -1);
 void free_plan(GemmPlan& p);
 template <typename R>
 void launch_synth(const ShtDev<R>& d, bool useH, const GemmPlan& plan, const R* B, long ldB, int ncols_real,

@@ -136,10 +136,11 @@ template void launch_convert<float>(const double*, float*, long, cudaStream_t);
 // by 16 for conflict-free shared reads and coalesced stores).
 constexpr int GT_R = 32, GT_C = 64, GT_K = 16;
 
-GemmPlan make_synth_plan(int T, int nh, int ncols_real, cudaStream_t s) {
+GemmPlan make_synth_plan(int T, int nh, int ncols_real, cudaStream_t s, int m_lo, int m_hi) {
   std::vector<int4> it;
   int tj = ceil_div(nh, GT_R), tc = ceil_div(ncols_real, GT_C);
-  for (int m = 0; m <= T; ++m)  // longest K first for load balance
+  if (m_hi < 0) m_hi = T;
+  for (int m = m_lo; m <= m_hi; ++m)  // longest K first for load balance
     for (int a = 0; a < tj; ++a)
       for (int b = 0; b < tc; ++b) it.push_back(make_int4(m, a, b, 0));
   GemmPlan p;
@@ -150,10 +151,11 @@ GemmPlan make_synth_plan(int T, int nh, int ncols_real, cudaStream_t s) {
   return p;
 }
 
-GemmPlan make_anal_plan(int T, int ncols_real, cudaStream_t s) {
+GemmPlan make_anal_plan(int T, int ncols_real, cudaStream_t s, int m_lo, int m_hi) {
   std::vector<int4> it;
   int tc = ceil_div(ncols_real, GT_C);
-  for (int m = 0; m <= T; ++m)
+  if (m_hi < 0) m_hi = T;
+  for (int m = m_lo; m <= m_hi; ++m)
     for (int a = 0; a < ceil_div(T - m + 1, GT_R); ++a)
       for (int b = 0; b < tc; ++b) it.push_back(make_int4(m, a, b, 0));
   GemmPlan p;

@@ -3,6 +3,9 @@
 // The per-order Legendre contractions of the transforms (the work SHTns
 // does inside shtns_sh_to_spat / shtns_spat_to_sh and the vector forms
 // behind src/shtns.f90) as tcgen05 MMAs with FP32 accumulators in TMEM.
+// Orders m >= 1 only: the tensor-core FP32 accumulation is not IEEE
+// round-to-nearest, and fields with a large global mean (ln ps, T) carry
+// it in order 0, so order 0 runs on the SIMT FMA path.
 // Each FP32 operand x is carried as hi + lo, hi = round(x) and
 // lo = round(x - hi) to TF32 (kind::tf32) or BF16 (kind::f16), and the
 // product is hi*hi + hi*lo + lo*hi ("x3").  The Legendre tables are split
@@ -634,9 +637,10 @@ void tc_synth(TcPlan& p, const long* d_moff, bool useH, const float* B, long ldB
   // 2) GEMM
   const int ct = (ncols + TC_M - 1) / TC_M, nt = (p.nh + p.nsyn - 1) / p.nsyn;
   std::vector<int4> it;
-  for (int m = 0; m <= p.T; ++m)
+  for (int m = 1; m <= p.T; ++m)  // order 0 (zonal means) runs on the IEEE SIMT path
     for (int a = 0; a < ct; ++a)
       for (int b2 = 0; b2 < nt; ++b2) it.push_back(make_int4(m, a, b2, 0));
+  if (it.empty()) return;
   int4* dit = cached_items(p, ((long)ncols << 2) | 0, it);
   TcArgs args;
   args.items = dit;
@@ -682,11 +686,12 @@ void tc_anal(TcPlan& p, const long* d_moff, bool useH, const float* G, long ldG,
   GD_LAUNCH_CHECK();
   const int ct = (ncols + TC_M - 1) / TC_M;
   std::vector<int4> it;
-  for (int m = 0; m <= p.T; ++m) {
+  for (int m = 1; m <= p.T; ++m) {  // order 0 runs on the IEEE SIMT path
     const int ke = (p.T - m + 2) / 2;
     for (int a = 0; a < ct; ++a)
       for (int b2 = 0; b2 < (ke + p.nana - 1) / p.nana; ++b2) it.push_back(make_int4(m, a, b2, 0));
   }
+  if (it.empty()) return;
   int4* dit = cached_items(p, ((long)ncols << 2) | 1, it);
   TcArgs args;
   args.items = dit;

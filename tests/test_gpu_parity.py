@@ -161,7 +161,7 @@ def test_step_fp32_close_to_fp64(oracle_mod):
     a, b = g.get_state(), o.get_state()
     assert rel(a["tv"], b["tv"]) < 1e-5
     assert rel(a["vrt"], b["vrt"]) < 1e-3
-    assert rel(a["lnps"], b["lnps"]) < 1e-5
+    assert rel(a["lnps"], b["lnps"]) < 2e-6
 
 
 def test_launch_count_and_graph_replay(oracle_mod):
@@ -232,4 +232,4 @@ def test_step_split_close_to_fp64(oracle_mod, prec):
     a, b = g.get_state(), o.get_state()
     assert rel(a["tv"], b["tv"]) < 1e-5
     assert rel(a["vrt"], b["vrt"]) < (2e-3 if prec == "tf32x3" else 2e-2)
-    assert rel(a["lnps"], b["lnps"]) < 1e-5
+    assert rel(a["lnps"], b["lnps"]) < 2e-6

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libgdcore.so")
-SOURCES = ["gd_sht.cu", "gd_grid.cu", "gd_spec.cu", "gd_tc.cu", "gd_dycore.cu"]
+SOURCES = ["gd_sht.cu", "gd_grid.cu", "gd_spec.cu", "gd_tc.cu", "gd_dycore.cu", "gd_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", os.path.join(ROOT, "include"), "-I", CSRC]

@@ -32,6 +32,7 @@ API_FUNCTIONS = [
     "gd_getdyntend", "gd_getphytend", "gd_advance", "gd_spectogrd", "gd_grdtospec",
     "gd_getuv", "gd_getvrtdivspec", "gd_getgrad", "gd_grid_info", "gd_get_grid", "gd_diag",
     "gd_set_stream", "gd_sync", "gd_launch_count", "gd_last_error", "gd_profile_step",
+    "gd_diag_static",
 ]
 PHASES = ["legendre_synth", "fft_synth", "columns", "fft_anal", "legendre_anal", "semi_implicit",
           "physics", "other"]
@@ -81,6 +82,8 @@ def load(build_if_missing=True):
               "gd_grdtospec", "gd_getuv", "gd_getvrtdivspec", "gd_getgrad", "gd_grid_info",
               "gd_get_grid", "gd_diag", "gd_sync", "gd_profile_step"]:
         getattr(L, f).restype = ctypes.c_int
+    L.gd_diag_static.restype = ctypes.c_int
+    L.gd_diag_static.argtypes = [vp, vp, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]
     _lib = L
     return L
 

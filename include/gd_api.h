@@ -147,6 +147,27 @@ int gd_diag(gd_ctx* ctx, double* out5);
    advances by one step.  nphase must be >= 8. */
 int gd_profile_step(gd_ctx* ctx, double* ms, int nphase);
 
+/* Allocation-free step diagnostics.  This entry point has no counterpart in
+   the reference; it exists for callers that cannot call cudaMalloc (a host
+   model whose device memory belongs to another runtime's pool allocator,
+   or a process whose device-memory budget is fully committed).  It computes
+   what gd_diag reports (out4[0] spdmax, [1] min ps hPa, [2] max ps hPa,
+   [3] ps tendency RMS hPa/hr; src/run.f90:159-161) from caller-provided,
+   device-accessible arrays: ug, vg [nlev][nlat][nlon], psg and dlnpsdt
+   [nlat][nlon], gauwts [nlat] (Gauss weights, sum 2), out4 [4] doubles.
+   No context is needed and nothing is allocated: the per-latitude scratch
+   is a fixed device array of GD_DIAG_STATIC_MAX_NLAT rows that every GPU
+   loading the library holds until exit; nlat above that limit is rejected
+   with GD_ERR_ARG.  The first call on a device looks up that array's
+   address with the device current; make that first call before any stream
+   capture.  All calls share the array, so calls that overlap on the GPU
+   race.  Work is enqueued on stream (cudaStream_t as void*, NULL = legacy
+   default stream) and is complete when the stream is. */
+#define GD_DIAG_STATIC_MAX_NLAT 4096
+int gd_diag_static(const double* ug, const double* vg, int nlev, const double* psg,
+                   const double* dlnpsdt, const double* gauwts, int nlat, int nlon, double* out4,
+                   void* stream);
+
 /* Runs the context on an external CUDA stream (cudaStream_t as void*). */
 int gd_set_stream(gd_ctx* ctx, void* stream);
 /* Waits for all work of the context. */

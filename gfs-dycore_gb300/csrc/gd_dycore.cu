@@ -383,8 +383,16 @@ class Dycore : public DycoreBase {
     // the r_kind values (semimp_data.f90:130,216-234)
     for (auto* v : {&am, &bm, &sv, &to})
       for (auto& x : *v) x = (double)(R)x;
-    amhyb = upload(toR(am));
-    bmhyb = upload(toR(bm));
+    // the stage kernel reads the L x L operators transposed (coalesced over
+    // the output level): upload A^T, B^T, and invert Y^T = (inv Y)^T below
+    std::vector<double> amT((long)L * L), bmT((long)L * L);
+    for (int i = 0; i < L; ++i)
+      for (int j = 0; j < L; ++j) {
+        amT[(long)j * L + i] = am[(long)i * L + j];
+        bmT[(long)j * L + i] = bm[(long)i * L + j];
+      }
+    amhyb = upload(toR(amT));
+    bmhyb = upload(toR(bmT));
     svhyb = upload(toR(sv));
     tor = upload(toR(to));
     std::vector<double> ym((long)L * L);
@@ -400,7 +408,7 @@ class Dycore : public DycoreBase {
         double f = (consts[s] * c.dt) * (consts[s] * c.dt) * ((double)n * (n + 1));
         double* y = &Y[((long)s * (T + 1) + n) * L * L];
         for (int i = 0; i < L; ++i)
-          for (int j = 0; j < L; ++j) y[(long)i * L + j] = (i == j ? 1.0 : 0.0) + f * ym[(long)i * L + j];
+          for (int j = 0; j < L; ++j) y[(long)i * L + j] = (i == j ? 1.0 : 0.0) + f * ym[(long)j * L + i];
       }
     double* dY = dalloc<double>(Y.size());
     GD_CUDA(cudaMemcpyAsync(dY, Y.data(), Y.size() * sizeof(double), cudaMemcpyHostToDevice, stream));

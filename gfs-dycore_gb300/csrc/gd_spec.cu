@@ -26,21 +26,23 @@ __device__ __forceinline__ V vz() {
   return v;
 }
 
-// Y[k][i] = sum_j A[k][j] X[j][i] for i < cnt (complex X, real A)
+// Y[i][k] = sum_j A[k][j] X[i][j] for i < cnt (complex X, real A).  AT
+// holds A transposed (AT[j][k] = A[k][j]) so a warp's loads of one j are
+// contiguous over k; the L x L matrices stay L1-resident.  X, Y index-major.
 template <typename R, typename V>
-__device__ __forceinline__ void smem_matvec(const R* __restrict__ A, const V* X, V* Y, int L, int cnt) {
+__device__ __forceinline__ void smem_matvec(const R* __restrict__ AT, const V* X, V* Y, int L, int cnt) {
   for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {
-    const int k = e / cnt, i = e - k * cnt;
+    const int i = e / L, k = e - i * L;
     R ax = 0, ay = 0;
-    const R* Ar = A + (long)k * L;
+    const V* Xi = X + i * L;
     for (int j = 0; j < L; ++j) {
-      const R aj = Ar[j];
-      const V x = X[j * QC + i];
+      const R aj = AT[(long)j * L + k];
+      const V x = Xi[j];
       ax += aj * x.x;
       ay += aj * x.y;
     }
-    Y[k * QC + i].x = ax;
-    Y[k * QC + i].y = ay;
+    Y[i * L + k].x = ax;
+    Y[i * L + k].y = ay;
   }
 }
 
@@ -74,7 +76,7 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
   typedef typename C2<R>::T V;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int L = a.L;
-  V* TV = reinterpret_cast<V*>(smraw);  // [L][QC]
+  V* TV = reinterpret_cast<V*>(smraw);  // [QC][L], index-major
   V* DV = TV + L * QC;
   V* Y = DV + L * QC;
   V* Y2 = Y + L * QC;
@@ -90,10 +92,10 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
   auto IDX = [&](int i) -> long { return a.moff[m0 + i] + (n - m0 - i); };
 
   for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {
-    const int k = e / cnt, i = e - k * cnt;
+    const int i = e / L, k = e - i * L;
     const long idx = IDX(i);
-    TV[k * QC + i] = ld2(a.S, idx, a.ldS, a.sc.tv + k);
-    DV[k * QC + i] = ld2(a.S, idx, a.ldS, a.sc.div + k);
+    TV[i * L + k] = ld2(a.S, idx, a.ldS, a.sc.tv + k);
+    DV[i * L + k] = ld2(a.S, idx, a.ldS, a.sc.div + k);
   }
   for (int i = threadIdx.x; i < cnt; i += blockDim.x) LN[i] = ld2(a.S, IDX(i), a.ldS, a.sc.lnps);
   __syncthreads();
@@ -103,8 +105,8 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
       R sx = 0, sy = 0;
       for (int k = 0; k < L; ++k) {
-        sx += a.svhyb[k] * DV[k * QC + i].x;
-        sy += a.svhyb[k] * DV[k * QC + i].y;
+        sx += a.svhyb[k] * DV[i * L + k].x;
+        sy += a.svhyb[k] * DV[i * L + k].y;
       }
       Y3[i].x = sx;
       Y3[i].y = sy;
@@ -114,16 +116,16 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
   const R dt = a.dt;
   // nonlinear tendencies, explicit part of the update
   for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {
-    const int k = e / cnt, i = e - k * cnt;
+    const int i = e / L, k = e - i * L;
     const long idx = IDX(i);
     V dvrt, ddiv, dtv;
     raw_tend(a, idx, k, lap, dvrt, ddiv, dtv);
     V ddl = vz<V>(), dtl = vz<V>();
     if (!a.explicit_) {
-      ddl.x = -lap * (Y[k * QC + i].x + a.tor[k] * LN[i].x);
-      ddl.y = -lap * (Y[k * QC + i].y + a.tor[k] * LN[i].y);
-      dtl.x = -Y2[k * QC + i].x;
-      dtl.y = -Y2[k * QC + i].y;
+      ddl.x = -lap * (Y[i * L + k].x + a.tor[k] * LN[i].x);
+      ddl.y = -lap * (Y[i * L + k].y + a.tor[k] * LN[i].y);
+      dtl.x = -Y2[i * L + k].x;
+      dtl.y = -Y2[i * L + k].y;
       ddiv.x -= ddl.x;
       ddiv.y -= ddl.y;
       dtv.x -= dtl.x;
@@ -171,8 +173,8 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
     svv.x = a.rerth * il * vr.x;
     svv.y = a.rerth * il * vr.y;
     st2(a.S, idx, a.ldS, a.sc.s + k, svv);
-    DV[k * QC + i] = dv;
-    TV[k * QC + i] = tv;
+    DV[i * L + k] = dv;
+    TV[i * L + k] = tv;
     for (int iq = 0; iq < a.nt; ++iq) {  // tracers, always explicit
       const int col = iq * L + k;
       V dq = ld2(a.AP, idx, a.ldAP, a.ap.qtend + col);
@@ -227,11 +229,11 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
     smem_matvec<R, V>(a.amhyb, TV, Y, L, cnt);
     __syncthreads();
     for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {
-      const int k = e / cnt, i = e - k * cnt;
+      const int i = e / L, k = e - i * L;
       V r;
-      r.x = DV[k * QC + i].x - c * lap * dt * (Y[k * QC + i].x + a.tor[k] * LN[i].x);
-      r.y = DV[k * QC + i].y - c * lap * dt * (Y[k * QC + i].y + a.tor[k] * LN[i].y);
-      Y2[k * QC + i] = r;
+      r.x = DV[i * L + k].x - c * lap * dt * (Y[i * L + k].x + a.tor[k] * LN[i].x);
+      r.y = DV[i * L + k].y - c * lap * dt * (Y[i * L + k].y + a.tor[k] * LN[i].y);
+      Y2[i * L + k] = r;
     }
     __syncthreads();
     const R* D = a.dhyb + ((long)s * (a.T + 1) + n) * L * L;
@@ -241,17 +243,17 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
       R sx = 0, sy = 0;
       for (int k = 0; k < L; ++k) {
-        sx += a.svhyb[k] * DV[k * QC + i].x;
-        sy += a.svhyb[k] * DV[k * QC + i].y;
+        sx += a.svhyb[k] * DV[i * L + k].x;
+        sy += a.svhyb[k] * DV[i * L + k].y;
       }
       Y3[i].x = sx;
       Y3[i].y = sy;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {
-      const int k = e / cnt, i = e - k * cnt;
-      TV[k * QC + i].x -= c * dt * Y[k * QC + i].x;
-      TV[k * QC + i].y -= c * dt * Y[k * QC + i].y;
+      const int i = e / L, k = e - i * L;
+      TV[i * L + k].x -= c * dt * Y[i * L + k].x;
+      TV[i * L + k].y -= c * dt * Y[i * L + k].y;
     }
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
       LN[i].x -= c * dt * Y3[i].x;
@@ -260,9 +262,9 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
     __syncthreads();
   }
   for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {
-    const int k = e / cnt, i = e - k * cnt;
+    const int i = e / L, k = e - i * L;
     const long idx = IDX(i);
-    V dv = DV[k * QC + i], tv = TV[k * QC + i];
+    V dv = DV[i * L + k], tv = TV[i * L + k];
     if (a.final_) {
       const R fd = R(1) - (a.disspec[idx] * a.diff_prof[k] - a.dmp_prof[k]) * dt;
       const R ft = R(1) - a.disspec[idx] * a.diff_prof[k] * dt;

@@ -39,11 +39,11 @@ struct StageArgs {
   R* TD1;
   R* TD2;
   long ldTD;
-  const R* amhyb;  // [L][L] row-major (row = output level)
-  const R* bmhyb;
+  const R* amhyb;  // [L][L] transposed: amhyb[j][k] = A(k, j), k = output level
+  const R* bmhyb;  // transposed likewise
   const R* svhyb;  // [L]
   const R* tor;    // [L]
-  const R* dhyb;   // [3][T+1][L][L]
+  const R* dhyb;   // [3][T+1][L][L], each matrix transposed
   const R* disspec;
   const R* diff_prof;
   const R* dmp_prof;

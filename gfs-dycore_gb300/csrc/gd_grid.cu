@@ -27,6 +27,23 @@ __device__ __forceinline__ float epstiny_of<float>() {
 }
 
 constexpr int LMAX = 128;
+constexpr int NTMAX = 8;  // tracers handled in registers by the column kernel
+
+// Thuburn (1993) limited half-level value at interior interface k
+// (dyn_run.f90:574-590): qa = level above the interface, qb = level below,
+// dm = dd[k-1], d0 = dd[k], dp = dd[k+1], upwind by the sign of etadot.
+template <typename R>
+__device__ __forceinline__ R thuburn_half(R qa, R qb, R dm, R d0, R dp, R eta) {
+  R h = R(0.5) * (qb + qa);
+  if (eta > R(0)) {
+    const R phi = dm / d0;
+    h = qa + (phi + fabs(phi)) / (R(1) + fabs(phi)) * (h - qa);
+  } else {
+    const R phi = dp / d0;
+    h = qb + (phi + fabs(phi)) / (R(1) + fabs(phi)) * (h - qb);
+  }
+  return h;
+}
 
 template <typename R>
 __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int inverse_only) {
@@ -44,19 +61,20 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
 
   const R ps = exp(S(a.s.lnps));
   const R dlx = S(a.s.dlnpsdx), dly = S(a.s.dlnpsdy);
-  R DB[LMAX], CB[LMAX], CG[LMAX], RL[LMAX], AL[LMAX];
+  auto PK = [&](int t) -> R { return ak[t] + bk[t] * ps; };
+  // rlnp and alfa of the top-down layer t (pressure_data.f90:89-96)
+  auto RLN = [&](int t, R pkt, R pkt1) -> R { return (t == 0) ? a.rlnp_top : log(pkt1 / pkt); };
+  R DB[LMAX], CB[LMAX];
 
-  // calc_pressdata + getomega prefix sums (top to bottom)
-  R pk_t = ak[0] + bk[0] * ps;
+  // pass 1, top to bottom: getomega prefix sums (dyn_run.f90:327-337)
+  R pk_t = PK(0);
   R db = R(0), cb = R(0);
   for (int t = 0; t < L; ++t) {
     const int b = L - 1 - t;
-    const R pk_t1 = ak[t + 1] + bk[t + 1] * ps;
+    const R pk_t1 = PK(t + 1);
     const R dp = pk_t1 - pk_t;
-    const R rl = (t == 0) ? a.rlnp_top : log(pk_t1 / pk_t);
-    const R al = (t == 0) ? a.log2sp : R(1) - (pk_t / dp) * rl;
-    const R u = S(a.s.u + b), v = S(a.s.v + b), dv = S(a.s.div + b);
-    const R cg = u * dlx + v * dly;
+    const R cg = S(a.s.u + b) * dlx + S(a.s.v + b) * dly;
+    const R dv = S(a.s.div + b);
     if (t == 0) {
       db = dv * dp;
       cb = cg * dbk[0];
@@ -66,68 +84,86 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
     }
     DB[t] = db;
     CB[t] = cb;
-    CG[t] = cg;
-    RL[t] = rl;
-    AL[t] = al;
-    pk_t = pk_t1;
-    if (a.prs) {  // Phillips layer pressure (pressure_data.f90:87-88)
-      const R pkt = ak[t] + bk[t] * ps;
+    if (a.prs)  // Phillips layer pressure (pressure_data.f90:87-88)
       a.prs[(long)b * ng + p] =
-          pow((pow(pk_t1, a.kappa) * pk_t1 - pow(pkt, a.kappa) * pkt) / ((a.kappa + R(1)) * dp), R(1) / a.kappa);
-    }
+          pow((pow(pk_t1, a.kappa) * pk_t1 - pow(pk_t, a.kappa) * pk_t) / ((a.kappa + R(1)) * dp), R(1) / a.kappa);
+    pk_t = pk_t1;
   }
   const R dlnpsdt = -DB[L - 1] / ps - CB[L - 1];
   a.psg[p] = ps;
   a.dlnpsdt[p] = dlnpsdt;
-  auto etadot = [&](int t) -> R {
+  auto etadot = [&](int t) -> R {  // dyn_run.f90:340-344
     if (t == 0 || t == L) return R(0);
     return -ps * (bk[t] * dlnpsdt + CB[t - 1]) - DB[t - 1];
   };
-  auto dlnpdt = [&](int t, R dv_b) -> R {
-    const R pkt = ak[t] + bk[t] * ps, pkt1 = ak[t + 1] + bk[t + 1] * ps;
-    const R dp = pkt1 - pkt;
+  // omega/p of layer t (dyn_run.f90:347-368) from its cg, divergence, rlnp, alfa
+  auto dlnpdt = [&](int t, R cg, R dv, R dp, R rl, R al) -> R {
     R wb, wc;
     if (t == 0) {
-      wb = AL[0] * (dv_b * dp + ps * CB[0] * dbk[0]);
-      wc = ps * CG[0] * dbk[0];
+      wb = al * (dv * dp + ps * CB[0] * dbk[0]);
+      wc = ps * cg * dbk[0];
     } else {
-      wb = RL[t] * (DB[t - 1] + ps * CB[t - 1]) + AL[t] * (dv_b * dp + ps * CG[t] * dbk[t]);
-      wc = ps * CG[t] * (dbk[t] + a.ck[t] * RL[t] / dp);
+      wb = rl * (DB[t - 1] + ps * CB[t - 1]) + al * (dv * dp + ps * cg * dbk[t]);
+      wc = ps * cg * (dbk[t] + a.ck[t] * rl / dp);
     }
     return (wc - wb) / dp;
   };
   if (a.etadot)
     for (int t = 0; t <= L; ++t) a.etadot[(long)t * ng + p] = etadot(t);
   if (a.dlnpdtg)
-    for (int t = 0; t < L; ++t) a.dlnpdtg[(long)(L - 1 - t) * ng + p] = dlnpdt(t, S(a.s.div + L - 1 - t));
+    for (int t = 0; t < L; ++t) {
+      const int b = L - 1 - t;
+      const R pkt = PK(t), pkt1 = PK(t + 1), dp = pkt1 - pkt;
+      const R rl = RLN(t, pkt, pkt1), al = (t == 0) ? a.log2sp : R(1) - (pkt / dp) * rl;
+      const R cg = S(a.s.u + b) * dlx + S(a.s.v + b) * dly;
+      a.dlnpdtg[(long)b * ng + p] = dlnpdt(t, cg, S(a.s.div + b), dp, rl, al);
+    }
   if (inverse_only) return;
 
   R* gA = a.gA;
   auto A = [&](int row) -> R& { return gA[(long)row * ng + p]; };
   const R fcor = a.omega2 * a.sinlat[j];
   const R dphx = a.dphisdx[p], dphy = a.dphisdy[p];
-  // getpresgrad suffix recurrences, vertical advection and tendencies,
-  // bottom to top
+  const int nt = min(a.nt, NTMAX);
+  const R eps = epstiny_of<R>();
+  // tracer windows q[b-1..b+2], carried limited half-level value at the
+  // bottom interface of the current level (half[L] = q[0])
+  R qm1[NTMAX], q0[NTMAX], q1[NTMAX], q2[NTMAX], hb[NTMAX];
+#pragma unroll
+  for (int iq = 0; iq < NTMAX; ++iq)
+    if (iq < nt) {
+      const int r0 = a.s.trc + iq * L;
+      qm1[iq] = R(0);
+      q0[iq] = S(r0);
+      q1[iq] = (L > 1) ? S(r0 + 1) : R(0);
+      q2[iq] = (L > 2) ? S(r0 + 2) : R(0);
+      hb[iq] = q0[iq];
+    }
+  // pass 2, bottom to top: getpresgrad suffix recurrences (dyn_run.f90:416-434),
+  // vertical advection (getvadv, :453-476; getvadv_tracers, :478-603) and the
+  // tendencies (:190-292)
   R cofb2 = R(0), px3u = R(0), px3v = R(0);
-  R um = R(0), vm = R(0), tm = R(0), dxm = R(0), dym = R(0);  // level b-1
+  R um = R(0), vm = R(0), tm = R(0), dxm = R(0), dym = R(0), rlm = R(0);  // layer below
   R uc = S(a.s.u), vc = S(a.s.v), tc = S(a.s.tv);
   for (int b = 0; b < L; ++b) {
     const int t = L - 1 - b;
     const R dtx = S(a.s.dtvdx + b), dty = S(a.s.dtvdy + b);
-    if (b > 0) {
-      const R pk2 = ak[t + 2] + bk[t + 2] * ps, pk1 = ak[t + 1] + bk[t + 1] * ps;
-      cofb2 = cofb2 - rd * (bk[t + 2] / pk2 - bk[t + 1] / pk1) * tm;
-      px3u = px3u - rd * RL[t + 1] * dxm;
-      px3v = px3v - rd * RL[t + 1] * dym;
-    }
-    const R pkt = ak[t] + bk[t] * ps, pkt1 = ak[t + 1] + bk[t + 1] * ps;
+    const R pkt = PK(t), pkt1 = PK(t + 1);
     const R dp = pkt1 - pkt;
-    const R cofb1 = (t == 0) ? -(R(1) / dp) * (AL[0] * dbk[0]) : -(R(1) / dp) * (bk[t] * RL[t] + AL[t] * dbk[t]);
-    const R cofa = -(R(1) / dp) * (bk[t + 1] * pkt / pkt1 - bk[t] + RL[t] * (bk[t] - pkt * dbk[t] / dp));
-    const R prsgx = cofb1 * rd * tc * ps * dlx - dphx + cofb2 * ps * dlx + px3u - rd * AL[t] * dtx -
-                    cofa * rd * tc * ps * dlx;
-    const R prsgy = cofb1 * rd * tc * ps * dly - dphy + cofb2 * ps * dly + px3v - rd * AL[t] * dty -
-                    cofa * rd * tc * ps * dly;
+    const R rl = RLN(t, pkt, pkt1);
+    const R al = (t == 0) ? a.log2sp : R(1) - (pkt / dp) * rl;
+    if (b > 0) {
+      const R pk2 = PK(t + 2);
+      cofb2 = cofb2 - rd * (bk[t + 2] / pk2 - bk[t + 1] / pkt1) * tm;
+      px3u = px3u - rd * rlm * dxm;
+      px3v = px3v - rd * rlm * dym;
+    }
+    const R cofb1 = (t == 0) ? -(R(1) / dp) * (al * dbk[0]) : -(R(1) / dp) * (bk[t] * rl + al * dbk[t]);
+    const R cofa = -(R(1) / dp) * (bk[t + 1] * pkt / pkt1 - bk[t] + rl * (bk[t] - pkt * dbk[t] / dp));
+    const R prsgx =
+        cofb1 * rd * tc * ps * dlx - dphx + cofb2 * ps * dlx + px3u - rd * al * dtx - cofa * rd * tc * ps * dlx;
+    const R prsgy =
+        cofb1 * rd * tc * ps * dly - dphy + cofb2 * ps * dly + px3v - rd * al * dty - cofa * rd * tc * ps * dly;
     R up = R(0), vp = R(0), tp = R(0);
     if (b + 1 < L) {
       up = S(a.s.u + b + 1);
@@ -151,72 +187,69 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
     vv *= h;
     vt *= h;
     const R dv_b = S(a.s.div + b);
-    R vq = a.kappa * dlnpdt(t, dv_b) * tc;
-    if (a.nt > 0) vq = vq / (R(1) + a.cvap_cp * S(a.s.trc + b));
+    const R cg = uc * dlx + vc * dly;
+    R vq = a.kappa * dlnpdt(t, cg, dv_b, dp, rl, al) * tc;
+    if (a.nt > 0) vq = vq / (R(1) + a.cvap_cp * q0[0]);
     const R vadvv = vv - prsgy, vadvu = vu - prsgx;
     const R vr = S(a.s.vrt + b);
     A(a.a.ttend + b) = -uc * dtx - vc * dty - vt + vq;
     A(a.a.fu + b) = uc * (vr + fcor) + vadvv;
     A(a.a.fv + b) = vc * (vr + fcor) - vadvu;
     A(a.a.ke + b) = R(0.5) * (uc * uc + vc * vc);
+    // tracers at level b: top interface kt = t (= L-1-b), bottom kb = t + 1
+#pragma unroll
+    for (int iq = 0; iq < NTMAX; ++iq) {
+      if (iq >= nt) continue;
+      R ht;
+      if (t == 0) {
+        ht = q0[iq];  // half[0] = q at the top level
+      } else {
+        // dd[k] = q(level below k) - q(level above k); interfaces kt-1, kt, kt+1
+        R dm, d0, dpp;
+        if (t - 1 == 0) {  // dd[0], top boundary (dyn_run.f90:507-513)
+          const R qt = q1[iq], qt1 = q0[iq];  // q[L-1] = q[b+1], q[L-2] = q[b]
+          dm = (qt >= R(0)) ? qt - fmax(R(0), R(2) * qt - qt1) : qt - fmin(R(0), R(2) * qt - qt1);
+        } else {
+          dm = q1[iq] - q2[iq];
+          if (fabs(dm) < eps) dm = copysign(eps, dm);
+        }
+        d0 = q0[iq] - q1[iq];
+        if (fabs(d0) < eps) d0 = copysign(eps, d0);
+        if (t + 1 == L) {  // dd[L], bottom boundary (dyn_run.f90:514-518)
+          const R qb = q0[iq], qb1 = q1[iq];
+          dpp = (qb >= R(0)) ? fmax(R(0), R(2) * qb - qb1) - qb : fmin(R(0), R(2) * qb - qb1) - qb;
+        } else {
+          dpp = qm1[iq] - q0[iq];
+          if (fabs(dpp) < eps) dpp = copysign(eps, dpp);
+        }
+        ht = thuburn_half(q1[iq], q0[iq], dm, d0, dpp, e0);
+      }
+      const R vadq = (R(1) / dp) * ((hb[iq] * e1 - ht * e0) + (q0[iq] * (e0 - e1)));
+      const int qd = a.s.dqdx + iq * L + b, qy = a.s.dqdy + iq * L + b;
+      A(a.a.qtend + iq * L + b) = -uc * S(qd) - vc * S(qy) - vadq;
+      hb[iq] = ht;
+      qm1[iq] = q0[iq];
+      q0[iq] = q1[iq];
+      q1[iq] = q2[iq];
+      q2[iq] = (b + 3 < L) ? S(a.s.trc + iq * L + b + 3) : R(0);
+    }
     um = uc;
     vm = vc;
     tm = tc;
     dxm = dtx;
     dym = dty;
+    rlm = rl;
     uc = up;
     vc = vp;
     tc = tp;
   }
   A(a.a.dlnps) = dlnpsdt;
-
-  // tracers: Thuburn (1993) flux-limited vertical advection + horizontal
-  // advection (dyn_run.f90:279-292, :478-603)
-  const R eps = epstiny_of<R>();
-  R DDs[LMAX + 1];
-  for (int iq = 0; iq < a.nt; ++iq) {
-    const int q0 = a.s.trc + iq * L;
-    auto Q = [&](int b) -> R { return S(q0 + b); };
-    for (int k = 1; k <= L - 1; ++k) DDs[k] = Q(L - k - 1) - Q(L - k);
-    {
-      const R qt = Q(L - 1), qt1 = Q(L - 2);
-      DDs[0] = (qt >= R(0)) ? qt - fmax(R(0), R(2) * qt - qt1) : qt - fmin(R(0), R(2) * qt - qt1);
-      const R qb = Q(0), qb1 = Q(1);
-      DDs[L] = (qb >= R(0)) ? fmax(R(0), R(2) * qb - qb1) - qb : fmin(R(0), R(2) * qb - qb1) - qb;
-    }
-    for (int k = 1; k <= L - 1; ++k)
-      if (fabs(DDs[k]) < eps) DDs[k] = copysign(eps, DDs[k]);
-    R hprev = Q(L - 1);
-    for (int k = 1; k <= L; ++k) {
-      R hk;
-      const R qk = Q(L - k);
-      if (k <= L - 1) {
-        const R qk1 = Q(L - k - 1);
-        hk = R(0.5) * (qk1 + qk);
-        if (etadot(k) > R(0)) {
-          const R phi = DDs[k - 1] / DDs[k];
-          hk = qk + (phi + fabs(phi)) / (R(1) + fabs(phi)) * (hk - qk);
-        } else {
-          const R phi = DDs[k + 1] / DDs[k];
-          hk = qk1 + (phi + fabs(phi)) / (R(1) + fabs(phi)) * (hk - qk1);
-        }
-      } else {
-        hk = Q(0);
-      }
-      const int t = k - 1, b = L - k;
-      const R pkt = ak[t] + bk[t] * ps, pkt1 = ak[t + 1] + bk[t + 1] * ps;
-      const R ek = etadot(k), ek1 = etadot(k - 1);
-      const R vadv = (R(1) / (pkt1 - pkt)) * ((hk * ek - hprev * ek1) + (qk * (ek1 - ek)));
-      const int qd = a.s.dqdx + iq * L + b, qy = a.s.dqdy + iq * L + b;
-      A(a.a.qtend + iq * L + b) = -S(a.s.u + b) * S(qd) - S(a.s.v + b) * S(qy) - vadv;
-      hprev = hk;
-    }
-  }
 }
 
 template <typename R>
 void launch_dyn_columns(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t s) {
   if (a.L > LMAX - 1) throw std::runtime_error("nlev too large for the column kernel");
+  if (a.nt > NTMAX) throw std::runtime_error("ntrac too large for the column kernel");
   long ng = (long)a.nlon * a.nlat;
   k_dyn_columns<R><<<ceil_div(ng, 128), 128, 0, s>>>(a, inverse_only ? 1 : 0);
   count_launch();

@@ -436,6 +436,210 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(a.tmem_cols));
 }
 
+// ---------------------------------------------- persistent variant --
+// One CTA per SM walks its items round-robin.  Warp 0: TMA producer;
+// warp 1: TMEM owner and MMA issuer; warps 2-5: epilogue (warp w reads TMEM
+// lane quadrant w % 4).  Two TMEM accumulator buffers (each E|O, 2N
+// columns) let the epilogue of one item overlap the loads and MMAs of the
+// next.  Every wait is bounded; on a timeout all roles fall through to the
+// common exit, which waits for outstanding copies and MMAs and frees TMEM.
+constexpr int TCP_THREADS = 192;
+
+struct TcItem {
+  int m, c0, n0, nk0, nk1, kp, K;
+  long xb;
+};
+__device__ __forceinline__ TcItem tc_item(const TcArgs& a, int idx) {
+  const int4 it = a.items[idx];
+  TcItem t;
+  t.m = it.x;
+  t.c0 = it.y * TC_M;
+  t.n0 = it.z * a.N;
+  t.K = a.T - t.m + 1;
+  if (a.mode == 0) {
+    const int ke = (t.K + 1) / 2, ko = t.K / 2;
+    t.kp = (ke + a.kc - 1) / a.kc * a.kc;
+    t.nk0 = (ke + a.kc - 1) / a.kc;
+    t.nk1 = (ko + a.kc - 1) / a.kc;
+    t.xb = a.xbase[t.m];
+  } else {
+    t.kp = 0;
+    t.nk0 = t.nk1 = (a.nh + a.kc - 1) / a.kc;
+    t.xb = 0;
+  }
+  return t;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(TCP_THREADS, 1)
+    k_tc_gemm_p(const __grid_constant__ CUtensorMap mA0h, const __grid_constant__ CUtensorMap mA0l,
+                const __grid_constant__ CUtensorMap mA1h, const __grid_constant__ CUtensorMap mA1l,
+                const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, TcArgs a,
+                int nitems) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t)1023);
+  const int N = a.N;
+  const uint32_t bytesA = TC_M * 128, bytesB = (uint32_t)N * 128;
+  const uint32_t stage_bytes = 2 * bytesA + 2 * bytesB;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + TC_NS * stage_bytes);
+  uint64_t* empty = full + TC_NS;
+  uint64_t* tfull = empty + TC_NS;  // [2] accumulator buffer ready
+  uint64_t* tempty = tfull + 2;     // [2] accumulator buffer drained
+  uint64_t* done = tempty + 2;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(a.tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < TC_NS; ++s) {
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&empty[s]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&tfull[b]), 1);
+      mbar_init(smem_u32(&tempty[b]), 4);  // one arrive per epilogue warp
+    }
+    mbar_init(smem_u32(done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+
+  if (tid == 0) {  // ------------------------------------------- producer
+    int fills[TC_NS] = {0, 0, 0};
+    long g = 0;
+    bool bad = false;
+    for (int idx = blockIdx.x; idx < nitems && !bad; idx += gridDim.x) {
+      const TcItem t = tc_item(a, idx);
+      const int total = t.nk0 + t.nk1;
+      for (int i = 0; i < total; ++i, ++g) {
+        const int s = (int)(g % TC_NS);
+        const long u = g / TC_NS;
+        if (u >= 1 && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), a.err, 11)) {
+          bad = true;
+          break;
+        }
+        const int acc = (i < t.nk0) ? 0 : 1, kk = acc ? i - t.nk0 : i;
+        unsigned char* st = sm + s * stage_bytes;
+        const uint32_t fb = smem_u32(&full[s]);
+        mbar_expect_tx(fb, stage_bytes);
+        const CUtensorMap* ah = acc ? &mA1h : &mA0h;
+        const CUtensorMap* al = acc ? &mA1l : &mA0l;
+        if (a.mode == 0) {
+          const int x = (int)(t.xb + (long)acc * t.kp + (long)kk * a.kc);
+          tma_2d(smem_u32(st), ah, x, a.coff + t.c0, fb);
+          tma_2d(smem_u32(st + bytesA), al, x, a.coff + t.c0, fb);
+          const int xt = acc * a.kepad + kk * a.kc;
+          tma_3d(smem_u32(st + 2 * bytesA), &mBh, xt, t.n0, t.m, fb);
+          tma_3d(smem_u32(st + 2 * bytesA + bytesB), &mBl, xt, t.n0, t.m, fb);
+        } else {
+          const int x = kk * a.kc;
+          tma_3d(smem_u32(st), ah, x, t.c0, t.m, fb);
+          tma_3d(smem_u32(st + bytesA), al, x, t.c0, t.m, fb);
+          const int yt = acc * a.kirows + t.n0;
+          tma_3d(smem_u32(st + 2 * bytesA), &mBh, x, yt, t.m, fb);
+          tma_3d(smem_u32(st + 2 * bytesA + bytesB), &mBl, x, yt, t.m, fb);
+        }
+        ++fills[s];
+      }
+    }
+    for (int s = 0; s < TC_NS; ++s)  // no copies left in flight at exit
+      if (fills[s] > 0) mbar_wait(smem_u32(&full[s]), (fills[s] - 1) & 1, a.err, 12);
+  } else if (tid == 32) {  // ------------------------------------ MMA issuer
+    long g = 0;
+    int titem = 0;
+    bool bad = false;
+    for (int idx = blockIdx.x; idx < nitems && !bad; idx += gridDim.x, ++titem) {
+      const TcItem t = tc_item(a, idx);
+      const int b = titem & 1, u = titem >> 1;
+      if (u >= 1 && !mbar_wait(smem_u32(&tempty[b]), (uint32_t)((u - 1) & 1), a.err, 13)) break;
+      tc_fence_after();
+      const int total = t.nk0 + t.nk1;
+      for (int i = 0; i < total; ++i, ++g) {
+        const int s = (int)(g % TC_NS);
+        const long uu = g / TC_NS;
+        if (!mbar_wait(smem_u32(&full[s]), (uint32_t)(uu & 1), a.err, 14)) {
+          bad = true;
+          break;
+        }
+        tc_fence_after();
+        const int acc = (i < t.nk0) ? 0 : 1, kk = acc ? i - t.nk0 : i;
+        unsigned char* st = sm + s * stage_bytes;
+        const uint64_t dah = smem_desc(smem_u32(st)), dal = smem_desc(smem_u32(st + bytesA));
+        const uint64_t dbh = smem_desc(smem_u32(st + 2 * bytesA)),
+                       dbl = smem_desc(smem_u32(st + 2 * bytesA + bytesB));
+        const uint32_t d = tbase + (uint32_t)(b * 2 * N + acc * N);
+#pragma unroll
+        for (int k4 = 0; k4 < 4; ++k4) {
+          const uint64_t o = (uint64_t)(2 * k4);
+          mma<KIND>(d, dah + o, dbh + o, a.idesc, (kk > 0 || k4 > 0) ? 1u : 0u);
+          mma<KIND>(d, dah + o, dbl + o, a.idesc, 1u);
+          mma<KIND>(d, dal + o, dbh + o, a.idesc, 1u);
+        }
+        mma_commit(smem_u32(&empty[s]));
+      }
+      if (!bad) mma_commit(smem_u32(&tfull[b]));
+    }
+    mma_commit(smem_u32(done));  // every issued MMA has completed at `done`
+  } else if (warp >= 2) {  // ------------------------------------- epilogue
+    const int q4 = warp & 3;  // TMEM lane quadrant of this warp
+    int titem = 0;
+    for (int idx = blockIdx.x; idx < nitems; idx += gridDim.x, ++titem) {
+      const TcItem t = tc_item(a, idx);
+      const int b = titem & 1, u = titem >> 1;
+      const bool ok = mbar_wait(smem_u32(&tfull[b]), (uint32_t)(u & 1), a.err, 15);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      tc_fence_after();
+      const int c = t.c0 + q4 * 32 + lane;
+      const uint32_t tw = tbase + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * 2 * N);
+      for (int g = 0; g < N; g += 16) {
+        float e[16], o[16];
+        tmem_ld16(tw + g, e);
+        if (t.nk1 > 0)
+          tmem_ld16(tw + N + g, o);
+        else
+#pragma unroll
+          for (int q = 0; q < 16; ++q) o[q] = 0.f;
+        if (c < a.ncols) {
+          if (a.mode == 0) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const int j = t.n0 + g + q;
+              if (j < a.nh) {
+                a.out[((long)t.m * a.nlat + j) * a.ldout + c] = e[q] + o[q];
+                a.out[((long)t.m * a.nlat + (a.nlat - 1 - j)) * a.ldout + c] = a.parityH ? o[q] - e[q] : e[q] - o[q];
+              }
+            }
+          } else {
+            const long base = a.moff[t.m];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const int qe = 2 * (t.n0 + g + q), qo = qe + 1;
+              if (qe < t.K) a.out[(base + qe) * a.ldout + c] = e[q];
+              if (qo < t.K) a.out[(base + qo) * a.ldout + c] = o[q];
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+    }
+  }
+  __syncwarp();
+  mbar_wait(smem_u32(done), 0, a.err, 16);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(a.tmem_cols));
+}
+
 // ------------------------------------------------------------ host side --
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -469,8 +673,8 @@ static void make_map(CUtensorMap* m, void* base, int kind, int rank, const uint6
 static int round_up(int x, int a) { return (x + a - 1) / a * a; }
 // N tile: multiple of 16, at most 160 so that three stages of
 // (2 x 128 + 2 x N) rows of 128 bytes fit in 227 KB of shared memory
-static int tile_n(int n) {
-  int nt = (n + 159) / 160;
+static int tile_n(int n, int cap) {
+  int nt = (n + cap - 1) / cap;
   return round_up((n + nt - 1) / nt, 16);
 }
 
@@ -493,8 +697,17 @@ void tc_init(TcPlan& p, int kind, int T, int nh, int nlat, int ncap, const long*
   const int kemax = (T + 2) / 2;  // even-degree count of m = 0
   p.kepad = round_up(kemax, p.kc);
   p.nhpad = round_up(nh, p.kc);
-  p.nsyn = tile_n(nh);
-  p.nana = tile_n(kemax);
+  {
+    const char* env = getenv("GD_TC_PERSISTENT");
+    p.persistent = !(env && env[0] == '0');
+    int dev = 0;
+    GD_CUDA(cudaGetDevice(&dev));
+    GD_CUDA(cudaDeviceGetAttribute(&p.nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  // persistent: two E|O accumulator buffers (4N TMEM columns) -> N <= 128
+  const int ncap_n = p.persistent ? 128 : 160;
+  p.nsyn = tile_n(nh, ncap_n);
+  p.nana = tile_n(kemax, ncap_n);
   p.kirows = round_up(kemax, p.nana);
   p.ncap = round_up(ncap, 32);
   p.xbase.assign(T + 1, 0);
@@ -577,20 +790,32 @@ static uint32_t tmem_cols_for(int N) {
   return c;
 }
 
-static size_t smem_for(int N) { return (size_t)TC_NS * (2 * TC_M * 128 + 2 * N * 128) + 1024 + 256; }
+static size_t smem_for(int N) { return (size_t)TC_NS * (2 * TC_M * 128 + 2 * N * 128) + 1024 + 512; }
 
 template <int KIND>
 static void launch_gemm(const TcPlan& p, const CUtensorMap& a0h, const CUtensorMap& a0l, const CUtensorMap& a1h,
                         const CUtensorMap& a1l, const CUtensorMap& bh, const CUtensorMap& bl, TcArgs& args,
                         int nitems, cudaStream_t s) {
   const size_t sm = smem_for(args.N);
-  if (sm > 227 * 1024 || args.N > 160 || args.N % 16) throw std::runtime_error("tc gemm: bad N tile");
-  static bool attr = false;
-  if (!attr) {
-    GD_CUDA(cudaFuncSetAttribute(k_tc_gemm<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    attr = true;
+  if (sm > 227 * 1024 || args.N > (p.persistent ? 128 : 160) || args.N % 16)
+    throw std::runtime_error("tc gemm: bad N tile");
+  if (p.persistent) {
+    args.tmem_cols = tmem_cols_for(2 * args.N);  // two E|O buffers
+    static bool attr_p = false;
+    if (!attr_p) {
+      GD_CUDA(cudaFuncSetAttribute(k_tc_gemm_p<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+      attr_p = true;
+    }
+    const int grid = std::min(nitems, p.nsm);
+    k_tc_gemm_p<KIND><<<grid, TCP_THREADS, sm, s>>>(a0h, a0l, a1h, a1l, bh, bl, args, nitems);
+  } else {
+    static bool attr = false;
+    if (!attr) {
+      GD_CUDA(cudaFuncSetAttribute(k_tc_gemm<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+      attr = true;
+    }
+    k_tc_gemm<KIND><<<nitems, TC_THREADS, sm, s>>>(a0h, a0l, a1h, a1l, bh, bl, args);
   }
-  k_tc_gemm<KIND><<<nitems, TC_THREADS, sm, s>>>(a0h, a0l, a1h, a1l, bh, bl, args);
   count_launch();
   GD_LAUNCH_CHECK();
 }

@@ -21,6 +21,8 @@ struct TcPlan {
   int nana = 0;     // N tile (degrees per parity) of the analysis GEMM
   int kirows = 0;   // rows per parity of the analysis tables
   int ncap = 0;     // real-column capacity of the staging buffers
+  bool persistent = true;  // persistent warp-specialised GEMM (N <= 128)
+  int nsm = 0;             // SMs of the device (persistent grid size)
   long xlen = 0;    // padded spectral length of the synthesis operand
   std::vector<long> xbase;  // [T+1] start of order m in the padded layout
   long* d_xbase = nullptr;

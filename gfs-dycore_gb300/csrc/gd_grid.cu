@@ -53,7 +53,9 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
   const int j = (int)(p / a.nlon);
   const int L = a.L;
   const R* gS = a.gS;
-  auto S = [&](int row) -> R { return gS[(long)row * ng + p]; };
+  // inputs through the read-only path: loads may be issued ahead of the
+  // stores to the (disjoint) analysis rows
+  auto S = [&](int row) -> R { return __ldg(gS + (long)row * ng + p); };
   const R* ak = a.ak;
   const R* bk = a.bk;
   const R* dbk = a.dbk;
@@ -69,6 +71,7 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
   // pass 1, top to bottom: getomega prefix sums (dyn_run.f90:327-337)
   R pk_t = PK(0);
   R db = R(0), cb = R(0);
+#pragma unroll 4
   for (int t = 0; t < L; ++t) {
     const int b = L - 1 - t;
     const R pk_t1 = PK(t + 1);
@@ -145,9 +148,21 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
   R cofb2 = R(0), px3u = R(0), px3v = R(0);
   R um = R(0), vm = R(0), tm = R(0), dxm = R(0), dym = R(0), rlm = R(0);  // layer below
   R uc = S(a.s.u), vc = S(a.s.v), tc = S(a.s.tv);
+  // inputs of the current level, loaded one level ahead
+  R n_dtx = S(a.s.dtvdx), n_dty = S(a.s.dtvdy), n_dv = S(a.s.div), n_vr = S(a.s.vrt);
+  R n_up = (L > 1) ? S(a.s.u + 1) : R(0), n_vp = (L > 1) ? S(a.s.v + 1) : R(0), n_tp = (L > 1) ? S(a.s.tv + 1) : R(0);
   for (int b = 0; b < L; ++b) {
     const int t = L - 1 - b;
-    const R dtx = S(a.s.dtvdx + b), dty = S(a.s.dtvdy + b);
+    const R dtx = n_dtx, dty = n_dty, dv_b = n_dv, vr = n_vr, up = n_up, vp = n_vp, tp = n_tp;
+    if (b + 1 < L) {
+      n_dtx = S(a.s.dtvdx + b + 1);
+      n_dty = S(a.s.dtvdy + b + 1);
+      n_dv = S(a.s.div + b + 1);
+      n_vr = S(a.s.vrt + b + 1);
+      n_up = (b + 2 < L) ? S(a.s.u + b + 2) : R(0);
+      n_vp = (b + 2 < L) ? S(a.s.v + b + 2) : R(0);
+      n_tp = (b + 2 < L) ? S(a.s.tv + b + 2) : R(0);
+    }
     const R pkt = PK(t), pkt1 = PK(t + 1);
     const R dp = pkt1 - pkt;
     const R rl = RLN(t, pkt, pkt1);
@@ -164,12 +179,6 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
         cofb1 * rd * tc * ps * dlx - dphx + cofb2 * ps * dlx + px3u - rd * al * dtx - cofa * rd * tc * ps * dlx;
     const R prsgy =
         cofb1 * rd * tc * ps * dly - dphy + cofb2 * ps * dly + px3v - rd * al * dty - cofa * rd * tc * ps * dly;
-    R up = R(0), vp = R(0), tp = R(0);
-    if (b + 1 < L) {
-      up = S(a.s.u + b + 1);
-      vp = S(a.s.v + b + 1);
-      tp = S(a.s.tv + b + 1);
-    }
     const R e1 = etadot(t + 1), e0 = etadot(t);
     const R h = R(0.5) / dp;
     R vu = R(0), vv = R(0), vt = R(0);
@@ -186,12 +195,10 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
     vu *= h;
     vv *= h;
     vt *= h;
-    const R dv_b = S(a.s.div + b);
     const R cg = uc * dlx + vc * dly;
     R vq = a.kappa * dlnpdt(t, cg, dv_b, dp, rl, al) * tc;
     if (a.nt > 0) vq = vq / (R(1) + a.cvap_cp * q0[0]);
     const R vadvv = vv - prsgy, vadvu = vu - prsgx;
-    const R vr = S(a.s.vrt + b);
     A(a.a.ttend + b) = -uc * dtx - vc * dty - vt + vq;
     A(a.a.fu + b) = uc * (vr + fcor) + vadvv;
     A(a.a.fv + b) = vc * (vr + fcor) - vadvu;

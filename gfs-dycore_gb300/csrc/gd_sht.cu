@@ -8,6 +8,7 @@
 // shtns_spat_to_sh (shtns.f90:195,199,225,229) and the vector forms
 // (shtns.f90:261,270,303,308,341,348).  Convention: orthonormal harmonics
 // without Condon-Shortley phase (shtns.f90:110), latitudes north to south.
+#include <cstdlib>
 #include <vector>
 
 #include "gd_kernels.h"
@@ -831,6 +832,234 @@ __global__ void __launch_bounds__(128) k_r2c_t(const int2* __restrict__ jobs, co
   }
 }
 
+// ---- four-step register FFTs (M = M1 * M2) --------------------------------
+// Step A: M1 independent M2-point DFTs (stride M1) in registers, then the
+// twiddle W_M^(n1 k2); one shared-memory exchange; step B: M2 independent
+// M1-point DFTs in registers.  Rows live in shared memory with one pad
+// element after every M1 values so the strided exchanges are bank-conflict
+// free.  The in-register DFTs are fully unrolled Stockham passes over the
+// compile-time radix plan; their twiddles come from the length-M table.
+template <int M, int M1>
+__device__ __forceinline__ int pad_addr(int n) {
+  return n + n / M1;
+}
+
+template <typename R, int N, int M, int SIGN, int S>
+__device__ __forceinline__ void reg_stages(typename C2<R>::T* x, typename C2<R>::T* y,
+                                           const typename C2<R>::T* __restrict__ tw) {
+  typedef typename C2<R>::T V;
+  if constexpr (S < FftPlanC<N>::count()) {
+    constexpr int p = FftPlanC<N>::radix(S), Ns = FftPlanC<N>::ns(S), nb = N / p;
+    constexpr int tstep = (M / N) * (N / (Ns * p));  // W_{Ns p} = W_M^(M/(Ns p))
+#pragma unroll
+    for (int jj = 0; jj < nb; ++jj) {
+      const int k = jj % Ns;
+      V v[4];
+#pragma unroll
+      for (int q = 0; q < p; ++q) {
+        V xv = x[jj + q * nb];
+        if (q > 0 && k > 0) {
+          V w = tw[k * q * tstep];
+          if (SIGN > 0) w.y = -w.y;
+          xv = cmul(xv, w);
+        }
+        v[q] = xv;
+      }
+      if (p == 2) {
+        V t = v[0];
+        v[0] = cadd(t, v[1]);
+        v[1] = csub(t, v[1]);
+      } else if (p == 4) {
+        V s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+        V s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+        V id13;
+        id13.x = -SIGN * d13.y;
+        id13.y = SIGN * d13.x;
+        v[0] = cadd(s02, s13);
+        v[2] = csub(s02, s13);
+        v[1] = cadd(d02, id13);
+        v[3] = csub(d02, id13);
+      } else {
+        const R c3 = R(-0.5), s3 = R(0.86602540378443864676) * R(SIGN);
+        V t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
+        V m1, m2;
+        m1.x = v[0].x + c3 * t1.x;
+        m1.y = v[0].y + c3 * t1.y;
+        m2.x = -s3 * t2.y;
+        m2.y = s3 * t2.x;
+        v[0] = cadd(v[0], t1);
+        v[1] = cadd(m1, m2);
+        v[2] = csub(m1, m2);
+      }
+      const int od = (jj / Ns) * Ns * p + k;
+#pragma unroll
+      for (int q = 0; q < p; ++q) y[od + q * Ns] = v[q];
+    }
+    reg_stages<R, N, M, SIGN, S + 1>(y, x, tw);
+  }
+}
+// in-register N-point DFT of x (y is scratch); the result is left in x
+template <typename R, int N, int M, int SIGN>
+__device__ __forceinline__ void reg_fft(typename C2<R>::T* x, typename C2<R>::T* y,
+                                        const typename C2<R>::T* __restrict__ tw) {
+  reg_stages<R, N, M, SIGN, 0>(x, y, tw);
+  if constexpr (FftPlanC<N>::count() % 2 == 1) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) x[i] = y[i];
+  }
+}
+
+// four-step FFT of NR rows held in buf (padded addressing), sign SIGN
+template <typename R, int M, int M1, int M2, int NR, int NT, int SIGN>
+__device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R>::T* __restrict__ tw) {
+  typedef typename C2<R>::T V;
+  constexpr int RP = M + M / M1;  // padded row length
+  // step A: thread (r, n1) -> M2-point DFT over n2 of x[n1 + M1 n2], twiddle, store in place
+  for (int e = threadIdx.x; e < NR * M1; e += NT) {
+    const int r = e / M1, n1 = e - r * M1;
+    V* row = buf + r * RP;
+    V x[M2], y[M2];
+#pragma unroll
+    for (int n2 = 0; n2 < M2; ++n2) x[n2] = row[pad_addr<M, M1>(n1 + M1 * n2)];
+    reg_fft<R, M2, M, SIGN>(x, y, tw);
+#pragma unroll
+    for (int k2 = 1; k2 < M2; ++k2) {
+      if (n1 > 0) {
+        V w = tw[n1 * k2];
+        if (SIGN > 0) w.y = -w.y;
+        x[k2] = cmul(x[k2], w);
+      }
+    }
+#pragma unroll
+    for (int k2 = 0; k2 < M2; ++k2) row[pad_addr<M, M1>(n1 + M1 * k2)] = x[k2];
+  }
+  __syncthreads();
+  // step B: thread (r, k2) -> M1-point DFT over n1 of Y[n1 + M1 k2]; result X[k2 + M2 k1]
+  static_assert(NR * M2 <= NT, "step B needs one task per thread");
+  const int e = threadIdx.x;
+  const int r = e / M2, k2 = e - r * M2;
+  V x[M1], y[M1];
+  if (e < NR * M2) {
+    V* row = buf + r * RP;
+#pragma unroll
+    for (int n1 = 0; n1 < M1; ++n1) x[n1] = row[pad_addr<M, M1>(n1 + M1 * k2)];
+    reg_fft<R, M1, M, SIGN>(x, y, tw);
+  }
+  __syncthreads();
+  if (e < NR * M2) {
+    V* row = buf + r * RP;
+#pragma unroll
+    for (int k1 = 0; k1 < M1; ++k1) row[pad_addr<M, M1>(k2 + M2 * k1)] = x[k1];
+  }
+  __syncthreads();
+}
+
+template <typename R, int M, int M1, int M2>
+__global__ void __launch_bounds__(((nr_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32) * 32)
+    k_c2r_4(const int2* __restrict__ jobs, const SynthDesc* __restrict__ descs, ShtDev<R> d,
+            const R* __restrict__ FP, long ldP, const R* __restrict__ FH, long ldH, R* __restrict__ grid) {
+  typedef typename C2<R>::T V;
+  constexpr int NR = nr_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = M + M / M1;
+  __shared__ V buf[NR * RP];
+  const int T = d.T, nlat = d.nlat, nlon = d.nlon;
+  const int2 jb = jobs[blockIdx.x];
+  const SynthDesc ds = descs[jb.x];
+  const int j = blockIdx.y, r0 = jb.y;
+  const int nr = min(NR, ds.count - r0);
+  const R rc = d.rcos[j], alpha = (R)ds.alpha, beta = (R)ds.beta;
+  for (int e = threadIdx.x; e < NR * (M / 2 + 1); e += NT) {
+    const int kk = e / NR, r = e - kk * NR;
+    V z1 = mk2<R>(R(0), R(0)), z2 = z1;
+    if (r < nr) {
+      const int k2 = M - kk;
+      const V x1 = synth_coef<R>(ds, kk, T, j, nlat, r0 + r, FP, ldP, FH, ldH, rc, alpha, beta);
+      const V x2 = (kk == 0) ? mk2<R>(R(0), R(0))
+                             : synth_coef<R>(ds, k2, T, j, nlat, r0 + r, FP, ldP, FH, ldH, rc, alpha, beta);
+      V A = cadd(x1, cconj(x2)), B = csub(x1, cconj(x2));
+      V Bw = cmul(B, cconj(d.twN[kk]));
+      z1.x = A.x - Bw.y;
+      z1.y = A.y + Bw.x;
+      if (kk > 0 && k2 != kk) {
+        V A2 = cadd(x2, cconj(x1)), B2 = csub(x2, cconj(x1));
+        V Bw2 = cmul(B2, cconj(d.twN[k2]));
+        z2.x = A2.x - Bw2.y;
+        z2.y = A2.y + Bw2.x;
+      }
+    }
+    buf[r * RP + pad_addr<M, M1>(kk)] = z1;
+    if (kk > 0 && M - kk != kk) buf[r * RP + pad_addr<M, M1>(M - kk)] = z2;
+  }
+  __syncthreads();
+  fft4<R, M, M1, M2, NR, NT, +1>(buf, d.twM);
+  for (int e = threadIdx.x; e < nr * M; e += NT) {
+    const int r = e / M, n = e - r * M;
+    *reinterpret_cast<V*>(grid + ((long)(ds.dst + r0 + r) * nlat + j) * nlon + 2 * n) =
+        buf[r * RP + pad_addr<M, M1>(n)];
+  }
+}
+
+template <typename R, int M, int M1, int M2>
+__global__ void __launch_bounds__(((nr_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32) * 32)
+    k_r2c_4(const int2* __restrict__ jobs, const AnalDesc* __restrict__ descs, ShtDev<R> d,
+            const R* __restrict__ grid, R* __restrict__ GP, long ldP, R* __restrict__ GH, long ldH) {
+  typedef typename C2<R>::T V;
+  constexpr int NR = nr_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = M + M / M1;
+  __shared__ V buf[NR * RP];
+  const int T = d.T, nlat = d.nlat, nlon = d.nlon;
+  const int2 jb = jobs[blockIdx.x];
+  const AnalDesc ds = descs[jb.x];
+  const int j = blockIdx.y, r0 = jb.y;
+  const int nr = min(NR, ds.count - r0);
+  for (int e = threadIdx.x; e < NR * M; e += NT) {
+    const int r = e / M, n = e - r * M;
+    V z = mk2<R>(R(0), R(0));
+    if (r < nr) z = *reinterpret_cast<const V*>(grid + ((long)(ds.src + r0 + r) * nlat + j) * nlon + 2 * n);
+    buf[r * RP + pad_addr<M, M1>(n)] = z;
+  }
+  __syncthreads();
+  fft4<R, M, M1, M2, NR, NT, -1>(buf, d.twM);
+  const R wn = d.wn[j] * R(0.5), rc = d.rcos[j];
+  for (int e = threadIdx.x; e < nr * (M / 2 + 1); e += NT) {
+    const int kk = e / nr, r = e - kk * nr;
+    const V Z1 = buf[r * RP + pad_addr<M, M1>(kk)], Z2 = buf[r * RP + pad_addr<M, M1>((M - kk) % M)];
+    for (int h = 0; h < 2; ++h) {
+      const int k = h ? M - kk : kk;
+      if (k > T || (h && (kk == 0 || M - kk == kk))) continue;
+      const V za = h ? Z2 : Z1, zb = h ? Z1 : Z2;
+      V E = cadd(za, cconj(zb)), O = csub(za, cconj(zb));
+      V Oi;
+      Oi.x = O.y;
+      Oi.y = -O.x;
+      V X = cadd(E, cmul(d.twN[k], Oi));
+      X.x *= wn;
+      X.y *= wn;
+      const int col = r0 + r;
+      if (ds.dstP >= 0) {
+        V y = X;
+        if (ds.imcosP) {
+          const R f = (R)k * rc;
+          y.x = -f * X.y;
+          y.y = f * X.x;
+        }
+        y.x *= (R)ds.scaleP;
+        y.y *= (R)ds.scaleP;
+        *reinterpret_cast<V*>(GP + ((long)k * nlat + j) * ldP + 2 * (ds.dstP + col)) = y;
+      }
+      if (ds.dstH >= 0) {
+        V y = X;
+        y.x *= (R)ds.scaleH;
+        y.y *= (R)ds.scaleH;
+        *reinterpret_cast<V*>(GH + ((long)k * nlat + j) * ldH + 2 * (ds.dstH + col)) = y;
+      }
+    }
+  }
+}
+
+template <int M, int M1, int M2>
+constexpr int nt4(int nr) {
+  return ((nr * (M1 > M2 ? M1 : M2) + 31) / 32) * 32;
+}
+
 template <typename R>
 static bool launch_c2r_fixed(const ShtDev<R>& d, const FftPlan& plan, const R* FP, long ldP, const R* FH, long ldH,
                              R* grid, cudaStream_t s) {
@@ -840,6 +1069,23 @@ static bool launch_c2r_fixed(const ShtDev<R>& d, const FftPlan& plan, const R* F
   case MM:                                                                                       \
     k_c2r_t<R, MM><<<grd, 128, 0, s>>>(plan.jobs, ds, d, FP, ldP, FH, ldH, grid);                \
     return true;
+  if (!getenv("GD_FFT_STOCKHAM")) {
+    constexpr int NR = nr_of<R>();
+    switch (d.M) {
+#define GD_C2R4(MM, A, B)                                                                         \
+  case MM:                                                                                        \
+    k_c2r_4<R, MM, A, B><<<grd, nt4<MM, A, B>(NR), 0, s>>>(plan.jobs, ds, d, FP, ldP, FH, ldH, grid); \
+    return true;
+      GD_C2R4(64, 8, 8)
+      GD_C2R4(96, 8, 12)
+      GD_C2R4(192, 12, 16)
+      GD_C2R4(384, 16, 24)
+      GD_C2R4(576, 24, 24)
+#undef GD_C2R4
+      default:
+        break;
+    }
+  }
   switch (d.M) {
     GD_C2R(32)
     GD_C2R(48)
@@ -865,6 +1111,23 @@ static bool launch_r2c_fixed(const ShtDev<R>& d, const FftPlan& plan, const R* g
   case MM:                                                                                       \
     k_r2c_t<R, MM><<<grd, 128, 0, s>>>(plan.jobs, ds, d, grid, GP, ldP, GH, ldH);                \
     return true;
+  if (!getenv("GD_FFT_STOCKHAM")) {
+    constexpr int NR = nr_of<R>();
+    switch (d.M) {
+#define GD_R2C4(MM, A, B)                                                                         \
+  case MM:                                                                                        \
+    k_r2c_4<R, MM, A, B><<<grd, nt4<MM, A, B>(NR), 0, s>>>(plan.jobs, ds, d, grid, GP, ldP, GH, ldH); \
+    return true;
+      GD_R2C4(64, 8, 8)
+      GD_R2C4(96, 8, 12)
+      GD_R2C4(192, 12, 16)
+      GD_R2C4(384, 16, 24)
+      GD_R2C4(576, 24, 24)
+#undef GD_R2C4
+      default:
+        break;
+    }
+  }
   switch (d.M) {
     GD_R2C(32)
     GD_R2C(48)

@@ -536,12 +536,12 @@ class Dycore : public DycoreBase {
       full.push_back({nt * L, sr.dqdx, -1, 0, 0, sc.trc, 0.0, ai});
       full.push_back({nt * L, sr.dqdy, 1, sc.trc - h0, -1, 0, ai, 0.0});
     }
-    c2rFull = make_c2r_plan<R>(full.data(), (int)full.size(), stream);
+    c2rFull = make_c2r_plan<R>(full.data(), (int)full.size(), stream, M);
     std::vector<SynthDesc> inv = {
         full[0], full[1], full[2], full[3], full[4], full[7], full[8], full[9],
     };
     if (nt > 0) inv.push_back(full[10]);
-    c2rInv = make_c2r_plan<R>(inv.data(), (int)inv.size(), stream);
+    c2rInv = make_c2r_plan<R>(inv.data(), (int)inv.size(), stream, M);
     std::vector<AnalDesc> an = {
         {L, ar.ttend, ap.ttend, 0, -1, 1.0, 0.0},
         {L, ar.ke, ap.ke, 0, -1, 1.0, 0.0},
@@ -550,9 +550,9 @@ class Dycore : public DycoreBase {
         {L, ar.fv, ap.imfv, 1, ah.mfv, 1.0, -1.0},
     };
     if (nt > 0) an.push_back({nt * L, ar.qtend, ap.qtend, 0, -1, 1.0, 0.0});
-    r2cDyn = make_r2c_plan<R>(an.data(), (int)an.size(), stream);
+    r2cDyn = make_r2c_plan<R>(an.data(), (int)an.size(), stream, M);
     AnalDesc ph = {3 * L + 1, 0, 0, 0, -1, 1.0, 0.0};
-    r2cPhys = make_r2c_plan<R>(&ph, 1, stream);
+    r2cPhys = make_r2c_plan<R>(&ph, 1, stream, M);
   }
 
   // ------------------------------------------------------------ passes --
@@ -881,7 +881,7 @@ class Dycore : public DycoreBase {
   void api_synth(const R* X, int ncs, bool needH, const std::vector<SynthDesc>& ds, int nrows, double* out) {
     do_synth(false, synth_plan(2 * ncs), X, ldS, 2 * ncs, FPb, ldS);
     if (needH) do_synth(true, synth_plan(2 * ncs), X, ldS, 2 * ncs, FHb, ldS);
-    FftPlan p = make_c2r_plan<R>(ds.data(), (int)ds.size(), stream);
+    FftPlan p = make_c2r_plan<R>(ds.data(), (int)ds.size(), stream, M);
     launch_c2r<R>(sd, p, FPb, ldS, FHb, ldS, gS, stream);
     grid_out(gS, nrows, out);
     free_fft_plan(p);
@@ -968,7 +968,7 @@ class Dycore : public DycoreBase {
     }
   }
   void api_anal(const std::vector<AnalDesc>& ds, int ncP, int ncH) {
-    FftPlan p = make_r2c_plan<R>(ds.data(), (int)ds.size(), stream);
+    FftPlan p = make_r2c_plan<R>(ds.data(), (int)ds.size(), stream, M);
     launch_r2c<R>(sd, p, gA, FPb, ldS, FHb, ldS, stream);
     do_anal(false, anal_plan(2 * ncP), FPb, ldS, 2 * ncP, AP, ldAP);
     if (ncH > 0) do_anal(true, anal_plan(2 * ncH), FHb, ldS, 2 * ncH, AH, ldAH);

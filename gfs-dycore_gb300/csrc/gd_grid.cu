@@ -29,6 +29,14 @@ __device__ __forceinline__ float epstiny_of<float>() {
 constexpr int LMAX = 128;
 constexpr int NTMAX = 8;  // tracers handled in registers by the column kernel
 
+// Division and logarithm of the column kernel: IEEE for the FP64 path (the
+// reference restated exactly), the hardware approximations for the FP32
+// state (relative error ~1e-7, below the FP32 state's own rounding).
+__device__ __forceinline__ double cdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float cdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double clog(double a) { return log(a); }
+__device__ __forceinline__ float clog(float a) { return __logf(a); }
+
 // Thuburn (1993) limited half-level value at interior interface k
 // (dyn_run.f90:574-590): qa = level above the interface, qb = level below,
 // dm = dd[k-1], d0 = dd[k], dp = dd[k+1], upwind by the sign of etadot.
@@ -36,17 +44,18 @@ template <typename R>
 __device__ __forceinline__ R thuburn_half(R qa, R qb, R dm, R d0, R dp, R eta) {
   R h = R(0.5) * (qb + qa);
   if (eta > R(0)) {
-    const R phi = dm / d0;
-    h = qa + (phi + fabs(phi)) / (R(1) + fabs(phi)) * (h - qa);
+    const R phi = cdiv(dm, d0);
+    h = qa + cdiv(phi + fabs(phi), R(1) + fabs(phi)) * (h - qa);
   } else {
-    const R phi = dp / d0;
-    h = qb + (phi + fabs(phi)) / (R(1) + fabs(phi)) * (h - qb);
+    const R phi = cdiv(dp, d0);
+    h = qb + cdiv(phi + fabs(phi), R(1) + fabs(phi)) * (h - qb);
   }
   return h;
 }
 
 template <typename R>
 __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int inverse_only) {
+  extern __shared__ __align__(16) unsigned char smcol[];
   const long ng = (long)a.nlon * a.nlat;
   const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= ng) return;
@@ -65,8 +74,12 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
   const R dlx = S(a.s.dlnpsdx), dly = S(a.s.dlnpsdy);
   auto PK = [&](int t) -> R { return ak[t] + bk[t] * ps; };
   // rlnp and alfa of the top-down layer t (pressure_data.f90:89-96)
-  auto RLN = [&](int t, R pkt, R pkt1) -> R { return (t == 0) ? a.rlnp_top : log(pkt1 / pkt); };
-  R DB[LMAX], CB[LMAX];
+  auto RLN = [&](int t, R pkt, R pkt1) -> R { return (t == 0) ? a.rlnp_top : clog(cdiv(pkt1, pkt)); };
+  // getomega prefix sums in shared memory, [t][thread]
+  R* DBs = reinterpret_cast<R*>(smcol);
+  R* CBs = DBs + (long)L * blockDim.x;
+  auto DB = [&](int t) -> R& { return DBs[t * blockDim.x + threadIdx.x]; };
+  auto CB = [&](int t) -> R& { return CBs[t * blockDim.x + threadIdx.x]; };
 
   // pass 1, top to bottom: getomega prefix sums (dyn_run.f90:327-337)
   R pk_t = PK(0);
@@ -85,41 +98,41 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
       db = db + dv * dp;
       cb = cb + cg * dbk[t];
     }
-    DB[t] = db;
-    CB[t] = cb;
+    DB(t) = db;
+    CB(t) = cb;
     if (a.prs)  // Phillips layer pressure (pressure_data.f90:87-88)
       a.prs[(long)b * ng + p] =
           pow((pow(pk_t1, a.kappa) * pk_t1 - pow(pk_t, a.kappa) * pk_t) / ((a.kappa + R(1)) * dp), R(1) / a.kappa);
     pk_t = pk_t1;
   }
-  const R dlnpsdt = -DB[L - 1] / ps - CB[L - 1];
+  const R dlnpsdt = -DB(L - 1) / ps - CB(L - 1);
   a.psg[p] = ps;
   a.dlnpsdt[p] = dlnpsdt;
   auto etadot = [&](int t) -> R {  // dyn_run.f90:340-344
     if (t == 0 || t == L) return R(0);
-    return -ps * (bk[t] * dlnpsdt + CB[t - 1]) - DB[t - 1];
+    return -ps * (bk[t] * dlnpsdt + CB(t - 1)) - DB(t - 1);
   };
   // omega/p of layer t (dyn_run.f90:347-368) from its cg, divergence, rlnp, alfa
-  auto dlnpdt = [&](int t, R cg, R dv, R dp, R rl, R al) -> R {
+  auto dlnpdt = [&](int t, R cg, R dv, R dp, R idp, R rl, R al) -> R {
     R wb, wc;
     if (t == 0) {
-      wb = al * (dv * dp + ps * CB[0] * dbk[0]);
+      wb = al * (dv * dp + ps * CB(0) * dbk[0]);
       wc = ps * cg * dbk[0];
     } else {
-      wb = rl * (DB[t - 1] + ps * CB[t - 1]) + al * (dv * dp + ps * cg * dbk[t]);
-      wc = ps * cg * (dbk[t] + a.ck[t] * rl / dp);
+      wb = rl * (DB(t - 1) + ps * CB(t - 1)) + al * (dv * dp + ps * cg * dbk[t]);
+      wc = ps * cg * (dbk[t] + a.ck[t] * rl * idp);
     }
-    return (wc - wb) / dp;
+    return (wc - wb) * idp;
   };
   if (a.etadot)
     for (int t = 0; t <= L; ++t) a.etadot[(long)t * ng + p] = etadot(t);
   if (a.dlnpdtg)
     for (int t = 0; t < L; ++t) {
       const int b = L - 1 - t;
-      const R pkt = PK(t), pkt1 = PK(t + 1), dp = pkt1 - pkt;
-      const R rl = RLN(t, pkt, pkt1), al = (t == 0) ? a.log2sp : R(1) - (pkt / dp) * rl;
+      const R pkt = PK(t), pkt1 = PK(t + 1), dp = pkt1 - pkt, idp = R(1) / dp;
+      const R rl = RLN(t, pkt, pkt1), al = (t == 0) ? a.log2sp : R(1) - (pkt * idp) * rl;
       const R cg = S(a.s.u + b) * dlx + S(a.s.v + b) * dly;
-      a.dlnpdtg[(long)b * ng + p] = dlnpdt(t, cg, S(a.s.div + b), dp, rl, al);
+      a.dlnpdtg[(long)b * ng + p] = dlnpdt(t, cg, S(a.s.div + b), dp, idp, rl, al);
     }
   if (inverse_only) return;
 
@@ -148,6 +161,9 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
   R cofb2 = R(0), px3u = R(0), px3v = R(0);
   R um = R(0), vm = R(0), tm = R(0), dxm = R(0), dym = R(0), rlm = R(0);  // layer below
   R uc = S(a.s.u), vc = S(a.s.v), tc = S(a.s.tv);
+  // pressure at the interfaces below the current layer, carried upward
+  bool ipk_valid = false;
+  R pk_below = R(0), ipk_below = R(0), ipk2 = R(0);
   // inputs of the current level, loaded one level ahead
   R n_dtx = S(a.s.dtvdx), n_dty = S(a.s.dtvdy), n_dv = S(a.s.div), n_vr = S(a.s.vrt);
   R n_up = (L > 1) ? S(a.s.u + 1) : R(0), n_vp = (L > 1) ? S(a.s.v + 1) : R(0), n_tp = (L > 1) ? S(a.s.tv + 1) : R(0);
@@ -163,24 +179,25 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
       n_vp = (b + 2 < L) ? S(a.s.v + b + 2) : R(0);
       n_tp = (b + 2 < L) ? S(a.s.tv + b + 2) : R(0);
     }
-    const R pkt = PK(t), pkt1 = PK(t + 1);
-    const R dp = pkt1 - pkt;
-    const R rl = RLN(t, pkt, pkt1);
-    const R al = (t == 0) ? a.log2sp : R(1) - (pkt / dp) * rl;
+    const R pkt = PK(t), pkt1 = ipk_valid ? pk_below : PK(t + 1);
+    const R ipk1 = ipk_valid ? ipk_below : R(1) / pkt1;  // 1 / pk(t+1), carried from below
+    const R ipkt = R(1) / pkt;                           // inf at the model top (pk = 0), unused there
+    const R dp = pkt1 - pkt, idp = R(1) / dp;
+    const R rl = (t == 0) ? a.rlnp_top : clog(pkt1 * ipkt);
+    const R al = (t == 0) ? a.log2sp : R(1) - (pkt * idp) * rl;
+    if (b > 0) cofb2 = cofb2 - rd * (bk[t + 2] * ipk2 - bk[t + 1] * ipk1) * tm;
     if (b > 0) {
-      const R pk2 = PK(t + 2);
-      cofb2 = cofb2 - rd * (bk[t + 2] / pk2 - bk[t + 1] / pkt1) * tm;
       px3u = px3u - rd * rlm * dxm;
       px3v = px3v - rd * rlm * dym;
     }
-    const R cofb1 = (t == 0) ? -(R(1) / dp) * (al * dbk[0]) : -(R(1) / dp) * (bk[t] * rl + al * dbk[t]);
-    const R cofa = -(R(1) / dp) * (bk[t + 1] * pkt / pkt1 - bk[t] + rl * (bk[t] - pkt * dbk[t] / dp));
+    const R cofb1 = (t == 0) ? -idp * (al * dbk[0]) : -idp * (bk[t] * rl + al * dbk[t]);
+    const R cofa = -idp * (bk[t + 1] * pkt * ipk1 - bk[t] + rl * (bk[t] - pkt * dbk[t] * idp));
     const R prsgx =
         cofb1 * rd * tc * ps * dlx - dphx + cofb2 * ps * dlx + px3u - rd * al * dtx - cofa * rd * tc * ps * dlx;
     const R prsgy =
         cofb1 * rd * tc * ps * dly - dphy + cofb2 * ps * dly + px3v - rd * al * dty - cofa * rd * tc * ps * dly;
     const R e1 = etadot(t + 1), e0 = etadot(t);
-    const R h = R(0.5) / dp;
+    const R h = R(0.5) * idp;
     R vu = R(0), vv = R(0), vt = R(0);
     if (b > 0) {
       vu += e1 * (um - uc);
@@ -196,8 +213,8 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
     vv *= h;
     vt *= h;
     const R cg = uc * dlx + vc * dly;
-    R vq = a.kappa * dlnpdt(t, cg, dv_b, dp, rl, al) * tc;
-    if (a.nt > 0) vq = vq / (R(1) + a.cvap_cp * q0[0]);
+    R vq = a.kappa * dlnpdt(t, cg, dv_b, dp, idp, rl, al) * tc;
+    if (a.nt > 0) vq = cdiv(vq, R(1) + a.cvap_cp * q0[0]);
     const R vadvv = vv - prsgy, vadvu = vu - prsgx;
     A(a.a.ttend + b) = -uc * dtx - vc * dty - vt + vq;
     A(a.a.fu + b) = uc * (vr + fcor) + vadvv;
@@ -231,7 +248,7 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
         }
         ht = thuburn_half(q1[iq], q0[iq], dm, d0, dpp, e0);
       }
-      const R vadq = (R(1) / dp) * ((hb[iq] * e1 - ht * e0) + (q0[iq] * (e0 - e1)));
+      const R vadq = idp * ((hb[iq] * e1 - ht * e0) + (q0[iq] * (e0 - e1)));
       const int qd = a.s.dqdx + iq * L + b, qy = a.s.dqdy + iq * L + b;
       A(a.a.qtend + iq * L + b) = -uc * S(qd) - vc * S(qy) - vadq;
       hb[iq] = ht;
@@ -246,6 +263,10 @@ __global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int invers
     dxm = dtx;
     dym = dty;
     rlm = rl;
+    ipk2 = ipk1;  // 1 / pk(t+1) becomes 1 / pk(t'+2) for the layer above
+    pk_below = pkt;
+    ipk_below = ipkt;
+    ipk_valid = true;
     uc = up;
     vc = vp;
     tc = tp;
@@ -258,7 +279,13 @@ void launch_dyn_columns(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t 
   if (a.L > LMAX - 1) throw std::runtime_error("nlev too large for the column kernel");
   if (a.nt > NTMAX) throw std::runtime_error("ntrac too large for the column kernel");
   long ng = (long)a.nlon * a.nlat;
-  k_dyn_columns<R><<<ceil_div(ng, 128), 128, 0, s>>>(a, inverse_only ? 1 : 0);
+  const size_t sm = 2 * (size_t)a.L * 128 * sizeof(R);
+  static bool attr = false;
+  if (!attr) {
+    GD_CUDA(cudaFuncSetAttribute(k_dyn_columns<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  k_dyn_columns<R><<<ceil_div(ng, 128), 128, sm, s>>>(a, inverse_only ? 1 : 0);
   count_launch();
   GD_LAUNCH_CHECK();
 }

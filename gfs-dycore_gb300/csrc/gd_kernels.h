@@ -68,11 +68,11 @@ struct FftPlan {
   int njobs = 0;
 };
 template <typename R>
-int fft_rows_per_cta();
+int fft_rows_per_cta(int M);
 template <typename R>
-FftPlan make_c2r_plan(const SynthDesc* descs, int ndesc, cudaStream_t s);
+FftPlan make_c2r_plan(const SynthDesc* descs, int ndesc, cudaStream_t s, int M);
 template <typename R>
-FftPlan make_r2c_plan(const AnalDesc* descs, int ndesc, cudaStream_t s);
+FftPlan make_r2c_plan(const AnalDesc* descs, int ndesc, cudaStream_t s, int M);
 void free_fft_plan(FftPlan& p);
 template <typename R>
 void launch_c2r(const ShtDev<R>& d, const FftPlan& plan, const R* FP, long ldP, const R* FH, long ldH, R* grid,

@@ -462,12 +462,18 @@ template <typename R>
 __host__ __device__ constexpr int nr_of() {
   return sizeof(R) == 8 ? 2 : 4;
 }
+// rows per CTA of the four-step kernels (64-byte contiguous Fourier chunks)
 template <typename R>
-int fft_rows_per_cta() {
-  return nr_of<R>();
+__host__ __device__ constexpr int nr4_of() {
+  return sizeof(R) == 8 ? 4 : 8;
 }
-template int fft_rows_per_cta<double>();
-template int fft_rows_per_cta<float>();
+static bool four_step_len(int M) { return M == 64 || M == 96 || M == 192 || M == 384 || M == 576; }
+template <typename R>
+int fft_rows_per_cta(int M) {
+  return (four_step_len(M) && !getenv("GD_FFT_STOCKHAM")) ? nr4_of<R>() : nr_of<R>();
+}
+template int fft_rows_per_cta<double>(int);
+template int fft_rows_per_cta<float>(int);
 
 struct FftArgs {
   int nrad;
@@ -955,11 +961,11 @@ __device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R
 }
 
 template <typename R, int M, int M1, int M2>
-__global__ void __launch_bounds__(((nr_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32) * 32)
+__global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32) * 32)
     k_c2r_4(const int2* __restrict__ jobs, const SynthDesc* __restrict__ descs, ShtDev<R> d,
             const R* __restrict__ FP, long ldP, const R* __restrict__ FH, long ldH, R* __restrict__ grid) {
   typedef typename C2<R>::T V;
-  constexpr int NR = nr_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = M + M / M1;
+  constexpr int NR = nr4_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = M + M / M1;
   __shared__ V buf[NR * RP];
   const int T = d.T, nlat = d.nlat, nlon = d.nlon;
   const int2 jb = jobs[blockIdx.x];
@@ -999,11 +1005,11 @@ __global__ void __launch_bounds__(((nr_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32)
 }
 
 template <typename R, int M, int M1, int M2>
-__global__ void __launch_bounds__(((nr_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32) * 32)
+__global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32) * 32)
     k_r2c_4(const int2* __restrict__ jobs, const AnalDesc* __restrict__ descs, ShtDev<R> d,
             const R* __restrict__ grid, R* __restrict__ GP, long ldP, R* __restrict__ GH, long ldH) {
   typedef typename C2<R>::T V;
-  constexpr int NR = nr_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = M + M / M1;
+  constexpr int NR = nr4_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = M + M / M1;
   __shared__ V buf[NR * RP];
   const int T = d.T, nlat = d.nlat, nlon = d.nlon;
   const int2 jb = jobs[blockIdx.x];
@@ -1070,7 +1076,7 @@ static bool launch_c2r_fixed(const ShtDev<R>& d, const FftPlan& plan, const R* F
     k_c2r_t<R, MM><<<grd, 128, 0, s>>>(plan.jobs, ds, d, FP, ldP, FH, ldH, grid);                \
     return true;
   if (!getenv("GD_FFT_STOCKHAM")) {
-    constexpr int NR = nr_of<R>();
+    constexpr int NR = nr4_of<R>();
     switch (d.M) {
 #define GD_C2R4(MM, A, B)                                                                         \
   case MM:                                                                                        \
@@ -1112,7 +1118,7 @@ static bool launch_r2c_fixed(const ShtDev<R>& d, const FftPlan& plan, const R* g
     k_r2c_t<R, MM><<<grd, 128, 0, s>>>(plan.jobs, ds, d, grid, GP, ldP, GH, ldH);                \
     return true;
   if (!getenv("GD_FFT_STOCKHAM")) {
-    constexpr int NR = nr_of<R>();
+    constexpr int NR = nr4_of<R>();
     switch (d.M) {
 #define GD_R2C4(MM, A, B)                                                                         \
   case MM:                                                                                        \
@@ -1146,8 +1152,8 @@ static bool launch_r2c_fixed(const ShtDev<R>& d, const FftPlan& plan, const R* g
 }
 
 template <typename R, typename D>
-static FftPlan make_plan(const D* descs, int ndesc, cudaStream_t s) {
-  const int NR = fft_rows_per_cta<R>();
+static FftPlan make_plan(const D* descs, int ndesc, cudaStream_t s, int M) {
+  const int NR = fft_rows_per_cta<R>(M);
   std::vector<int2> jobs;
   for (int i = 0; i < ndesc; ++i)
     for (int r = 0; r < descs[i].count; r += NR) jobs.push_back(make_int2(i, r));
@@ -1162,17 +1168,17 @@ static FftPlan make_plan(const D* descs, int ndesc, cudaStream_t s) {
   return p;
 }
 template <typename R>
-FftPlan make_c2r_plan(const SynthDesc* descs, int ndesc, cudaStream_t s) {
-  return make_plan<R>(descs, ndesc, s);
+FftPlan make_c2r_plan(const SynthDesc* descs, int ndesc, cudaStream_t s, int M) {
+  return make_plan<R>(descs, ndesc, s, M);
 }
 template <typename R>
-FftPlan make_r2c_plan(const AnalDesc* descs, int ndesc, cudaStream_t s) {
-  return make_plan<R>(descs, ndesc, s);
+FftPlan make_r2c_plan(const AnalDesc* descs, int ndesc, cudaStream_t s, int M) {
+  return make_plan<R>(descs, ndesc, s, M);
 }
-template FftPlan make_c2r_plan<double>(const SynthDesc*, int, cudaStream_t);
-template FftPlan make_c2r_plan<float>(const SynthDesc*, int, cudaStream_t);
-template FftPlan make_r2c_plan<double>(const AnalDesc*, int, cudaStream_t);
-template FftPlan make_r2c_plan<float>(const AnalDesc*, int, cudaStream_t);
+template FftPlan make_c2r_plan<double>(const SynthDesc*, int, cudaStream_t, int);
+template FftPlan make_c2r_plan<float>(const SynthDesc*, int, cudaStream_t, int);
+template FftPlan make_r2c_plan<double>(const AnalDesc*, int, cudaStream_t, int);
+template FftPlan make_r2c_plan<float>(const AnalDesc*, int, cudaStream_t, int);
 
 void free_fft_plan(FftPlan& p) {
   if (p.jobs) cudaFree(p.jobs);
@@ -1184,7 +1190,7 @@ void free_fft_plan(FftPlan& p) {
 
 template <typename R>
 static size_t fft_smem(int M) {
-  return 2 * (size_t)fft_rows_per_cta<R>() * M * sizeof(typename C2<R>::T);
+  return 2 * (size_t)nr_of<R>() * M * sizeof(typename C2<R>::T);
 }
 
 template <typename R>

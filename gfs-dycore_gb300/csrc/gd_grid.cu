@@ -27,7 +27,6 @@ __device__ __forceinline__ float epstiny_of<float>() {
 }
 
 constexpr int LMAX = 128;
-constexpr int NTMAX = 8;  // tracers handled in registers by the column kernel
 
 // Division and logarithm of the column kernel: IEEE for the FP64 path (the
 // reference restated exactly), the hardware approximations for the FP32
@@ -53,239 +52,301 @@ __device__ __forceinline__ R thuburn_half(R qa, R qb, R dm, R d0, R dp, R eta) {
   return h;
 }
 
+// Limited tracer value at interior interface t (0 < t < L) whose level
+// below is b = L-1-t: qm = q[b-1], q0 = q[b], q1 = q[b+1], q2 = q[b+2].
+// dd[k] = q(level below k) - q(level above k), clamped away from zero;
+// the one-sided boundary differences of dyn_run.f90:507-518.
 template <typename R>
-__global__ void __launch_bounds__(128) k_dyn_columns(ColumnArgs<R> a, int inverse_only) {
+__device__ __forceinline__ R half_at(int t, int L, R qm, R q0, R q1, R q2, R eta) {
+  const R eps = epstiny_of<R>();
+  R dm, d0, dp;
+  if (t == 1) {  // dd[0], top boundary
+    dm = (q1 >= R(0)) ? q1 - fmax(R(0), R(2) * q1 - q0) : q1 - fmin(R(0), R(2) * q1 - q0);
+  } else {
+    dm = q1 - q2;
+    if (fabs(dm) < eps) dm = copysign(eps, dm);
+  }
+  d0 = q0 - q1;
+  if (fabs(d0) < eps) d0 = copysign(eps, d0);
+  if (t + 1 == L) {  // dd[L], bottom boundary
+    dp = (q0 >= R(0)) ? fmax(R(0), R(2) * q0 - q1) - q0 : fmin(R(0), R(2) * q0 - q1) - q0;
+  } else {
+    dp = qm - q0;
+    if (fabs(dp) < eps) dp = copysign(eps, dp);
+  }
+  return thuburn_half(q1, q0, dm, d0, dp, eta);
+}
+
+// Level-parallel column kernel.  A CTA owns 32 adjacent grid columns (one per
+// lane, so every load and store is a 128-byte row segment) and splits the L
+// levels into blocks of LB, one block per warp.  The vertical recurrences
+// are scans: each thread sums its block, the block sums meet in shared
+// memory, and every thread adds the sums of the blocks above it (getomega's
+// top-down prefix sums, dyn_run.f90:327-337) or below it (getpresgrad's
+// bottom-up sums, :416-434).  etadot at the interfaces goes through shared
+// memory to the two levels that use it.  Phases:
+//   1. block sums of div dp, cg dbk (top-down) and of the pressure-gradient
+//      terms (bottom-up); Phillips layer pressure (pressure_data.f90:87-88);
+//   2. block offsets, dlnps/dt, etadot at the block's interfaces
+//      (dyn_run.f90:340-344);
+//   3. omega/p (:347-368), pressure gradient, vertical advection of u, v,
+//      Tv (getvadv, :453-476) and the tendencies (:190-292);
+//   4. tracers, one at a time: Thuburn-limited vertical advection
+//      (getvadv_tracers, :478-603) and horizontal advection.
+// Levels are indexed b bottom (0) to top; interface quantities t top (0)
+// to bottom; layer t = L-1-b.
+template <typename R, int LB>
+__global__ void __launch_bounds__(512) k_dyn_columns(ColumnArgs<R> a, int inverse_only) {
   extern __shared__ __align__(16) unsigned char smcol[];
-  const long ng = (long)a.nlon * a.nlat;
-  const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= ng) return;
-  const int j = (int)(p / a.nlon);
+  const int lane = threadIdx.x, w = threadIdx.y, NW = blockDim.y;
   const int L = a.L;
+  const long ng = (long)a.nlon * a.nlat;
+  const long pq = (long)blockIdx.x * 32 + lane;
+  const bool valid = pq < ng;
+  const long p = valid ? pq : ng - 1;  // lanes past the end compute a copy and store nothing
+  const int j = (int)(p / a.nlon);
+  R* part = reinterpret_cast<R*>(smcol);  // [5][NW][32] block sums
+  R* etas = part + 5 * NW * 32;            // [L+1][32] etadot
+  auto PART = [&](int q, int ww) -> R& { return part[(q * NW + ww) * 32 + lane]; };
+  auto ETA = [&](int t) -> R& { return etas[t * 32 + lane]; };
   const R* gS = a.gS;
-  // inputs through the read-only path: loads may be issued ahead of the
-  // stores to the (disjoint) analysis rows
   auto S = [&](int row) -> R { return __ldg(gS + (long)row * ng + p); };
   const R* ak = a.ak;
   const R* bk = a.bk;
   const R* dbk = a.dbk;
   const R rd = a.rd;
-
   const R ps = exp(S(a.s.lnps));
   const R dlx = S(a.s.dlnpsdx), dly = S(a.s.dlnpsdy);
-  auto PK = [&](int t) -> R { return ak[t] + bk[t] * ps; };
-  // rlnp and alfa of the top-down layer t (pressure_data.f90:89-96)
+  auto PK = [&](int t) -> R { return __ldg(ak + t) + __ldg(bk + t) * ps; };
   auto RLN = [&](int t, R pkt, R pkt1) -> R { return (t == 0) ? a.rlnp_top : clog(cdiv(pkt1, pkt)); };
-  // getomega prefix sums in shared memory, [t][thread]
-  R* DBs = reinterpret_cast<R*>(smcol);
-  R* CBs = DBs + (long)L * blockDim.x;
-  auto DB = [&](int t) -> R& { return DBs[t * blockDim.x + threadIdx.x]; };
-  auto CB = [&](int t) -> R& { return CBs[t * blockDim.x + threadIdx.x]; };
+  const int b0 = w * LB;
+  const int nb = max(0, min(LB, L - b0));
 
-  // pass 1, top to bottom: getomega prefix sums (dyn_run.f90:327-337)
-  R pk_t = PK(0);
-  R db = R(0), cb = R(0);
-#pragma unroll 4
-  for (int t = 0; t < L; ++t) {
-    const int b = L - 1 - t;
-    const R pk_t1 = PK(t + 1);
-    const R dp = pk_t1 - pk_t;
-    const R cg = S(a.s.u + b) * dlx + S(a.s.v + b) * dly;
-    const R dv = S(a.s.div + b);
-    if (t == 0) {
-      db = dv * dp;
-      cb = cg * dbk[0];
-    } else {
-      db = db + dv * dp;
-      cb = cb + cg * dbk[t];
-    }
-    DB(t) = db;
-    CB(t) = cb;
-    if (a.prs)  // Phillips layer pressure (pressure_data.f90:87-88)
-      a.prs[(long)b * ng + p] =
-          pow((pow(pk_t1, a.kappa) * pk_t1 - pow(pk_t, a.kappa) * pk_t) / ((a.kappa + R(1)) * dp), R(1) / a.kappa);
-    pk_t = pk_t1;
-  }
-  const R dlnpsdt = -DB(L - 1) / ps - CB(L - 1);
-  a.psg[p] = ps;
-  a.dlnpsdt[p] = dlnpsdt;
-  auto etadot = [&](int t) -> R {  // dyn_run.f90:340-344
-    if (t == 0 || t == L) return R(0);
-    return -ps * (bk[t] * dlnpsdt + CB(t - 1)) - DB(t - 1);
-  };
-  // omega/p of layer t (dyn_run.f90:347-368) from its cg, divergence, rlnp, alfa
-  auto dlnpdt = [&](int t, R cg, R dv, R dp, R idp, R rl, R al) -> R {
-    R wb, wc;
-    if (t == 0) {
-      wb = al * (dv * dp + ps * CB(0) * dbk[0]);
-      wc = ps * cg * dbk[0];
-    } else {
-      wb = rl * (DB(t - 1) + ps * CB(t - 1)) + al * (dv * dp + ps * cg * dbk[t]);
-      wc = ps * cg * (dbk[t] + a.ck[t] * rl * idp);
-    }
-    return (wc - wb) * idp;
-  };
-  if (a.etadot)
-    for (int t = 0; t <= L; ++t) a.etadot[(long)t * ng + p] = etadot(t);
-  if (a.dlnpdtg)
-    for (int t = 0; t < L; ++t) {
-      const int b = L - 1 - t;
-      const R pkt = PK(t), pkt1 = PK(t + 1), dp = pkt1 - pkt, idp = R(1) / dp;
-      const R rl = RLN(t, pkt, pkt1), al = (t == 0) ? a.log2sp : R(1) - (pkt * idp) * rl;
+  // phase 1
+  R xdb[LB], xcb[LB];
+  R s2 = R(0), su = R(0), sv = R(0);
+#pragma unroll
+  for (int i = 0; i < LB; ++i) {
+    xdb[i] = R(0);
+    xcb[i] = R(0);
+    if (i < nb) {
+      const int b = b0 + i, t = L - 1 - b;
+      const R pkt = PK(t), pkt1 = PK(t + 1), dp = pkt1 - pkt;
       const R cg = S(a.s.u + b) * dlx + S(a.s.v + b) * dly;
-      a.dlnpdtg[(long)b * ng + p] = dlnpdt(t, cg, S(a.s.div + b), dp, idp, rl, al);
+      xdb[i] = S(a.s.div + b) * dp;
+      xcb[i] = cg * __ldg(dbk + t);
+      if (t > 0) {  // terms of the sums over the layers below a layer
+        const R rl = clog(cdiv(pkt1, pkt));
+        s2 += (__ldg(bk + t + 1) * (R(1) / pkt1) - __ldg(bk + t) * (R(1) / pkt)) * S(a.s.tv + b);
+        su += rl * S(a.s.dtvdx + b);
+        sv += rl * S(a.s.dtvdy + b);
+      }
+      if (a.prs && valid)
+        a.prs[(long)b * ng + p] =
+            pow((pow(pkt1, a.kappa) * pkt1 - pow(pkt, a.kappa) * pkt) / ((a.kappa + R(1)) * dp), R(1) / a.kappa);
     }
-  if (inverse_only) return;
+  }
+  // exclusive top-down prefix within the block (its top level is i = nb-1)
+  R dbs = R(0), cbs = R(0);
+#pragma unroll
+  for (int i = LB - 1; i >= 0; --i) {
+    const R d = xdb[i], c = xcb[i];
+    xdb[i] = dbs;
+    xcb[i] = cbs;
+    dbs += d;
+    cbs += c;
+  }
+  PART(0, w) = dbs;
+  PART(1, w) = cbs;
+  PART(2, w) = s2;
+  PART(3, w) = su;
+  PART(4, w) = sv;
+  __syncthreads();
 
+  // phase 2: offsets from the blocks above (DB, CB) and below (the rest)
+  R dbo = R(0), cbo = R(0), dbt = R(0), cbt = R(0);
+  for (int ww = NW - 1; ww >= 0; --ww) {
+    const R d = PART(0, ww), c = PART(1, ww);
+    if (ww == w) {
+      dbo = dbt;
+      cbo = cbt;
+    }
+    dbt += d;
+    cbt += c;
+  }
+  R S2 = R(0), SU = R(0), SV = R(0);
+  for (int ww = 0; ww < w; ++ww) {
+    S2 += PART(2, ww);
+    SU += PART(3, ww);
+    SV += PART(4, ww);
+  }
+  const R dlnpsdt = -dbt / ps - cbt;
+#pragma unroll
+  for (int i = 0; i < LB; ++i) {
+    xdb[i] += dbo;  // DB(t-1), CB(t-1) of layer t
+    xcb[i] += cbo;
+    if (i < nb) {
+      const int t = L - 1 - (b0 + i);
+      const R e = (t == 0) ? R(0) : -ps * (__ldg(bk + t) * dlnpsdt + xcb[i]) - xdb[i];
+      ETA(t) = e;
+      if (a.etadot && valid) a.etadot[(long)t * ng + p] = e;
+    }
+  }
+  if (w == 0) {
+    ETA(L) = R(0);
+    if (valid) {
+      if (a.etadot) a.etadot[(long)L * ng + p] = R(0);
+      a.psg[p] = ps;
+      a.dlnpsdt[p] = dlnpsdt;
+      if (!inverse_only) a.gA[(long)a.a.dlnps * ng + p] = dlnpsdt;
+    }
+  }
+  if (inverse_only && !a.dlnpdtg) return;  // uniform over the CTA
+  __syncthreads();
+
+  // phase 3
   R* gA = a.gA;
-  auto A = [&](int row) -> R& { return gA[(long)row * ng + p]; };
+  auto A = [&](int row, R v) {
+    if (valid) gA[(long)row * ng + p] = v;
+  };
   const R fcor = a.omega2 * a.sinlat[j];
   const R dphx = a.dphisdx[p], dphy = a.dphisdy[p];
-  const int nt = min(a.nt, NTMAX);
-  const R eps = epstiny_of<R>();
-  // tracer windows q[b-1..b+2], carried limited half-level value at the
-  // bottom interface of the current level (half[L] = q[0])
-  R qm1[NTMAX], q0[NTMAX], q1[NTMAX], q2[NTMAX], hb[NTMAX];
+  R uu[LB], vv[LB];
+  R um = R(0), vm = R(0), tm = R(0);
+  R uc = R(0), vc = R(0), tc = R(0);
+  if (nb > 0) {
+    if (b0 > 0) {
+      um = S(a.s.u + b0 - 1);
+      vm = S(a.s.v + b0 - 1);
+      tm = S(a.s.tv + b0 - 1);
+    }
+    uc = S(a.s.u + b0);
+    vc = S(a.s.v + b0);
+    tc = S(a.s.tv + b0);
+  }
 #pragma unroll
-  for (int iq = 0; iq < NTMAX; ++iq)
-    if (iq < nt) {
-      const int r0 = a.s.trc + iq * L;
-      qm1[iq] = R(0);
-      q0[iq] = S(r0);
-      q1[iq] = (L > 1) ? S(r0 + 1) : R(0);
-      q2[iq] = (L > 2) ? S(r0 + 2) : R(0);
-      hb[iq] = q0[iq];
-    }
-  // pass 2, bottom to top: getpresgrad suffix recurrences (dyn_run.f90:416-434),
-  // vertical advection (getvadv, :453-476; getvadv_tracers, :478-603) and the
-  // tendencies (:190-292)
-  R cofb2 = R(0), px3u = R(0), px3v = R(0);
-  R um = R(0), vm = R(0), tm = R(0), dxm = R(0), dym = R(0), rlm = R(0);  // layer below
-  R uc = S(a.s.u), vc = S(a.s.v), tc = S(a.s.tv);
-  // pressure at the interfaces below the current layer, carried upward
-  bool ipk_valid = false;
-  R pk_below = R(0), ipk_below = R(0), ipk2 = R(0);
-  // inputs of the current level, loaded one level ahead
-  R n_dtx = S(a.s.dtvdx), n_dty = S(a.s.dtvdy), n_dv = S(a.s.div), n_vr = S(a.s.vrt);
-  R n_up = (L > 1) ? S(a.s.u + 1) : R(0), n_vp = (L > 1) ? S(a.s.v + 1) : R(0), n_tp = (L > 1) ? S(a.s.tv + 1) : R(0);
-  for (int b = 0; b < L; ++b) {
-    const int t = L - 1 - b;
-    const R dtx = n_dtx, dty = n_dty, dv_b = n_dv, vr = n_vr, up = n_up, vp = n_vp, tp = n_tp;
+  for (int i = 0; i < LB; ++i) {
+    uu[i] = uc;
+    vv[i] = vc;
+    if (i >= nb) continue;
+    const int b = b0 + i, t = L - 1 - b;
+    R up = R(0), vp = R(0), tp = R(0);
     if (b + 1 < L) {
-      n_dtx = S(a.s.dtvdx + b + 1);
-      n_dty = S(a.s.dtvdy + b + 1);
-      n_dv = S(a.s.div + b + 1);
-      n_vr = S(a.s.vrt + b + 1);
-      n_up = (b + 2 < L) ? S(a.s.u + b + 2) : R(0);
-      n_vp = (b + 2 < L) ? S(a.s.v + b + 2) : R(0);
-      n_tp = (b + 2 < L) ? S(a.s.tv + b + 2) : R(0);
+      up = S(a.s.u + b + 1);
+      vp = S(a.s.v + b + 1);
+      tp = S(a.s.tv + b + 1);
     }
-    const R pkt = PK(t), pkt1 = ipk_valid ? pk_below : PK(t + 1);
-    const R ipk1 = ipk_valid ? ipk_below : R(1) / pkt1;  // 1 / pk(t+1), carried from below
-    const R ipkt = R(1) / pkt;                           // inf at the model top (pk = 0), unused there
-    const R dp = pkt1 - pkt, idp = R(1) / dp;
-    const R rl = (t == 0) ? a.rlnp_top : clog(pkt1 * ipkt);
+    const R pkt = PK(t), pkt1 = PK(t + 1), dp = pkt1 - pkt, idp = R(1) / dp;
+    const R rl = RLN(t, pkt, pkt1);
     const R al = (t == 0) ? a.log2sp : R(1) - (pkt * idp) * rl;
-    if (b > 0) cofb2 = cofb2 - rd * (bk[t + 2] * ipk2 - bk[t + 1] * ipk1) * tm;
-    if (b > 0) {
-      px3u = px3u - rd * rlm * dxm;
-      px3v = px3v - rd * rlm * dym;
-    }
-    const R cofb1 = (t == 0) ? -idp * (al * dbk[0]) : -idp * (bk[t] * rl + al * dbk[t]);
-    const R cofa = -idp * (bk[t + 1] * pkt * ipk1 - bk[t] + rl * (bk[t] - pkt * dbk[t] * idp));
-    const R prsgx =
-        cofb1 * rd * tc * ps * dlx - dphx + cofb2 * ps * dlx + px3u - rd * al * dtx - cofa * rd * tc * ps * dlx;
-    const R prsgy =
-        cofb1 * rd * tc * ps * dly - dphy + cofb2 * ps * dly + px3v - rd * al * dty - cofa * rd * tc * ps * dly;
-    const R e1 = etadot(t + 1), e0 = etadot(t);
-    const R h = R(0.5) * idp;
-    R vu = R(0), vv = R(0), vt = R(0);
-    if (b > 0) {
-      vu += e1 * (um - uc);
-      vv += e1 * (vm - vc);
-      vt += e1 * (tm - tc);
-    }
-    if (b + 1 < L) {
-      vu += e0 * (uc - up);
-      vv += e0 * (vc - vp);
-      vt += e0 * (tc - tp);
-    }
-    vu *= h;
-    vv *= h;
-    vt *= h;
     const R cg = uc * dlx + vc * dly;
-    R vq = a.kappa * dlnpdt(t, cg, dv_b, dp, idp, rl, al) * tc;
-    if (a.nt > 0) vq = cdiv(vq, R(1) + a.cvap_cp * q0[0]);
-    const R vadvv = vv - prsgy, vadvu = vu - prsgx;
-    A(a.a.ttend + b) = -uc * dtx - vc * dty - vt + vq;
-    A(a.a.fu + b) = uc * (vr + fcor) + vadvv;
-    A(a.a.fv + b) = vc * (vr + fcor) - vadvu;
-    A(a.a.ke + b) = R(0.5) * (uc * uc + vc * vc);
-    // tracers at level b: top interface kt = t (= L-1-b), bottom kb = t + 1
-#pragma unroll
-    for (int iq = 0; iq < NTMAX; ++iq) {
-      if (iq >= nt) continue;
-      R ht;
-      if (t == 0) {
-        ht = q0[iq];  // half[0] = q at the top level
-      } else {
-        // dd[k] = q(level below k) - q(level above k); interfaces kt-1, kt, kt+1
-        R dm, d0, dpp;
-        if (t - 1 == 0) {  // dd[0], top boundary (dyn_run.f90:507-513)
-          const R qt = q1[iq], qt1 = q0[iq];  // q[L-1] = q[b+1], q[L-2] = q[b]
-          dm = (qt >= R(0)) ? qt - fmax(R(0), R(2) * qt - qt1) : qt - fmin(R(0), R(2) * qt - qt1);
-        } else {
-          dm = q1[iq] - q2[iq];
-          if (fabs(dm) < eps) dm = copysign(eps, dm);
-        }
-        d0 = q0[iq] - q1[iq];
-        if (fabs(d0) < eps) d0 = copysign(eps, d0);
-        if (t + 1 == L) {  // dd[L], bottom boundary (dyn_run.f90:514-518)
-          const R qb = q0[iq], qb1 = q1[iq];
-          dpp = (qb >= R(0)) ? fmax(R(0), R(2) * qb - qb1) - qb : fmin(R(0), R(2) * qb - qb1) - qb;
-        } else {
-          dpp = qm1[iq] - q0[iq];
-          if (fabs(dpp) < eps) dpp = copysign(eps, dpp);
-        }
-        ht = thuburn_half(q1[iq], q0[iq], dm, d0, dpp, e0);
+    const R dv = S(a.s.div + b);
+    const R dbkt = __ldg(dbk + t);
+    R wb, wc;
+    if (t == 0) {
+      wb = al * (dv * dp + ps * (cg * dbkt) * dbkt);
+      wc = ps * cg * dbkt;
+    } else {
+      wb = rl * (xdb[i] + ps * xcb[i]) + al * (dv * dp + ps * cg * dbkt);
+      wc = ps * cg * (dbkt + __ldg(a.ck + t) * rl * idp);
+    }
+    const R dlnpdt = (wc - wb) * idp;  // omega / p
+    if (a.dlnpdtg && valid) a.dlnpdtg[(long)b * ng + p] = dlnpdt;
+    if (!inverse_only) {
+      const R dtx = S(a.s.dtvdx + b), dty = S(a.s.dtvdy + b);
+      const R bkt = __ldg(bk + t), bkt1 = __ldg(bk + t + 1);
+      const R ipk1 = R(1) / pkt1;
+      const R cofb2 = -rd * S2, px3u = -rd * SU, px3v = -rd * SV;
+      const R cofb1 = (t == 0) ? -idp * (al * dbkt) : -idp * (bkt * rl + al * dbkt);
+      const R cofa = -idp * (bkt1 * pkt * ipk1 - bkt + rl * (bkt - pkt * dbkt * idp));
+      const R prsgx =
+          cofb1 * rd * tc * ps * dlx - dphx + cofb2 * ps * dlx + px3u - rd * al * dtx - cofa * rd * tc * ps * dlx;
+      const R prsgy =
+          cofb1 * rd * tc * ps * dly - dphy + cofb2 * ps * dly + px3v - rd * al * dty - cofa * rd * tc * ps * dly;
+      const R e1 = ETA(t + 1), e0 = ETA(t);
+      const R h = R(0.5) * idp;
+      R vu = R(0), vvv = R(0), vt = R(0);
+      if (b > 0) {
+        vu += e1 * (um - uc);
+        vvv += e1 * (vm - vc);
+        vt += e1 * (tm - tc);
       }
-      const R vadq = idp * ((hb[iq] * e1 - ht * e0) + (q0[iq] * (e0 - e1)));
-      const int qd = a.s.dqdx + iq * L + b, qy = a.s.dqdy + iq * L + b;
-      A(a.a.qtend + iq * L + b) = -uc * S(qd) - vc * S(qy) - vadq;
-      hb[iq] = ht;
-      qm1[iq] = q0[iq];
-      q0[iq] = q1[iq];
-      q1[iq] = q2[iq];
-      q2[iq] = (b + 3 < L) ? S(a.s.trc + iq * L + b + 3) : R(0);
+      if (b + 1 < L) {
+        vu += e0 * (uc - up);
+        vvv += e0 * (vc - vp);
+        vt += e0 * (tc - tp);
+      }
+      vu *= h;
+      vvv *= h;
+      vt *= h;
+      R vq = a.kappa * dlnpdt * tc;
+      if (a.nt > 0) vq = cdiv(vq, R(1) + a.cvap_cp * S(a.s.trc + b));
+      const R vr = S(a.s.vrt + b);
+      A(a.a.ttend + b, -uc * dtx - vc * dty - vt + vq);
+      A(a.a.fu + b, uc * (vr + fcor) + (vvv - prsgy));
+      A(a.a.fv + b, vc * (vr + fcor) - (vu - prsgx));
+      A(a.a.ke + b, R(0.5) * (uc * uc + vc * vc));
+      if (t > 0) {
+        S2 += (bkt1 * ipk1 - bkt * (R(1) / pkt)) * tc;
+        SU += rl * dtx;
+        SV += rl * dty;
+      }
     }
     um = uc;
     vm = vc;
     tm = tc;
-    dxm = dtx;
-    dym = dty;
-    rlm = rl;
-    ipk2 = ipk1;  // 1 / pk(t+1) becomes 1 / pk(t'+2) for the layer above
-    pk_below = pkt;
-    ipk_below = ipkt;
-    ipk_valid = true;
     uc = up;
     vc = vp;
     tc = tp;
   }
-  A(a.a.dlnps) = dlnpsdt;
+  if (inverse_only) return;
+
+  // phase 4: tracers
+  for (int iq = 0; iq < a.nt; ++iq) {
+    const int r0 = a.s.trc + iq * L;
+    auto Q = [&](int b) -> R { return (b >= 0 && b < L) ? S(r0 + b) : R(0); };
+    R qm = Q(b0 - 1), q0 = Q(b0), q1 = Q(b0 + 1), q2 = Q(b0 + 2);
+    // limited value at the bottom interface of level b0 (half[L] = q[0])
+    R hb = (b0 == 0) ? q0 : half_at(L - b0, L, Q(b0 - 2), qm, q0, q1, ETA(L - b0));
+#pragma unroll
+    for (int i = 0; i < LB; ++i) {
+      if (i >= nb) continue;
+      const int b = b0 + i, t = L - 1 - b;
+      const R e0 = ETA(t), e1 = ETA(t + 1);
+      const R ht = (t == 0) ? q0 : half_at(t, L, qm, q0, q1, q2, e0);
+      const R idp = R(1) / (PK(t + 1) - PK(t));
+      const R vadq = idp * ((hb * e1 - ht * e0) + (q0 * (e0 - e1)));
+      A(a.a.qtend + iq * L + b, -uu[i] * S(a.s.dqdx + iq * L + b) - vv[i] * S(a.s.dqdy + iq * L + b) - vadq);
+      hb = ht;
+      qm = q0;
+      q0 = q1;
+      q1 = q2;
+      q2 = Q(b + 3);
+    }
+  }
+}
+
+template <typename R, int LB>
+static void launch_cols_lb(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t s) {
+  const long ng = (long)a.nlon * a.nlat;
+  const int nw = ceil_div(a.L, LB);
+  const size_t sm = (size_t)(5 * nw + a.L + 1) * 32 * sizeof(R);
+  if (sm > 48 * 1024)
+    GD_CUDA(cudaFuncSetAttribute(k_dyn_columns<R, LB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_dyn_columns<R, LB><<<(unsigned)ceil_div(ng, 32), dim3(32, nw), sm, s>>>(a, inverse_only ? 1 : 0);
 }
 
 template <typename R>
 void launch_dyn_columns(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t s) {
-  if (a.L > LMAX - 1) throw std::runtime_error("nlev too large for the column kernel");
-  if (a.nt > NTMAX) throw std::runtime_error("ntrac too large for the column kernel");
-  long ng = (long)a.nlon * a.nlat;
-  const size_t sm = 2 * (size_t)a.L * 128 * sizeof(R);
-  static bool attr = false;
-  if (!attr) {
-    GD_CUDA(cudaFuncSetAttribute(k_dyn_columns<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr = true;
-  }
-  k_dyn_columns<R><<<ceil_div(ng, 128), 128, sm, s>>>(a, inverse_only ? 1 : 0);
+  if (a.L < 1 || a.L > LMAX) throw std::runtime_error("nlev out of range for the column kernel");
+  // levels per warp: at most 16 warps per CTA
+  static const int lb_env = getenv("GD_COL_LB") ? atoi(getenv("GD_COL_LB")) : 0;
+  int lb = lb_env == 4 || lb_env == 8 ? lb_env : (a.L <= 32 ? 4 : 8);
+  if (ceil_div(a.L, lb) > 16) lb = 8;
+  if (lb == 4)
+    launch_cols_lb<R, 4>(a, inverse_only, s);
+  else
+    launch_cols_lb<R, 8>(a, inverse_only, s);
   count_launch();
   GD_LAUNCH_CHECK();
 }

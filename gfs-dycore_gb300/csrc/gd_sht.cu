@@ -849,6 +849,13 @@ template <int M, int M1>
 __device__ __forceinline__ int pad_addr(int n) {
   return n + n / M1;
 }
+// Row pitch (complex elements): the padded length plus an extra offset chosen
+// by counting shared-memory wavefronts of all four phases (gather, step A,
+// step B, store) for 8 rows of float2 per CTA.
+template <int M, int M1>
+constexpr int row_pitch4() {
+  return M + M / M1 + (M == 192 ? 12 : M == 384 ? 10 : M == 576 ? 2 : 0);
+}
 
 template <typename R, int N, int M, int SIGN, int S>
 __device__ __forceinline__ void reg_stages(typename C2<R>::T* x, typename C2<R>::T* y,
@@ -919,7 +926,7 @@ __device__ __forceinline__ void reg_fft(typename C2<R>::T* x, typename C2<R>::T*
 template <typename R, int M, int M1, int M2, int NR, int NT, int SIGN>
 __device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R>::T* __restrict__ tw) {
   typedef typename C2<R>::T V;
-  constexpr int RP = M + M / M1;  // padded row length
+  constexpr int RP = row_pitch4<M, M1>();
   // step A: thread (r, n1) -> M2-point DFT over n2 of x[n1 + M1 n2], twiddle, store in place
   for (int e = threadIdx.x; e < NR * M1; e += NT) {
     const int r = e / M1, n1 = e - r * M1;
@@ -965,7 +972,7 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
     k_c2r_4(const int2* __restrict__ jobs, const SynthDesc* __restrict__ descs, ShtDev<R> d,
             const R* __restrict__ FP, long ldP, const R* __restrict__ FH, long ldH, R* __restrict__ grid) {
   typedef typename C2<R>::T V;
-  constexpr int NR = nr4_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = M + M / M1;
+  constexpr int NR = nr4_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = row_pitch4<M, M1>();
   __shared__ V buf[NR * RP];
   const int T = d.T, nlat = d.nlat, nlon = d.nlon;
   const int2 jb = jobs[blockIdx.x];
@@ -1009,7 +1016,7 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
     k_r2c_4(const int2* __restrict__ jobs, const AnalDesc* __restrict__ descs, ShtDev<R> d,
             const R* __restrict__ grid, R* __restrict__ GP, long ldP, R* __restrict__ GH, long ldH) {
   typedef typename C2<R>::T V;
-  constexpr int NR = nr4_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = M + M / M1;
+  constexpr int NR = nr4_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = row_pitch4<M, M1>();
   __shared__ V buf[NR * RP];
   const int T = d.T, nlat = d.nlat, nlon = d.nlon;
   const int2 jb = jobs[blockIdx.x];

@@ -52,6 +52,21 @@ struct C2<float> {
   typedef float2 T;
 };
 
+// two complex values in one aligned load (16 bytes FP32, 32 bytes FP64)
+struct __align__(32) GdDouble4 {
+  double x, y, z, w;
+};
+template <typename R>
+struct C4;
+template <>
+struct C4<double> {
+  typedef GdDouble4 T;
+};
+template <>
+struct C4<float> {
+  typedef float4 T;
+};
+
 template <typename R>
 __host__ __device__ inline typename C2<R>::T mk2(R x, R y) {
   typename C2<R>::T v;

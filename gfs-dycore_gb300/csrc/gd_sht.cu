@@ -933,7 +933,7 @@ __device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R
     V* row = buf + r * RP;
     V x[M2], y[M2];
 #pragma unroll
-    for (int n2 = 0; n2 < M2; ++n2) x[n2] = row[pad_addr<M, M1>(n1 + M1 * n2)];
+    for (int n2 = 0; n2 < M2; ++n2) x[n2] = row[n1 + (M1 + 1) * n2];  // pad_addr(n1 + M1 n2), n1 < M1
     reg_fft<R, M2, M, SIGN>(x, y, tw);
 #pragma unroll
     for (int k2 = 1; k2 < M2; ++k2) {
@@ -944,7 +944,7 @@ __device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R
       }
     }
 #pragma unroll
-    for (int k2 = 0; k2 < M2; ++k2) row[pad_addr<M, M1>(n1 + M1 * k2)] = x[k2];
+    for (int k2 = 0; k2 < M2; ++k2) row[n1 + (M1 + 1) * k2] = x[k2];
   }
   __syncthreads();
   // step B: thread (r, k2) -> M1-point DFT over n1 of Y[n1 + M1 k2]; result X[k2 + M2 k1]
@@ -953,9 +953,9 @@ __device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R
   const int r = e / M2, k2 = e - r * M2;
   V x[M1], y[M1];
   if (e < NR * M2) {
-    V* row = buf + r * RP;
+    const V* row = buf + r * RP + (M1 + 1) * k2;  // pad_addr(n1 + M1 k2) = n1 + (M1 + 1) k2
 #pragma unroll
-    for (int n1 = 0; n1 < M1; ++n1) x[n1] = row[pad_addr<M, M1>(n1 + M1 * k2)];
+    for (int n1 = 0; n1 < M1; ++n1) x[n1] = row[n1];
     reg_fft<R, M1, M, SIGN>(x, y, tw);
   }
   __syncthreads();
@@ -967,8 +967,13 @@ __device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R
   __syncthreads();
 }
 
+// Minimum resident CTAs per SM: these kernels are latency-bound and run
+// best at the occupancy their shared memory allows (measured: c2r with 5,
+// r2c with 4 CTAs of 8 FP32 rows of 576 points; without a bound the
+// compiler takes more registers and fewer CTAs fit).
+constexpr int C2R4_MINB = 5, R2C4_MINB = 4;
 template <typename R, int M, int M1, int M2>
-__global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32) * 32)
+__global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, C2R4_MINB)
     k_c2r_4(const int2* __restrict__ jobs, const SynthDesc* __restrict__ descs, ShtDev<R> d,
             const R* __restrict__ FP, long ldP, const R* __restrict__ FH, long ldH, R* __restrict__ grid) {
   typedef typename C2<R>::T V;
@@ -1012,7 +1017,7 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
 }
 
 template <typename R, int M, int M1, int M2>
-__global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32) * 32)
+__global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, R2C4_MINB)
     k_r2c_4(const int2* __restrict__ jobs, const AnalDesc* __restrict__ descs, ShtDev<R> d,
             const R* __restrict__ grid, R* __restrict__ GP, long ldP, R* __restrict__ GH, long ldH) {
   typedef typename C2<R>::T V;
@@ -1023,11 +1028,28 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
   const AnalDesc ds = descs[jb.x];
   const int j = blockIdx.y, r0 = jb.y;
   const int nr = min(NR, ds.count - r0);
-  for (int e = threadIdx.x; e < NR * M; e += NT) {
-    const int r = e / M, n = e - r * M;
-    V z = mk2<R>(R(0), R(0));
-    if (r < nr) z = *reinterpret_cast<const V*>(grid + ((long)(ds.src + r0 + r) * nlat + j) * nlon + 2 * n);
-    buf[r * RP + pad_addr<M, M1>(n)] = z;
+  // Rows loaded two complex values per load, in batches issued ahead of use.
+  typedef typename C4<R>::T V4;
+  constexpr int NE = NR * M / 2, NIT = (NE + NT - 1) / NT, GB = 3;
+  for (int it0 = 0; it0 < NIT; it0 += GB) {
+    V4 z[GB];
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int e = threadIdx.x + (it0 + u) * NT;
+      z[u].x = z[u].y = z[u].z = z[u].w = R(0);
+      if (it0 + u < NIT && e < NE) {
+        const int r = e / (M / 2), n = 2 * (e - r * (M / 2));
+        if (r < nr) z[u] = *reinterpret_cast<const V4*>(grid + ((long)(ds.src + r0 + r) * nlat + j) * nlon + 2 * n);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int e = threadIdx.x + (it0 + u) * NT;
+      if (it0 + u >= NIT || e >= NE) continue;
+      const int r = e / (M / 2), n = 2 * (e - r * (M / 2));
+      buf[r * RP + pad_addr<M, M1>(n)] = mk2<R>(z[u].x, z[u].y);
+      buf[r * RP + pad_addr<M, M1>(n + 1)] = mk2<R>(z[u].z, z[u].w);
+    }
   }
   __syncthreads();
   fft4<R, M, M1, M2, NR, NT, -1>(buf, d.twM);

@@ -10,6 +10,7 @@
 namespace gd {
 
 constexpr int QC = 16;  // spectral coefficients (same degree n) per CTA
+static_assert(QC % 4 == 0, "the matvec works on groups of four coefficients");
 
 std::vector<int4> make_stage_items(int T, int qc) {
   std::vector<int4> it;
@@ -28,21 +29,37 @@ __device__ __forceinline__ V vz() {
 
 // Y[i][k] = sum_j A[k][j] X[i][j] for i < cnt (complex X, real A).  AT
 // holds A transposed (AT[j][k] = A[k][j]) so a warp's loads of one j are
-// contiguous over k; the L x L matrices stay L1-resident.  X, Y index-major.
+// contiguous over k; the L x L matrices stay L1-resident.  X, Y index-major
+// with QC rows.  A thread owns one output level k of four coefficients, so
+// each matrix element it loads feeds eight FMAs; the X reads are warp
+// broadcasts.  Rows past cnt are computed from unused shared memory and
+// not stored.
 template <typename R, typename V>
 __device__ __forceinline__ void smem_matvec(const R* __restrict__ AT, const V* X, V* Y, int L, int cnt) {
-  for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {
-    const int i = e / L, k = e - i * L;
-    R ax = 0, ay = 0;
-    const V* Xi = X + i * L;
+  const int nq = (cnt + 3) >> 2;
+  for (int e = threadIdx.x; e < L * nq; e += blockDim.x) {
+    const int q = e / L, k = e - q * L;
+    const int i0 = 4 * q;
+    R ax[4], ay[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) ax[u] = ay[u] = R(0);
+    const V* X0 = X + i0 * L;
+#pragma unroll 4
     for (int j = 0; j < L; ++j) {
-      const R aj = AT[(long)j * L + k];
-      const V x = Xi[j];
-      ax += aj * x.x;
-      ay += aj * x.y;
+      const R aj = __ldg(AT + j * L + k);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const V x = X0[u * L + j];
+        ax[u] += aj * x.x;
+        ay[u] += aj * x.y;
+      }
     }
-    Y[i * L + k].x = ax;
-    Y[i * L + k].y = ay;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (i0 + u < cnt) {
+        Y[(i0 + u) * L + k].x = ax[u];
+        Y[(i0 + u) * L + k].y = ay[u];
+      }
   }
 }
 
@@ -88,7 +105,7 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
   const R il = (n == 0) ? R(0) : R(1) / lap;
   const int s = a.stage;
   R* TDs = s == 0 ? a.TD0 : (s == 1 ? a.TD1 : a.TD2);
-  const R* TDr[3] = {a.TD0, a.TD1, a.TD2};
+  auto TDr = [&](int r) -> const R* { return r == 0 ? a.TD0 : (r == 1 ? a.TD1 : a.TD2); };
   auto IDX = [&](int i) -> long { return a.moff[m0 + i] + (n - m0 - i); };
 
   for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {
@@ -142,11 +159,11 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
     for (int r = 0; r <= s; ++r) {
       V x_vr = dvrt, x_dv = ddiv, x_tv = dtv, x_dl = ddl, x_tl = dtl;
       if (r < s) {
-        x_vr = ld2(TDr[r], idx, a.ldTD, a.tc.dvrt + k);
-        x_dv = ld2(TDr[r], idx, a.ldTD, a.tc.ddiv + k);
-        x_tv = ld2(TDr[r], idx, a.ldTD, a.tc.dtv + k);
-        x_dl = ld2(TDr[r], idx, a.ldTD, a.tc.ddl + k);
-        x_tl = ld2(TDr[r], idx, a.ldTD, a.tc.dtl + k);
+        x_vr = ld2(TDr(r), idx, a.ldTD, a.tc.dvrt + k);
+        x_dv = ld2(TDr(r), idx, a.ldTD, a.tc.ddiv + k);
+        x_tv = ld2(TDr(r), idx, a.ldTD, a.tc.dtv + k);
+        x_dl = ld2(TDr(r), idx, a.ldTD, a.tc.ddl + k);
+        x_tl = ld2(TDr(r), idx, a.ldTD, a.tc.dtl + k);
       }
       svr.x += a.ce[r] * x_vr.x;
       svr.y += a.ce[r] * x_vr.y;
@@ -182,7 +199,7 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
       V q = ld2(a.S0, idx, a.ldS, a.sc.trc + col);
       V sq = vz<V>();
       for (int r = 0; r <= s; ++r) {
-        V x = (r < s) ? ld2(TDr[r], idx, a.ldTD, a.tc.dtrc + col) : dq;
+        V x = (r < s) ? ld2(TDr(r), idx, a.ldTD, a.tc.dtrc + col) : dq;
         sq.x += a.ce[r] * x.x;
         sq.y += a.ce[r] * x.y;
       }
@@ -213,8 +230,8 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
     for (int r = 0; r <= s; ++r) {
       V x = dl, xp = dpl;
       if (r < s) {
-        x = ld2(TDr[r], idx, a.ldTD, a.tc.dlnps);
-        xp = ld2(TDr[r], idx, a.ldTD, a.tc.dpl);
+        x = ld2(TDr(r), idx, a.ldTD, a.tc.dlnps);
+        xp = ld2(TDr(r), idx, a.ldTD, a.tc.dpl);
       }
       sl.x += a.ce[r] * x.x + a.ci[r] * xp.x;
       sl.y += a.ce[r] * x.y + a.ci[r] * xp.y;

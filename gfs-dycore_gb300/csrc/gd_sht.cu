@@ -844,7 +844,8 @@ __global__ void __launch_bounds__(128) k_r2c_t(const int2* __restrict__ jobs, co
 // M1-point DFTs in registers.  Rows live in shared memory with one pad
 // element after every M1 values so the strided exchanges are bank-conflict
 // free.  The in-register DFTs are fully unrolled Stockham passes over the
-// compile-time radix plan; their twiddles come from the length-M table.
+// compile-time radix plan with compile-time twiddles; the twiddle between
+// the steps comes from the length-M table.
 template <int M, int M1>
 __device__ __forceinline__ int pad_addr(int n) {
   return n + n / M1;
@@ -857,65 +858,125 @@ constexpr int row_pitch4() {
   return M + M / M1 + (M == 192 ? 12 : M == 384 ? 10 : M == 576 ? 2 : 0);
 }
 
-template <typename R, int N, int M, int SIGN, int S>
-__device__ __forceinline__ void reg_stages(typename C2<R>::T* x, typename C2<R>::T* y,
-                                           const typename C2<R>::T* __restrict__ tw) {
+// cos and sin of 2 pi a / b at compile time: exact octant reduction in
+// integers, then Taylor series on an angle of at most pi/4 (the terms fall
+// below 1e-17 of the sum after 12 of them).  Used for the twiddles of the
+// in-register DFTs, which become immediate operands.
+struct CtCS {
+  double c, s;
+};
+constexpr double ct_taylor_cos(double t) {
+  double term = 1.0, sum = 1.0;
+  for (int i = 1; i <= 14; ++i) {
+    term *= -t * t / ((2.0 * i - 1.0) * (2.0 * i));
+    sum += term;
+  }
+  return sum;
+}
+constexpr double ct_taylor_sin(double t) {
+  double term = t, sum = t;
+  for (int i = 1; i <= 14; ++i) {
+    term *= -t * t / ((2.0 * i) * (2.0 * i + 1.0));
+    sum += term;
+  }
+  return sum;
+}
+constexpr CtCS ct_cs_turn(long a, long b) {  // angle 2 pi a / b
+  long r = a % b;
+  if (r < 0) r += b;
+  // fraction f = r / b of a turn; reduce to [0, 1/8] with exact rationals
+  // in units of 1 / (8 b)
+  long u = 8 * r;  // f * 8b
+  const long B8 = 8 * b;
+  double sc = 1.0, ss = 1.0;
+  bool swap = false;
+  if (u > B8 / 2) {  // f in (1/2, 1): cos(2pi - x) = cos x, sin = -sin
+    u = B8 - u;
+    ss = -ss;
+  }
+  if (u > B8 / 4) {  // f in (1/4, 1/2]: cos(pi - x) = -cos x, sin = sin
+    u = B8 / 2 - u;
+    sc = -sc;
+  }
+  if (u > B8 / 8) {  // f in (1/8, 1/4]: cos x = sin(pi/2 - x)
+    u = B8 / 4 - u;
+    swap = true;
+  }
+  const double t = 2.0 * 3.14159265358979323846264338327950288 * (double)u / (double)B8;
+  const double c0 = ct_taylor_cos(t), s0 = ct_taylor_sin(t);
+  return CtCS{sc * (swap ? s0 : c0), ss * (swap ? c0 : s0)};
+}
+// x * W_M^E for SIGN < 0 (W = exp(-2 pi i / M)), x * conj(W_M^E) for SIGN > 0
+template <typename R, int SIGN, long E, long M>
+__device__ __forceinline__ typename C2<R>::T ct_twiddle(typename C2<R>::T x) {
+  if constexpr (E % M == 0) {
+    return x;
+  } else {
+    constexpr CtCS cs = ct_cs_turn(E, M);
+    constexpr R wc = (R)cs.c, ws = (R)(SIGN > 0 ? cs.s : -cs.s);
+    typename C2<R>::T r;
+    r.x = x.x * wc - x.y * ws;
+    r.y = x.x * ws + x.y * wc;
+    return r;
+  }
+}
+
+// one radix-p butterfly (index JJ of the stage) and the rest of the stage
+template <typename R, int N, int M, int SIGN, int S, int JJ>
+__device__ __forceinline__ void reg_bfly(const typename C2<R>::T* x, typename C2<R>::T* y) {
   typedef typename C2<R>::T V;
-  if constexpr (S < FftPlanC<N>::count()) {
-    constexpr int p = FftPlanC<N>::radix(S), Ns = FftPlanC<N>::ns(S), nb = N / p;
-    constexpr int tstep = (M / N) * (N / (Ns * p));  // W_{Ns p} = W_M^(M/(Ns p))
-#pragma unroll
-    for (int jj = 0; jj < nb; ++jj) {
-      const int k = jj % Ns;
-      V v[4];
-#pragma unroll
-      for (int q = 0; q < p; ++q) {
-        V xv = x[jj + q * nb];
-        if (q > 0 && k > 0) {
-          V w = tw[k * q * tstep];
-          if (SIGN > 0) w.y = -w.y;
-          xv = cmul(xv, w);
-        }
-        v[q] = xv;
-      }
-      if (p == 2) {
-        V t = v[0];
-        v[0] = cadd(t, v[1]);
-        v[1] = csub(t, v[1]);
-      } else if (p == 4) {
-        V s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
-        V s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
-        V id13;
-        id13.x = -SIGN * d13.y;
-        id13.y = SIGN * d13.x;
-        v[0] = cadd(s02, s13);
-        v[2] = csub(s02, s13);
-        v[1] = cadd(d02, id13);
-        v[3] = csub(d02, id13);
-      } else {
-        const R c3 = R(-0.5), s3 = R(0.86602540378443864676) * R(SIGN);
-        V t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
-        V m1, m2;
-        m1.x = v[0].x + c3 * t1.x;
-        m1.y = v[0].y + c3 * t1.y;
-        m2.x = -s3 * t2.y;
-        m2.y = s3 * t2.x;
-        v[0] = cadd(v[0], t1);
-        v[1] = cadd(m1, m2);
-        v[2] = csub(m1, m2);
-      }
-      const int od = (jj / Ns) * Ns * p + k;
-#pragma unroll
-      for (int q = 0; q < p; ++q) y[od + q * Ns] = v[q];
+  constexpr int p = FftPlanC<N>::radix(S), Ns = FftPlanC<N>::ns(S), nb = N / p;
+  if constexpr (JJ < nb) {
+    constexpr int k = JJ % Ns;
+    constexpr long tstep = (M / N) * (N / (Ns * p));  // W_{Ns p} = W_M^(M/(Ns p))
+    V v[4];
+    v[0] = x[JJ];
+    v[1] = ct_twiddle<R, SIGN, 1L * k * tstep, M>(x[JJ + nb]);
+    if constexpr (p > 2) v[2] = ct_twiddle<R, SIGN, 2L * k * tstep, M>(x[JJ + 2 * nb]);
+    if constexpr (p > 3) v[3] = ct_twiddle<R, SIGN, 3L * k * tstep, M>(x[JJ + 3 * nb]);
+    if constexpr (p == 2) {
+      V t = v[0];
+      v[0] = cadd(t, v[1]);
+      v[1] = csub(t, v[1]);
+    } else if constexpr (p == 4) {
+      V s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+      V s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+      V id13;
+      id13.x = -SIGN * d13.y;
+      id13.y = SIGN * d13.x;
+      v[0] = cadd(s02, s13);
+      v[2] = csub(s02, s13);
+      v[1] = cadd(d02, id13);
+      v[3] = csub(d02, id13);
+    } else {
+      const R c3 = R(-0.5), s3 = R(0.86602540378443864676) * R(SIGN);
+      V t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
+      V m1, m2;
+      m1.x = v[0].x + c3 * t1.x;
+      m1.y = v[0].y + c3 * t1.y;
+      m2.x = -s3 * t2.y;
+      m2.y = s3 * t2.x;
+      v[0] = cadd(v[0], t1);
+      v[1] = cadd(m1, m2);
+      v[2] = csub(m1, m2);
     }
-    reg_stages<R, N, M, SIGN, S + 1>(y, x, tw);
+    constexpr int od = (JJ / Ns) * Ns * p + k;
+#pragma unroll
+    for (int q = 0; q < p; ++q) y[od + q * Ns] = v[q];
+    reg_bfly<R, N, M, SIGN, S, JJ + 1>(x, y);
+  }
+}
+template <typename R, int N, int M, int SIGN, int S>
+__device__ __forceinline__ void reg_stages(typename C2<R>::T* x, typename C2<R>::T* y) {
+  if constexpr (S < FftPlanC<N>::count()) {
+    reg_bfly<R, N, M, SIGN, S, 0>(x, y);
+    reg_stages<R, N, M, SIGN, S + 1>(y, x);
   }
 }
 // in-register N-point DFT of x (y is scratch); the result is left in x
 template <typename R, int N, int M, int SIGN>
-__device__ __forceinline__ void reg_fft(typename C2<R>::T* x, typename C2<R>::T* y,
-                                        const typename C2<R>::T* __restrict__ tw) {
-  reg_stages<R, N, M, SIGN, 0>(x, y, tw);
+__device__ __forceinline__ void reg_fft(typename C2<R>::T* x, typename C2<R>::T* y) {
+  reg_stages<R, N, M, SIGN, 0>(x, y);
   if constexpr (FftPlanC<N>::count() % 2 == 1) {
 #pragma unroll
     for (int i = 0; i < N; ++i) x[i] = y[i];
@@ -934,7 +995,7 @@ __device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R
     V x[M2], y[M2];
 #pragma unroll
     for (int n2 = 0; n2 < M2; ++n2) x[n2] = row[n1 + (M1 + 1) * n2];  // pad_addr(n1 + M1 n2), n1 < M1
-    reg_fft<R, M2, M, SIGN>(x, y, tw);
+    reg_fft<R, M2, M, SIGN>(x, y);
 #pragma unroll
     for (int k2 = 1; k2 < M2; ++k2) {
       if (n1 > 0) {
@@ -956,7 +1017,7 @@ __device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R
     const V* row = buf + r * RP + (M1 + 1) * k2;  // pad_addr(n1 + M1 k2) = n1 + (M1 + 1) k2
 #pragma unroll
     for (int n1 = 0; n1 < M1; ++n1) x[n1] = row[n1];
-    reg_fft<R, M1, M, SIGN>(x, y, tw);
+    reg_fft<R, M1, M, SIGN>(x, y);
   }
   __syncthreads();
   if (e < NR * M2) {
@@ -977,7 +1038,10 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
     k_c2r_4(const int2* __restrict__ jobs, const SynthDesc* __restrict__ descs, ShtDev<R> d,
             const R* __restrict__ FP, long ldP, const R* __restrict__ FH, long ldH, R* __restrict__ grid) {
   typedef typename C2<R>::T V;
+  typedef typename C4<R>::T V4;
   constexpr int NR = nr4_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = row_pitch4<M, M1>();
+  constexpr int KS = NT / NR;  // order stride of one thread in the gather
+  static_assert(NT % NR == 0 && M1 % 2 == 0, "thread maps of the four-step kernels");
   __shared__ V buf[NR * RP];
   const int T = d.T, nlat = d.nlat, nlon = d.nlon;
   const int2 jb = jobs[blockIdx.x];
@@ -985,14 +1049,52 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
   const int j = blockIdx.y, r0 = jb.y;
   const int nr = min(NR, ds.count - r0);
   const R rc = d.rcos[j], alpha = (R)ds.alpha, beta = (R)ds.beta;
-  for (int e = threadIdx.x; e < NR * (M / 2 + 1); e += NT) {
-    const int kk = e / NR, r = e - kk * NR;
+  // gather: the thread's row r is fixed, its orders are kq, kq + KS, ...
+  const int r = threadIdx.x % NR, kq = threadIdx.x / NR;
+  const bool live = r < nr;
+  const R* pa = nullptr;
+  const R* pb = nullptr;
+  long sa = 0, sb = 0;  // distance between consecutive orders
+  if (live && ds.srcA >= 0) {
+    const long ld = ds.srcA == 0 ? ldP : ldH;
+    pa = (ds.srcA == 0 ? FP : FH) + (long)j * ld + 2 * (ds.colA + r0 + r);
+    sa = (long)nlat * ld;
+  }
+  if (live && ds.srcB >= 0) {
+    const long ld = ds.srcB == 0 ? ldP : ldH;
+    pb = (ds.srcB == 0 ? FP : FH) + (long)j * ld + 2 * (ds.colB + r0 + r);
+    sb = (long)nlat * ld;
+  }
+  V* brow = buf + r * RP;
+  for (int kk = kq; kk <= M / 2; kk += KS) {
+    const int k2 = M - kk;
     V z1 = mk2<R>(R(0), R(0)), z2 = z1;
-    if (r < nr) {
-      const int k2 = M - kk;
-      const V x1 = synth_coef<R>(ds, kk, T, j, nlat, r0 + r, FP, ldP, FH, ldH, rc, alpha, beta);
-      const V x2 = (kk == 0) ? mk2<R>(R(0), R(0))
-                             : synth_coef<R>(ds, k2, T, j, nlat, r0 + r, FP, ldP, FH, ldH, rc, alpha, beta);
+    if (live && kk <= T) {  // kk > T: both orders above the truncation, z = 0
+      // x_k = alpha A_k + beta (i k / cos) B_k, zero above the truncation
+      V x1 = z1, x2 = z1;
+      if (pa) {
+        const V v1 = *reinterpret_cast<const V*>(pa + kk * sa);
+        x1.x = alpha * v1.x;
+        x1.y = alpha * v1.y;
+        if (kk > 0 && k2 <= T) {
+          const V v2 = *reinterpret_cast<const V*>(pa + k2 * sa);
+          x2.x = alpha * v2.x;
+          x2.y = alpha * v2.y;
+        }
+      }
+      if (pb) {
+        const V v1 = *reinterpret_cast<const V*>(pb + kk * sb);
+        const R f1 = beta * (R)kk * rc;
+        x1.x -= f1 * v1.y;
+        x1.y += f1 * v1.x;
+        if (kk > 0 && k2 <= T) {
+          const V v2 = *reinterpret_cast<const V*>(pb + k2 * sb);
+          const R f2 = beta * (R)k2 * rc;
+          x2.x -= f2 * v2.y;
+          x2.y += f2 * v2.x;
+        }
+      }
+      if (kk == 0) x1.y = R(0);
       V A = cadd(x1, cconj(x2)), B = csub(x1, cconj(x2));
       V Bw = cmul(B, cconj(d.twN[kk]));
       z1.x = A.x - Bw.y;
@@ -1004,15 +1106,28 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
         z2.y = A2.y + Bw2.x;
       }
     }
-    buf[r * RP + pad_addr<M, M1>(kk)] = z1;
-    if (kk > 0 && M - kk != kk) buf[r * RP + pad_addr<M, M1>(M - kk)] = z2;
+    brow[pad_addr<M, M1>(kk)] = z1;
+    if (kk > 0 && k2 != kk) brow[pad_addr<M, M1>(k2)] = z2;
   }
   __syncthreads();
   fft4<R, M, M1, M2, NR, NT, +1>(buf, d.twM);
-  for (int e = threadIdx.x; e < nr * M; e += NT) {
-    const int r = e / M, n = e - r * M;
-    *reinterpret_cast<V*>(grid + ((long)(ds.dst + r0 + r) * nlat + j) * nlon + 2 * n) =
-        buf[r * RP + pad_addr<M, M1>(n)];
+  // store: two complex values (n even, n + 1; adjacent in the padded row)
+  // per store, NR * M / 2 stores spread evenly over the threads
+  constexpr int NS = NR * M / 2;
+#pragma unroll 4
+  for (int it = 0; it < (NS + NT - 1) / NT; ++it) {
+    const int e = threadIdx.x + it * NT;
+    const int rr = e / (M / 2), q = e - rr * (M / 2);
+    if (e < NS && rr < nr) {
+      const int pn = rr * RP + pad_addr<M, M1>(2 * q);
+      const V u = buf[pn], w = buf[pn + 1];
+      V4 o;
+      o.x = u.x;
+      o.y = u.y;
+      o.z = w.x;
+      o.w = w.y;
+      *reinterpret_cast<V4*>(grid + ((long)(ds.dst + r0 + rr) * nlat + j) * nlon + 4 * q) = o;
+    }
   }
 }
 
@@ -1021,15 +1136,18 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
     k_r2c_4(const int2* __restrict__ jobs, const AnalDesc* __restrict__ descs, ShtDev<R> d,
             const R* __restrict__ grid, R* __restrict__ GP, long ldP, R* __restrict__ GH, long ldH) {
   typedef typename C2<R>::T V;
+  typedef typename C4<R>::T V4;
   constexpr int NR = nr4_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = row_pitch4<M, M1>();
+  constexpr int KS = NT / NR;
+  static_assert(NT % NR == 0 && M1 % 2 == 0, "thread maps of the four-step kernels");
   __shared__ V buf[NR * RP];
   const int T = d.T, nlat = d.nlat, nlon = d.nlon;
   const int2 jb = jobs[blockIdx.x];
   const AnalDesc ds = descs[jb.x];
   const int j = blockIdx.y, r0 = jb.y;
   const int nr = min(NR, ds.count - r0);
-  // Rows loaded two complex values per load, in batches issued ahead of use.
-  typedef typename C4<R>::T V4;
+  // load: two complex values per load, NR * M / 2 loads spread evenly over
+  // the threads, in batches issued ahead of their use; rows past nr zero
   constexpr int NE = NR * M / 2, NIT = (NE + NT - 1) / NT, GB = 3;
   for (int it0 = 0; it0 < NIT; it0 += GB) {
     V4 z[GB];
@@ -1038,25 +1156,34 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
       const int e = threadIdx.x + (it0 + u) * NT;
       z[u].x = z[u].y = z[u].z = z[u].w = R(0);
       if (it0 + u < NIT && e < NE) {
-        const int r = e / (M / 2), n = 2 * (e - r * (M / 2));
-        if (r < nr) z[u] = *reinterpret_cast<const V4*>(grid + ((long)(ds.src + r0 + r) * nlat + j) * nlon + 2 * n);
+        const int rr = e / (M / 2), q = e - rr * (M / 2);
+        if (rr < nr) z[u] = *reinterpret_cast<const V4*>(grid + ((long)(ds.src + r0 + rr) * nlat + j) * nlon + 4 * q);
       }
     }
 #pragma unroll
     for (int u = 0; u < GB; ++u) {
       const int e = threadIdx.x + (it0 + u) * NT;
       if (it0 + u >= NIT || e >= NE) continue;
-      const int r = e / (M / 2), n = 2 * (e - r * (M / 2));
-      buf[r * RP + pad_addr<M, M1>(n)] = mk2<R>(z[u].x, z[u].y);
-      buf[r * RP + pad_addr<M, M1>(n + 1)] = mk2<R>(z[u].z, z[u].w);
+      const int rr = e / (M / 2), q = e - rr * (M / 2);
+      const int pn = rr * RP + pad_addr<M, M1>(2 * q);
+      buf[pn] = mk2<R>(z[u].x, z[u].y);
+      buf[pn + 1] = mk2<R>(z[u].z, z[u].w);
     }
   }
   __syncthreads();
   fft4<R, M, M1, M2, NR, NT, -1>(buf, d.twM);
   const R wn = d.wn[j] * R(0.5), rc = d.rcos[j];
-  for (int e = threadIdx.x; e < nr * (M / 2 + 1); e += NT) {
-    const int kk = e / nr, r = e - kk * nr;
-    const V Z1 = buf[r * RP + pad_addr<M, M1>(kk)], Z2 = buf[r * RP + pad_addr<M, M1>((M - kk) % M)];
+  const int r = threadIdx.x % NR, kq = threadIdx.x / NR;
+  if (r >= nr) return;
+  const int col = r0 + r;
+  R* pP = ds.dstP >= 0 ? GP + (long)j * ldP + 2 * (ds.dstP + col) : nullptr;
+  R* pH = ds.dstH >= 0 ? GH + (long)j * ldH + 2 * (ds.dstH + col) : nullptr;
+  const long sP = (long)nlat * ldP, sH = (long)nlat * ldH;
+  const R scP = (R)ds.scaleP, scH = (R)ds.scaleH;
+  const V* brow = buf + r * RP;
+  for (int kk = kq; kk <= M / 2; kk += KS) {
+    const V Z1 = brow[pad_addr<M, M1>(kk)], Z2 = brow[pad_addr<M, M1>((M - kk) % M)];
+#pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int k = h ? M - kk : kk;
       if (k > T || (h && (kk == 0 || M - kk == kk))) continue;
@@ -1068,23 +1195,22 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
       V X = cadd(E, cmul(d.twN[k], Oi));
       X.x *= wn;
       X.y *= wn;
-      const int col = r0 + r;
-      if (ds.dstP >= 0) {
+      if (pP) {
         V y = X;
         if (ds.imcosP) {
           const R f = (R)k * rc;
           y.x = -f * X.y;
           y.y = f * X.x;
         }
-        y.x *= (R)ds.scaleP;
-        y.y *= (R)ds.scaleP;
-        *reinterpret_cast<V*>(GP + ((long)k * nlat + j) * ldP + 2 * (ds.dstP + col)) = y;
+        y.x *= scP;
+        y.y *= scP;
+        *reinterpret_cast<V*>(pP + k * sP) = y;
       }
-      if (ds.dstH >= 0) {
+      if (pH) {
         V y = X;
-        y.x *= (R)ds.scaleH;
-        y.y *= (R)ds.scaleH;
-        *reinterpret_cast<V*>(GH + ((long)k * nlat + j) * ldH + 2 * (ds.dstH + col)) = y;
+        y.x *= scH;
+        y.y *= scH;
+        *reinterpret_cast<V*>(pH + k * sH) = y;
       }
     }
   }

@@ -37,6 +37,9 @@ WORKLOADS = {
     "T254L64": (254, 768, 384, 64, 3, 300.0),
     "T126L64": (126, 384, 190, 64, 3, 600.0),
     "T42L20": (42, 128, 64, 20, 0, 1200.0),
+    # the T574 grid and transform lengths with a quarter of the levels: the
+    # case for ncu captures, which must stay within a few GB of device memory
+    "T574L16": (574, 1152, 576, 16, 1, 150.0),
 }
 METRIC = "simulated days/day at T574L64: mixed-precision vs FP64 GPU at stated error"
 
@@ -53,7 +56,7 @@ def make_state(name, seed):
     from gdpy import inputs
 
     T, nlon, nlat, L, nt, dt = WORKLOADS[name]
-    if name == "T574L64":
+    if name in ("T574L64", "T574L16"):
         return inputs.balanced_jet_state(T, nlat, L, seed=seed, ntrac=nt)
     if name in ("T126L64", "T254L64"):
         return inputs.smooth_random_state(T, L, ntrac=nt, seed=seed)

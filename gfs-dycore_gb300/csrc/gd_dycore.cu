@@ -92,6 +92,7 @@ class Dycore : public DycoreBase {
   SynthRows sr;
   AnalRows ar;
   long ldS, ldTD, ldAP, ldAH, ldFP, ldFH, ldGP, ldGH;
+  long nlm_rows = 0;  // allocated rows of the synthesis sources: nlm rounded up to even
   GemmPlan synP, synH, anaP, anaH, anaPhys;
   FftPlan c2rFull, c2rInv, r2cDyn, r2cPhys;
   Tableau tb;
@@ -127,7 +128,7 @@ class Dycore : public DycoreBase {
         auto it = synth0_cache.find(ncr);
         if (it == synth0_cache.end()) it = synth0_cache.emplace(ncr, make_synth_plan(T, nh, ncr, stream, 0, 0)).first;
         launch_synth<R>(sd, useH, it->second, B, ldB, ncr, F, ldF, stream);
-        tc_synth(*tcp, moff, useH, B, ldB, ncr, F, ldF, stream);
+        tc_synth(*tcp, moff, useH, B, ldB, nlm_rows, ncr, F, ldF, stream);
         return;
       }
     }
@@ -479,9 +480,10 @@ class Dycore : public DycoreBase {
     ldFH = pad2(sc.ncol - 2 * L);
     ldGP = pad2(ap.ncol);
     ldGH = pad2(ah.ncol);
-    S = dalloc<R>((size_t)nlm * ldS);
+    nlm_rows = nlm + (nlm & 1);  // the tensor-core synthesis reads rows in pairs
+    S = dalloc<R>((size_t)nlm_rows * ldS);
     S0 = dalloc<R>((size_t)nlm * ldS);
-    GD_CUDA(cudaMemsetAsync(S, 0, sizeof(R) * nlm * ldS, stream));
+    GD_CUDA(cudaMemsetAsync(S, 0, sizeof(R) * nlm_rows * ldS, stream));
     for (int i = 0; i < 3; ++i) TD[i] = dalloc<R>((size_t)nlm * ldTD);
     AP = dalloc<R>((size_t)nlm * ldAP);
     AH = dalloc<R>((size_t)nlm * ldAH);
@@ -909,7 +911,10 @@ class Dycore : public DycoreBase {
   }
   R* X_ = nullptr;
   R* scratchX() {
-    if (!X_) X_ = dalloc<R>((size_t)nlm * ldS);
+    if (!X_) {
+      X_ = dalloc<R>((size_t)nlm_rows * ldS);
+      GD_CUDA(cudaMemsetAsync(X_, 0, sizeof(R) * nlm_rows * ldS, stream));
+    }
     return X_;
   }
   void spec_in(const double* h, int nb, R* X, int col) {

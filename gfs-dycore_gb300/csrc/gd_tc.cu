@@ -25,6 +25,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <array>
 #include <cstring>
 #include <vector>
 
@@ -640,6 +641,255 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(a.tmem_cols));
 }
 
+// ------------------------------------------- fused-split variant (TF32) --
+// The persistent kernel above reads operands that split kernels have
+// already transposed into K-major hi/lo arrays.  This variant reads the raw
+// FP32 data instead.  Warp 0 loads, per K chunk, the raw tile in its natural
+// column-contiguous layout (synthesis: 32 degrees of one parity of the
+// spectral array; analysis: 32 northern latitude rows of the Fourier array
+// and their 32 mirrored southern rows) together with the table tiles.  Four
+// converter warps (6-9) turn the raw tile into the A operand directly in
+// tensor memory: the thread on TMEM lane c owns batch column c, masks
+// degrees beyond the truncation and latitudes beyond the equator, forms
+// G_N +- G_S for the analysis, splits to hi + lo and writes both 32-column
+// rows with one tcgen05.st each.  The MMAs read A from TMEM (two slots
+// beside the double-buffered accumulators), so shared memory holds only
+// the TMA ring, which is 4-6 stages deep.  The split is the same as in
+// k_tc_split_x/g, so results match the unfused path bit for bit.
+constexpr int TCF_THREADS = 320;
+constexpr int TCF_MAXNS = 6;
+
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]), "r"(v[16]), "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]), "r"(v[24]), "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31]) : "memory");
+}
+__device__ __forceinline__ void mma_tf32_ta(uint32_t dtmem, uint32_t atmem, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(dtmem),
+      "r"(atmem), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__global__ void __launch_bounds__(TCF_THREADS, 1)
+    k_tc_gemm_f(const __grid_constant__ CUtensorMap mRaw, const __grid_constant__ CUtensorMap mBh,
+                const __grid_constant__ CUtensorMap mBl, TcArgs a, int nitems, int ns, uint32_t raw_bytes) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t)1023);
+  const int N = a.N, kc = a.kc;
+  const uint32_t tab_bytes = (uint32_t)N * 128;
+  const uint32_t raw_off = 2 * tab_bytes;
+  const uint32_t stage_bytes = (raw_off + raw_bytes + 1023) & ~1023u;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + (size_t)ns * stage_bytes);
+  uint64_t* empty = full + ns;
+  uint64_t* afull = empty + ns;   // [2] A slot written by the converters
+  uint64_t* aempty = afull + 2;   // [2] A slot read by the MMAs
+  uint64_t* tfull = aempty + 2;   // [2] accumulator buffer ready
+  uint64_t* tempty = tfull + 2;   // [2] accumulator buffer drained
+  uint64_t* done = tempty + 2;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t acol = 4u * (uint32_t)N;  // TMEM column of A slot 0 (hi 32 columns, lo 32 columns)
+
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(a.tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < ns; ++s) {
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&empty[s]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&afull[b]), 4);  // one arrive per converter warp
+      mbar_init(smem_u32(&aempty[b]), 1);
+      mbar_init(smem_u32(&tfull[b]), 1);
+      mbar_init(smem_u32(&tempty[b]), 4);
+    }
+    mbar_init(smem_u32(done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+
+  if (tid == 0) {  // ------------------------------------------- producer
+    int fills[TCF_MAXNS] = {0, 0, 0, 0, 0, 0};
+    long g = 0;
+    bool bad = false;
+    for (int idx = blockIdx.x; idx < nitems && !bad; idx += gridDim.x) {
+      const TcItem t = tc_item(a, idx);
+      const int total = t.nk0 + t.nk1;
+      for (int i = 0; i < total; ++i, ++g) {
+        const int s = (int)(g % ns);
+        const long u = g / ns;
+        if (u >= 1 && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), a.err, 21)) {
+          bad = true;
+          break;
+        }
+        const int acc = (i < t.nk0) ? 0 : 1, kk = acc ? i - t.nk0 : i;
+        unsigned char* st = sm + (size_t)s * stage_bytes;
+        const uint32_t fb = smem_u32(&full[s]);
+        mbar_expect_tx(fb, 2 * tab_bytes + raw_bytes);
+        if (a.mode == 0) {
+          const int xt = acc * a.kepad + kk * kc;
+          tma_3d(smem_u32(st), &mBh, xt, t.n0, t.m, fb);
+          tma_3d(smem_u32(st + tab_bytes), &mBl, xt, t.n0, t.m, fb);
+          // degrees q = acc + 2 (kk kc + i) of order m: spectral rows moff[m] + q,
+          // addressed as (row pair, parity slot)
+          const long r0 = a.moff[t.m] + acc + 2L * kk * kc;
+          tma_3d(smem_u32(st + raw_off), &mRaw, t.c0, (int)(r0 & 1), (int)(r0 >> 1), fb);
+        } else {
+          const int x = kk * kc;
+          const int yt = acc * a.kirows + t.n0;
+          tma_3d(smem_u32(st), &mBh, x, yt, t.m, fb);
+          tma_3d(smem_u32(st + tab_bytes), &mBl, x, yt, t.m, fb);
+          tma_3d(smem_u32(st + raw_off), &mRaw, t.c0, x, t.m, fb);
+          tma_3d(smem_u32(st + raw_off + raw_bytes / 2), &mRaw, t.c0, a.nlat - x - kc, t.m, fb);
+        }
+        ++fills[s];
+      }
+    }
+    for (int s = 0; s < ns; ++s)  // no copies left in flight at exit
+      if (fills[s] > 0) mbar_wait(smem_u32(&full[s]), (fills[s] - 1) & 1, a.err, 22);
+  } else if (tid == 32) {  // ------------------------------------ MMA issuer
+    long g = 0;
+    int titem = 0;
+    bool bad = false;
+    for (int idx = blockIdx.x; idx < nitems && !bad; idx += gridDim.x, ++titem) {
+      const TcItem t = tc_item(a, idx);
+      const int b = titem & 1, u = titem >> 1;
+      if (u >= 1 && !mbar_wait(smem_u32(&tempty[b]), (uint32_t)((u - 1) & 1), a.err, 23)) break;
+      tc_fence_after();
+      const int total = t.nk0 + t.nk1;
+      for (int i = 0; i < total; ++i, ++g) {
+        const int s = (int)(g % ns), cs = (int)(g & 1);
+        if (!mbar_wait(smem_u32(&full[s]), (uint32_t)((g / ns) & 1), a.err, 24) ||
+            !mbar_wait(smem_u32(&afull[cs]), (uint32_t)((g >> 1) & 1), a.err, 25)) {
+          bad = true;
+          break;
+        }
+        tc_fence_after();
+        const int acc = (i < t.nk0) ? 0 : 1, kk = acc ? i - t.nk0 : i;
+        unsigned char* st = sm + (size_t)s * stage_bytes;
+        const uint32_t ah = tbase + acol + 64u * (uint32_t)cs, al = ah + 32u;
+        const uint64_t dbh = smem_desc(smem_u32(st)), dbl = smem_desc(smem_u32(st + tab_bytes));
+        const uint32_t d = tbase + (uint32_t)(b * 2 * N + acc * N);
+#pragma unroll
+        for (int k4 = 0; k4 < 4; ++k4) {  // K = 8 TF32 per MMA: 8 TMEM columns of A, 32 bytes of B
+          const uint64_t o = (uint64_t)(2 * k4);
+          const uint32_t ka = 8u * (uint32_t)k4;
+          mma_tf32_ta(d, ah + ka, dbh + o, a.idesc, (kk > 0 || k4 > 0) ? 1u : 0u);
+          mma_tf32_ta(d, ah + ka, dbl + o, a.idesc, 1u);
+          mma_tf32_ta(d, al + ka, dbh + o, a.idesc, 1u);
+        }
+        mma_commit(smem_u32(&empty[s]));
+        mma_commit(smem_u32(&aempty[cs]));
+      }
+      if (!bad) mma_commit(smem_u32(&tfull[b]));
+    }
+    mma_commit(smem_u32(done));
+  } else if (warp >= 6) {  // ----------------------------------- converters
+    const int q4 = warp & 3;      // TMEM lane quadrant of this warp
+    const int c = q4 * 32 + lane;  // batch column = row of A = TMEM lane
+    const uint32_t arow = tbase + ((uint32_t)(q4 * 32) << 16) + acol;
+    long g = 0;
+    bool bad = false;
+    for (int idx = blockIdx.x; idx < nitems && !bad; idx += gridDim.x) {
+      const TcItem t = tc_item(a, idx);
+      const int total = t.nk0 + t.nk1;
+      for (int i = 0; i < total; ++i, ++g) {
+        const int s = (int)(g % ns), cs = (int)(g & 1);
+        bool ok = mbar_wait(smem_u32(&full[s]), (uint32_t)((g / ns) & 1), a.err, 26);
+        if (ok && g >= 2) ok = mbar_wait(smem_u32(&aempty[cs]), (uint32_t)(((g >> 1) - 1) & 1), a.err, 27);
+        if (!__all_sync(0xffffffffu, ok)) {
+          bad = true;
+          break;
+        }
+        tc_fence_after();
+        const int acc = (i < t.nk0) ? 0 : 1, kk = acc ? i - t.nk0 : i;
+        const float* raw = reinterpret_cast<const float*>(sm + (size_t)s * stage_bytes + raw_off);
+        int nv;  // valid K entries of this chunk: ii < nv
+        bool plus = true;
+        if (a.mode == 0) {
+          const int q0 = acc + 2 * kk * kc;  // degree offset of entry 0
+          nv = q0 < t.K ? (t.K - q0 + 1) / 2 : 0;
+        } else {
+          nv = a.nh - kk * kc;
+          plus = (acc == 0) != (a.parityH != 0);
+        }
+        uint32_t h[32], l[32];
+#pragma unroll
+        for (int ii = 0; ii < 32; ++ii) {
+          float v = raw[ii * TC_M + c];
+          if (a.mode == 1) {
+            const float w = raw[(2 * kc - 1 - ii) * TC_M + c];  // mirrored row nlat-1-j
+            v = plus ? v + w : v - w;
+          }
+          if (ii >= nv) v = 0.f;
+          Elem<TC_TF32>::splitf(v, h[ii], l[ii]);
+        }
+        tmem_st32(arow + 64u * (uint32_t)cs, h);
+        tmem_st32(arow + 64u * (uint32_t)cs + 32u, l);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&afull[cs])) : "memory");
+      }
+    }
+  } else if (warp >= 2) {  // ------------------------------------- epilogue
+    const int q4 = warp & 3;
+    int titem = 0;
+    for (int idx = blockIdx.x; idx < nitems; idx += gridDim.x, ++titem) {
+      const TcItem t = tc_item(a, idx);
+      const int b = titem & 1, u = titem >> 1;
+      const bool ok = mbar_wait(smem_u32(&tfull[b]), (uint32_t)(u & 1), a.err, 28);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      tc_fence_after();
+      const int c = t.c0 + q4 * 32 + lane;
+      const uint32_t tw = tbase + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * 2 * N);
+      for (int g = 0; g < N; g += 16) {
+        float e[16], o[16];
+        tmem_ld16(tw + g, e);
+        if (t.nk1 > 0)
+          tmem_ld16(tw + N + g, o);
+        else
+#pragma unroll
+          for (int q = 0; q < 16; ++q) o[q] = 0.f;
+        if (c < a.ncols) {
+          if (a.mode == 0) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const int j = t.n0 + g + q;
+              if (j < a.nh) {
+                a.out[((long)t.m * a.nlat + j) * a.ldout + c] = e[q] + o[q];
+                a.out[((long)t.m * a.nlat + (a.nlat - 1 - j)) * a.ldout + c] = a.parityH ? o[q] - e[q] : e[q] - o[q];
+              }
+            }
+          } else {
+            const long base = a.moff[t.m];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const int qe = 2 * (t.n0 + g + q), qo = qe + 1;
+              if (qe < t.K) a.out[(base + qe) * a.ldout + c] = e[q];
+              if (qo < t.K) a.out[(base + qo) * a.ldout + c] = o[q];
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+    }
+  }
+  __syncwarp();
+  mbar_wait(smem_u32(done), 0, a.err, 29);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(a.tmem_cols));
+}
+
 // ------------------------------------------------------------ host side --
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -668,6 +918,27 @@ static void make_map(CUtensorMap* m, void* base, int kind, int rank, const uint6
                            rank, base, gd, gs, bx, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) throw CudaError("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+}
+
+// untiled-swizzle FP32 map over raw data (the fused path's loads)
+static void make_raw_map(CUtensorMap* m, const void* base, const uint64_t* dims, const uint64_t* strides,
+                         const uint32_t* box) {
+  cuuint64_t gd[3] = {dims[0], dims[1], dims[2]}, gs[2] = {strides[0], strides[1]};
+  cuuint32_t bx[3] = {box[0], box[1], box[2]}, estr[3] = {1, 1, 1};
+  CUresult r = encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), gd, gs, bx, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw CudaError("cuTensorMapEncodeTiled (raw) failed: " + std::to_string((int)r));
+}
+static const CUtensorMap& cached_raw_map(TcPlan& p, const void* base, const uint64_t* dims, const uint64_t* strides,
+                                         const uint32_t* box) {
+  const std::array<uint64_t, 9> key = {(uint64_t)(uintptr_t)base, dims[0], dims[1], dims[2], strides[0],
+                                       strides[1], box[0], box[1], box[2]};
+  for (auto& kv : p.raw_maps)
+    if (kv.first == key) return kv.second;
+  p.raw_maps.emplace_back(key, CUtensorMap{});
+  make_raw_map(&p.raw_maps.back().second, base, dims, strides, box);
+  return p.raw_maps.back().second;
 }
 
 static int round_up(int x, int a) { return (x + a - 1) / a * a; }
@@ -704,8 +975,9 @@ void tc_init(TcPlan& p, int kind, int T, int nh, int nlat, int ncap, const long*
     GD_CUDA(cudaGetDevice(&dev));
     GD_CUDA(cudaDeviceGetAttribute(&p.nsm, cudaDevAttrMultiProcessorCount, dev));
   }
-  // persistent: two E|O accumulator buffers (4N TMEM columns) -> N <= 128
-  const int ncap_n = p.persistent ? 128 : 160;
+  // persistent: two E|O accumulator buffers (4N TMEM columns) -> N <= 128;
+  // the fused TF32 path also keeps two A slots in TMEM -> N <= 96
+  const int ncap_n = !p.persistent ? 160 : kind == TC_TF32 ? 96 : 128;
   p.nsyn = tile_n(nh, ncap_n);
   p.nana = tile_n(kemax, ncap_n);
   p.kirows = round_up(kemax, p.nana);
@@ -776,6 +1048,7 @@ void tc_free(TcPlan& p) {
   for (void* d : p.allocs) cudaFree(d);
   p.allocs.clear();
   p.item_cache.clear();
+  p.raw_maps.clear();
   p.d_xmap = nullptr;
 }
 
@@ -831,9 +1104,75 @@ static int4* cached_items(TcPlan& p, long key, const std::vector<int4>& it) {
   return d;
 }
 
-void tc_synth(TcPlan& p, const long* d_moff, bool useH, const float* B, long ldB, int ncols, float* F, long ldF,
-              cudaStream_t s) {
+static bool fused_ok(const TcPlan& p, const void* base, long ld) {
+  static const bool off = [] {
+    const char* e = getenv("GD_TC_FUSED");
+    return e && e[0] == '0';
+  }();
+  return !off && p.kind == TC_TF32 && p.persistent && p.nsyn <= 96 && p.nana <= 96 && ((uintptr_t)base % 16) == 0 &&
+         ld % 4 == 0;
+}
+
+static void launch_fused(const TcPlan& p, const CUtensorMap& raw, const CUtensorMap& bh, const CUtensorMap& bl,
+                         TcArgs& args, int nitems, uint32_t raw_bytes, cudaStream_t s) {
+  const uint32_t stage = (uint32_t)round_up(2 * args.N * 128 + (int)raw_bytes, 1024);
+  const size_t avail = 227 * 1024 - 1024 - 256;
+  const int ns = (int)std::min<size_t>(TCF_MAXNS, avail / stage);
+  // TMEM: two E|O accumulator buffers (4N columns) + two A slots (128 columns)
+  if (ns < 2 || args.N > 96 || args.N % 16) throw std::runtime_error("tc fused gemm: bad tile");
+  const size_t sm = (size_t)ns * stage + 1024 + 256;
+  args.tmem_cols = 512;
+  static bool attr = false;
+  if (!attr) {
+    GD_CUDA(cudaFuncSetAttribute(k_tc_gemm_f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    attr = true;
+  }
+  const int grid = std::min(nitems, p.nsm);
+  k_tc_gemm_f<<<grid, TCF_THREADS, sm, s>>>(raw, bh, bl, args, nitems, ns, raw_bytes);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+
+void tc_synth(TcPlan& p, const long* d_moff, bool useH, const float* B, long ldB, long nrowsB, int ncols, float* F,
+              long ldF, cudaStream_t s) {
   if (ncols > p.ncap) throw std::runtime_error("tc_synth: too many columns");
+  const long nlm = (long)(p.T + 1) * (p.T + 2) / 2;
+  if (fused_ok(p, B, ldB) && 2 * (nrowsB / 2) >= nlm) {
+    const int ct = (ncols + TC_M - 1) / TC_M, nt = (p.nh + p.nsyn - 1) / p.nsyn;
+    std::vector<int4> it;
+    for (int m = 1; m <= p.T; ++m)  // order 0 (zonal means) runs on the IEEE SIMT path
+      for (int a = 0; a < ct; ++a)
+        for (int b2 = 0; b2 < nt; ++b2) it.push_back(make_int4(m, a, b2, 0));
+    if (it.empty()) return;
+    TcArgs args;
+    args.items = cached_items(p, ((long)ncols << 2) | 0, it);
+    args.mode = 0;
+    args.T = p.T;
+    args.nh = p.nh;
+    args.nlat = p.nlat;
+    args.N = p.nsyn;
+    args.kc = p.kc;
+    args.kepad = p.kepad;
+    args.kirows = p.kirows;
+    args.xbase = p.d_xbase;
+    args.moff = d_moff;
+    args.parityH = useH ? 1 : 0;
+    args.ncols = ncols;
+    args.coff = 0;
+    args.out = F;
+    args.ldout = ldF;
+    args.err = p.d_err;
+    args.idesc = make_idesc(p.kind, p.nsyn);
+    // spectral rows viewed as (column, parity slot, row pair): a chunk is one
+    // parity slot of kc consecutive pairs
+    const uint64_t dims[3] = {(uint64_t)ncols, 2, (uint64_t)(nrowsB / 2)};
+    const uint64_t strides[2] = {(uint64_t)ldB * 4, (uint64_t)ldB * 8};
+    const uint32_t box[3] = {TC_M, 1, (uint32_t)p.kc};
+    const CUtensorMap& raw = cached_raw_map(p, B, dims, strides, box);
+    const int t = useH ? 1 : 0;
+    launch_fused(p, raw, p.m_tsyn[t][0], p.m_tsyn[t][1], args, (int)it.size(), (uint32_t)(p.kc * TC_M * 4), s);
+    return;
+  }
   // 1) split the spectral columns into the padded K-major staging
   if (!p.d_xmap) {
     std::vector<long> hm(p.T + 2);
@@ -899,6 +1238,44 @@ void tc_synth(TcPlan& p, const long* d_moff, bool useH, const float* B, long ldB
 void tc_anal(TcPlan& p, const long* d_moff, bool useH, const float* G, long ldG, int ncols, float* A, long ldA,
              cudaStream_t s) {
   if (ncols > p.ncap) throw std::runtime_error("tc_anal: too many columns");
+  if (fused_ok(p, G, ldG)) {
+    const int ct = (ncols + TC_M - 1) / TC_M;
+    std::vector<int4> it;
+    for (int m = 1; m <= p.T; ++m) {  // order 0 runs on the IEEE SIMT path
+      const int ke = (p.T - m + 2) / 2;
+      for (int a = 0; a < ct; ++a)
+        for (int b2 = 0; b2 < (ke + p.nana - 1) / p.nana; ++b2) it.push_back(make_int4(m, a, b2, 0));
+    }
+    if (it.empty()) return;
+    TcArgs args;
+    args.items = cached_items(p, ((long)ncols << 2) | 1, it);
+    args.mode = 1;
+    args.T = p.T;
+    args.nh = p.nh;
+    args.nlat = p.nlat;
+    args.N = p.nana;
+    args.kc = p.kc;
+    args.kepad = p.kepad;
+    args.kirows = p.kirows;
+    args.xbase = p.d_xbase;
+    args.moff = d_moff;
+    args.parityH = useH ? 1 : 0;
+    args.ncols = ncols;
+    args.coff = 0;
+    args.out = A;
+    args.ldout = ldA;
+    args.err = p.d_err;
+    args.idesc = make_idesc(p.kind, p.nana);
+    // Fourier rows [m][lat][column]: a chunk is kc northern latitudes plus
+    // the kc mirrored southern ones
+    const uint64_t dims[3] = {(uint64_t)ncols, (uint64_t)p.nlat, (uint64_t)p.T + 1};
+    const uint64_t strides[2] = {(uint64_t)ldG * 4, (uint64_t)ldG * 4 * p.nlat};
+    const uint32_t box[3] = {TC_M, (uint32_t)p.kc, 1};
+    const CUtensorMap& raw = cached_raw_map(p, G, dims, strides, box);
+    const int t = useH ? 1 : 0;
+    launch_fused(p, raw, p.m_tana[t][0], p.m_tana[t][1], args, (int)it.size(), (uint32_t)(2 * p.kc * TC_M * 4), s);
+    return;
+  }
   dim3 g((unsigned)((p.nhpad + 31) / 32), (unsigned)((ncols + 31) / 32), (unsigned)(p.T + 1)), b(32, 8);
   if (p.kind == TC_TF32)
     k_tc_split_g<TC_TF32><<<g, b, 0, s>>>(G, ldG, ncols, p.nh, p.nlat, p.nhpad, p.ncap, (uint32_t*)p.gp[0],

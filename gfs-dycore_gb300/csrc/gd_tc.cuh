@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda.h>
 
+#include <array>
+
 #include "gd_kernels.h"
 
 namespace gd {
@@ -35,6 +37,7 @@ struct TcPlan {
   void* gm[2] = {nullptr, nullptr};
   CUtensorMap m_tsyn[2][2], m_tana[2][2], m_x[2], m_gp[2], m_gm[2];
   std::vector<std::pair<long, int4*>> item_cache;  // work lists by (ncols, direction)
+  std::vector<std::pair<std::array<uint64_t, 9>, CUtensorMap>> raw_maps;  // fused-path maps by geometry
   int* d_xmap = nullptr;  // padded synthesis position -> spectral index (or -1)
   int* d_err = nullptr;   // device error flag (bounded waits)
   std::vector<void*> allocs;
@@ -46,9 +49,11 @@ void tc_init(TcPlan& p, int kind, int T, int nh, int nlat, int ncap, const long*
 void tc_free(TcPlan& p);
 
 // F[m][j][c] (real columns c0.. of the GEMM) = Legendre synthesis of the
-// real columns [0, ncols) of B[idx][.] (row pitch ldB), tensor-core path.
-void tc_synth(TcPlan& p, const long* d_moff, bool useH, const float* B, long ldB, int ncols, float* F, long ldF,
-              cudaStream_t s);
+// real columns [0, ncols) of B[idx][.] (row pitch ldB, nrowsB rows
+// allocated), tensor-core path.  The fused path reads B in pairs of rows,
+// so it needs 2 floor(nrowsB / 2) >= nlm; otherwise the split path runs.
+void tc_synth(TcPlan& p, const long* d_moff, bool useH, const float* B, long ldB, long nrowsB, int ncols, float* F,
+              long ldF, cudaStream_t s);
 // A[idx][c] = Legendre analysis of G[m][j][c] (real columns [0, ncols)).
 void tc_anal(TcPlan& p, const long* d_moff, bool useH, const float* G, long ldG, int ncols, float* A, long ldA,
              cudaStream_t s);

@@ -152,13 +152,17 @@ struct Elem<TC_TF32> {
     hi = h;
     lo = l;
   }
+  // Round to nearest TF32, ties away from zero, on the bit pattern: adding
+  // half a TF32 unit (bit 12) to the sign-magnitude encoding and clearing the
+  // 13 low bits (the same result as cvt.rna.tf32.f32 for finite inputs, in two
+  // full-rate integer operations).
+  __device__ static uint32_t rna(float f) { return (__float_as_uint(f) + 0x1000u) & 0xFFFFE000u; }
+  // lo = f - hi is exact in FP32 (at most 13 significant bits); the tensor
+  // core reads its leading TF32 bits
   __device__ static void splitf(float f, T& hi, T& lo) {
-    uint32_t h, l;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(f));
-    float r = f - __uint_as_float(h);
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(r));
+    const uint32_t h = rna(f);
     hi = h;
-    lo = l;
+    lo = __float_as_uint(f - __uint_as_float(h));
   }
 };
 template <>
@@ -648,19 +652,20 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
 // column-contiguous layout (synthesis: 32 degrees of one parity of the
 // spectral array; analysis: 32 northern latitude rows of the Fourier array
 // and their 32 mirrored southern rows) together with the table tiles.  Four
-// converter warps (6-9) turn the raw tile into the A operand directly in
-// tensor memory: the thread on TMEM lane c owns batch column c, masks
+// converter warps (6-13) turn the raw tile into the A operand directly in
+// tensor memory: two threads on TMEM lane c (one per half of the chunk's 32
+// K entries, in warps w and w + 4) own batch column c, mask
 // degrees beyond the truncation and latitudes beyond the equator, forms
-// G_N +- G_S for the analysis, splits to hi + lo and writes both 32-column
-// rows with one tcgen05.st each.  The MMAs read A from TMEM (two slots
+// G_N +- G_S for the analysis, split to hi + lo and write their 16 columns of
+// each with one tcgen05.st.  The MMAs read A from TMEM (two slots
 // beside the double-buffered accumulators), so shared memory holds only
 // the TMA ring, which is 4-6 stages deep.  The split is the same as in
 // k_tc_split_x/g, so results match the unfused path bit for bit.
-constexpr int TCF_THREADS = 320;
+constexpr int TCF_THREADS = 448;  // producer, MMA, 4 epilogue, 8 converter warps
 constexpr int TCF_MAXNS = 6;
 
-__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* v) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]), "r"(v[16]), "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]), "r"(v[24]), "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31]) : "memory");
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};" ::"r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]) : "memory");
 }
 __device__ __forceinline__ void mma_tf32_ta(uint32_t dtmem, uint32_t atmem, uint64_t b, uint32_t idesc, uint32_t acc) {
   asm volatile(
@@ -678,12 +683,14 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
   const uint32_t tab_bytes = (uint32_t)N * 128;
   const uint32_t raw_off = 2 * tab_bytes;
   const uint32_t stage_bytes = (raw_off + raw_bytes + 1023) & ~1023u;
+  // full[s]: the TMA copies of a chunk landed; used[s]: the MMAs of the chunk
+  // in stage s completed (frees the stage for the producer and, two chunks
+  // later, the A slot for the converters); afull[2]: an A slot is written
   uint64_t* full = reinterpret_cast<uint64_t*>(sm + (size_t)ns * stage_bytes);
-  uint64_t* empty = full + ns;
-  uint64_t* afull = empty + ns;   // [2] A slot written by the converters
-  uint64_t* aempty = afull + 2;   // [2] A slot read by the MMAs
-  uint64_t* tfull = aempty + 2;   // [2] accumulator buffer ready
-  uint64_t* tempty = tfull + 2;   // [2] accumulator buffer drained
+  uint64_t* used = full + ns;
+  uint64_t* afull = used + ns;
+  uint64_t* tfull = afull + 2;   // [2] accumulator buffer ready
+  uint64_t* tempty = tfull + 2;  // [2] accumulator buffer drained
   uint64_t* done = tempty + 2;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -697,11 +704,10 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
   if (tid == 0) {
     for (int s = 0; s < ns; ++s) {
       mbar_init(smem_u32(&full[s]), 1);
-      mbar_init(smem_u32(&empty[s]), 1);
+      mbar_init(smem_u32(&used[s]), 1);
     }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(smem_u32(&afull[b]), 4);  // one arrive per converter warp
-      mbar_init(smem_u32(&aempty[b]), 1);
+      mbar_init(smem_u32(&afull[b]), 8);  // one arrive per converter warp
       mbar_init(smem_u32(&tfull[b]), 1);
       mbar_init(smem_u32(&tempty[b]), 4);
     }
@@ -723,7 +729,7 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
       for (int i = 0; i < total; ++i, ++g) {
         const int s = (int)(g % ns);
         const long u = g / ns;
-        if (u >= 1 && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((u - 1) & 1), a.err, 21)) {
+        if (u >= 1 && !mbar_wait(smem_u32(&used[s]), (uint32_t)((u - 1) & 1), a.err, 21)) {
           bad = true;
           break;
         }
@@ -783,16 +789,16 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
           mma_tf32_ta(d, ah + ka, dbl + o, a.idesc, 1u);
           mma_tf32_ta(d, al + ka, dbh + o, a.idesc, 1u);
         }
-        mma_commit(smem_u32(&empty[s]));
-        mma_commit(smem_u32(&aempty[cs]));
+        mma_commit(smem_u32(&used[s]));
       }
       if (!bad) mma_commit(smem_u32(&tfull[b]));
     }
     mma_commit(smem_u32(done));
   } else if (warp >= 6) {  // ----------------------------------- converters
-    const int q4 = warp & 3;      // TMEM lane quadrant of this warp
-    const int c = q4 * 32 + lane;  // batch column = row of A = TMEM lane
-    const uint32_t arow = tbase + ((uint32_t)(q4 * 32) << 16) + acol;
+    const int q4 = warp & 3;                // TMEM lane quadrant of this warp
+    const int c = q4 * 32 + lane;           // batch column = row of A = TMEM lane
+    const int k0 = ((warp - 6) >> 2) * 16;  // this thread's half of the chunk's K entries
+    const uint32_t arow = tbase + ((uint32_t)(q4 * 32) << 16) + acol + (uint32_t)k0;
     long g = 0;
     bool bad = false;
     for (int idx = blockIdx.x; idx < nitems && !bad; idx += gridDim.x) {
@@ -800,13 +806,11 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
       const int total = t.nk0 + t.nk1;
       for (int i = 0; i < total; ++i, ++g) {
         const int s = (int)(g % ns), cs = (int)(g & 1);
-        bool ok = mbar_wait(smem_u32(&full[s]), (uint32_t)((g / ns) & 1), a.err, 26);
-        if (ok && g >= 2) ok = mbar_wait(smem_u32(&aempty[cs]), (uint32_t)(((g >> 1) - 1) & 1), a.err, 27);
-        if (!__all_sync(0xffffffffu, ok)) {
+        const bool okf = mbar_wait(smem_u32(&full[s]), (uint32_t)((g / ns) & 1), a.err, 26);
+        if (!__all_sync(0xffffffffu, okf)) {
           bad = true;
           break;
         }
-        tc_fence_after();
         const int acc = (i < t.nk0) ? 0 : 1, kk = acc ? i - t.nk0 : i;
         const float* raw = reinterpret_cast<const float*>(sm + (size_t)s * stage_bytes + raw_off);
         int nv;  // valid K entries of this chunk: ii < nv
@@ -818,19 +822,32 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
           nv = a.nh - kk * kc;
           plus = (acc == 0) != (a.parityH != 0);
         }
-        uint32_t h[32], l[32];
+        // convert before waiting for the A slot: the loads and the split
+        // overlap the MMAs still reading it
+        uint32_t h[16], l[16];
 #pragma unroll
-        for (int ii = 0; ii < 32; ++ii) {
+        for (int e = 0; e < 16; ++e) {
+          const int ii = k0 + e;
           float v = raw[ii * TC_M + c];
           if (a.mode == 1) {
             const float w = raw[(2 * kc - 1 - ii) * TC_M + c];  // mirrored row nlat-1-j
             v = plus ? v + w : v - w;
           }
           if (ii >= nv) v = 0.f;
-          Elem<TC_TF32>::splitf(v, h[ii], l[ii]);
+          Elem<TC_TF32>::splitf(v, h[e], l[e]);
         }
-        tmem_st32(arow + 64u * (uint32_t)cs, h);
-        tmem_st32(arow + 64u * (uint32_t)cs + 32u, l);
+        // the slot's previous contents fed chunk g - 2
+        if (g >= 2) {
+          const long gp = g - 2;
+          const bool oku = mbar_wait(smem_u32(&used[gp % ns]), (uint32_t)((gp / ns) & 1), a.err, 27);
+          if (!__all_sync(0xffffffffu, oku)) {
+            bad = true;
+            break;
+          }
+        }
+        tc_fence_after();
+        tmem_st16(arow + 64u * (uint32_t)cs, h);
+        tmem_st16(arow + 64u * (uint32_t)cs + 32u, l);
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         tc_fence_before();
         __syncwarp();

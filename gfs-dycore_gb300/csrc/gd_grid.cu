@@ -34,6 +34,8 @@ constexpr int LMAX = 128;
 __device__ __forceinline__ double cdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ float cdiv(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ double clog(double a) { return log(a); }
+__device__ __forceinline__ double crcp(double a) { return 1.0 / a; }
+__device__ __forceinline__ float crcp(float a) { return __fdividef(1.f, a); }
 __device__ __forceinline__ float clog(float a) { return __logf(a); }
 
 // Thuburn (1993) limited half-level value at interior interface k
@@ -95,8 +97,9 @@ __device__ __forceinline__ R half_at(int t, int L, R qm, R q0, R q1, R q2, R eta
 //      (getvadv_tracers, :478-603) and horizontal advection.
 // Levels are indexed b bottom (0) to top; interface quantities t top (0)
 // to bottom; layer t = L-1-b.
+// at most 8 warps (LB is chosen so), and 4 resident CTAs per SM for the FP32 state
 template <typename R, int LB>
-__global__ void __launch_bounds__(512) k_dyn_columns(ColumnArgs<R> a, int inverse_only) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_dyn_columns(ColumnArgs<R> a, int inverse_only) {
   extern __shared__ __align__(16) unsigned char smcol[];
   const int lane = threadIdx.x, w = threadIdx.y, NW = blockDim.y;
   const int L = a.L;
@@ -125,19 +128,25 @@ __global__ void __launch_bounds__(512) k_dyn_columns(ColumnArgs<R> a, int invers
   // phase 1
   R xdb[LB], xcb[LB];
   R s2 = R(0), su = R(0), sv = R(0);
+  // pressure and its reciprocal at the bottom interface of the current level,
+  // carried upward (the top interface of level i is the bottom one of i + 1)
+  R pkb = PK(L - b0), ipkb = crcp(pkb);
 #pragma unroll
   for (int i = 0; i < LB; ++i) {
     xdb[i] = R(0);
     xcb[i] = R(0);
     if (i < nb) {
       const int b = b0 + i, t = L - 1 - b;
-      const R pkt = PK(t), pkt1 = PK(t + 1), dp = pkt1 - pkt;
+      const R pkt = PK(t), pkt1 = pkb, dp = pkt1 - pkt;
+      const R ipkt = t > 0 ? crcp(pkt) : R(0), ipk1 = ipkb;
+      pkb = pkt;
+      ipkb = ipkt;
       const R cg = S(a.s.u + b) * dlx + S(a.s.v + b) * dly;
       xdb[i] = S(a.s.div + b) * dp;
       xcb[i] = cg * __ldg(dbk + t);
       if (t > 0) {  // terms of the sums over the layers below a layer
         const R rl = clog(cdiv(pkt1, pkt));
-        s2 += (__ldg(bk + t + 1) * (R(1) / pkt1) - __ldg(bk + t) * (R(1) / pkt)) * S(a.s.tv + b);
+        s2 += (__ldg(bk + t + 1) * ipk1 - __ldg(bk + t) * ipkt) * S(a.s.tv + b);
         su += rl * S(a.s.dtvdx + b);
         sv += rl * S(a.s.dtvdy + b);
       }
@@ -211,7 +220,8 @@ __global__ void __launch_bounds__(512) k_dyn_columns(ColumnArgs<R> a, int invers
   };
   const R fcor = a.omega2 * a.sinlat[j];
   const R dphx = a.dphisdx[p], dphy = a.dphisdy[p];
-  R uu[LB], vv[LB];
+  R uu[LB], vv[LB], idpa[LB];
+  R pkb3 = PK(L - b0), ipkb3 = crcp(pkb3);
   R um = R(0), vm = R(0), tm = R(0);
   R uc = R(0), vc = R(0), tc = R(0);
   if (nb > 0) {
@@ -228,6 +238,7 @@ __global__ void __launch_bounds__(512) k_dyn_columns(ColumnArgs<R> a, int invers
   for (int i = 0; i < LB; ++i) {
     uu[i] = uc;
     vv[i] = vc;
+    idpa[i] = R(0);
     if (i >= nb) continue;
     const int b = b0 + i, t = L - 1 - b;
     R up = R(0), vp = R(0), tp = R(0);
@@ -236,7 +247,11 @@ __global__ void __launch_bounds__(512) k_dyn_columns(ColumnArgs<R> a, int invers
       vp = S(a.s.v + b + 1);
       tp = S(a.s.tv + b + 1);
     }
-    const R pkt = PK(t), pkt1 = PK(t + 1), dp = pkt1 - pkt, idp = R(1) / dp;
+    const R pkt = PK(t), pkt1 = pkb3, dp = pkt1 - pkt, idp = crcp(dp);
+    const R ipkt = t > 0 ? crcp(pkt) : R(0), ipk1 = ipkb3;  // 1/pk(t) is unused at the model top (pk = 0)
+    pkb3 = pkt;
+    ipkb3 = ipkt;
+    idpa[i] = idp;
     const R rl = RLN(t, pkt, pkt1);
     const R al = (t == 0) ? a.log2sp : R(1) - (pkt * idp) * rl;
     const R cg = uc * dlx + vc * dly;
@@ -255,7 +270,6 @@ __global__ void __launch_bounds__(512) k_dyn_columns(ColumnArgs<R> a, int invers
     if (!inverse_only) {
       const R dtx = S(a.s.dtvdx + b), dty = S(a.s.dtvdy + b);
       const R bkt = __ldg(bk + t), bkt1 = __ldg(bk + t + 1);
-      const R ipk1 = R(1) / pkt1;
       const R cofb2 = -rd * S2, px3u = -rd * SU, px3v = -rd * SV;
       const R cofb1 = (t == 0) ? -idp * (al * dbkt) : -idp * (bkt * rl + al * dbkt);
       const R cofa = -idp * (bkt1 * pkt * ipk1 - bkt + rl * (bkt - pkt * dbkt * idp));
@@ -287,7 +301,7 @@ __global__ void __launch_bounds__(512) k_dyn_columns(ColumnArgs<R> a, int invers
       A(a.a.fv + b, vc * (vr + fcor) - (vu - prsgx));
       A(a.a.ke + b, R(0.5) * (uc * uc + vc * vc));
       if (t > 0) {
-        S2 += (bkt1 * ipk1 - bkt * (R(1) / pkt)) * tc;
+        S2 += (bkt1 * ipk1 - bkt * ipkt) * tc;
         SU += rl * dtx;
         SV += rl * dty;
       }
@@ -314,7 +328,7 @@ __global__ void __launch_bounds__(512) k_dyn_columns(ColumnArgs<R> a, int invers
       const int b = b0 + i, t = L - 1 - b;
       const R e0 = ETA(t), e1 = ETA(t + 1);
       const R ht = (t == 0) ? q0 : half_at(t, L, qm, q0, q1, q2, e0);
-      const R idp = R(1) / (PK(t + 1) - PK(t));
+      const R idp = idpa[i];
       const R vadq = idp * ((hb * e1 - ht * e0) + (q0 * (e0 - e1)));
       A(a.a.qtend + iq * L + b, -uu[i] * S(a.s.dqdx + iq * L + b) - vv[i] * S(a.s.dqdy + iq * L + b) - vadq);
       hb = ht;
@@ -339,14 +353,13 @@ static void launch_cols_lb(const ColumnArgs<R>& a, bool inverse_only, cudaStream
 template <typename R>
 void launch_dyn_columns(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t s) {
   if (a.L < 1 || a.L > LMAX) throw std::runtime_error("nlev out of range for the column kernel");
-  // levels per warp: at most 16 warps per CTA
-  static const int lb_env = getenv("GD_COL_LB") ? atoi(getenv("GD_COL_LB")) : 0;
-  int lb = lb_env == 4 || lb_env == 8 ? lb_env : (a.L <= 32 ? 4 : 8);
-  if (ceil_div(a.L, lb) > 16) lb = 8;
-  if (lb == 4)
+  // levels per warp: at most 8 warps per CTA
+  if (a.L <= 32)
     launch_cols_lb<R, 4>(a, inverse_only, s);
-  else
+  else if (a.L <= 64)
     launch_cols_lb<R, 8>(a, inverse_only, s);
+  else
+    launch_cols_lb<R, 16>(a, inverse_only, s);
   count_launch();
   GD_LAUNCH_CHECK();
 }

@@ -67,6 +67,11 @@ template <typename R>
 __device__ __forceinline__ typename C2<R>::T ld2(const R* base, long row, long ld, int col) {
   return *reinterpret_cast<const typename C2<R>::T*>(base + row * ld + 2 * col);
 }
+// read-only path for arrays no thread of the launch writes
+template <typename R>
+__device__ __forceinline__ typename C2<R>::T ldg2(const R* base, long row, long ld, int col) {
+  return __ldg(reinterpret_cast<const typename C2<R>::T*>(base + row * ld + 2 * col));
+}
 template <typename R>
 __device__ __forceinline__ void st2(R* base, long row, long ld, int col, typename C2<R>::T v) {
   *reinterpret_cast<typename C2<R>::T*>(base + row * ld + 2 * col) = v;
@@ -78,18 +83,18 @@ template <typename R>
 __device__ __forceinline__ void raw_tend(const StageArgs<R>& a, long idx, int k, R lap, typename C2<R>::T& dvrt,
                                          typename C2<R>::T& ddiv, typename C2<R>::T& dtv) {
   typedef typename C2<R>::T V;
-  const V imfv = ld2(a.AP, idx, a.ldAP, a.ap.imfv + k), imfu = ld2(a.AP, idx, a.ldAP, a.ap.imfu + k);
-  const V fu = ld2(a.AH, idx, a.ldAH, a.ah.fu + k), mfv = ld2(a.AH, idx, a.ldAH, a.ah.mfv + k);
-  const V ke = ld2(a.AP, idx, a.ldAP, a.ap.ke + k);
+  const V imfv = ldg2(a.AP, idx, a.ldAP, a.ap.imfv + k), imfu = ldg2(a.AP, idx, a.ldAP, a.ap.imfu + k);
+  const V fu = ldg2(a.AH, idx, a.ldAH, a.ah.fu + k), mfv = ldg2(a.AH, idx, a.ldAH, a.ah.mfv + k);
+  const V ke = ldg2(a.AP, idx, a.ldAP, a.ap.ke + k);
   dvrt.x = -(imfu.x + mfv.x) * a.ainv;
   dvrt.y = -(imfu.y + mfv.y) * a.ainv;
   ddiv.x = (imfv.x + fu.x) * a.ainv - (lap * a.ainv2) * ke.x;
   ddiv.y = (imfv.y + fu.y) * a.ainv - (lap * a.ainv2) * ke.y;
-  dtv = ld2(a.AP, idx, a.ldAP, a.ap.ttend + k);
+  dtv = ldg2(a.AP, idx, a.ldAP, a.ap.ttend + k);
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_stage(StageArgs<R> a) {
   typedef typename C2<R>::T V;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int L = a.L;
@@ -153,17 +158,17 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
     st2(TDs, idx, a.ldTD, a.tc.dtv + k, dtv);
     st2(TDs, idx, a.ldTD, a.tc.ddl + k, ddl);
     st2(TDs, idx, a.ldTD, a.tc.dtl + k, dtl);
-    V vr = ld2(a.S0, idx, a.ldS, a.sc.vrt + k), dv = ld2(a.S0, idx, a.ldS, a.sc.div + k),
-      tv = ld2(a.S0, idx, a.ldS, a.sc.tv + k);
+    V vr = ldg2(a.S0, idx, a.ldS, a.sc.vrt + k), dv = ldg2(a.S0, idx, a.ldS, a.sc.div + k),
+      tv = ldg2(a.S0, idx, a.ldS, a.sc.tv + k);
     V svr = vz<V>(), sdv = vz<V>(), stv = vz<V>();
     for (int r = 0; r <= s; ++r) {
       V x_vr = dvrt, x_dv = ddiv, x_tv = dtv, x_dl = ddl, x_tl = dtl;
       if (r < s) {
-        x_vr = ld2(TDr(r), idx, a.ldTD, a.tc.dvrt + k);
-        x_dv = ld2(TDr(r), idx, a.ldTD, a.tc.ddiv + k);
-        x_tv = ld2(TDr(r), idx, a.ldTD, a.tc.dtv + k);
-        x_dl = ld2(TDr(r), idx, a.ldTD, a.tc.ddl + k);
-        x_tl = ld2(TDr(r), idx, a.ldTD, a.tc.dtl + k);
+        x_vr = ldg2(TDr(r), idx, a.ldTD, a.tc.dvrt + k);
+        x_dv = ldg2(TDr(r), idx, a.ldTD, a.tc.ddiv + k);
+        x_tv = ldg2(TDr(r), idx, a.ldTD, a.tc.dtv + k);
+        x_dl = ldg2(TDr(r), idx, a.ldTD, a.tc.ddl + k);
+        x_tl = ldg2(TDr(r), idx, a.ldTD, a.tc.dtl + k);
       }
       svr.x += a.ce[r] * x_vr.x;
       svr.y += a.ce[r] * x_vr.y;
@@ -194,12 +199,12 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
     TV[i * L + k] = tv;
     for (int iq = 0; iq < a.nt; ++iq) {  // tracers, always explicit
       const int col = iq * L + k;
-      V dq = ld2(a.AP, idx, a.ldAP, a.ap.qtend + col);
+      V dq = ldg2(a.AP, idx, a.ldAP, a.ap.qtend + col);
       st2(TDs, idx, a.ldTD, a.tc.dtrc + col, dq);
-      V q = ld2(a.S0, idx, a.ldS, a.sc.trc + col);
+      V q = ldg2(a.S0, idx, a.ldS, a.sc.trc + col);
       V sq = vz<V>();
       for (int r = 0; r <= s; ++r) {
-        V x = (r < s) ? ld2(TDr(r), idx, a.ldTD, a.tc.dtrc + col) : dq;
+        V x = (r < s) ? ldg2(TDr(r), idx, a.ldTD, a.tc.dtrc + col) : dq;
         sq.x += a.ce[r] * x.x;
         sq.y += a.ce[r] * x.y;
       }
@@ -215,7 +220,7 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
   __syncthreads();  // LN (current ln ps) is read above and replaced below
   for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
     const long idx = IDX(i);
-    V dl = ld2(a.AP, idx, a.ldAP, a.ap.dlnps);
+    V dl = ldg2(a.AP, idx, a.ldAP, a.ap.dlnps);
     V dpl = vz<V>();
     if (!a.explicit_) {
       dpl.x = -Y3[i].x;
@@ -225,13 +230,13 @@ __global__ void __launch_bounds__(256) k_stage(StageArgs<R> a) {
     }
     st2(TDs, idx, a.ldTD, a.tc.dlnps, dl);
     st2(TDs, idx, a.ldTD, a.tc.dpl, dpl);
-    V ln = ld2(a.S0, idx, a.ldS, a.sc.lnps);
+    V ln = ldg2(a.S0, idx, a.ldS, a.sc.lnps);
     V sl = vz<V>();
     for (int r = 0; r <= s; ++r) {
       V x = dl, xp = dpl;
       if (r < s) {
-        x = ld2(TDr(r), idx, a.ldTD, a.tc.dlnps);
-        xp = ld2(TDr(r), idx, a.ldTD, a.tc.dpl);
+        x = ldg2(TDr(r), idx, a.ldTD, a.tc.dlnps);
+        xp = ldg2(TDr(r), idx, a.ldTD, a.tc.dpl);
       }
       sl.x += a.ce[r] * x.x + a.ci[r] * xp.x;
       sl.y += a.ce[r] * x.y + a.ci[r] * xp.y;
@@ -337,8 +342,8 @@ __global__ void k_assemble(StageArgs<R> a, R* TD, int nlm) {
     st2(TD, idx, a.ldTD, a.tc.ddiv + k, ddiv);
     st2(TD, idx, a.ldTD, a.tc.dtv + k, dtv);
     for (int iq = 0; iq < a.nt; ++iq)
-      st2(TD, idx, a.ldTD, a.tc.dtrc + iq * a.L + k, ld2(a.AP, idx, a.ldAP, a.ap.qtend + iq * a.L + k));
-    if (k == 0) st2(TD, idx, a.ldTD, a.tc.dlnps, ld2(a.AP, idx, a.ldAP, a.ap.dlnps));
+      st2(TD, idx, a.ldTD, a.tc.dtrc + iq * a.L + k, ldg2(a.AP, idx, a.ldAP, a.ap.qtend + iq * a.L + k));
+    if (k == 0) st2(TD, idx, a.ldTD, a.tc.dlnps, ldg2(a.AP, idx, a.ldAP, a.ap.dlnps));
   }
 }
 template <typename R>

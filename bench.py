@@ -139,20 +139,16 @@ def gpu_arm(args):
     import torch
 
     from gdpy import core, inputs
+    from gdpy.replicas import ReplicaGroup
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = world > 1
-    if dist:
-        import torch.distributed as tdist
-
-        tdist.init_process_group("nccl")
     torch.cuda.set_device(local)
+    grp = ReplicaGroup("nccl")  # replicas: one independent member per rank
+    rank, world = grp.rank, grp.world
     name = args.workload
     T, nlon, nlat, L, nt, dt = WORKLOADS[name]
     ak, bk = inputs.hybrid_coords(L)
-    st = make_state(name, seed=rank)
+    st = make_state(name, seed=grp.member_seed())
     trc = st["trc"] if nt else None
     stream = torch.cuda.Stream()  # a capturable stream shared with the library
 
@@ -163,8 +159,7 @@ def gpu_arm(args):
         return g
 
     def barrier():
-        if dist:
-            tdist.barrier()
+        grp.barrier()
         torch.cuda.synchronize()
 
     def timed(g, steps, warmup):
@@ -177,19 +172,15 @@ def gpu_arm(args):
             g.advance(steps)
             e1.record(stream)
             barrier()
-        ms = e0.elapsed_time(e1)
-        if dist:
-            t = torch.tensor([ms], device="cuda")
-            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = grp.max_over_ranks(e0.elapsed_time(e1))
         return ms, g.launch_count() - n0, ck.summary()
 
     # fast-precision step (the headline)
     g = ctx(args.precision)
     ms, launches, clocks = timed(g, args.steps, args.warmup)
     ms_step = ms / args.steps
-    dpd = dt * 1e3 / ms_step  # simulated seconds per wall second == simulated days per day
-    value = dpd * world
+    # simulated seconds per wall second == simulated days per day, summed over ranks
+    value = grp.job_rate(dt * args.steps, ms * 1e-3)
     phases = g.profile_step()
     fast_state = g.get_state()
     steps_done = args.warmup + args.steps + 1
@@ -236,12 +227,8 @@ def gpu_arm(args):
         g._chk(lib.gd_get_state(g.h, P(pinned["vrt"]), P(pinned["div"]), P(pinned["tv"]),
                                 P(pinned["trc"]) if nt else None, P(pinned["lnps"])))
     barrier()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
-    if dist:
-        t = torch.tensor([e2e_ms], device="cuda")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e = dict(value=(86400.0 * 1e3 / e2e_ms) * dt / 86400.0 * world, unit="simulated days/day",
+    e2e_ms = grp.max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps)
+    e2e = dict(value=grp.job_rate(dt, e2e_ms * 1e-3), unit="simulated days/day",
                h2d_bytes_per_step=h2d, d2h_bytes_per_step=h2d, ms_per_step=e2e_ms)
 
     # roofline of the dominant phase
@@ -279,8 +266,7 @@ def gpu_arm(args):
             out["cpu_baseline"] = cpu_baseline(name, args.cpu_levels)
         print(json.dumps(out))
     g.close()
-    if dist:
-        tdist.destroy_process_group()
+    grp.close()
 
 
 def cpu_baseline(name, levels, nthreads=None):

@@ -14,9 +14,12 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libgdcore.so")
-SOURCES = ["gd_sht.cu", "gd_grid.cu", "gd_spec.cu", "gd_tc.cu", "gd_dycore.cu", "gd_noalloc.cu"]
+SOURCES = ["gd_sht.cu", "gd_grid.cu", "gd_spec.cu", "gd_tc.cu", "gd_dycore.cu", "gd_noalloc.cu", "gd_pattern.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+# host code: no FMA contraction (the single-precision pattern set-up is
+# specified operation by operation)
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "--expt-relaxed-constexpr",
          "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
 

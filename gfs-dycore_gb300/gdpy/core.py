@@ -33,6 +33,9 @@ API_FUNCTIONS = [
     "gd_getuv", "gd_getvrtdivspec", "gd_getgrad", "gd_grid_info", "gd_get_grid", "gd_diag",
     "gd_set_stream", "gd_sync", "gd_launch_count", "gd_last_error", "gd_profile_step",
     "gd_diag_static",
+    "gd_pattern_init", "gd_pattern_start", "gd_pattern_advance", "gd_pattern_getnoise", "gd_pattern_get",
+    "gd_pattern_set", "gd_pattern_spectra", "gd_pattern_destroy", "gd_pattern_set_stream", "gd_pattern_sync",
+    "gd_pattern_launch_count", "gd_pattern_last_error",
 ]
 PHASES = ["legendre_synth", "fft_synth", "columns", "fft_anal", "legendre_anal", "semi_implicit",
           "physics", "other"]
@@ -84,6 +87,18 @@ def load(build_if_missing=True):
         getattr(L, f).restype = ctypes.c_int
     L.gd_diag_static.restype = ctypes.c_int
     L.gd_diag_static.argtypes = [vp, vp, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]
+    d, i = ctypes.c_double, ctypes.c_int
+    L.gd_pattern_init.argtypes = [d, d, d, d, i, i, i, i, d, i, i, ctypes.POINTER(vp)]
+    for f in ["gd_pattern_start", "gd_pattern_destroy", "gd_pattern_sync"]:
+        getattr(L, f).argtypes = [vp]
+    L.gd_pattern_advance.argtypes = [vp, i]
+    for f in ["gd_pattern_getnoise", "gd_pattern_get", "gd_pattern_set", "gd_pattern_set_stream"]:
+        getattr(L, f).argtypes = [vp, vp]
+    L.gd_pattern_spectra.argtypes = [vp, vp, vp, vp]
+    L.gd_pattern_launch_count.restype = ctypes.c_longlong
+    L.gd_pattern_launch_count.argtypes = [vp]
+    L.gd_pattern_last_error.restype = ctypes.c_char_p
+    L.gd_pattern_last_error.argtypes = [vp]
     _lib = L
     return L
 
@@ -245,3 +260,73 @@ class Dycore:
         o = np.zeros(5)
         self._chk(load().gd_diag(self.h, _p(o)))
         return dict(spdmax=o[0], psmin=o[1], psmax=o[2], pstend=o[3], pdryini=o[4])
+
+
+class Pattern:
+    """One stochastic pattern generator (gd_pattern): patterngenerator.f90's
+    random_pattern with its own Mersenne-twister stream and nfields patterns."""
+
+    def __init__(self, lscale, delt, tscale, stdev, iseed, jcap, nlon=0, nlat=0, normalization=None,
+                 nfields=1, device=0):
+        L = load()
+        if normalization is None:
+            normalization = 2.0 * float(np.float32(np.pi))  # stoch_data.f90: 2.*pi in r_kind
+        h = ctypes.c_void_p()
+        rc = L.gd_pattern_init(lscale, delt, tscale, stdev, iseed, nlon, nlat, jcap, normalization, nfields,
+                               device, ctypes.byref(h))
+        if rc != GD_OK:
+            raise GdError(rc, L.gd_pattern_last_error(None).decode())
+        self.h = h
+        self.jcap, self.nfields = jcap, nfields
+        self.nlm = (jcap + 1) * (jcap + 2) // 2
+
+    def _chk(self, rc):
+        if rc != GD_OK:
+            raise GdError(rc, load().gd_pattern_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().gd_pattern_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def start(self):
+        self._chk(load().gd_pattern_start(self.h))
+
+    def advance(self, nsteps=1):
+        self._chk(load().gd_pattern_advance(self.h, nsteps))
+
+    def getnoise(self):
+        out = np.zeros(self.nlm, np.complex128)
+        self._chk(load().gd_pattern_getnoise(self.h, _p(out)))
+        return out
+
+    def get(self):
+        out = np.zeros((self.nfields, self.nlm), np.complex128)
+        self._chk(load().gd_pattern_get(self.h, _p(out)))
+        return out
+
+    def set(self, spec):
+        a = np.ascontiguousarray(spec, np.complex128).reshape(self.nfields, self.nlm)
+        self._chk(load().gd_pattern_set(self.h, _p(a)))
+
+    def spectra(self):
+        vs = np.zeros(self.nlm)
+        v1 = np.zeros(self.jcap + 1)
+        phi = np.zeros(1)
+        self._chk(load().gd_pattern_spectra(self.h, _p(vs), _p(v1), _p(phi)))
+        return vs, v1, float(phi[0])
+
+    def set_stream(self, stream):
+        self._chk(load().gd_pattern_set_stream(self.h, ctypes.c_void_p(stream)))
+
+    def sync(self):
+        self._chk(load().gd_pattern_sync(self.h))
+
+    def launch_count(self):
+        return load().gd_pattern_launch_count(self.h)

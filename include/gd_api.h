@@ -168,6 +168,48 @@ int gd_diag_static(const double* ug, const double* vg, int nlev, const double* p
                    const double* dlnpsdt, const double* gauwts, int nlat, int nlon, double* out4,
                    void* stream);
 
+/* ---- stochastic pattern generator (src/patterngenerator.f90) -------------
+   AR(1) random patterns in spherical-harmonic space with a Gaussian spatial
+   covariance of length scale lscale (m) and e-folding time tscale (s), drawn
+   from the w3lib Mersenne twister (src/w3lib/mersenne_twister.f) as the
+   reference does; single-precision arithmetic as in the reference's default
+   build.  One generator owns one random stream and nfields patterns that
+   draw from it in turn (stoch_data.f90:120-142 uses one stream for all
+   levels).  Spectral arrays are double _Complex[nfields][nlm], m-major
+   triangular (the reference's complex(ndimspec, nfields)). */
+typedef struct gd_pattern gd_pattern;
+/* patterngenerator_init (patterngenerator.f90:33-65) + gaussian_spect
+   (:145-177).  normalization is the reference's normfact (2*pi in every
+   call of stoch_data.f90); iseed 0 takes a seed from the clock, as the
+   reference does. */
+int gd_pattern_init(double lscale, double delt, double tscale, double stdev, int iseed, int nlon, int nlat,
+                    int jcap, double normalization, int nfields, int device, gd_pattern** out);
+/* The start of a pattern (stoch_data.f90:58, 81, 104, 124-127):
+   spec = stdev * getnoise * varspectrum, field after field. */
+int gd_pattern_start(gd_pattern* p);
+/* patterngenerator_advance (patterngenerator.f90:134-143) nsteps times,
+   advancing every field in turn at each step. */
+int gd_pattern_advance(gd_pattern* p, int nsteps);
+/* getnoise (patterngenerator.f90:115-132): one draw of unit-variance white
+   noise, noise = double _Complex[nlm]. */
+int gd_pattern_getnoise(gd_pattern* p, double* noise);
+/* The patterns (the reference's spec_sppt & co.), read and written. */
+int gd_pattern_get(gd_pattern* p, double* spec);
+int gd_pattern_set(gd_pattern* p, const double* spec);
+/* rpattern%varspectrum [nlm], %varspectrum1d [jcap+1] and %phi; any output
+   may be NULL. */
+int gd_pattern_spectra(gd_pattern* p, double* varspectrum, double* varspectrum1d, double* phi);
+/* patterngenerator_destroy (patterngenerator.f90:67-71). */
+int gd_pattern_destroy(gd_pattern* p);
+/* Runs the generator on an external CUDA stream (cudaStream_t as void*). */
+int gd_pattern_set_stream(gd_pattern* p, void* stream);
+/* Waits for the generator's work. */
+int gd_pattern_sync(gd_pattern* p);
+/* Number of GPU kernel launches issued by the generator so far. */
+long long gd_pattern_launch_count(gd_pattern* p);
+/* Text of the last error on p (or of the last failed gd_pattern_init if NULL). */
+const char* gd_pattern_last_error(gd_pattern* p);
+
 /* Runs the context on an external CUDA stream (cudaStream_t as void*). */
 int gd_set_stream(gd_ctx* ctx, void* stream);
 /* Waits for all work of the context. */

@@ -227,3 +227,100 @@ class Oracle:
         o = np.zeros(5)
         lib().ora_diag(self.h, _p(o))
         return dict(spdmax=o[0], psmin=o[1], psmax=o[2], pstend=o[3], pdryini=o[4])
+
+
+# ---- stochastic pattern generator (gd_pattern_oracle.cpp) --------------------
+def _pattern_lib():
+    L = lib()
+    if getattr(L, "_pattern_ready", False):
+        return L
+    vp, fp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)
+    dp = vp  # arrays are passed as raw pointers
+    L.ora_mt_uniform.argtypes = [ctypes.c_int, ctypes.c_int, fp]
+    L.ora_mt_gauss.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), fp]
+    L.ora_mt_kat.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
+    L.ora_mt_kat.restype = ctypes.c_uint32
+    L.ora_pattern_create.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+    L.ora_pattern_create.restype = vp
+    L.ora_pattern_destroy.argtypes = [vp]
+    L.ora_pattern_start.argtypes = [vp]
+    L.ora_pattern_advance.argtypes = [vp, ctypes.c_int]
+    L.ora_pattern_get.argtypes = [vp, dp]
+    L.ora_pattern_getnoise.argtypes = [vp, dp]
+    L.ora_pattern_spectra.argtypes = [vp, dp, dp, dp]
+    L.ora_pattern_varspec.argtypes = [vp, ctypes.c_int]
+    L.ora_pattern_varspec.restype = ctypes.c_double
+    L.ora_pattern_getvarspectrum.argtypes = [vp, ctypes.c_int, dp]
+    L._pattern_ready = True
+    return L
+
+
+def mt_uniform(seed, n):
+    """w3lib random_setseed(seed) then random_number of n values (float32)."""
+    out = np.zeros(n, np.float32)
+    _pattern_lib().ora_mt_uniform(seed, n, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    return out
+
+
+def mt_gauss(seed, counts):
+    """random_setseed(seed) then one random_gauss call per entry of counts."""
+    counts = np.ascontiguousarray(counts, np.int32)
+    out = np.zeros(int(counts.sum()), np.float32)
+    _pattern_lib().ora_mt_gauss(seed, len(counts), counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    return out
+
+
+def mt_kat():
+    """(this MT19937's 10000th output, std::mt19937's) from the standard seed 5489."""
+    z = ctypes.c_uint32(0)
+    y = _pattern_lib().ora_mt_kat(ctypes.byref(z))
+    return int(y), int(z.value)
+
+
+class PatternOracle:
+    """Single-precision restatement of patterngenerator.f90 (random_pattern)."""
+
+    def __init__(self, lscale, delt, tscale, stdev, iseed, jcap, normalization=2 * np.float32(np.pi),
+                 nfields=1):
+        L = _pattern_lib()
+        self.jcap, self.nfields = jcap, nfields
+        self.nlm = (jcap + 1) * (jcap + 2) // 2
+        self.h = L.ora_pattern_create(lscale, delt, tscale, stdev, iseed, jcap, float(normalization), nfields)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _pattern_lib().ora_pattern_destroy(self.h)
+            self.h = None
+
+    def start(self):
+        _pattern_lib().ora_pattern_start(self.h)
+
+    def advance(self, nsteps=1):
+        _pattern_lib().ora_pattern_advance(self.h, nsteps)
+
+    def get(self):
+        out = np.zeros((self.nfields, self.nlm), np.complex128)
+        _pattern_lib().ora_pattern_get(self.h, _p(out))
+        return out
+
+    def getnoise(self):
+        out = np.zeros(self.nlm, np.complex128)
+        _pattern_lib().ora_pattern_getnoise(self.h, _p(out))
+        return out
+
+    def spectra(self):
+        vs = np.zeros(self.nlm)
+        v1 = np.zeros(self.jcap + 1)
+        phi = np.zeros(1)
+        _pattern_lib().ora_pattern_spectra(self.h, _p(vs), _p(v1), _p(phi))
+        return vs, v1, float(phi[0])
+
+    def varspec(self, field=0):
+        return _pattern_lib().ora_pattern_varspec(self.h, field)
+
+    def getvarspectrum(self, field=0):
+        out = np.zeros(self.jcap + 1)
+        _pattern_lib().ora_pattern_getvarspectrum(self.h, field, _p(out))
+        return out

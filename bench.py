@@ -264,9 +264,52 @@ def gpu_arm(args):
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(name, args.cpu_levels)
+        # the next row beside the step: the stochastic pattern generator
+        out["pattern_generator"] = pattern_generator_rate()
         print(json.dumps(out))
     g.close()
     grp.close()
+
+
+def pattern_generator_rate(steps=40, cpu_steps=3):
+    """The stochastic pattern generator (src/patterngenerator.f90) at T574:
+    one AR(1) pattern (SPPT-like: 250 km, tau 6 h, dt 150 s), GPU steps per
+    second through the C ABI, and the single-precision CPU oracle's on the
+    same stream.  Each step draws 2 nlm = 331200 Gaussians from one
+    Mersenne-twister stream, which bounds it (a sequential recurrence), not
+    HBM."""
+    import torch
+
+    from gdpy import core
+
+    jcap, args = 574, (250e3, 150.0, 21600.0, 0.8, 7)
+    g = core.Pattern(*args, jcap)
+    g.start()
+    g.advance(2)
+    g.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(torch.cuda.default_stream())
+    g.advance(steps)
+    e1.record(torch.cuda.default_stream())
+    g.sync()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    g.close()
+    out = dict(workload="T574 one pattern", ms_per_step=ms, steps_per_s=1e3 / ms,
+               gaussians_per_s=2 * (jcap + 1) * (jcap + 2) / 2 * 1e3 / ms)
+    try:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py
+
+        o = oracle_py.PatternOracle(*args, jcap)
+        o.start()
+        t0 = time.perf_counter()
+        o.advance(cpu_steps)
+        out["cpu_port_ms_per_step"] = (time.perf_counter() - t0) * 1e3 / cpu_steps
+    except Exception as e:  # the oracle is optional here
+        out["cpu_port_ms_per_step"] = None
+        out["cpu_note"] = str(e)[:120]
+    return out
 
 
 def cpu_baseline(name, levels, nthreads=None):

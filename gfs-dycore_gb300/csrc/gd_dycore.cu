@@ -122,13 +122,30 @@ class Dycore : public DycoreBase {
   double *P64keep = nullptr, *H64keep = nullptr;
   bool split_mode() const { return c.precision == GD_PREC_TF32X3 || c.precision == GD_PREC_BF16X3; }
   std::map<int, GemmPlan> synth0_cache, anal0_cache;  // order-0-only SIMT work lists
+  // Side stream of the split modes: order 0 runs on the SIMT path beside the
+  // tensor-core GEMM of orders m >= 1 (disjoint output rows; the small SIMT
+  // CTAs fit in the SM resources the persistent GEMM leaves free).  Forked
+  // and joined with events on the context's stream, so a graph captured on
+  // that stream captures both branches.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  void fork() {
+    GD_CUDA(cudaEventRecord(ev_fork, stream));
+    GD_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+  }
+  void join() {
+    GD_CUDA(cudaEventRecord(ev_join, side));
+    GD_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
+  }
   void do_synth(bool useH, const GemmPlan& plan, const R* B, long ldB, int ncr, R* F, long ldF) {
     if constexpr (std::is_same<R, float>::value) {
       if (tcp) {
         auto it = synth0_cache.find(ncr);
         if (it == synth0_cache.end()) it = synth0_cache.emplace(ncr, make_synth_plan(T, nh, ncr, stream, 0, 0)).first;
-        launch_synth<R>(sd, useH, it->second, B, ldB, ncr, F, ldF, stream);
+        fork();
         tc_synth(*tcp, moff, useH, B, ldB, nlm_rows, ncr, F, ldF, stream);
+        launch_synth<R>(sd, useH, it->second, B, ldB, ncr, F, ldF, side);
+        join();
         return;
       }
     }
@@ -139,8 +156,10 @@ class Dycore : public DycoreBase {
       if (tcp) {
         auto it = anal0_cache.find(ncr);
         if (it == anal0_cache.end()) it = anal0_cache.emplace(ncr, make_anal_plan(T, ncr, stream, 0, 0)).first;
-        launch_anal<R>(sd, useH, it->second, G, ldG, ncr, A, ldA, stream);
+        fork();
         tc_anal(*tcp, moff, useH, G, ldG, ncr, A, ldA, stream);
+        launch_anal<R>(sd, useH, it->second, G, ldG, ncr, A, ldA, side);
+        join();
         return;
       }
     }
@@ -191,6 +210,9 @@ class Dycore : public DycoreBase {
     init_plans();
     if (split_mode()) {
       if constexpr (std::is_same<R, float>::value) {
+        GD_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        GD_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+        GD_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
         tcp.reset(new TcPlan());
         const int ncap = 2 * std::max(sc.ncol, ap.ncol);
         tc_init(*tcp, c.precision == GD_PREC_TF32X3 ? TC_TF32 : TC_BF16, T, nh, nlat, ncap, toff, P64keep, H64keep,
@@ -220,7 +242,11 @@ class Dycore : public DycoreBase {
     free_fft_plan(r2cDyn);
     free_fft_plan(r2cPhys);
     if (stream) cudaStreamSynchronize(stream);
+    if (side) cudaStreamSynchronize(side);
     for (void* p : allocs) cudaFree(p);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     if (stream && own_stream) cudaStreamDestroy(stream);
   }
 

@@ -243,6 +243,17 @@ def gpu_arm(args):
                     peak=pk["bf16"], unit="TFLOP/s", frac=achieved / pk["bf16"], traffic=None,
                     peak_source=pk["src"] + " bf16 burst",
                     note="SIMT FMA path; tensor peak shown for scale" if args.precision in ("fp32", "fp64") else "")
+        if args.precision in ("tf32x3", "bf16x3"):
+            # three products are issued per algorithmic one
+            roof["issued_tflops"] = 3 * achieved
+        if args.precision == "tf32x3" and name == "T574L64":
+            # DRAM bytes per k_tc_gemm_f launch, averaged over the four launches of a dynamics stage, from
+            # the single-pass ncu capture in profiles/tc_gemm_f_T574L64_tf32x3.md (they equal the
+            # algorithmic bytes to within 2%)
+            roof["traffic"] = 2.13e9
+            roof["traffic_unit"] = "bytes per launch (ncu)"
+            # the kind::tf32 rate measured on this GPU with a tcgen05.mma throughput probe
+            roof["tf32_tflops_measured"] = 1290.0
     else:
         key = {"fft_synth": "c2r_bytes", "fft_anal": "r2c_bytes", "columns": "col_bytes"}.get(dom)
         byt = wc[key] if key else None

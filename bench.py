@@ -248,8 +248,8 @@ def gpu_arm(args):
             roof["issued_tflops"] = 3 * achieved
         if args.precision == "tf32x3" and name == "T574L64":
             # DRAM bytes per k_tc_gemm_f launch, averaged over the four launches of a dynamics stage, from
-            # the single-pass ncu capture in profiles/tc_gemm_f_T574L64_tf32x3.md (they equal the
-            # algorithmic bytes to within 2%)
+            # a single-pass ncu capture of dram__bytes_read.sum + dram__bytes_write.sum on this workload
+            # (they equal the algorithmic bytes to within 2%)
             roof["traffic"] = 2.13e9
             roof["traffic_unit"] = "bytes per launch (ncu)"
             # the kind::tf32 rate measured on this GPU with a tcgen05.mma throughput probe

@@ -16,6 +16,7 @@
 #include "../../include/gd_api.h"
 #include "gd_grid.cuh"
 #include "gd_kernels.h"
+#include "gd_pattern.cuh"
 #include "gd_spec.cuh"
 #include "gd_tc.cuh"
 #include <type_traits>
@@ -51,6 +52,7 @@ class DycoreBase {
   virtual void diag(double*) = 0;
   virtual void profile_step(double*, int) = 0;
   virtual void check() = 0;
+  virtual void set_sppt(gd_pattern*, double, double) = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = true;
   std::string err;
@@ -345,6 +347,7 @@ class Dycore : public DycoreBase {
     ck = upload(toR(ckv));
     for (int k = 0; k <= L; ++k) si[L - k] = a[k] / 101300.0 + b[k];  // pressure_data.f90:65-67
     for (int k = 0; k < L; ++k) slv[k] = 0.5 * (si[k] + si[k + 1]);
+    sl_levels = slv;
     // setdampspec (dyn_init.f90:450-494)
     int ndiss = c.ndiss == 0 ? 8 : c.ndiss;
     double efold = c.efold, fshk = c.fshk;
@@ -709,6 +712,8 @@ class Dycore : public DycoreBase {
     h.krada = (R)GD_FLIT(1.f / (40.f * 86400.f));
     h.kradb = (R)GD_FLIT(1.f / (4.f * 86400.f));
     h.expo = (R)GD_FLIT(2.f / 7.f);
+    h.sppt = sppt ? spptg : nullptr;
+    h.vfact = vfact_d;
     return h;
   }
   void phys_pass() {
@@ -729,9 +734,49 @@ class Dycore : public DycoreBase {
       mark(PH_PHYS);
     }
   }
+  // Stochastically perturbed physics: an attached pattern (gd_pattern) is
+  // advanced one step at the start of every step and put on the grid with the
+  // logit transform (run.f90:277-281); the physics tendencies are scaled by
+  // 1 + vfact(k) * pattern (phy_run_gfs.f90:617-620), vfact tapering to 0
+  // between sigma sigbot and sigtop (stoch_data.f90:86-94).
+  gd_pattern* sppt = nullptr;
+  R* spptg = nullptr;
+  R* vfact_d = nullptr;
+  std::vector<double> sl_levels;
+  void set_sppt(gd_pattern* p, double sigtop, double sigbot) override {
+    if (p) {
+      if (pattern_device(p) != c.device) throw std::invalid_argument("gd_set_sppt: pattern on another device");
+      if (pattern_jcap(p) > T) throw std::invalid_argument("gd_set_sppt: pattern truncation above the model's");
+      if (!(sigbot > sigtop)) throw std::invalid_argument("gd_set_sppt: need sigbot > sigtop");
+      std::vector<double> vf(L);
+      for (int k = 0; k < L; ++k) {
+        const double s = sl_levels[k];
+        vf[k] = 1.0;
+        if (s < sigbot && s > sigtop)
+          vf[k] = (s - sigtop) / (sigbot - sigtop);
+        else if (s <= sigtop)
+          vf[k] = 0.0;
+      }
+      if (!spptg) spptg = dalloc<R>(ng);
+      if (!vfact_d) vfact_d = dalloc<R>(L);
+      std::vector<R> vr(vf.begin(), vf.end());
+      GD_CUDA(cudaMemcpyAsync(vfact_d, vr.data(), sizeof(R) * L, cudaMemcpyHostToDevice, stream));
+      GD_CUDA(cudaStreamSynchronize(stream));
+    }
+    sppt = p;
+    if (gexec) {  // the captured step changes
+      GD_CUDA(cudaStreamSynchronize(stream));
+      GD_CUDA(cudaGraphExecDestroy(gexec));
+      gexec = nullptr;
+    }
+  }
   // advance (run.f90:194-565)
   void step() {
     mark(-1);
+    if (sppt) {
+      pattern_advance_on(sppt, 1, stream);
+      launch_pattern_grid<R>(sd, pattern_spec(sppt), pattern_jcap(sppt), spptg, stream);
+    }
     GD_CUDA(cudaMemcpyAsync(S0, S, sizeof(R) * nlm * ldS, cudaMemcpyDeviceToDevice, stream));
     mark(PH_OTHER);
     for (int s = 0; s < 3; ++s) {
@@ -1077,6 +1122,7 @@ class Dycore : public DycoreBase {
     else if (n == "prs") src = prs, rows = L;
     else if (n == "dphisdx") src = dphisdx, rows = 1;
     else if (n == "dphisdy") src = dphisdy, rows = 1;
+    else if (n == "sppt" && sppt) src = spptg, rows = 1;
     if (!src || rows == 0) return GD_ERR_ARG;
     grid_out(src, rows, out);
     return GD_OK;
@@ -1279,6 +1325,33 @@ int gd_profile_step(gd_ctx* ctx, double* ms, int nphase) {
     return GD_ERR_ARG;
   }
   return guarded(ctx, [&] { ctx->d->profile_step(ms, nphase); });
+}
+int gd_set_sppt(gd_ctx* ctx, gd_pattern* pattern, double sigtop, double sigbot) {
+  return guarded(ctx, [&] { ctx->d->set_sppt(pattern, sigtop, sigbot); });
+}
+int gd_ensemble_advance(gd_ctx** ctxs, int n, double t, int nsteps) {
+  if (!ctxs || n < 1 || nsteps < 0) return GD_ERR_ARG;
+  for (int i = 0; i < n; ++i)
+    if (!ctxs[i] || !ctxs[i]->d) return GD_ERR_ARG;
+  (void)t;
+  // members step in turn, each on its own stream: their steps overlap on the GPU
+  for (int s = 0; s < nsteps; ++s)
+    for (int i = 0; i < n; ++i) {
+      const int rc = guarded(ctxs[i], [&] {
+        GD_CUDA(cudaSetDevice(ctxs[i]->cfg.device));
+        ctxs[i]->d->advance(1);
+      });
+      if (rc != GD_OK) return rc;
+    }
+  for (int i = 0; i < n; ++i) {
+    const int rc = guarded(ctxs[i], [&] {
+      GD_CUDA(cudaSetDevice(ctxs[i]->cfg.device));
+      GD_CUDA(cudaStreamSynchronize(ctxs[i]->d->stream));
+      ctxs[i]->d->check();
+    });
+    if (rc != GD_OK) return rc;
+  }
+  return GD_OK;
 }
 int gd_set_stream(gd_ctx* ctx, void* stream) {
   return guarded(ctx, [&] {

@@ -392,9 +392,10 @@ __global__ void __launch_bounds__(256) k_hs(HsArgs<R> a) {
     const R tv = a.gS[(long)(a.s.tv + b) * ng + p];
     const R vr = a.gS[(long)(a.s.vrt + b) * ng + p];
     const R dv = a.gS[(long)(a.s.div + b) * ng + p];
-    a.gA[(long)b * ng + p] = (a.krada + (a.kradb - a.krada) * bl * c4) * (teq - tv);
-    a.gA[(long)(L + b) * ng + p] = -(bl * a.kdrag) * vr;
-    a.gA[(long)(2 * L + b) * ng + p] = -(bl * a.kdrag) * dv;
+    const R f = a.sppt ? R(1) + a.vfact[b] * a.sppt[p] : R(1);
+    a.gA[(long)b * ng + p] = f * ((a.krada + (a.kradb - a.krada) * bl * c4) * (teq - tv));
+    a.gA[(long)(L + b) * ng + p] = f * (-(bl * a.kdrag) * vr);
+    a.gA[(long)(2 * L + b) * ng + p] = f * (-(bl * a.kdrag) * dv);
   }
 }
 template <typename R>

@@ -49,6 +49,10 @@ struct HsArgs {
   const R* gS;
   SynthRows s;
   R* gA;  // rows: dtv [0,L), dvrt [L,2L), ddiv [2L,3L)
+  // stochastically perturbed tendencies (phy_run_gfs.f90:617-620 applied to
+  // the HS forcing): x (1 + vfact[b] sppt[p]); sppt null: unperturbed
+  const R* sppt;  // [nlat*nlon]
+  const R* vfact;  // [L] bottom to top
   R kappa;
   R sigbot, kdrag, krada, kradb, expo;
 };

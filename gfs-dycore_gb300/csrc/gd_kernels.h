@@ -22,6 +22,11 @@ struct ShtDev {
   int nrad, rad[12];              // radix plan of M
 };
 
+// Stochastic-physics pattern (truncation pj <= T, FP32 coefficients) on the
+// grid [nlat][nlon], logit-transformed as run.f90:281 does.
+template <typename R>
+void launch_pattern_grid(const ShtDev<R>& d, const float2* spec, int pj, R* out, cudaStream_t s);
+
 // FP64 grid + table construction on the device.
 void launch_gauss(int nlat, double* mu, double* w, cudaStream_t s);
 void launch_legendre_tables(int T, int nh, const double* mu, const long* toff, double* P64, double* H64,

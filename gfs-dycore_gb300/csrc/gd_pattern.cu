@@ -29,6 +29,7 @@
 
 #include "gd_api.h"
 #include "gd_common.cuh"
+#include "gd_pattern.cuh"
 
 namespace gd {
 namespace {
@@ -252,19 +253,38 @@ struct gd_pattern {
     for (int i = 0; i < nlm; ++i) vs[i] = vs[i] / sv;
     for (int n = 0; n <= jcap; ++n) vs1d[n] = vs1d[n] / var;
   }
-  void draw(long pairs) {  // the next `pairs` accepted Gaussian pairs into d_g
-    gd::k_mt_gauss<<<1, gd::GT, 0, stream>>>(d_mt, d_st, d_g, pairs);
+  void draw(long pairs, cudaStream_t s) {  // the next `pairs` accepted Gaussian pairs into d_g
+    gd::k_mt_gauss<<<1, gd::GT, 0, s>>>(d_mt, d_st, d_g, pairs);
     ++launches;
     GD_LAUNCH_CHECK();
   }
-  void update(float2* x, int nf_, int nsteps, int mode) {
+  void update(float2* x, int nf_, int nsteps, int mode, cudaStream_t s) {
     const long n = (long)nf_ * nlm;
-    gd::k_pattern_update<<<gd::ceil_div(n, 256), 256, 0, stream>>>(x, d_vs, d_dego, d_g, nlm, nf_, nsteps, mode,
-                                                                   phi, stdev, nf);
+    gd::k_pattern_update<<<gd::ceil_div(n, 256), 256, 0, s>>>(x, d_vs, d_dego, d_g, nlm, nf_, nsteps, mode, phi,
+                                                              stdev, nf);
     ++launches;
     GD_LAUNCH_CHECK();
+  }
+  void advance_on(int nsteps, cudaStream_t s) {
+    for (int s0 = 0; s0 < nsteps; s0 += gsteps) {
+      const int ns = std::min(gsteps, nsteps - s0);
+      draw((long)ns * nfields * nlm, s);
+      update(d_spec, nfields, ns, 1, s);
+    }
   }
 };
+
+// internal interface for the dycore's stochastic physics (gd_pattern.cuh)
+namespace gd {
+void pattern_advance_on(gd_pattern* p, int nsteps, cudaStream_t s) {
+  p->advance_on(nsteps, s);
+  count_launch(2 * ((nsteps + p->gsteps - 1) / p->gsteps));
+}
+const float2* pattern_spec(const gd_pattern* p) { return p->d_spec; }
+int pattern_jcap(const gd_pattern* p) { return p->jcap; }
+int pattern_device(const gd_pattern* p) { return p->device; }
+int pattern_nfields(const gd_pattern* p) { return p->nfields; }
+}  // namespace gd
 
 namespace {
 template <typename F>
@@ -365,27 +385,21 @@ int gd_pattern_set_stream(gd_pattern* p, void* stream) {
 
 int gd_pattern_start(gd_pattern* p) {
   return pguard(p, [&] {
-    p->draw((long)p->nfields * p->nlm);
-    p->update(p->d_spec, p->nfields, 1, 0);
+    p->draw((long)p->nfields * p->nlm, p->stream);
+    p->update(p->d_spec, p->nfields, 1, 0, p->stream);
   });
 }
 
 int gd_pattern_advance(gd_pattern* p, int nsteps) {
   if (p && nsteps < 0) return GD_ERR_ARG;
-  return pguard(p, [&] {
-    for (int s0 = 0; s0 < nsteps; s0 += p->gsteps) {
-      const int ns = std::min(p->gsteps, nsteps - s0);
-      p->draw((long)ns * p->nfields * p->nlm);
-      p->update(p->d_spec, p->nfields, ns, 1);
-    }
-  });
+  return pguard(p, [&] { p->advance_on(nsteps, p->stream); });
 }
 
 int gd_pattern_getnoise(gd_pattern* p, double* noise) {
   if (p && !noise) return GD_ERR_ARG;
   return pguard(p, [&] {
-    p->draw(p->nlm);
-    p->update(p->d_noise, 1, 1, 2);
+    p->draw(p->nlm, p->stream);
+    p->update(p->d_noise, 1, 1, 2, p->stream);
     std::vector<float2> h(p->nlm);
     GD_CUDA(cudaMemcpyAsync(h.data(), p->d_noise, sizeof(float2) * p->nlm, cudaMemcpyDeviceToHost, p->stream));
     GD_CUDA(cudaStreamSynchronize(p->stream));

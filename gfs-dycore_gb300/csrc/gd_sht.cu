@@ -366,6 +366,55 @@ void fft_init_tables(int nlon, typename C2<R>::T* twM, typename C2<R>::T* twN, c
 template void fft_init_tables<double>(int, double2*, double2*, cudaStream_t);
 template void fft_init_tables<float>(int, float2*, float2*, cudaStream_t);
 
+// The stochastic-physics pattern on the grid (run.f90:277-281): spectogrd of
+// a pattern truncated at pj <= T (coefficients m-major triangular at pj, FP32)
+// with the model's own Legendre tables, then the logit transform
+// 2 / (1 + exp(g)) - 1 that keeps perturbed tendencies from changing sign.
+// One CTA per latitude: the orders' Fourier coefficients in shared memory,
+// then the real Fourier sum g = F_0 + 2 sum_m Re(F_m e^{i m lambda}).
+template <typename R>
+__global__ void k_pattern_grid(ShtDev<R> d, const float2* __restrict__ spec, int pj, R* __restrict__ out) {
+  typedef typename C2<R>::T V;
+  extern __shared__ __align__(16) unsigned char smpg[];
+  V* F = reinterpret_cast<V*>(smpg);
+  const int j = blockIdx.x;
+  const bool south = j >= d.nh;
+  const int jh = south ? d.nlat - 1 - j : j;
+  for (int m = threadIdx.x; m <= pj; m += blockDim.x) {
+    const int K = d.T + 1 - m;
+    const R* Pm = d.P + d.toff[m] + (long)jh * K;
+    const long po = (long)m * (pj + 1) - (long)m * (m - 1) / 2;  // (n = m, m) in the pattern's layout
+    R re = R(0), im = R(0);
+    for (int n = m; n <= pj; ++n) {
+      R pv = Pm[n - m];
+      if (south && ((n - m) & 1)) pv = -pv;  // P_n^m(-mu) = (-1)^(n-m) P_n^m(mu)
+      const float2 c = spec[po + n - m];
+      re += pv * (R)c.x;
+      im += pv * (R)c.y;
+    }
+    F[m] = mk2<R>(re, im);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < d.nlon; i += blockDim.x) {
+    R g = F[0].x;
+    for (int m = 1; m <= pj; ++m) {
+      R sn, cs;
+      sincospi(R(2) * (R)(((long)m * i) % d.nlon) / (R)d.nlon, &sn, &cs);
+      g += R(2) * (F[m].x * cs - F[m].y * sn);
+    }
+    out[(long)j * d.nlon + i] = R(2) / (R(1) + exp(g)) - R(1);
+  }
+}
+template <typename R>
+void launch_pattern_grid(const ShtDev<R>& d, const float2* spec, int pj, R* out, cudaStream_t s) {
+  if (pj < 0 || pj > d.T) throw std::invalid_argument("pattern truncation above the model's");
+  k_pattern_grid<R><<<d.nlat, 128, (size_t)(pj + 1) * sizeof(typename C2<R>::T), s>>>(d, spec, pj, out);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template void launch_pattern_grid<double>(const ShtDev<double>&, const float2*, int, double*, cudaStream_t);
+template void launch_pattern_grid<float>(const ShtDev<float>&, const float2*, int, float*, cudaStream_t);
+
 template <typename V>
 __device__ __forceinline__ V cmul(V a, V b) {
   V r;

@@ -35,7 +35,7 @@ API_FUNCTIONS = [
     "gd_diag_static",
     "gd_pattern_init", "gd_pattern_start", "gd_pattern_advance", "gd_pattern_getnoise", "gd_pattern_get",
     "gd_pattern_set", "gd_pattern_spectra", "gd_pattern_destroy", "gd_pattern_set_stream", "gd_pattern_sync",
-    "gd_pattern_launch_count", "gd_pattern_last_error",
+    "gd_pattern_launch_count", "gd_pattern_last_error", "gd_set_sppt", "gd_ensemble_advance",
 ]
 PHASES = ["legendre_synth", "fft_synth", "columns", "fft_anal", "legendre_anal", "semi_implicit",
           "physics", "other"]
@@ -99,6 +99,8 @@ def load(build_if_missing=True):
     L.gd_pattern_launch_count.argtypes = [vp]
     L.gd_pattern_last_error.restype = ctypes.c_char_p
     L.gd_pattern_last_error.argtypes = [vp]
+    L.gd_set_sppt.argtypes = [vp, vp, d, d]
+    L.gd_ensemble_advance.argtypes = [ctypes.POINTER(vp), i, d, i]
     _lib = L
     return L
 
@@ -185,6 +187,11 @@ class Dycore:
         self._chk(load().gd_getphytend(self.h, _p(d[0]), _p(d[1]), _p(d[2]), None, None))
         return dict(dvrt=d[0], ddiv=d[1], dtv=d[2])
 
+    def set_sppt(self, pattern, sigtop=0.05, sigbot=0.10):
+        """Attach a Pattern as stochastically perturbed physics (None detaches)."""
+        self._sppt = pattern  # keep the generator alive while attached
+        self._chk(load().gd_set_sppt(self.h, pattern.h if pattern is not None else None, sigtop, sigbot))
+
     def advance(self, nsteps=1, t=0.0):
         self._chk(load().gd_advance(self.h, ctypes.c_double(t), int(nsteps)))
 
@@ -251,7 +258,7 @@ class Dycore:
     def get_grid(self, name):
         L = self.nlev
         rows = dict(ug=L, vg=L, vrtg=L, divg=L, tvg=L, dlnpdtg=L, prs=L, etadot=L + 1,
-                    trcg=max(self.ntrac, 1) * L, lnpsg=1, psg=1, dlnpsdt=1, dphisdx=1, dphisdy=1)
+                    trcg=max(self.ntrac, 1) * L, lnpsg=1, psg=1, dlnpsdt=1, dphisdx=1, dphisdy=1, sppt=1)
         out = np.zeros((rows[name], self.nlat, self.nlon))
         self._chk(load().gd_get_grid(self.h, name.encode(), _p(out)))
         return out
@@ -330,3 +337,12 @@ class Pattern:
 
     def launch_count(self):
         return load().gd_pattern_launch_count(self.h)
+
+
+def ensemble_advance(members, nsteps=1):
+    """gd_ensemble_advance: step all members, overlapping on the GPU."""
+    arr = (ctypes.c_void_p * len(members))(*[m.h.value if hasattr(m.h, "value") else m.h for m in members])
+    rc = load().gd_ensemble_advance(arr, len(members), 0.0, nsteps)
+    if rc != GD_OK:
+        raise GdError(rc, "gd_ensemble_advance failed: " + "; ".join(
+            load().gd_last_error(m.h).decode() for m in members))

@@ -130,7 +130,9 @@ int gd_grid_info(gd_ctx* ctx, double* lats, double* gauwts, double* areawts, int
                  int* order, double* lap, double* invlap);
 
 /* Grid fields of the last getdyntend: "ug" "vg" "vrtg" "divg" "tvg" "trcg"
-   "dlnpdtg" "etadot" "lnpsg" "psg" "dlnpsdt" "prs" "dphisdx" "dphisdy". */
+   "dlnpdtg" "etadot" "lnpsg" "psg" "dlnpsdt" "prs" "dphisdx" "dphisdy", and "sppt"
+   (the logit-transformed stochastic-physics pattern of the last step, while
+   one is attached). */
 int gd_get_grid(gd_ctx* ctx, const char* name, double* out);
 
 /* Step diagnostics of src/run.f90:159-161 after the last step:
@@ -209,6 +211,24 @@ int gd_pattern_sync(gd_pattern* p);
 long long gd_pattern_launch_count(gd_pattern* p);
 /* Text of the last error on p (or of the last failed gd_pattern_init if NULL). */
 const char* gd_pattern_last_error(gd_pattern* p);
+
+/* Stochastically perturbed physics (SPPT).  Attaches pattern (NULL
+   detaches) to ctx: at the start of every gd_advance step the pattern is
+   advanced one AR(1) step and put on the grid with the logit transform
+   2/(1+exp(g))-1 (src/run.f90:277-281), and the physics tendencies are scaled
+   by 1 + vfact(k) * pattern (src/phy_run_gfs.f90:617-620), vfact 1 below
+   sigma sigbot, 0 above sigtop, linear between (src/stoch_data.f90:86-94,
+   sigbot 0.10, sigtop 0.05 there).  Here the physics is the Held-Suarez
+   forcing, whose Tv, vorticity and divergence tendencies are scaled on the
+   grid.  The pattern must live on ctx's device with a truncation at most
+   ctx's; it is advanced on ctx's stream. */
+int gd_set_sppt(gd_ctx* ctx, gd_pattern* pattern, double sigtop, double sigbot);
+/* Advances n independent contexts (ensemble members, any mix of
+   truncations) by nsteps steps each: the members step in turn, each on its
+   own stream and captured step graph, so their steps overlap on the GPU;
+   returns when all are done.  No counterpart in the reference, which runs one
+   member per process. */
+int gd_ensemble_advance(gd_ctx** ctxs, int n, double t, int nsteps);
 
 /* Runs the context on an external CUDA stream (cudaStream_t as void*). */
 int gd_set_stream(gd_ctx* ctx, void* stream);

@@ -445,6 +445,12 @@ void invert(std::vector<double>& a, int n) {
   a.swap(inv);
 }
 
+extern "C" {
+void ora_pattern_advance(void* h, int nsteps);
+void ora_pattern_get(void* h, double* out);
+int ora_pattern_jcap(void* h);
+}
+
 struct Dycore {
   ora_config c;
   Sht sh;
@@ -857,6 +863,41 @@ struct Dycore {
     return sh.w[p / nlon] / (2.0 * nlon);
   }
 
+  // Stochastically perturbed physics: a pattern of the single-precision
+  // generator (gd_pattern_oracle.cpp) advanced at the start of each step and
+  // put on the grid with the logit transform (run.f90:277-281); the HS
+  // tendencies are scaled by 1 + vfact(k) pattern (phy_run_gfs.f90:617-620)
+  // with vfact from stoch_data.f90:86-94.
+  void* sppt = nullptr;
+  std::vector<double> spptg, vfactv;
+  void set_sppt(void* pat, double sigtop, double sigbot) {
+    sppt = pat;
+    vfactv.assign(L, 1.0);
+    for (int k = 0; k < L; ++k) {
+      if (sl[k] < sigbot && sl[k] > sigtop)
+        vfactv[k] = (sl[k] - sigtop) / (sigbot - sigtop);
+      else if (sl[k] <= sigtop)
+        vfactv[k] = 0.0;
+    }
+  }
+  void sppt_step() {
+    ora_pattern_advance(sppt, 1);
+    const int pj = ora_pattern_jcap(sppt), T = c.ntrunc;
+    std::vector<double> pc((size_t)(pj + 1) * (pj + 2));  // complex pairs
+    ora_pattern_get(sppt, pc.data());
+    std::vector<cplx> full(nlm, cplx(0, 0));
+    long pi = 0, fi = 0;
+    for (int m = 0; m <= T; ++m)
+      for (int n = m; n <= T; ++n, ++fi)
+        if (m <= pj && n <= pj) {
+          full[fi] = cplx(pc[2 * pi], pc[2 * pi + 1]);
+          ++pi;
+        }
+    spptg.assign(ng, 0.0);
+    sh.spectogrd(full.data(), spptg.data());
+    for (long p = 0; p < ng; ++p) spptg[p] = 2.0 / (1.0 + exp(spptg[p])) - 1.0;
+  }
+
   // phy_run_hs.f90:22-84
   void getphytend(cplx* dvrt, cplx* ddiv, cplx* dtv, cplx* dtrc, cplx* dlnps) {
     const double sigbot = FLIT(0.7f), delthz = 10., tempstrat = 200.;
@@ -877,9 +918,10 @@ struct Dycore {
         if (bl < 0) bl = 0;
         if (teq < tempstrat) teq = tempstrat;
         double cl = cos(la);
-        f1[p] = (krada + (kradb - krada) * bl * cl * cl * cl * cl) * (teq - tvg[o]);
-        f2[p] = -(bl * kdrag) * vrtg[o];
-        f3[p] = -(bl * kdrag) * divg[o];
+        const double f = sppt ? 1.0 + vfactv[k] * spptg[p] : 1.0;
+        f1[p] = f * ((krada + (kradb - krada) * bl * cl * cl * cl * cl) * (teq - tvg[o]));
+        f2[p] = f * (-(bl * kdrag) * vrtg[o]);
+        f3[p] = f * (-(bl * kdrag) * divg[o]);
       }
       sh.grdtospec(f1.data(), &dtv[k * NL]);
       sh.grdtospec(f2.data(), &dvrt[k * NL]);
@@ -892,6 +934,7 @@ struct Dycore {
 
   // run.f90:194-565 (IAU, stochastic and DFI branches are out of scope)
   void advance(double) {
+    if (sppt) sppt_step();
     const long NS = (long)L * nlm, NT = (long)nt * L * nlm;
     const double dt = c.dt;
     std::vector<cplx> vrt0 = vrt, div0 = div, tv0 = tv, trc0 = trc, lnps0 = lnps;
@@ -1198,6 +1241,9 @@ void ora_getdyntend(void* h, int rkstage, int inverse_only, double* dvrt, double
   std::copy(f.begin(), f.end(), C(dlnps));
 }
 
+void ora_set_sppt(void* h, void* pattern, double sigtop, double sigbot) {
+  static_cast<Dycore*>(h)->set_sppt(pattern, sigtop, sigbot);
+}
 void ora_advance(void* h, double t, int nsteps) {
   Dycore* d = D(h);
   for (int s = 0; s < nsteps; ++s) {

@@ -320,6 +320,7 @@ void ora_pattern_spectra(void* h, double* varspectrum, double* varspectrum1d, do
   for (int n = 0; n <= p->ntrunc; ++n) varspectrum1d[n] = p->varspectrum1d[n];
   *phi = p->phi;
 }
+int ora_pattern_jcap(void* h) { return static_cast<Pattern*>(h)->ntrunc; }
 double ora_pattern_varspec(void* h, int field) {
   Pattern* p = static_cast<Pattern*>(h);
   return p->computevarspec(p->spec.data() + (size_t)field * p->nlm);

@@ -175,6 +175,13 @@ class Oracle:
         lib().ora_getphytend(self.h, _p(d[0]), _p(d[1]), _p(d[2]))
         return dict(dvrt=d[0], ddiv=d[1], dtv=d[2])
 
+    def set_sppt(self, pattern, sigtop=0.05, sigbot=0.10):
+        """Attach a PatternOracle as stochastically perturbed physics."""
+        self._sppt = pattern
+        L = lib()
+        L.ora_set_sppt.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
+        L.ora_set_sppt(self.h, pattern.h, sigtop, sigbot)
+
     def advance(self, nsteps=1, t=0.0):
         lib().ora_advance(self.h, ctypes.c_double(t), nsteps)
 

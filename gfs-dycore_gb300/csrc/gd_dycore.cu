@@ -53,6 +53,7 @@ class DycoreBase {
   virtual void profile_step(double*, int) = 0;
   virtual void check() = 0;
   virtual void set_sppt(gd_pattern*, double, double) = 0;
+  virtual double get_pdryini() = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = true;
   std::string err;
@@ -1127,6 +1128,12 @@ class Dycore : public DycoreBase {
     grid_out(src, rows, out);
     return GD_OK;
   }
+  double get_pdryini() override {
+    double h = 0.0;
+    GD_CUDA(cudaMemcpyAsync(&h, pdryini, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    GD_CUDA(cudaStreamSynchronize(stream));
+    return h;
+  }
   void diag(double* out) override {
     launch_diag<R>(gS + (long)sr.u * ng, gS + (long)sr.v * ng, L, psg, dlnpsdt, w, nlat, nlon, diagbuf, diagout,
                    stream);
@@ -1145,6 +1152,7 @@ struct gd_ctx {
   std::unique_ptr<gd::DycoreBase> d;
   gd_config cfg;
   std::string err;
+  std::vector<double> topo;  // orography of the last gd_set_state (complex [nlm]), for gd_write_sig
 };
 
 static std::string g_init_error;
@@ -1257,7 +1265,12 @@ int gd_set_state(gd_ctx* ctx, const double* vrt, const double* div, const double
     if (ctx) ctx->err = "gd_set_state: null state array";
     return GD_ERR_ARG;
   }
-  return guarded(ctx, [&] { ctx->d->set_state(vrt, div, tv, trc, lnps, topo); });
+  return guarded(ctx, [&] {
+    ctx->d->set_state(vrt, div, tv, trc, lnps, topo);
+    const long n2 = (long)(ctx->cfg.ntrunc + 1) * (ctx->cfg.ntrunc + 2);
+    if (topo) ctx->topo.assign(topo, topo + n2);
+    else ctx->topo.assign((size_t)n2, 0.0);
+  });
 }
 int gd_get_state(gd_ctx* ctx, double* vrt, double* div, double* tv, double* trc, double* lnps) {
   return guarded(ctx, [&] { ctx->d->get_state(vrt, div, tv, trc, lnps); });
@@ -1353,6 +1366,74 @@ int gd_ensemble_advance(gd_ctx** ctxs, int n, double t, int nsteps) {
   }
   return GD_OK;
 }
+// ln(1000) on the (0,0) coefficient: the constant field c has coefficient
+// c * sqrt(4 pi) with orthonormal harmonics.  dyn_init.f90:46-48 and :160-162
+// make the same change on the grid (spectogrd, x1000 or /1000 of exp,
+// log, grdtospec), which returns the band-limited field exactly.
+static const double kLn1000Y00 = std::log(1000.0) * std::sqrt(4.0 * 3.14159265358979323846);
+
+int gd_read_sig(gd_ctx* ctx, const char* path, gd_sighead* head) {
+  if (!ctx || !ctx->d) return GD_ERR_ARG;
+  if (!path || !head) {
+    ctx->err = "gd_read_sig: null argument";
+    return GD_ERR_ARG;
+  }
+  const gd_config& c = ctx->cfg;
+  const size_t n2 = (size_t)(c.ntrunc + 1) * (c.ntrunc + 2), L = (size_t)c.nlev, nt = (size_t)c.ntrac;
+  std::vector<double> vrt, div, tv, trc, lnps, topo;
+  try {
+    vrt.resize(n2 * L), div.resize(n2 * L), tv.resize(n2 * L), trc.resize(n2 * L * nt);
+    lnps.resize(n2), topo.resize(n2);
+  } catch (const std::bad_alloc&) {
+    ctx->err = "gd_read_sig: host allocation failed";
+    return GD_ERR_NOMEM;
+  }
+  const int rc = gd_sigio_read(path, c.ntrunc, c.nlev, c.ntrac, head, vrt.data(), div.data(), tv.data(),
+                               nt ? trc.data() : nullptr, lnps.data(), topo.data());
+  if (rc != GD_OK) {
+    ctx->err = gd_sigio_last_error();
+    return rc;
+  }
+  lnps[0] += kLn1000Y00;  // ln(ps in cb) -> ln(ps in Pa)
+  return gd_set_state(ctx, vrt.data(), div.data(), tv.data(), nt ? trc.data() : nullptr, lnps.data(),
+                      topo.data());
+}
+
+int gd_write_sig(gd_ctx* ctx, const char* path, double fhour, gd_sighead* head) {
+  if (!ctx || !ctx->d) return GD_ERR_ARG;
+  if (!path || !head) {
+    ctx->err = "gd_write_sig: null argument";
+    return GD_ERR_ARG;
+  }
+  const gd_config& c = ctx->cfg;
+  if (head->jcap != c.ntrunc || head->levs != c.nlev || head->ntrac < c.ntrac) {
+    ctx->err = "gd_write_sig: header jcap/levs/ntrac do not match the context";
+    return GD_ERR_ARG;
+  }
+  const size_t n2 = (size_t)(c.ntrunc + 1) * (c.ntrunc + 2), L = (size_t)c.nlev, nt = (size_t)c.ntrac;
+  std::vector<double> vrt, div, tv, trc, lnps;
+  try {
+    vrt.resize(n2 * L), div.resize(n2 * L), tv.resize(n2 * L), trc.resize(n2 * L * nt), lnps.resize(n2);
+  } catch (const std::bad_alloc&) {
+    ctx->err = "gd_write_sig: host allocation failed";
+    return GD_ERR_NOMEM;
+  }
+  double pdry = 0.0;
+  int rc = guarded(ctx, [&] {
+    ctx->d->get_state(vrt.data(), div.data(), tv.data(), nt ? trc.data() : nullptr, lnps.data());
+    pdry = ctx->d->get_pdryini();
+  });
+  if (rc != GD_OK) return rc;
+  lnps[0] -= kLn1000Y00;  // ln(ps in Pa) -> ln(ps in cb)
+  if (ctx->topo.size() != n2) ctx->topo.assign(n2, 0.0);
+  head->fhour = (float)fhour;
+  head->pdryini = (float)(pdry / 1000.0);
+  rc = gd_sigio_write(path, head, c.ntrac, vrt.data(), div.data(), tv.data(), nt ? trc.data() : nullptr,
+                      lnps.data(), ctx->topo.data());
+  if (rc != GD_OK) ctx->err = gd_sigio_last_error();
+  return rc;
+}
+
 int gd_set_stream(gd_ctx* ctx, void* stream) {
   return guarded(ctx, [&] {
     GD_CUDA(cudaStreamSynchronize(ctx->d->stream));

@@ -14,7 +14,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libgdcore.so")
-SOURCES = ["gd_sht.cu", "gd_grid.cu", "gd_spec.cu", "gd_tc.cu", "gd_dycore.cu", "gd_noalloc.cu", "gd_pattern.cu"]
+SOURCES = ["gd_sht.cu", "gd_grid.cu", "gd_spec.cu", "gd_tc.cu", "gd_dycore.cu", "gd_noalloc.cu", "gd_pattern.cu",
+           "gd_sigio.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no FMA contraction (the single-precision pattern set-up is
 # specified operation by operation)
@@ -44,7 +45,7 @@ def build(verbose=False, force=False, extra=()):
     objs, jobs = [], []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append([nvcc(), *ARCH, *FLAGS, *extra, "-c", s, "-o", o])

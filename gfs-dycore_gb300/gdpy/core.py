@@ -24,6 +24,7 @@ GD_ERR_STATE = -3
 GD_ERR_NOMEM = -4
 GD_ERR_UNSUPPORTED = -5
 GD_ERR_NUMERIC = -6
+GD_ERR_IO = -7
 
 PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3}
 
@@ -36,6 +37,8 @@ API_FUNCTIONS = [
     "gd_pattern_init", "gd_pattern_start", "gd_pattern_advance", "gd_pattern_getnoise", "gd_pattern_get",
     "gd_pattern_set", "gd_pattern_spectra", "gd_pattern_destroy", "gd_pattern_set_stream", "gd_pattern_sync",
     "gd_pattern_launch_count", "gd_pattern_last_error", "gd_set_sppt", "gd_ensemble_advance",
+    "gd_sigio_head_init", "gd_sigio_read_head", "gd_sigio_read", "gd_sigio_write", "gd_sigio_config",
+    "gd_read_sig", "gd_write_sig", "gd_sigio_last_error",
 ]
 PHASES = ["legendre_synth", "fft_synth", "columns", "fft_anal", "legendre_anal", "semi_implicit",
           "physics", "other"]
@@ -101,6 +104,16 @@ def load(build_if_missing=True):
     L.gd_pattern_last_error.argtypes = [vp]
     L.gd_set_sppt.argtypes = [vp, vp, d, d]
     L.gd_ensemble_advance.argtypes = [ctypes.POINTER(vp), i, d, i]
+    cp = ctypes.c_char_p
+    L.gd_sigio_head_init.argtypes = [vp]
+    L.gd_sigio_read_head.argtypes = [cp, vp]
+    L.gd_sigio_read.argtypes = [cp, i, i, i, vp, vp, vp, vp, vp, vp, vp]
+    L.gd_sigio_write.argtypes = [cp, vp, i, vp, vp, vp, vp, vp, vp]
+    L.gd_sigio_config.argtypes = [vp, vp, vp, vp]
+    L.gd_read_sig.argtypes = [vp, cp, vp]
+    L.gd_write_sig.argtypes = [vp, cp, d, vp]
+    L.gd_sigio_last_error.restype = ctypes.c_char_p
+    L.gd_sigio_last_error.argtypes = []
     _lib = L
     return L
 
@@ -170,6 +183,18 @@ class Dycore:
         lnps = np.zeros(n, np.complex128)
         self._chk(load().gd_get_state(self.h, _p(vrt), _p(div), _p(tv), _p(trc), _p(lnps)))
         return dict(vrt=vrt, div=div, tv=tv, trc=trc[: self.ntrac], lnps=lnps)
+
+    def read_sig(self, path):
+        """readin_sig + init_dyn's ln(ps) conversion (gd_read_sig); returns the header."""
+        from . import sigio
+
+        return sigio.read_into(self, path)
+
+    def write_sig(self, path, fhour, head):
+        """wrtout_sig (gd_write_sig) with head, a sigio.SigHead."""
+        from . import sigio
+
+        sigio.write_from(self, path, fhour, head)
 
     # ---- dynamics ----
     def getdyntend(self, rkstage=1, inverse_only=False):

@@ -230,6 +230,105 @@ int gd_set_sppt(gd_ctx* ctx, gd_pattern* pattern, double sigtop, double sigbot);
    member per process. */
 int gd_ensemble_advance(gd_ctx** ctxs, int n, double t, int nsteps);
 
+/* ---- sigma files (src/sigio_module.f90) ----------------------------------
+   The GFS spectral "sigma" file: big-endian Fortran unformatted sequential
+   records (4-byte length markers before and after each record), in either
+   header version the reference reads: ivs 200509 ('GFS SIG ' label, header
+   records of 32, 4*(nhead+ndata), 200, 4*(levs+1)*nvcoord, 8*(5+ntrac)
+   bytes, then cpi and ri when mod(idvm/10,10) == 3) or 198410 (a 32-byte
+   ON85 label and one 250-word record).  The data records follow: orography,
+   ln(ps in cb), levs temperature records, levs (divergence, vorticity)
+   pairs, ntrac*levs tracer records, nxgr grid records of lonb*latb words,
+   and nxss scalars; nc = (jcap+1)(jcap+2) words each, 4-byte floats unless
+   irealf == 2 (8-byte).  Records are read and written whole; a record of
+   2^31 bytes or more (gfortran subrecords) is not supported.
+   All file calls are host-only (no GPU) and thread-safe on distinct files;
+   gd_sigio_last_error() reports the calling thread's last failure. */
+#define GD_ERR_IO (-7)             /* file cannot be opened, read or written, or
+                                      is not a sigma file of a known version   */
+#define GD_SIG_MAXLEVS 256         /* levels a header can describe            */
+#define GD_SIG_MAXTRAC 100         /* tracers a header can describe           */
+#define GD_SIG_FILL (-9999.0f)     /* sigio_realfill / sigio_intfill          */
+
+/* type sigio_head (sigio_module.f90:337-379), fixed-size.  vcoord(k,j) of
+   the Fortran header is vcoord[j-1][k-1] (k = 1..levs+1 bottom to top,
+   j = 1..nvcoord <= 3); cfvars holds 5+ntrac blank-padded 8-character
+   names; cpi and ri hold ntrac+1 values when mod(idvm/10,10) == 3.  nxgr,
+   nxss, nhead, ndata are derived from the other fields (sigio_adhead,
+   sigio_module.f90:1323-1382) on every read and write. */
+typedef struct gd_sighead {
+  char clabsig[32];
+  float fhour;
+  int idate[4];                        /* hour, month, day, year          */
+  float si[101], sl[100], ak[101], bk[101];
+  int jcap, levs, itrun, iorder, irealf, igen, latf, lonf, latb, lonb, latr, lonr;
+  int ntrac, icen2, iens[2], idpp, idsl, idvc, idvm, idvt, idrun, idusr;
+  float pdryini;                       /* cb                               */
+  int ncldt, ixgr, ivs, nvcoord;
+  float vcoord[3][GD_SIG_MAXLEVS + 1];
+  char cfvars[5 + GD_SIG_MAXTRAC][8];
+  int nxgr, nxss, nhead, ndata;
+  float cpi[GD_SIG_MAXTRAC + 1], ri[GD_SIG_MAXTRAC + 1];
+} gd_sighead;
+
+/* The default-initialised sigio_head: every number the fill value, every
+   label blank (sigio_module.f90:338-379). */
+int gd_sigio_head_init(gd_sighead* head);
+/* sigio_sropen + sigio_srhead (sigio_module.f90:430-442, 470-576).  As in
+   the reference, a 200509 header comes back with si, sl, ak, bk and pdryini
+   set to the fill value (the file's pdryini word is not kept), and a 198410
+   header with jcap..ixgr truncated from its real-valued ext words, ntrac at
+   least 1, and vcoord taken from its sigma/hybrid words by idvc. */
+int gd_sigio_read_head(const char* path, gd_sighead* head);
+/* readin_sig (src/dyn_init.f90:120-149) = sigio_srohdc + copyspecin: reads
+   header and data and renormalises every spectral field from the NCEP
+   normalisation to the model's orthonormal one, c = sqrt(2 pi) *
+   (re, im) per coefficient (dyn_init.f90:93-104, pi the reference's
+   single-rounded con_pi), sequentially with no reordering.  Values pass
+   through single precision as in the reference (irealf 2 data are rounded
+   to float by sigio_srdata).  The file must have truncation jcap, levs
+   levels and at least ntrac tracers (the first ntrac are read); outputs
+   are double _Complex: vrt, div, tv [levs][nlm], trc [ntrac][levs][nlm],
+   lnps (ln of ps in cb, as stored) and topo (orography, m) [nlm],
+   nlm = (jcap+1)(jcap+2)/2; any output may be NULL. */
+int gd_sigio_read(const char* path, int jcap, int levs, int ntrac, gd_sighead* head, double* vrt,
+                  double* div, double* tv, double* trc, double* lnps, double* topo);
+/* copyspecout + sigio_swohdc (dyn_init.f90:106-118, sigio_module.f90:942-962,
+   578-676, 836-915): writes head (its version chooses the header layout;
+   nxgr/nxss/nhead/ndata are recomputed into it) and the spectral fields
+   divided by sqrt(2 pi) and rounded to float (then widened when irealf ==
+   2).  trc holds ntrac <= head->ntrac tracers; the remaining tracer
+   records, and any extra grid/scalar records the header declares, are
+   written as zeros (the reference writes its unset buffers there).  A 198410
+   header with a sigma coordinate whose vcoord(1,1) is 1 gets its layer
+   values from sigio_modpr (sigio_module.f90:1207-1321) at ps = 1. */
+int gd_sigio_write(const char* path, gd_sighead* head, int ntrac, const double* vrt, const double* div,
+                   const double* tv, const double* trc, const double* lnps, const double* topo);
+/* The model configuration a header implies (src/params.f90:250-264 and
+   src/dyn_init.f90:52-66): cfg->ntrunc = jcap, nlon = lonb, nlat = latb,
+   nlev = levs, pdryini = 1000 * head pdryini (Pa), 0 when above 1e5 Pa; ak, bk
+   [levs+1] top to bottom from the hybrid vcoord, reversed.  A header whose
+   pdryini is the fill value (every 200509 header as read) gives 0, i.e. the
+   first step's dry mass; the reference would take -9.999e6 Pa there.  Other
+   cfg fields are left as they are; idvc other than 2 returns
+   GD_ERR_UNSUPPORTED as the reference stops there. */
+int gd_sigio_config(const gd_sighead* head, gd_config* cfg, double* ak, double* bk);
+/* readin_sig and the start of init_dyn on a context (dyn_init.f90:44-48):
+   reads path (jcap, levs must be ctx's, at least ctx's ntrac tracers),
+   converts ln(ps in cb) to ln(ps in Pa) -- the reference's spectogrd,
+   1000*exp, log, grdtospec round trip, which for the band-limited field is
+   the constant ln(1000) added to the (0,0) coefficient, done here that way
+   -- and sets the state and orography as gd_set_state does. */
+int gd_read_sig(gd_ctx* ctx, const char* path, gd_sighead* head);
+/* wrtout_sig (dyn_init.f90:151-191): head->fhour = fhour, head->pdryini =
+   the context's pdryini / 1000 (cb); writes the context's state with ln(ps)
+   back in cb (the constant ln(1000) taken off the (0,0) coefficient) and
+   the orography of the last gd_set_state / gd_read_sig.  head's jcap and
+   levs must be ctx's and head->ntrac at least ctx's ntrac. */
+int gd_write_sig(gd_ctx* ctx, const char* path, double fhour, gd_sighead* head);
+/* Text of the calling thread's last sigma-file failure. */
+const char* gd_sigio_last_error(void);
+
 /* Runs the context on an external CUDA stream (cudaStream_t as void*). */
 int gd_set_stream(gd_ctx* ctx, void* stream);
 /* Waits for all work of the context. */

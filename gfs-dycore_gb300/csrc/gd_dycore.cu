@@ -17,6 +17,8 @@
 #include "gd_grid.cuh"
 #include "gd_kernels.h"
 #include "gd_pattern.cuh"
+#include "gd_dcmip.h"
+#include "gd_physics.cuh"
 #include "gd_spec.cuh"
 #include "gd_tc.cuh"
 #include <type_traits>
@@ -85,6 +87,11 @@ class Dycore : public DycoreBase {
   R *FPb = nullptr, *FHb = nullptr, *gS = nullptr, *gA = nullptr;
   R *psg = nullptr, *dlnpsdt = nullptr, *dlnpdtg = nullptr, *etadot = nullptr, *prs = nullptr;
   R *dphisdx = nullptr, *dphisdy = nullptr;
+  // DCMIP simple physics (phy_data.f90): latitude, precipitation rate,
+  // precipitable water, accumulated precipitation
+  R *latr = nullptr, *precip = nullptr, *pwat = nullptr, *apcp = nullptr;
+  double *pmoist = nullptr, *pwatg = nullptr;
+  bool simple() const { return c.dcmip >= 0 && !c.dry; }
   double *pdryini = nullptr, *pmean = nullptr, *rowsum = nullptr, *diagbuf = nullptr, *diagout = nullptr;
   int4* stage_items = nullptr;
   int nstage_items = 0;
@@ -96,8 +103,8 @@ class Dycore : public DycoreBase {
   AnalRows ar;
   long ldS, ldTD, ldAP, ldAH, ldFP, ldFH, ldGP, ldGH;
   long nlm_rows = 0;  // allocated rows of the synthesis sources: nlm rounded up to even
-  GemmPlan synP, synH, anaP, anaH, anaPhys;
-  FftPlan c2rFull, c2rInv, r2cDyn, r2cPhys;
+  GemmPlan synP, synH, anaP, anaH, anaPhys, anaSimple;
+  FftPlan c2rFull, c2rInv, r2cDyn, r2cPhys, r2cSimple;
   Tableau tb;
   // per-phase CUDA-event profiling of one eager step (gd_profile_step)
   enum { PH_LSYN, PH_FSYN, PH_COL, PH_FANA, PH_LANA, PH_SEMI, PH_PHYS, PH_OTHER, PH_N };
@@ -305,6 +312,7 @@ class Dycore : public DycoreBase {
     wn = upload(toR(wnv));
     sinlat = upload(toR(sl));
     coslat = upload(toR(cl));
+    latr = upload(toR(h_lat));
     twM = dalloc<V>(M);
     twN = dalloc<V>(M + 1);
     fft_init_tables<R>(nlon, twM, twN, stream);
@@ -534,6 +542,12 @@ class Dycore : public DycoreBase {
     GD_CUDA(cudaMemsetAsync(dphisdy, 0, sizeof(R) * ng, stream));
     pdryini = dalloc<double>(1);
     pmean = dalloc<double>(1);
+    pmoist = dalloc<double>(1);
+    pwatg = dalloc<double>(1);
+    precip = dalloc<R>(ng);
+    pwat = dalloc<R>(ng);
+    apcp = dalloc<R>(ng);
+    for (R* z : {precip, pwat, apcp}) GD_CUDA(cudaMemsetAsync(z, 0, sizeof(R) * ng, stream));
     rowsum = dalloc<double>(nlat);
     diagbuf = dalloc<double>(4 * nlat);
     diagout = dalloc<double>(8);
@@ -585,6 +599,20 @@ class Dycore : public DycoreBase {
     r2cDyn = make_r2c_plan<R>(an.data(), (int)an.size(), stream, M);
     AnalDesc ph = {3 * L + 1, 0, 0, 0, -1, 1.0, 0.0};
     r2cPhys = make_r2c_plan<R>(&ph, 1, stream, M);
+    if (simple()) {
+      // grid rows: Tv [0,L), q [L,2L), u [2L,3L), v [3L,4L), fixer 4L.  As in
+      // getvrtdivspec: GP gets i m/cos V (vorticity) and i m/cos U
+      // (divergence), GH gets U and -V.
+      std::vector<AnalDesc> sd_ = {
+          {L, 0, 0, 0, -1, 1.0, 0.0},
+          {L, L, L, 0, -1, 1.0, 0.0},
+          {L, 2 * L, 3 * L + 1, 1, 0, 1.0, 1.0},
+          {L, 3 * L, 2 * L + 1, 1, L, 1.0, -1.0},
+      };
+      if (c.massfix) sd_.push_back({1, 4 * L, 2 * L, 0, -1, 1.0, 0.0});
+      r2cSimple = make_r2c_plan<R>(sd_.data(), (int)sd_.size(), stream, M);
+      anaSimple = make_anal_plan(T, 2 * (4 * L + 1), stream);
+    }
   }
 
   // ------------------------------------------------------------ passes --
@@ -631,9 +659,13 @@ class Dycore : public DycoreBase {
   void dyn_pass(int stage, bool want_extra) {
     synthesis(c2rFull);
     launch_dyn_columns<R>(column_args(want_extra), false, stream);
-    if (stage == 0) {  // pdry on stage 1 (dyn_run.f90:135-153); dry runs only
+    if (stage == 0) {  // pdry on stage 1 (dyn_run.f90:135-153)
       launch_area_mean_ps<R>(psg, w, nlat, nlon, rowsum, pmean, stream);
-      launch_pdry_init(pmean, pdryini, stream);
+      const bool moist = !c.dry && nt > 0;
+      if (moist)
+        launch_area_pmoist<R>(gS + (long)sr.trc * ng, c.dcmip > 0 ? 1 : nt, L, psg, ak, bk, w, nlat, nlon, rowsum,
+                              pmoist, stream);
+      launch_pdry_init(pmean, moist ? pmoist : nullptr, pdryini, stream);
     }
     mark(PH_COL);
     launch_r2c<R>(sd, r2cDyn, gA, FPb, ldGP, FHb, ldGH, stream);
@@ -717,12 +749,60 @@ class Dycore : public DycoreBase {
     h.vfact = vfact_d;
     return h;
   }
+  SimpleArgs<R> simple_args() {
+    SimpleArgs<R> a;
+    a.L = L;
+    a.nlon = nlon;
+    a.nlat = nlat;
+    a.ak = ak;
+    a.bk = bk;
+    a.dbk = dbk;
+    a.lat = latr;
+    a.gS = gS;
+    a.s = sr;
+    a.psg = psg;
+    a.gA = gA;
+    a.precip = precip;
+    a.pwat = pwat;
+    a.apcp = apcp;
+    a.dt = (R)c.dt;
+    a.test = (c.dcmip / 10 == 4) ? 1 : 0;
+    a.turbflux = (c.dcmip == 43 || c.dcmip / 10 == 5) ? 1 : 0;
+    a.fvirt = (R)(Phys::rv / Phys::rd - 1.0);
+    a.qmin = (R)GD_FLIT(1.e-10f);
+    a.grav = (R)Phys::grav;
+    a.kappa = (R)(Phys::rd / Phys::cp);
+    return a;
+  }
+  // DCMIP simple physics on the grid, its increments analysed (scalar Tv and
+  // q, vector u, v) with the dry-mass fixer row
+  void simple_pass() {
+    launch_simple_physics<R>(simple_args(), stream);
+    if (c.massfix) {
+      launch_area_mean_ps<R>(psg, w, nlat, nlon, rowsum, pmean, stream);
+      launch_area_mean_ps<R>(pwat, w, nlat, nlon, rowsum, pwatg, stream);
+      launch_massfix_grid<R>(psg, pdryini, pmean, pwatg, Phys::grav, (int)ng, gA + (long)4 * L * ng, stream);
+    }
+    mark(PH_PHYS);
+    launch_r2c<R>(sd, r2cSimple, gA, FPb, ldGP, FHb, ldGH, stream);
+    mark(PH_FANA);
+    do_anal(false, anaSimple, FPb, ldGP, 2 * (4 * L + 1), AP, ldAP);
+    do_anal(true, anaH, FHb, ldGH, 2 * ah.ncol, AH, ldAH);
+    mark(PH_LANA);
+  }
   void phys_pass() {
     inverse_pass(false);
+    if (simple()) {
+      simple_pass();
+      launch_simple_update<R>(S, ldS, sc, L, nlm, AP, ldAP, AH, ldAH, c.massfix, (R)c.dt, (R)(1.0 / Phys::rerth),
+                              lapv, (R)Phys::rerth, stream);
+      mark(PH_PHYS);
+      return;
+    }
     if (c.heldsuarez) launch_hs_forcing<R>(hs_args(), stream);
     if (c.massfix) {
       launch_area_mean_ps<R>(psg, w, nlat, nlon, rowsum, pmean, stream);
-      launch_massfix_grid<R>(psg, pdryini, pmean, (int)ng, gA + (long)3 * L * ng, stream);
+      launch_massfix_grid<R>(psg, pdryini, pmean, nullptr, Phys::grav, (int)ng, gA + (long)3 * L * ng, stream);
     }
     mark(PH_PHYS);
     if (c.heldsuarez || c.massfix) {
@@ -927,6 +1007,39 @@ class Dycore : public DycoreBase {
   }
   void getphytend(double* dvrt, double* ddiv, double* dtv, double* dtrc, double* dlnps) override {
     if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
+    if (simple()) {  // phy_run_simple.f90:145-160 on the grid of the last getdyntend
+      launch_simple_physics<R>(simple_args(), stream);
+      launch_r2c<R>(sd, r2cSimple, gA, FPb, ldGP, FHb, ldGH, stream);
+      do_anal(false, anaSimple, FPb, ldGP, 2 * (4 * L + 1), AP, ldAP);
+      do_anal(true, anaH, FHb, ldGH, 2 * ah.ncol, AH, ldAH);
+      const R ai = (R)(1.0 / Phys::rerth);
+      // vorticity and divergence to AP columns [2L+1, 4L+1)
+      launch_combine<R>(AP, ldAP, 2 * L + 1, AH, ldAH, 0, AP, ldAP, 2 * L + 1, 2 * L, nlm, ai, stream);
+      double* tmp = dalloc<double>(2L * nlm * L);
+      const size_t n1 = 2 * (size_t)L * nlm;
+      auto out = [&](int col, double* h) {
+        if (!h) return;
+        spec_out(AP, ldAP, col, L, h, tmp);
+        for (size_t i = 0; i < n1; ++i) h[i] = h[i] / c.dt;
+      };
+      out(0, dtv);
+      out(2 * L + 1, dvrt);
+      out(3 * L + 1, ddiv);
+      if (dtrc) {
+        memset(dtrc, 0, sizeof(double) * 2 * (size_t)nt * L * nlm);
+        out(L, dtrc);
+      }
+      release(tmp);
+      if (dlnps) memset(dlnps, 0, sizeof(double) * 2 * (size_t)nlm);
+      return;
+    }
+    if (c.dcmip >= 0 || !c.heldsuarez) {  // dry DCMIP or no physics: zero tendencies
+      for (double* h : {dvrt, ddiv, dtv})
+        if (h) memset(h, 0, sizeof(double) * 2 * (size_t)L * nlm);
+      if (dtrc) memset(dtrc, 0, sizeof(double) * 2 * (size_t)nt * L * nlm);
+      if (dlnps) memset(dlnps, 0, sizeof(double) * 2 * (size_t)nlm);
+      return;
+    }
     launch_hs_forcing<R>(hs_args(), stream);
     launch_r2c<R>(sd, r2cPhys, gA, FPb, ldGP, FHb, ldGH, stream);
     do_anal(false, anaPhys, FPb, ldGP, 2 * (3 * L + 1), AP, ldAP);
@@ -1124,6 +1237,9 @@ class Dycore : public DycoreBase {
     else if (n == "dphisdx") src = dphisdx, rows = 1;
     else if (n == "dphisdy") src = dphisdy, rows = 1;
     else if (n == "sppt" && sppt) src = spptg, rows = 1;
+    else if (n == "precip") src = precip, rows = 1;
+    else if (n == "apcp") src = apcp, rows = 1;
+    else if (n == "pwat") src = pwat, rows = 1;
     if (!src || rows == 0) return GD_ERR_ARG;
     grid_out(src, rows, out);
     return GD_OK;
@@ -1153,6 +1269,7 @@ struct gd_ctx {
   gd_config cfg;
   std::string err;
   std::vector<double> topo;  // orography of the last gd_set_state (complex [nlm]), for gd_write_sig
+  std::vector<double> ak, bk;  // the vertical coordinate gd_init was given
 };
 
 static std::string g_init_error;
@@ -1210,6 +1327,7 @@ int gd_default_config(gd_config* c) {
   c->taustratdamp = 5.0 * 86400.0;
   c->pdryini = 0.0;
   c->device = 0;
+  c->dcmip = -1;
   return GD_OK;
 }
 
@@ -1228,13 +1346,18 @@ int gd_init(const gd_config* cfg, const double* ak, const double* bk, gd_ctx** o
   else if (c.ntrac < 0) why = "ntrac must be >= 0";
   else if (!(c.dt > 0)) why = "dt must be positive";
   else if (c.precision < GD_PREC_FP64 || c.precision > GD_PREC_BF16X3) why = "unknown precision";
-  else if (!c.dry && c.ntrac > 0) why = "moist mass bookkeeping (dry = 0 with tracers) is not supported";
+  else if (c.dcmip >= 0 && c.heldsuarez) why = "heldsuarez and dcmip cannot both be set";
+  else if (c.dcmip >= 0 && c.dcmip / 10 != 4 && c.dcmip / 10 != 5) why = "dcmip must be 4x or 5x (or -1)";
+  else if (c.dcmip >= 0 && !c.dry && c.ntrac < 1) why = "moist DCMIP physics needs ntrac >= 1 (humidity)";
+  else if (c.dcmip >= 0 && !c.dry && c.nlev > 128) why = "DCMIP physics supports at most 128 levels";
   if (!why.empty()) {
     g_init_error = "gd_init: " + why;
     return (why.find("not supported") != std::string::npos) ? GD_ERR_UNSUPPORTED : GD_ERR_ARG;
   }
   gd_ctx* ctx = new gd_ctx();
   ctx->cfg = c;
+  ctx->ak.assign(ak, ak + c.nlev + 1);
+  ctx->bk.assign(bk, bk + c.nlev + 1);
   try {
     if (c.precision == GD_PREC_FP64)
       ctx->d.reset(new gd::Dycore<double>(c, ak, bk));
@@ -1432,6 +1555,92 @@ int gd_write_sig(gd_ctx* ctx, const char* path, double fhour, gd_sighead* head) 
                       lnps.data(), ctx->topo.data());
   if (rc != GD_OK) ctx->err = gd_sigio_last_error();
   return rc;
+}
+
+int gd_dcmip_ics(gd_ctx* ctx, int testcase) {
+  if (!ctx || !ctx->d) return GD_ERR_ARG;
+  const gd_config& c = ctx->cfg;
+  const int tc = testcase / 10;
+  const int L = c.nlev, nt = c.ntrac, nlon = c.nlon, nlat = c.nlat;
+  const bool moist = !c.dry;
+  std::string why;
+  if (testcase < 0 || (tc != 4 && tc != 5)) why = "testcase must be 4x or 5x";
+  else if (tc == 5 && !moist) why = "the tropical cyclone case needs dry = 0";
+  else if (tc == 4 && nt < 3) why = "the baroclinic wave case writes 3 tracers (ntrac >= 3)";
+  else if (tc == 5 && nt < 1) why = "the tropical cyclone case writes humidity (ntrac >= 1)";
+  if (!why.empty()) {
+    ctx->err = "gd_dcmip_ics: " + why;
+    return GD_ERR_ARG;
+  }
+  const long ng = (long)nlon * nlat, nlm = (long)(c.ntrunc + 1) * (c.ntrunc + 2) / 2;
+  const double fv = gd::Phys::rv / gd::Phys::rd - 1.0, kap = gd::Phys::rd / gd::Phys::cp;
+  std::vector<double> lats(nlat);
+  int rc = gd_grid_info(ctx, lats.data(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+  if (rc != GD_OK) return rc;
+  auto LON = [&](long p) { return 2.0 * 3.14159265358979323846 * (double)(p % nlon) / nlon; };
+  auto LAT = [&](long p) { return lats[p / nlon]; };
+  // calc_pressdata (pressure_data.f90:58-100) on the host: prs [L][ng] bottom to top
+  std::vector<double> prs((size_t)L * ng);
+  auto pressdata = [&](const std::vector<double>& lnpsg) {
+    for (long p = 0; p < ng; ++p) {
+      const double ps = std::exp(lnpsg[p]);
+      for (int k = 0; k < L; ++k) {
+        const double pu = ctx->ak[k] + ctx->bk[k] * ps, pl = ctx->ak[k + 1] + ctx->bk[k + 1] * ps;
+        prs[(size_t)(L - 1 - k) * ng + p] =
+            std::pow((std::pow(pl, kap) * pl - std::pow(pu, kap) * pu) / ((kap + 1.) * (pl - pu)), 1. / kap);
+      }
+    }
+  };
+  std::vector<double> psg(ng), lnpsg(ng);
+  if (tc == 4) {
+    std::fill(psg.begin(), psg.end(), 1.e5);
+  } else {  // a first pass only for ps (dyn_init.f90:359-373)
+    for (long p = 0; p < ng; ++p) lnpsg[p] = std::log(1.015e5);
+    pressdata(lnpsg);
+    for (long p = 0; p < ng; ++p) psg[p] = gd::dcmip::test5(LON(p), LAT(p), prs[p]).ps;
+  }
+  for (long p = 0; p < ng; ++p) lnpsg[p] = std::log(psg[p]);
+  pressdata(lnpsg);
+  std::vector<double> ug((size_t)L * ng), vg(ug.size()), tvg(ug.size()), trcg((size_t)nt * L * ng, 0.0), phis(ng);
+  for (int k = 0; k < L; ++k)
+    for (long p = 0; p < ng; ++p) {
+      const size_t o = (size_t)k * ng + p;
+      double t, q;
+      if (tc == 4) {
+        const gd::dcmip::Point4 r = gd::dcmip::test4(moist, LON(p), LAT(p), prs[o]);
+        ug[o] = r.u, vg[o] = r.v, t = r.t, q = r.q, phis[p] = r.phis;
+        trcg[(size_t)(1 * L + k) * ng + p] = r.q1;
+        trcg[(size_t)(2 * L + k) * ng + p] = r.q2;
+      } else {
+        const gd::dcmip::Point5 r = gd::dcmip::test5(LON(p), LAT(p), prs[o]);
+        ug[o] = r.u, vg[o] = r.v, t = r.t, q = r.q, phis[p] = r.phis;
+      }
+      tvg[o] = moist ? t * (1. + fv * q) : t;
+      trcg[o] = moist ? q : 0.0;  // tracer 1
+    }
+  std::vector<double> vrt(2 * (size_t)L * nlm), div(vrt.size()), tv(vrt.size()), trc(2 * (size_t)nt * L * nlm),
+      lnps(2 * (size_t)nlm), topo(2 * (size_t)nlm);
+  for (long p = 0; p < ng; ++p) phis[p] = phis[p] / gd::Phys::grav;
+  if ((rc = gd_getvrtdivspec(ctx, L, ug.data(), vg.data(), vrt.data(), div.data())) != GD_OK) return rc;
+  if ((rc = gd_grdtospec(ctx, L, tvg.data(), tv.data())) != GD_OK) return rc;
+  if (nt > 0 && (rc = gd_grdtospec(ctx, nt * L, trcg.data(), trc.data())) != GD_OK) return rc;
+  if ((rc = gd_grdtospec(ctx, 1, lnpsg.data(), lnps.data())) != GD_OK) return rc;
+  if ((rc = gd_grdtospec(ctx, 1, phis.data(), topo.data())) != GD_OK) return rc;
+  return gd_set_state(ctx, vrt.data(), div.data(), tv.data(), nt ? trc.data() : nullptr, lnps.data(), topo.data());
+}
+
+int gd_dcmip_point(int testcase, int moist, double lon, double lat, double p, double* out) {
+  if (!out || testcase < 0 || (testcase / 10 != 4 && testcase / 10 != 5)) return GD_ERR_ARG;
+  if (testcase / 10 == 4) {
+    const gd::dcmip::Point4 r = gd::dcmip::test4(moist != 0, lon, lat, p);
+    const double v[8] = {r.u, r.v, r.t, r.phis, r.ps, r.q, r.q1, r.q2};
+    memcpy(out, v, sizeof(v));
+  } else {
+    const gd::dcmip::Point5 r = gd::dcmip::test5(lon, lat, p);
+    const double v[8] = {r.u, r.v, r.t, r.phis, r.ps, r.q, 0.0, 0.0};
+    memcpy(out, v, sizeof(v));
+  }
+  return GD_OK;
 }
 
 int gd_set_stream(gd_ctx* ctx, void* stream) {

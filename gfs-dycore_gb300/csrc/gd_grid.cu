@@ -448,29 +448,33 @@ void launch_area_mean_ps(const R* psg, const double* w, int nlat, int nlon, doub
 template void launch_area_mean_ps<double>(const double*, const double*, int, int, double*, double*, cudaStream_t);
 template void launch_area_mean_ps<float>(const float*, const double*, int, int, double*, double*, cudaStream_t);
 
-__global__ void k_pdry_init(const double* pmean, double* pdryini) {
-  if (threadIdx.x == 0 && *pdryini == 0.0) *pdryini = *pmean;
+__global__ void k_pdry_init(const double* pmean, const double* pmoist, double* pdryini) {
+  if (threadIdx.x == 0 && *pdryini == 0.0) *pdryini = *pmean - (pmoist ? *pmoist : 0.0);
 }
-void launch_pdry_init(const double* pmean, double* pdryini, cudaStream_t s) {
-  k_pdry_init<<<1, 32, 0, s>>>(pmean, pdryini);
+void launch_pdry_init(const double* pmean, const double* pmoist, double* pdryini, cudaStream_t s) {
+  k_pdry_init<<<1, 32, 0, s>>>(pmean, pmoist, pdryini);
   count_launch();
   GD_LAUNCH_CHECK();
 }
 
 template <typename R>
-__global__ void k_massfix_grid(const R* psg, const double* pdryini, const double* pmean, long ng, R* out) {
-  const R pcorr = (R)(*pdryini / *pmean);
+__global__ void k_massfix_grid(const R* psg, const double* pdryini, const double* pmean, const double* pwatg,
+                               double grav, long ng, R* out) {
+  const R pcorr = (R)((*pdryini + grav * (pwatg ? *pwatg : 0.0)) / *pmean);
   for (long p = (long)blockIdx.x * blockDim.x + threadIdx.x; p < ng; p += (long)gridDim.x * blockDim.x)
     out[p] = log(psg[p] * pcorr);
 }
 template <typename R>
-void launch_massfix_grid(const R* psg, const double* pdryini, const double* pmean, int ng, R* out, cudaStream_t s) {
-  k_massfix_grid<R><<<ceil_div(ng, 256), 256, 0, s>>>(psg, pdryini, pmean, ng, out);
+void launch_massfix_grid(const R* psg, const double* pdryini, const double* pmean, const double* pwatg, double grav,
+                         int ng, R* out, cudaStream_t s) {
+  k_massfix_grid<R><<<ceil_div(ng, 256), 256, 0, s>>>(psg, pdryini, pmean, pwatg, grav, ng, out);
   count_launch();
   GD_LAUNCH_CHECK();
 }
-template void launch_massfix_grid<double>(const double*, const double*, const double*, int, double*, cudaStream_t);
-template void launch_massfix_grid<float>(const float*, const double*, const double*, int, float*, cudaStream_t);
+template void launch_massfix_grid<double>(const double*, const double*, const double*, const double*, double, int,
+                                          double*, cudaStream_t);
+template void launch_massfix_grid<float>(const float*, const double*, const double*, const double*, double, int,
+                                         float*, cudaStream_t);
 
 // per latitude: max wind speed over levels, min/max ps, area-weighted sum of
 // (36 ps dlnps/dt)^2

@@ -64,10 +64,15 @@ template <typename R>
 void launch_area_mean_ps(const R* psg, const double* w, int nlat, int nlon, double* rowsum, double* out,
                          cudaStream_t s);
 // pdry on stage 1: sets *pdryini if it is 0 (dyn_run.f90:135-153)
-void launch_pdry_init(const double* pmean, double* pdryini, cudaStream_t s);
+// pdryini = pmean - pmoist when pdryini is 0 (dyn_run.f90:146-150); pmoist
+// may be null (dry runs)
+void launch_pdry_init(const double* pmean, const double* pmoist, double* pdryini, cudaStream_t s);
 // grid row log(ps*pcorr), pcorr = pdryini / pmean (dyn_run.f90:626-631)
 template <typename R>
-void launch_massfix_grid(const R* psg, const double* pdryini, const double* pmean, int ng, R* out, cudaStream_t s);
+// log(ps pcorr), pcorr = (pdryini + grav pwatg) / pmean (dyn_run.f90:621-631);
+// pwatg may be null (no precipitable water)
+void launch_massfix_grid(const R* psg, const double* pdryini, const double* pmean, const double* pwatg, double grav,
+                         int ng, R* out, cudaStream_t s);
 // diagnostics of run.f90:159-161 -> out[0..3]
 template <typename R>
 void launch_diag(const R* u, const R* v, int L, const R* psg, const R* dlnpsdt, const double* w, int nlat, int nlon,

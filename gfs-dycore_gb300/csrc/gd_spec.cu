@@ -416,6 +416,70 @@ template void launch_phys_update<float>(float*, long, const SpecCols&, int, int,
                                         float, const float*, float, cudaStream_t);
 
 template <typename R>
+__global__ void k_simple_update(R* S, long ldS, SpecCols sc, int L, int nlm, const R* AP, long ldAP, const R* AH,
+                                long ldAH, int massfix, R dt, R ainv, const R* lapv, R rerth) {
+  typedef typename C2<R>::T V;
+  const long total = (long)nlm * (L + 1);
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const long idx = e / (L + 1);
+    const int k = (int)(e - idx * (L + 1));
+    if (k == L) {  // ln(ps): dry-mass fixer (dyn_run.f90:633, run.f90:538)
+      if (massfix) {
+        V ln = ld2(S, idx, ldS, sc.lnps);
+        V ws = ld2(AP, idx, ldAP, 2 * L);
+        V d;
+        d.x = (ws.x - ln.x) / dt;
+        d.y = (ws.y - ln.y) / dt;
+        ln.x = ln.x + dt * d.x;
+        ln.y = ln.y + dt * d.y;
+        st2(S, idx, ldS, sc.lnps, ln);
+      }
+      continue;
+    }
+    const R lap = lapv[idx];
+    const R il = (idx == 0) ? R(0) : R(1) / lap;
+    V tv = ld2(S, idx, ldS, sc.tv + k), q = ld2(S, idx, ldS, sc.trc + k);
+    V vr = ld2(S, idx, ldS, sc.vrt + k), dv = ld2(S, idx, ldS, sc.div + k);
+    const V at = ld2(AP, idx, ldAP, k), aq = ld2(AP, idx, ldAP, L + k);
+    const V pv = ld2(AP, idx, ldAP, 2 * L + 1 + k), pd = ld2(AP, idx, ldAP, 3 * L + 1 + k);
+    const V hv = ld2(AH, idx, ldAH, k), hd = ld2(AH, idx, ldAH, L + k);
+    tv.x += dt * (at.x / dt);
+    tv.y += dt * (at.y / dt);
+    q.x += dt * (aq.x / dt);
+    q.y += dt * (aq.y / dt);
+    vr.x += dt * ((pv.x + hv.x) * ainv / dt);
+    vr.y += dt * ((pv.y + hv.y) * ainv / dt);
+    dv.x += dt * ((pd.x + hd.x) * ainv / dt);
+    dv.y += dt * ((pd.y + hd.y) * ainv / dt);
+    st2(S, idx, ldS, sc.tv + k, tv);
+    st2(S, idx, ldS, sc.trc + k, q);
+    st2(S, idx, ldS, sc.vrt + k, vr);
+    st2(S, idx, ldS, sc.div + k, dv);
+    V s_, c_;
+    s_.x = rerth * il * vr.x;
+    s_.y = rerth * il * vr.y;
+    c_.x = rerth * il * dv.x;
+    c_.y = rerth * il * dv.y;
+    st2(S, idx, ldS, sc.s + k, s_);
+    st2(S, idx, ldS, sc.c + k, c_);
+  }
+}
+template <typename R>
+void launch_simple_update(R* S, long ldS, const SpecCols& sc, int L, int nlm, const R* AP, long ldAP, const R* AH,
+                          long ldAH, int massfix, R dt, R ainv, const R* lapv, R rerth, cudaStream_t s) {
+  long total = (long)nlm * (L + 1);
+  k_simple_update<R><<<std::min(ceil_div(total, 256), 8192), 256, 0, s>>>(S, ldS, sc, L, nlm, AP, ldAP, AH, ldAH,
+                                                                         massfix, dt, ainv, lapv, rerth);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template void launch_simple_update<double>(double*, long, const SpecCols&, int, int, const double*, long,
+                                           const double*, long, int, double, double, const double*, double,
+                                           cudaStream_t);
+template void launch_simple_update<float>(float*, long, const SpecCols&, int, int, const float*, long, const float*,
+                                          long, int, float, float, const float*, float, cudaStream_t);
+
+template <typename R>
 __global__ void k_sc(R* S, long ldS, SpecCols sc, int L, int nlm, const R* lapv, R rerth) {
   typedef typename C2<R>::T V;
   const long total = (long)nlm * L;

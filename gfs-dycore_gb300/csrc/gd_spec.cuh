@@ -69,6 +69,17 @@ template <typename R>
 void launch_phys_update(R* S, long ldS, const SpecCols& sc, int L, int nt, int nlm, const R* AP, long ldAP,
                         int massfix, int heldsuarez, R dt, const R* lapv, R rerth, cudaStream_t s);
 
+// Physics adjustment for the DCMIP simple physics (phy_run_simple.f90:145-160
+// then run.f90:526-538): analyses of the grid increments in AP columns [0,L)
+// Tv, [L,2L) q, 2L dry-mass fixer, [2L+1,3L+1) and [3L+1,4L+1) the
+// i m/cos parts of vorticity and divergence, AH columns [0,L) and [L,2L)
+// their d/dphi parts; tendency = analysis / dt (vorticity, divergence scaled
+// by 1/a), state += dt * tendency for Tv, tracer 1, vorticity, divergence;
+// lnps from the fixer (or unchanged); recomputes s, c.
+template <typename R>
+void launch_simple_update(R* S, long ldS, const SpecCols& sc, int L, int nlm, const R* AP, long ldAP, const R* AH,
+                          long ldAH, int massfix, R dt, R ainv, const R* lapv, R rerth, cudaStream_t s);
+
 // s = a invlap vrt, c = a invlap div for all coefficients.
 template <typename R>
 void launch_sc(R* S, long ldS, const SpecCols& sc, int L, int nlm, const R* lapv, R rerth, cudaStream_t s);

@@ -38,7 +38,8 @@ API_FUNCTIONS = [
     "gd_pattern_set", "gd_pattern_spectra", "gd_pattern_destroy", "gd_pattern_set_stream", "gd_pattern_sync",
     "gd_pattern_launch_count", "gd_pattern_last_error", "gd_set_sppt", "gd_ensemble_advance",
     "gd_sigio_head_init", "gd_sigio_read_head", "gd_sigio_read", "gd_sigio_write", "gd_sigio_config",
-    "gd_read_sig", "gd_write_sig", "gd_sigio_last_error",
+    "gd_read_sig", "gd_write_sig", "gd_sigio_last_error", "gd_dcmip_ics",
+    "gd_dcmip_point",
 ]
 PHASES = ["legendre_synth", "fft_synth", "columns", "fft_anal", "legendre_anal", "semi_implicit",
           "physics", "other"]
@@ -53,6 +54,7 @@ class GdConfig(ctypes.Structure):
         ("ndiss", ctypes.c_int), ("efold", ctypes.c_double), ("hdif_fac", ctypes.c_double),
         ("hdif_fac2", ctypes.c_double), ("fshk", ctypes.c_double),
         ("taustratdamp", ctypes.c_double), ("pdryini", ctypes.c_double), ("device", ctypes.c_int),
+        ("dcmip", ctypes.c_int),
     ]
 
 
@@ -114,6 +116,8 @@ def load(build_if_missing=True):
     L.gd_write_sig.argtypes = [vp, cp, d, vp]
     L.gd_sigio_last_error.restype = ctypes.c_char_p
     L.gd_sigio_last_error.argtypes = []
+    L.gd_dcmip_ics.argtypes = [vp, i]
+    L.gd_dcmip_point.argtypes = [i, i, d, d, d, vp]
     _lib = L
     return L
 
@@ -130,6 +134,15 @@ def default_config(**kw):
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def dcmip_point(testcase, lon, lat, p, moist=True):
+    """gd_dcmip_point: (u, v, T, phis, ps, q, q1, q2) of a DCMIP-2012 case at one point."""
+    out = np.zeros(8)
+    rc = load().gd_dcmip_point(int(testcase), int(moist), float(lon), float(lat), float(p), _p(out))
+    if rc != GD_OK:
+        raise GdError(rc, "gd_dcmip_point: bad arguments")
+    return out
 
 
 class Dycore:
@@ -184,6 +197,10 @@ class Dycore:
         self._chk(load().gd_get_state(self.h, _p(vrt), _p(div), _p(tv), _p(trc), _p(lnps)))
         return dict(vrt=vrt, div=div, tv=tv, trc=trc[: self.ntrac], lnps=lnps)
 
+    def dcmip_ics(self, testcase):
+        """DCMIP-2012 test 4x (baroclinic wave) or 5x (tropical cyclone) initial state (gd_dcmip_ics)."""
+        self._chk(load().gd_dcmip_ics(self.h, int(testcase)))
+
     def read_sig(self, path):
         """readin_sig + init_dyn's ln(ps) conversion (gd_read_sig); returns the header."""
         from . import sigio
@@ -209,8 +226,11 @@ class Dycore:
     def getphytend(self):
         L, n = self.nlev, self.nlm
         d = [np.zeros((L, n), np.complex128) for _ in range(3)]
-        self._chk(load().gd_getphytend(self.h, _p(d[0]), _p(d[1]), _p(d[2]), None, None))
-        return dict(dvrt=d[0], ddiv=d[1], dtv=d[2])
+        dtrc = np.zeros((max(self.ntrac, 1), L, n), np.complex128)
+        dl = np.zeros(n, np.complex128)
+        self._chk(load().gd_getphytend(self.h, _p(d[0]), _p(d[1]), _p(d[2]), _p(dtrc) if self.ntrac else None,
+                                       _p(dl)))
+        return dict(dvrt=d[0], ddiv=d[1], dtv=d[2], dtrc=dtrc[: self.ntrac], dlnps=dl)
 
     def set_sppt(self, pattern, sigtop=0.05, sigbot=0.10):
         """Attach a Pattern as stochastically perturbed physics (None detaches)."""
@@ -283,7 +303,8 @@ class Dycore:
     def get_grid(self, name):
         L = self.nlev
         rows = dict(ug=L, vg=L, vrtg=L, divg=L, tvg=L, dlnpdtg=L, prs=L, etadot=L + 1,
-                    trcg=max(self.ntrac, 1) * L, lnpsg=1, psg=1, dlnpsdt=1, dphisdx=1, dphisdy=1, sppt=1)
+                    trcg=max(self.ntrac, 1) * L, lnpsg=1, psg=1, dlnpsdt=1, dphisdx=1, dphisdy=1, sppt=1,
+                    precip=1, apcp=1, pwat=1)
         out = np.zeros((rows[name], self.nlat, self.nlon))
         self._chk(load().gd_get_grid(self.h, name.encode(), _p(out)))
         return out

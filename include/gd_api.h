@@ -63,6 +63,11 @@ typedef struct gd_config {
   double hdif_fac, hdif_fac2, fshk, taustratdamp; /* params.f90:76-86      */
   double pdryini;      /* 0 -> set on the first stage-1 call               */
   int device;          /* CUDA device ordinal                               */
+  int dcmip;           /* params.f90:62 dcmip: -1 none; 4x or 5x selects the
+                          DCMIP simple physics plugin (phy_run_simple.f90;
+                          moist unless dry, turbulent fluxes for 43 and 5x,
+                          latitude-dependent SST for 4x) -- not together
+                          with heldsuarez                                 */
 } gd_config;
 
 typedef struct gd_ctx gd_ctx;
@@ -130,9 +135,11 @@ int gd_grid_info(gd_ctx* ctx, double* lats, double* gauwts, double* areawts, int
                  int* order, double* lap, double* invlap);
 
 /* Grid fields of the last getdyntend: "ug" "vg" "vrtg" "divg" "tvg" "trcg"
-   "dlnpdtg" "etadot" "lnpsg" "psg" "dlnpsdt" "prs" "dphisdx" "dphisdy", and "sppt"
+   "dlnpdtg" "etadot" "lnpsg" "psg" "dlnpsdt" "prs" "dphisdx" "dphisdy", "sppt"
    (the logit-transformed stochastic-physics pattern of the last step, while
-   one is attached). */
+   one is attached), and the physics fields of phy_data.f90 "precip" (mm/s),
+   "apcp" (mm, accumulated), "pwat" (kg/m^2) -- zero but for the moist
+   DCMIP physics. */
 int gd_get_grid(gd_ctx* ctx, const char* name, double* out);
 
 /* Step diagnostics of src/run.f90:159-161 after the last step:
@@ -229,6 +236,21 @@ int gd_set_sppt(gd_ctx* ctx, gd_pattern* pattern, double sigtop, double sigbot);
    returns when all are done.  No counterpart in the reference, which runs one
    member per process. */
 int gd_ensemble_advance(gd_ctx** ctxs, int n, double t, int nsteps);
+
+/* DCMIP-2012 initial state (dcmip_ics, src/dyn_init.f90:330-416) on ctx's grid:
+   testcase 4x the baroclinic wave (src/dcmip_initial_conditions_test_4_v3.f90;
+   ps = 1e5 Pa; tracers 2 and 3 potential temperature and |Ertel PV|;
+   humidity in tracer 1 unless dry), 5x the tropical cyclone
+   (src/dcmip_initial_conditions_test_5_v1.f90; moist only).  The point
+   values are evaluated on the host at the model's layer pressures (its ak,
+   bk and the case's ps), Tv = T (1 + fvirt q), and transformed with ctx's
+   own transforms (winds through gd_getvrtdivspec, orography phis/g) into
+   the state, as gd_set_state.  Needs ntrac >= 3 for 4x, >= 1 for 5x. */
+int gd_dcmip_ics(gd_ctx* ctx, int testcase);
+/* The analytic state of gd_dcmip_ics at one point, host only (no context):
+   out[8] = u, v, T, phis, ps, q, q1, q2 (q1, q2 zero for 5x) at longitude,
+   latitude (radians) and pressure p (Pa); moist as for test 4. */
+int gd_dcmip_point(int testcase, int moist, double lon, double lat, double p, double* out);
 
 /* ---- sigma files (src/sigio_module.f90) ----------------------------------
    The GFS spectral "sigma" file: big-endian Fortran unformatted sequential

@@ -37,6 +37,7 @@ const double RV = FLIT(4.6150e+2f);
 const double CP = FLIT(1.0046e+3f);
 const double CVAP = FLIT(1.8460e+3f);
 const double KAPPA = RD / CP;  // con_rocp, evaluated in r_kind
+const double FVIRT = RV / RD - 1.;  // con_fvirt
 
 // src/semimp_data.f90:74-88 (Lorenz 3-cycle + trapezoidal IMEX tableau)
 const double A21 = FLIT(1.f / 3.f), A31 = FLIT(1.f / 6.f), A32 = FLIT(1.f / 2.f);
@@ -451,6 +452,132 @@ void ora_pattern_get(void* h, double* out);
 int ora_pattern_jcap(void* h);
 }
 
+// x**n for an integer n, as Fortran evaluates an integer power
+double ipow(double x, int n) {
+  double r = 1.0;
+  for (int i = 0; i < n; ++i) r *= x;
+  return r;
+}
+
+// DCMIP simple physics for one column (src/simple_physics_v5_1.f90:1-462,
+// Reed and Jablonowski 2012): large-scale condensation, then with turbflux
+// the implicit surface fluxes of momentum, heat and moisture at the lowest
+// level and the implicit boundary-layer diffusion (a tridiagonal solve per
+// variable, eliminated bottom up and substituted top down).  Arrays are top
+// (0) to bottom (n-1); pint has n+1 interfaces.  All arithmetic in double,
+// the constants are the routine's own.  w holds 12 (n+1) scratch values.
+void simple_column(int n, double dtime, double lat, double* t, double* q, double* u, double* v, const double* pmid,
+                   const double* pint, const double* pdel, const double* rpdel, double ps, double* precl, int test,
+                   bool turbflux, double* w) {
+  const double gravit = 9.80616, rair = 287.0, cpair = 1.0045e3, latvap = 2.5e6, rh2o = 461.5;
+  const double epsilo = rair / rh2o, zvir = (rh2o / rair) - 1.0, a = 6371220.0, omega = 7.29212e-5;
+  const double pi = 4.0 * atan(1.0);
+  const double C = 0.0011, SST_tc = 302.15, T0 = 273.16, e0 = 610.78, rhow = 1000.0;
+  const double Cd0 = 0.0007, Cd1 = 0.000065, Cm = 0.002, v20 = 20.0, p0 = 100000.0;
+  const double pbltop = 85000., pblconst = 10000., T00 = 288.0, u0 = 35.0, latw = 2.0 * pi / 9.0;
+  const double eta0 = 0.252, etav = (1. - eta0) * 0.5 * pi;
+  const double q0 = (double)0.021f;  // a literal without a kind suffix
+  const double rk = rair / cpair;
+  const int nb = n - 1;  // the lowest level
+  // height of the lowest level (from the state before any update)
+  const double dlnpint = log(ps) - log(pint[nb]);
+  const double za = rair / gravit * t[nb] * (1. + zvir * q[nb]) * 0.5 * dlnpint;
+  double Tsurf;
+  if (test == 1) {
+    const double sl = sin(lat), cl = cos(lat);
+    Tsurf = (T00 + pi * u0 / rair * 1.5 * sin(etav) * pow(cos(etav), 0.5) *
+                       ((-2. * ipow(sl, 6) * (cl * cl + 1. / 3.) + 10. / 63.) * u0 * pow(cos(etav), 1.5) +
+                        (8. / 5. * ipow(cl, 3) * (sl * sl + 2. / 3.) - pi / 4.) * a * omega * 0.5)) /
+            (1. + zvir * q0 * exp(-ipow(lat / latw, 4)));
+  } else {
+    Tsurf = SST_tc;
+  }
+  // large-scale condensation
+  *precl = 0.0;
+  for (int k = 0; k < n; ++k) {
+    const double qsat = epsilo * e0 / pmid[k] * exp(-latvap / rh2o * ((1. / t[k]) - 1. / T0));
+    if (q[k] > qsat) {
+      const double tmp =
+          1. / dtime * (q[k] - qsat) / (1. + (latvap / cpair) * (epsilo * latvap * qsat / (rair * (t[k] * t[k]))));
+      t[k] = t[k] + (latvap / cpair * tmp) * dtime;
+      q[k] = q[k] + (-tmp) * dtime;
+      *precl = *precl + tmp * pdel[k] / (gravit * rhow);
+    }
+  }
+  if (!turbflux) return;
+  double* Km = w;
+  double* Ke = w + (n + 1);
+  double* CA = w + 2 * (n + 1);
+  double* CC = w + 3 * (n + 1);
+  double* CAm = w + 4 * (n + 1);
+  double* CCm = w + 5 * (n + 1);
+  double* CE = w + 6 * (n + 1);
+  double* CEm = w + 7 * (n + 1);
+  double* CF = w + 8 * (n + 1);  // CFu, CFv, CFt, CFq interleaved by 4 (n+1 rows)
+  const double wind = sqrt(u[nb] * u[nb] + v[nb] * v[nb]);
+  double Cd;
+  Ke[n] = C * wind * za;
+  if (wind < v20) {
+    Cd = Cd0 + Cd1 * wind;
+    Km[n] = Cd * wind * za;
+  } else {
+    Cd = Cm;
+    Km[n] = Cm * wind * za;
+  }
+  for (int k = 0; k < n; ++k) {
+    if (pint[k] >= pbltop) {
+      Km[k] = Km[n];
+      Ke[k] = Ke[n];
+    } else {
+      const double x = pbltop - pint[k];
+      Km[k] = Km[n] * exp(-(x * x) / (pblconst * pblconst));
+      Ke[k] = Ke[n] * exp(-(x * x) / (pblconst * pblconst));
+    }
+  }
+  // surface fluxes, implicit in the lowest level
+  const double qsats = epsilo * e0 / ps * exp(-latvap / rh2o * ((1. / Tsurf) - 1. / T0));
+  u[nb] = u[nb] / (1. + Cd * wind * dtime / za);
+  v[nb] = v[nb] / (1. + Cd * wind * dtime / za);
+  t[nb] = (t[nb] + C * wind * Tsurf * dtime / za) / (1. + C * wind * dtime / za);
+  q[nb] = (q[nb] + C * wind * qsats * dtime / za) / (1. + C * wind * dtime / za);
+  // boundary-layer diffusion
+  for (int k = 0; k < n - 1; ++k) {
+    const double rho = (pint[k + 1] / (rair * (t[k + 1] + t[k]) / 2.0));
+    const double dpm = pmid[k + 1] - pmid[k];
+    CAm[k] = rpdel[k] * dtime * gravit * gravit * Km[k + 1] * rho * rho / dpm;
+    CCm[k + 1] = rpdel[k + 1] * dtime * gravit * gravit * Km[k + 1] * rho * rho / dpm;
+    CA[k] = rpdel[k] * dtime * gravit * gravit * Ke[k + 1] * rho * rho / dpm;
+    CC[k + 1] = rpdel[k + 1] * dtime * gravit * gravit * Ke[k + 1] * rho * rho / dpm;
+  }
+  CAm[n - 1] = 0.;
+  CCm[0] = 0.;
+  CEm[n] = 0.;
+  CA[n - 1] = 0.;
+  CC[0] = 0.;
+  CE[n] = 0.;
+  for (int i = 0; i < 4; ++i) CF[4 * n + i] = 0.;
+  for (int k = n - 1; k >= 0; --k) {
+    const double de = 1. + CA[k] + CC[k] - CA[k] * CE[k + 1];
+    const double dm = 1. + CAm[k] + CCm[k] - CAm[k] * CEm[k + 1];
+    CE[k] = CC[k] / de;
+    CEm[k] = CCm[k] / dm;
+    CF[4 * k + 0] = (u[k] + CAm[k] * CF[4 * (k + 1) + 0]) / dm;
+    CF[4 * k + 1] = (v[k] + CAm[k] * CF[4 * (k + 1) + 1]) / dm;
+    CF[4 * k + 2] = (pow(p0 / pmid[k], rk) * t[k] + CA[k] * CF[4 * (k + 1) + 2]) / de;
+    CF[4 * k + 3] = (q[k] + CA[k] * CF[4 * (k + 1) + 3]) / de;
+  }
+  u[0] = CF[0];
+  v[0] = CF[1];
+  t[0] = CF[2] * pow(pmid[0] / p0, rk);
+  q[0] = CF[3];
+  for (int k = 1; k < n; ++k) {
+    u[k] = CEm[k] * u[k - 1] + CF[4 * k + 0];
+    v[k] = CEm[k] * v[k - 1] + CF[4 * k + 1];
+    t[k] = (CE[k] * t[k - 1] * pow(p0 / pmid[k - 1], rk) + CF[4 * k + 2]) * pow(pmid[k] / p0, rk);
+    q[k] = CE[k] * q[k - 1] + CF[4 * k + 3];
+  }
+}
+
 struct Dycore {
   ora_config c;
   Sht sh;
@@ -472,6 +599,9 @@ struct Dycore {
   std::vector<double> disspec, diff_prof, dmp_prof;
   std::vector<double> lapv, invlapv;
   std::vector<int> degree, order;
+  // phy_data.f90: instantaneous precipitation (mm/s), accumulated (mm),
+  // precipitable water (kg/m^2)
+  std::vector<double> precip, apcp, pwat;
 
   long G(int k) const { return (long)k * ng; }
 
@@ -499,6 +629,7 @@ struct Dycore {
     etadot.assign((long)(L + 1) * ng, 0);
     lnpsg.assign(ng, 0);
     psg = dlnpsdt = phis = dphisdx = dphisdy = dlnpsdx = dlnpsdy = lnpsg;
+    precip = apcp = pwat = lnpsg;
     ak.assign(ak_, ak_ + L + 1);
     bk.assign(bk_, bk_ + L + 1);
     dbk.resize(L);
@@ -773,8 +904,9 @@ struct Dycore {
     if (rkstage == 1) {  // dyn_run.f90:135-153
       double pmoist = 0;
       if (!c.dry) {
+        const int ntuse = c.dcmip > 0 ? 1 : nt;
         for (int k = 0; k < L; ++k)
-          for (int q = 0; q < nt; ++q)
+          for (int q = 0; q < ntuse; ++q)
             for (long p = 0; p < ng; ++p)
               pmoist += areawt(p) * dpk[G(L - 1 - k) + p] * trcg[((long)q * L + k) * ng + p];
       }
@@ -898,8 +1030,93 @@ struct Dycore {
     for (long p = 0; p < ng; ++p) spptg[p] = 2.0 / (1.0 + exp(spptg[p])) - 1.0;
   }
 
-  // phy_run_hs.f90:22-84
+  // The physics plugin of the build: Held-Suarez (phy_run_hs.f90) or DCMIP
+  // simple physics (phy_run_simple.f90); none gives zero tendencies.
   void getphytend(cplx* dvrt, cplx* ddiv, cplx* dtv, cplx* dtrc, cplx* dlnps) {
+    if (c.heldsuarez) {
+      getphytend_hs(dvrt, ddiv, dtv, dtrc, dlnps);
+    } else if (c.dcmip >= 0 && !c.dry) {
+      getphytend_simple(dvrt, ddiv, dtv, dtrc, dlnps, c.dt);
+    } else {  // phy_run_simple.f90:178-191 (dry), or no physics
+      const long NS = (long)L * nlm;
+      std::fill(dvrt, dvrt + NS, cplx(0));
+      std::fill(ddiv, ddiv + NS, cplx(0));
+      std::fill(dtv, dtv + NS, cplx(0));
+      std::fill(dtrc, dtrc + (long)nt * NS, cplx(0));
+      std::fill(dlnps, dlnps + nlm, cplx(0));
+      std::fill(precip.begin(), precip.end(), 0.0);
+      std::fill(apcp.begin(), apcp.end(), 0.0);
+      std::fill(pwat.begin(), pwat.end(), 0.0);
+    }
+  }
+
+  // phy_run_simple.f90:26-176: per column, the state (Tv to T with humidity
+  // clipped at qmin, levels flipped to top-down) through simple_column,
+  // back to Tv; grid increments to spectral tendencies (/dtx); precip, pwat,
+  // apcp.  dcmip 4x uses the latitude-dependent SST (test 1), 5x the
+  // constant one; turbulent fluxes for 43 and 5x.
+  void getphytend_simple(cplx* dvrt, cplx* ddiv, cplx* dtv, cplx* dtrc, cplx* dlnps, double dtx) {
+    const int test = (c.dcmip / 10 == 4) ? 1 : 0;
+    const bool turbflux = (c.dcmip == 43 || c.dcmip / 10 == 5);
+    const double qmin = FLIT(1.e-10f);
+    std::vector<double> dtdt((long)L * ng), dudt((long)L * ng), dvdt((long)L * ng), dqdt((long)L * ng);
+#pragma omp parallel
+    {
+      std::vector<double> gt(L), gq(L), gu(L), gv(L), prsl(L), prsi(L + 1), delp(L), rdelp(L), w(12 * (L + 1));
+#pragma omp for schedule(dynamic, 64)
+      for (long p = 0; p < ng; ++p) {
+        for (int k = 0; k < L; ++k) {  // bottom-up k, top-down L-1-k
+          const long o = G(k) + p;
+          const double qq = trcg[o];
+          gq[L - 1 - k] = qq;
+          gu[L - 1 - k] = ug[o];
+          gv[L - 1 - k] = vg[o];
+          gt[L - 1 - k] = tvg[o] / (1. + FVIRT * std::max(qmin, qq));
+          prsl[L - 1 - k] = prs[o];
+        }
+        for (int t = 0; t <= L; ++t) prsi[t] = pk[(long)t * ng + p];
+        for (int t = 0; t < L; ++t) {
+          delp[t] = prsi[t + 1] - prsi[t];
+          rdelp[t] = 1. / delp[t];
+        }
+        double precl = 0;
+        simple_column(L, dtx, sh.lat[p / nlon], gt.data(), gq.data(), gu.data(), gv.data(), prsl.data(), prsi.data(),
+                      delp.data(), rdelp.data(), psg[p], &precl, test, turbflux, w.data());
+        precip[p] = precl * 1000.;
+        for (int t = 0; t < L; ++t) gt[t] = gt[t] * (1. + FVIRT * std::max(qmin, gq[t]));
+        double pw = 0;
+        for (int k = 0; k < L; ++k) {
+          const long o = G(k) + p;
+          dtdt[o] = gt[L - 1 - k] - tvg[o];
+          dqdt[o] = gq[L - 1 - k] - trcg[o];
+          dudt[o] = gu[L - 1 - k] - ug[o];
+          dvdt[o] = gv[L - 1 - k] - vg[o];
+          pw += dpk[G(L - 1 - k) + p] * (dqdt[o] + trcg[o]);
+        }
+        pwat[p] = pw;
+      }
+    }
+    for (long p = 0; p < ng; ++p) pwat[p] = pwat[p] / GRAV;
+    const long NL = nlm, NS = (long)L * nlm;
+    std::fill(dtrc, dtrc + (long)nt * NS, cplx(0));
+#pragma omp parallel for schedule(dynamic)
+    for (int k = 0; k < L; ++k) {
+      sh.grdtospec(&dtdt[G(k)], &dtv[k * NL]);
+      sh.getvrtdivspec(&dudt[G(k)], &dvdt[G(k)], &dvrt[k * NL], &ddiv[k * NL], RERTH);
+      sh.grdtospec(&dqdt[G(k)], &dtrc[k * NL]);
+    }
+    for (long q = 0; q < NL; ++q) dlnps[q] = 0;
+    for (long q = 0; q < NS; ++q) {
+      dtv[q] = dtv[q] / dtx;
+      dvrt[q] = dvrt[q] / dtx;
+      ddiv[q] = ddiv[q] / dtx;
+      dtrc[q] = dtrc[q] / dtx;
+    }
+    for (long p = 0; p < ng; ++p) apcp[p] = apcp[p] + precip[p] * dtx;
+  }
+
+  // phy_run_hs.f90:22-84
+  void getphytend_hs(cplx* dvrt, cplx* ddiv, cplx* dtv, cplx* dtrc, cplx* dlnps) {
     const double sigbot = FLIT(0.7f), delthz = 10., tempstrat = 200.;
     const double kdrag = FLIT(1.f / (1.f * 86400.f)), krada = FLIT(1.f / (40.f * 86400.f)),
                  kradb = FLIT(1.f / (4.f * 86400.f));
@@ -1078,15 +1295,7 @@ struct Dycore {
     // time-split physics (run.f90:509-538)
     if (!c.adiabatic) {
       getdyntend(dvrt1.data(), ddiv1.data(), dtv1.data(), dtrc1.data(), dlnps1.data(), 3, true);
-      if (c.heldsuarez) {
-        getphytend(dvrt1.data(), ddiv1.data(), dtv1.data(), dtrc1.data(), dlnps1.data());
-      } else {
-        std::fill(dvrt1.begin(), dvrt1.end(), 0);
-        std::fill(ddiv1.begin(), ddiv1.end(), 0);
-        std::fill(dtv1.begin(), dtv1.end(), 0);
-        std::fill(dtrc1.begin(), dtrc1.end(), 0);
-        std::fill(dlnps1.begin(), dlnps1.end(), 0);
-      }
+      getphytend(dvrt1.data(), ddiv1.data(), dtv1.data(), dtrc1.data(), dlnps1.data());
       for (long q = 0; q < NS; ++q) {
         vrt[q] += dt * dvrt1[q];
         div[q] += dt * ddiv1[q];
@@ -1098,9 +1307,10 @@ struct Dycore {
     }
   }
 
-  // dyn_run.f90:605-634 with pwat = 0 (phy_data_stub)
+  // dyn_run.f90:605-634 (pwat is 0 but for the moist simple physics)
   void dry_mass_fixer(cplx* dlnpsdt_, double dtx) {
     double pwatg = 0.0, pmean = 0.0;
+    for (long p = 0; p < ng; ++p) pwatg += areawt(p) * pwat[p];
     for (long p = 0; p < ng; ++p) pmean += areawt(p) * psg[p];
     double pcorr = (pdryini + GRAV * pwatg) / pmean;
     std::vector<double> g(ng);
@@ -1157,6 +1367,7 @@ void ora_default_config(ora_config* c) {
   c->taustratdamp = 5. * 86400.;
   c->pdryini = 0;
   c->nthreads = 0;
+  c->dcmip = -1;
 }
 
 void* ora_create(const ora_config* c, const double* ak, const double* bk) {
@@ -1270,6 +1481,9 @@ int ora_get_grid(void* h, const char* name, double* out) {
   else if (n == "prs") v = &d->prs;
   else if (n == "dphisdx") v = &d->dphisdx;
   else if (n == "dphisdy") v = &d->dphisdy;
+  else if (n == "precip") v = &d->precip;
+  else if (n == "apcp") v = &d->apcp;
+  else if (n == "pwat") v = &d->pwat;
   if (!v) return -1;
   std::copy(v->begin(), v->end(), out);
   return 0;
@@ -1317,11 +1531,27 @@ void ora_damp(void* h, double* disspec, double* diff_prof, double* dmp_prof) {
 
 void ora_diag(void* h, double* out5) { D(h)->diag(out5); }
 
-void ora_getphytend(void* h, double* dvrt, double* ddiv, double* dtv) {
+void ora_simple_columns(int ncol, int n, double dtime, const double* lat, double* t, double* q, double* u, double* v,
+                        const double* pmid, const double* pint, const double* ps, double* precl, int test,
+                        int turbflux) {
+  std::vector<double> pdel(n), rpdel(n), w(12 * (n + 1));
+  for (int i = 0; i < ncol; ++i) {
+    const double* pi = pint + (long)i * (n + 1);
+    for (int k = 0; k < n; ++k) {
+      pdel[k] = pi[k + 1] - pi[k];
+      rpdel[k] = 1. / pdel[k];
+    }
+    const long o = (long)i * n;
+    simple_column(n, dtime, lat[i], t + o, q + o, u + o, v + o, pmid + o, pi, pdel.data(), rpdel.data(), ps[i],
+                  precl + i, test, turbflux != 0, w.data());
+  }
+}
+
+void ora_getphytend(void* h, double* dvrt, double* ddiv, double* dtv, double* dtrc, double* dlnps) {
   Dycore* d = D(h);
   long NS = (long)d->L * d->nlm;
   std::vector<cplx> e((long)d->nt * NS + 1), f(d->nlm);
-  d->getphytend(C(dvrt), C(ddiv), C(dtv), e.data(), f.data());
+  d->getphytend(C(dvrt), C(ddiv), C(dtv), dtrc ? C(dtrc) : e.data(), dlnps ? C(dlnps) : f.data());
 }
 
 }  // extern "C"

@@ -40,6 +40,7 @@ typedef struct ora_config {
   double hdif_fac, hdif_fac2, fshk, taustratdamp;
   double pdryini;  /* 0 -> set on first stage-1 call (dyn_run.f90:147) */
   int nthreads;    /* OpenMP threads, 0 -> default */
+  int dcmip;       /* params.f90:62 (-1 none; 4x, 5x: DCMIP simple physics) */
 } ora_config;
 
 void ora_default_config(ora_config* c);
@@ -67,7 +68,8 @@ void ora_getdyntend(void* h, int rkstage, int inverse_only, double* dvrt, double
 void ora_advance(void* h, double t, int nsteps);
 
 /* grid field readback after the last getdyntend: name in
-   ug vg vrtg divg tvg trcg dlnpdtg etadot lnpsg psg dlnpsdt prs */
+   ug vg vrtg divg tvg trcg dlnpdtg etadot lnpsg psg dlnpsdt prs, and the
+   physics fields precip apcp pwat (phy_data.f90) */
 int ora_get_grid(void* h, const char* name, double* out);
 void ora_grid_info(void* h, double* lats, double* gauwts, double* areawts, int* degree,
                    int* order, double* lap, double* invlap);
@@ -81,7 +83,12 @@ void ora_damp(void* h, double* disspec, double* diff_prof, double* dmp_prof);
 /* spdmax, psmin(hPa), psmax(hPa), pstendmean, pdryini */
 void ora_diag(void* h, double* out5);
 /* HS forcing tendencies from current grid state (phy_run_hs.f90:22) */
-void ora_getphytend(void* h, double* dvrt, double* ddiv, double* dtv);
+void ora_getphytend(void* h, double* dvrt, double* ddiv, double* dtv, double* dtrc, double* dlnps);
+/* simple_physics_v5_1.f90 on ncol independent columns [ncol][n] top to
+   bottom (pint [ncol][n+1]); t, q, u, v updated in place, precl out (m/s) */
+void ora_simple_columns(int ncol, int n, double dtime, const double* lat, double* t, double* q, double* u, double* v,
+                        const double* pmid, const double* pint, const double* ps, double* precl, int test,
+                        int turbflux);
 
 #ifdef __cplusplus
 }

@@ -34,7 +34,7 @@ class OraConfig(ctypes.Structure):
         ("ndiss", ctypes.c_int), ("efold", ctypes.c_double), ("hdif_fac", ctypes.c_double),
         ("hdif_fac2", ctypes.c_double), ("fshk", ctypes.c_double),
         ("taustratdamp", ctypes.c_double), ("pdryini", ctypes.c_double),
-        ("nthreads", ctypes.c_int),
+        ("nthreads", ctypes.c_int), ("dcmip", ctypes.c_int),
     ]
 
 
@@ -172,8 +172,10 @@ class Oracle:
     def getphytend(self):
         L, n = self.nlev, self.nlm
         d = [np.zeros((L, n), np.complex128) for _ in range(3)]
-        lib().ora_getphytend(self.h, _p(d[0]), _p(d[1]), _p(d[2]))
-        return dict(dvrt=d[0], ddiv=d[1], dtv=d[2])
+        dtrc = np.zeros((max(self.ntrac, 1), L, n), np.complex128)
+        dl = np.zeros(n, np.complex128)
+        lib().ora_getphytend(self.h, _p(d[0]), _p(d[1]), _p(d[2]), _p(dtrc), _p(dl))
+        return dict(dvrt=d[0], ddiv=d[1], dtv=d[2], dtrc=dtrc[: self.ntrac], dlnps=dl)
 
     def set_sppt(self, pattern, sigtop=0.05, sigbot=0.10):
         """Attach a PatternOracle as stochastically perturbed physics."""
@@ -188,7 +190,8 @@ class Oracle:
     def get_grid(self, name):
         L = self.nlev
         shapes = dict(ug=L, vg=L, vrtg=L, divg=L, tvg=L, dlnpdtg=L, prs=L, etadot=L + 1,
-                      trcg=max(self.ntrac, 1) * L, lnpsg=1, psg=1, dlnpsdt=1, dphisdx=1, dphisdy=1)
+                      trcg=max(self.ntrac, 1) * L, lnpsg=1, psg=1, dlnpsdt=1, dphisdx=1, dphisdy=1,
+                      precip=1, apcp=1, pwat=1)
         out = np.zeros((shapes[name], self.nlat, self.nlon))
         rc = lib().ora_get_grid(self.h, name.encode(), _p(out))
         assert rc == 0
@@ -234,6 +237,18 @@ class Oracle:
         o = np.zeros(5)
         lib().ora_diag(self.h, _p(o))
         return dict(spdmax=o[0], psmin=o[1], psmax=o[2], pstend=o[3], pdryini=o[4])
+
+
+def simple_columns(dtime, lat, t, q, u, v, pmid, pint, ps, test, turbflux):
+    """simple_physics_v5_1.f90 on independent columns (top to bottom);
+    returns updated (t, q, u, v) and precl."""
+    arr = lambda a: np.ascontiguousarray(a, np.float64).copy()
+    t, q, u, v = arr(t), arr(q), arr(u), arr(v)
+    ncol, n = t.shape
+    precl = np.zeros(ncol)
+    lib().ora_simple_columns(ncol, n, ctypes.c_double(dtime), _p(arr(lat)), _p(t), _p(q), _p(u), _p(v),
+                             _p(arr(pmid)), _p(arr(pint)), _p(arr(ps)), _p(precl), int(test), int(turbflux))
+    return t, q, u, v, precl
 
 
 # ---- stochastic pattern generator (gd_pattern_oracle.cpp) --------------------

@@ -44,7 +44,9 @@ def test_default_config_matches_reference_namelist_defaults():
     (dict(nlev=2), core.GD_ERR_ARG),
     (dict(dt=0.0), core.GD_ERR_ARG),
     (dict(precision=9), core.GD_ERR_ARG),
-    (dict(dry=0, ntrac=1), core.GD_ERR_UNSUPPORTED),
+    (dict(dcmip=51, heldsuarez=1), core.GD_ERR_ARG),
+    (dict(dcmip=30, heldsuarez=0), core.GD_ERR_ARG),
+    (dict(dcmip=51, heldsuarez=0, dry=0, ntrac=0), core.GD_ERR_ARG),
 ])
 def test_init_rejects_bad_config_without_gpu(kw, code):
     ak, bk = inputs.hybrid_coords(20)

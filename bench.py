@@ -275,11 +275,60 @@ def gpu_arm(args):
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(name, args.cpu_levels)
-        # the next row beside the step: the stochastic pattern generator
+        # the next rows beside the step: the stochastic pattern generator and the
+        # DCMIP simple physics
         out["pattern_generator"] = pattern_generator_rate()
+        if not args.no_dcmip:
+            out["dcmip_simple_physics"] = dcmip_rate(args.precision)
         print(json.dumps(out))
     g.close()
     grp.close()
+
+
+def dcmip_rate(precision, steps=10, warmup=3):
+    """The DCMIP simple-physics plugin (src/phy_run_simple.f90 around
+    src/simple_physics_v5_1.f90) in the full step: the moist baroclinic wave
+    with surface fluxes and boundary-layer mixing (dcmip 43; DCMIP-2012 test 4
+    initial state from gd_dcmip_ics; 3 tracers) at T574L64, dt 150 s.  The
+    column kernel's roofline counts the algorithmic bytes of one launch: Tv,
+    q, u, v read and their four increments written at every level, plus ps
+    read, precipitation and precipitable water written and the accumulated
+    precipitation read and written: (8 L + 5) nlat nlon words."""
+    import torch
+
+    from gdpy import core, inputs
+
+    T, nlon, nlat, L, nt, dt = 574, 1152, 576, 64, 3, 150.0
+    ak, bk = inputs.hybrid_coords(L)
+    g = core.Dycore(T, nlon, nlat, L, ak, bk, ntrac=nt, dt=dt, precision=precision, heldsuarez=False, dry=False,
+                    dcmip=43)
+    stream = torch.cuda.Stream()
+    g.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
+    g.dcmip_ics(43)
+    ics_s = time.perf_counter() - t0
+    g.advance(warmup)
+    g.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    g.advance(steps)
+    e1.record(stream)
+    g.sync()
+    ms = e0.elapsed_time(e1) / steps
+    ph = g.profile_step()
+    rsize = 8 if precision == "fp64" else 4
+    byt = (8 * L + 5) * nlat * nlon * rsize
+    cms = ph["column_physics"]
+    hbm = peaks()
+    achieved = byt / (cms * 1e-3) / 1e9
+    apcp = g.get_grid("apcp")
+    g.close()
+    return dict(workload="DCMIP-2012 4-3 moist baroclinic wave, simple physics, T574L64 ntrac 3 dt 150 s",
+                precision=precision, ms_per_step=ms, days_per_day=dt / (ms * 1e-3), initial_state_s=ics_s,
+                phases_ms=ph, max_accumulated_precip_mm=float(apcp.max()),
+                column_kernel=dict(kernel="k_simple_physics", bound="hbm", ms=cms, bytes=byt, achieved=achieved,
+                                   peak=hbm["hbm"], unit="GB/s", frac=achieved / hbm["hbm"],
+                                   peak_source=hbm["src"]))
 
 
 def pattern_generator_rate(steps=40, cpu_steps=3):
@@ -386,6 +435,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-levels", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-dcmip", action="store_true", help="skip the DCMIP simple-physics side measurement")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gd":
         args.warmup = 3

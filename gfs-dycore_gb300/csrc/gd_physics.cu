@@ -61,8 +61,11 @@ struct SimpleConst {
 }  // namespace
 
 // Thread per column; LMAX bounds the level count of the per-thread arrays.
+// The sweeps are dependent chains per thread, so the kernel lives on
+// occupancy: 16 CTAs of 128 threads per SM for the FP32 state (32
+// registers), 5 for FP64.
 template <typename R, int LMAX>
-__global__ void __launch_bounds__(128) k_simple_physics(SimpleArgs<R> a) {
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 16 : 5) k_simple_physics(SimpleArgs<R> a) {
   typedef SimpleConst<R> K;
   const long ng = (long)a.nlon * a.nlat;
   const long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -87,6 +90,7 @@ __global__ void __launch_bounds__(128) k_simple_physics(SimpleArgs<R> a) {
     if (sizeof(R) == 4) return (a.ak[t + 1] - a.ak[t]) + a.dbk[t] * ps;
     return PK(t + 1) - PK(t);
   };
+  auto PDELX = [&](int t) -> R { return PK(t + 1) - PK(t); };  // as in PMID
   auto TEMP = [&](R tv, R q) -> R { return tv / (R(1) + a.fvirt * max(a.qmin, q)); };
   // large-scale condensation of one level (simple_physics_v5_1.f90:226-255)
   R precl = R(0);
@@ -150,66 +154,77 @@ __global__ void __launch_bounds__(128) k_simple_physics(SimpleArgs<R> a) {
       Cd = R(K::Cm);
       Kmn = R(K::Cm) * wind * za;
     }
-    auto TAPER = [&](int i, R kb) -> R {  // at interface i (top-down), tapered above pbltop
+    // interface i (top-down): the vertical taper of the exchange coefficients
+    // above pbltop, shared by Km and Ke
+    auto TAPER = [&](int i) -> R {
       const R pint = PK(i);
-      if (pint >= R(K::pbltop)) return kb;
+      if (pint >= R(K::pbltop)) return R(1);
       const R x = R(K::pbltop) - pint;
-      return kb * exp(-(x * x) / (R(K::pblconst) * R(K::pblconst)));
+      return exp(-(x * x) / (R(K::pblconst) * R(K::pblconst)));
     };
     const R qsats = epsilo * e0 / ps * exp(-latvap / rh2o * ((R(1) / Tsurf) - R(1) / T0));
+    // pk^kappa pk at interface i, each computed once (layer pressures of two layers)
+    auto PKK = [&](int i) -> R {
+      const R pk = PK(i);
+      return pow(pk, a.kappa) * pk;
+    };
+    auto PMID2 = [&](int t, R kku, R kkl) -> R {  // Phillips layer pressure from the interface terms
+      return pow((kkl - kku) / ((a.kappa + R(1)) * PDELX(t)), R(1) / a.kappa);
+    };
     // sweep 1: bottom to top, level k with the level below (k+1) and above (k-1)
-    R ce[LMAX], cem[LMAX], cfu[LMAX], cfv[LMAX], cft[LMAX], cfq[LMAX], pmv[LMAX];
-    R tk = tb, qk = qb, uk = ub, vk = vb, pmk = PMID(nb), pdk = PDEL(nb);
+    R ce[LMAX], cem[LMAX], cfu[LMAX], cfv[LMAX], cft[LMAX], cfq[LMAX], exv[LMAX];
+    R kkl = PKK(nb + 1), kku = PKK(nb);
+    R tk = tb, qk = qb, uk = ub, vk = vb, pmk = PMID2(nb, kku, kkl), pdk = PDEL(nb);
     condense(tk, qk, pmk, pdk);
     uk = uk / (R(1) + Cd * wind * dt / za);
     vk = vk / (R(1) + Cd * wind * dt / za);
     tk = (tk + C * wind * Tsurf * dt / za) / (R(1) + C * wind * dt / za);
     qk = (qk + C * wind * qsats * dt / za) / (R(1) + C * wind * dt / za);
-    R t1 = R(0), pm1 = R(0), ce1 = R(0), cem1 = R(0), fu1 = R(0), fv1 = R(0), ft1 = R(0), fq1 = R(0);
+    // the interface below the current level: dt g^2 K rho^2 / dpm for Km and Ke
+    R xm1 = R(0), xe1 = R(0);
+    R ce1 = R(0), cem1 = R(0), fu1 = R(0), fv1 = R(0), ft1 = R(0), fq1 = R(0);
     for (int k = nb; k >= 0; --k) {
-      R tu = R(0), qu = R(0), uu = R(0), vu = R(0), pmu = R(0), pdu = R(0);
+      R tu = R(0), qu = R(0), uu = R(0), vu = R(0), pmu = R(0), pdu = R(0), xm = R(0), xe = R(0);
       if (k > 0) {
         qu = IN(a.s.trc, k - 1);
         tu = TEMP(IN(a.s.tv, k - 1), qu);
         uu = IN(a.s.u, k - 1);
         vu = IN(a.s.v, k - 1);
-        pmu = PMID(k - 1);
+        const R kkn = PKK(k - 1);
+        pmu = PMID2(k - 1, kkn, kku);
+        kku = kkn;
         pdu = PDEL(k - 1);
         condense(tu, qu, pmu, pdu);
+        // interface k, between k-1 and k
+        const R rho = (PK(k) / (rair * (tk + tu) / R(2)));
+        const R x = dt * gravit * gravit * rho * rho / (pmk - pmu);
+        const R tp = TAPER(k);
+        xm = x * (Kmn * tp);
+        xe = x * (Ken * tp);
       }
       const R rpd = R(1) / pdk;
-      R CA = R(0), CAm = R(0), CC = R(0), CCm = R(0);
-      if (k < nb) {  // interface k+1
-        const R rho = (PK(k + 1) / (rair * (t1 + tk) / R(2)));
-        const R dpm = pm1 - pmk;
-        CAm = rpd * dt * gravit * gravit * TAPER(k + 1, Kmn) * rho * rho / dpm;
-        CA = rpd * dt * gravit * gravit * TAPER(k + 1, Ken) * rho * rho / dpm;
-      }
-      if (k > 0) {  // interface k
-        const R rho = (PK(k) / (rair * (tk + tu) / R(2)));
-        const R dpm = pmk - pmu;
-        CCm = rpd * dt * gravit * gravit * TAPER(k, Kmn) * rho * rho / dpm;
-        CC = rpd * dt * gravit * gravit * TAPER(k, Ken) * rho * rho / dpm;
-      }
+      const R CAm = rpd * xm1, CA = rpd * xe1, CCm = rpd * xm, CC = rpd * xe;
       const R de = R(1) + CA + CC - CA * ce1;
       const R dm = R(1) + CAm + CCm - CAm * cem1;
+      const R ex = pow(p0 / pmk, rk);
       ce[k] = CC / de;
       cem[k] = CCm / dm;
       cfu[k] = (uk + CAm * fu1) / dm;
       cfv[k] = (vk + CAm * fv1) / dm;
-      cft[k] = (pow(p0 / pmk, rk) * tk + CA * ft1) / de;
+      cft[k] = (ex * tk + CA * ft1) / de;
       cfq[k] = (qk + CA * fq1) / de;
-      pmv[k] = pmk;
-      t1 = tk, pm1 = pmk, ce1 = ce[k], cem1 = cem[k], fu1 = cfu[k], fv1 = cfv[k], ft1 = cft[k], fq1 = cfq[k];
+      exv[k] = ex;
+      xm1 = xm, xe1 = xe;
+      ce1 = ce[k], cem1 = cem[k], fu1 = cfu[k], fv1 = cfv[k], ft1 = cft[k], fq1 = cfq[k];
       tk = tu, qk = qu, uk = uu, vk = vu, pmk = pmu, pdk = pdu;
     }
-    // sweep 2: top to bottom
-    R un = cfu[0], vn = cfv[0], tn = cft[0] * pow(pmv[0] / p0, rk), qn = cfq[0];
+    // sweep 2: top to bottom, potential temperature back to temperature
+    R un = cfu[0], vn = cfv[0], tn = cft[0] / exv[0], qn = cfq[0];
     emit(0, tn, qn, un, vn);
     for (int k = 1; k < L; ++k) {
       un = cem[k] * un + cfu[k];
       vn = cem[k] * vn + cfv[k];
-      tn = (ce[k] * tn * pow(p0 / pmv[k - 1], rk) + cft[k]) * pow(pmv[k] / p0, rk);
+      tn = (ce[k] * tn * exv[k - 1] + cft[k]) / exv[k];
       qn = ce[k] * qn + cfq[k];
       emit(k, tn, qn, un, vn);
     }

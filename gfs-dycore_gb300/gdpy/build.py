@@ -60,7 +60,7 @@ def build(verbose=False, force=False, extra=()):
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(run, jobs))
     if jobs or not os.path.exists(LIB):
-        run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+        run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lpthread"])
     return LIB
 
 

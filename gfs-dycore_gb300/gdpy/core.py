@@ -42,7 +42,7 @@ API_FUNCTIONS = [
     "gd_dcmip_point",
 ]
 PHASES = ["legendre_synth", "fft_synth", "columns", "fft_anal", "legendre_anal", "semi_implicit",
-          "physics", "other"]
+          "physics", "other", "column_physics"]
 
 
 class GdConfig(ctypes.Structure):

@@ -45,6 +45,10 @@ class DycoreBase {
   virtual void getdyntend(int, int, double*, double*, double*, double*, double*) = 0;
   virtual void getphytend(double*, double*, double*, double*, double*) = 0;
   virtual void advance(int nsteps) = 0;
+  virtual void set_iau(int nf, const double* fhrs, double delthrs, const double* vrt, const double* div,
+                       const double* tv, const double* trc, const double* lnps) = 0;
+  virtual void dfi(double t, int ntdfi) = 0;
+  double t_cur = 0.0;  // model time (s) of the next step, for the IAU forcing
   virtual void spectogrd(int, const double*, double*) = 0;
   virtual void grdtospec(int, const double*, double*) = 0;
   virtual void getuv(int, const double*, const double*, double*, double*) = 0;
@@ -61,6 +65,21 @@ class DycoreBase {
   bool own_stream = true;
   std::string err;
 };
+
+// set_dfi_wts (run.f90:567-588): Lanczos-windowed sinc weights over 2 n + 1
+// steps, normalised to sum 1.  The angles are single precision, as
+// acos(-1.) * (k - n) / n is for a literal without a kind suffix.
+void dfi_weights(int n, double* w) {
+  const float pif = 3.14159265358979323846f;
+  double tot = 0.0;
+  for (int k = 0; k <= 2 * n; ++k) {
+    const double sx = (double)(pif * (float)(k - n) / (float)n);
+    const double wx = (double)(pif * (float)(k - n) / (float)(n + 1));
+    w[k] = (k != n) ? sin(wx) / wx * sin(sx) / sx : 1.0;
+    tot += w[k];
+  }
+  for (int k = 0; k <= 2 * n; ++k) w[k] = w[k] / tot;
+}
 
 template <typename R>
 class Dycore : public DycoreBase {
@@ -722,6 +741,7 @@ class Dycore : public DycoreBase {
       a.ci[r] = c.explicit_ ? R(0) : (R)ci[s][r];
     }
     a.cimp = c.explicit_ ? R(0) : (R)cimp[s];
+    a.F = iau_nf ? iau_F : nullptr;
     a.sc = sc;
     a.tc = tc;
     a.ap = ap;
@@ -853,6 +873,98 @@ class Dycore : public DycoreBase {
       gexec = nullptr;
     }
   }
+  // IAU (iau_module.f90): increments analysis - first guess at nf times,
+  // a forcing interpolated in time, constant over the RK stages of a step
+  R *iau_inc = nullptr, *iau_F = nullptr;
+  int iau_nf = 0;
+  std::vector<double> iau_fh;
+  double iau_delthrs = 6.0;
+  void set_iau(int nf, const double* fhrs, double delthrs, const double* vrt, const double* div, const double* tv,
+               const double* trc, const double* lnps) override {
+    if (nf == 0) {
+      iau_nf = 0;
+    } else {
+      if (nf < 2) throw std::invalid_argument("IAU needs at least two times");
+      for (int n = 1; n < nf; ++n)
+        if (fhrs[n] - fhrs[n - 1] != fhrs[1] - fhrs[0])
+          throw std::invalid_argument("IAU times must be equally spaced (iau_module.f90:41-46)");
+      if (!(delthrs > 0)) throw std::invalid_argument("IAU interval must be positive");
+      if (!vrt || !div || !tv || !lnps || (nt > 0 && !trc)) throw std::invalid_argument("IAU increments missing");
+      const long per = (long)nlm * ldS;
+      if (iau_inc) release(iau_inc);
+      iau_inc = dalloc<R>((size_t)nf * per);
+      GD_CUDA(cudaMemsetAsync(iau_inc, 0, sizeof(R) * nf * per, stream));
+      if (!iau_F) iau_F = dalloc<R>((size_t)per);
+      GD_CUDA(cudaMemsetAsync(iau_F, 0, sizeof(R) * per, stream));
+      double* st = staging();
+      const long nS = 2L * nlm * L, nT = 2L * nlm * L * nt, nP = 2L * nlm;
+      for (int n = 0; n < nf; ++n) {
+        R* dst = iau_inc + n * per;
+        auto put = [&](const double* h, int nb, int col) {
+          GD_CUDA(cudaMemcpyAsync(st, h, sizeof(double) * 2 * (long)nb * nlm, cudaMemcpyHostToDevice, stream));
+          launch_ref2int<R>(st, nb, nlm, dst, ldS, col, stream);
+          GD_CUDA(cudaStreamSynchronize(stream));
+        };
+        put(vrt + n * nS, L, sc.vrt);
+        put(div + n * nS, L, sc.div);
+        put(tv + n * nS, L, sc.tv);
+        if (nt > 0) put(trc + n * nT, nt * L, sc.trc);
+        put(lnps + n * nP, 1, sc.lnps);
+      }
+      iau_fh.assign(fhrs, fhrs + nf);
+      iau_delthrs = delthrs;
+      iau_nf = nf;
+    }
+    if (gexec) {  // the captured step changes
+      GD_CUDA(cudaStreamSynchronize(stream));
+      GD_CUDA(cudaGraphExecDestroy(gexec));
+      gexec = nullptr;
+    }
+  }
+  // getiauforcing (iau_module.f90:88-135) at time t into iau_F
+  void iau_forcing(double t) {
+    const int nf = iau_nf;
+    const double dtiau = iau_delthrs * 3600.;
+    int ia = 0, ib = 0;
+    double ca = 0.0, cb = 0.0;
+    if (t < iau_fh[0] * 3600. || t > iau_fh[nf - 1] * 3600.) {
+      // outside the window: no forcing
+    } else if (t == 3600. * iau_fh[nf - 1]) {
+      ia = nf - 1, ca = 1.0;
+    } else if (t == 3600. * iau_fh[0]) {
+      ia = 0, ca = 1.0;
+    } else {
+      int n = 0;
+      while (n < nf && !(iau_fh[n] * 3600. > t)) ++n;
+      const double delt = (iau_fh[n] - (t / 3600.)) / (iau_fh[n] - iau_fh[n - 1]);
+      ia = n, ca = 1. - delt;
+      ib = n - 1, cb = delt;
+    }
+    launch_iau_forcing<R>(iau_F, iau_inc, ldS, sc, (3 + nt) * L, nlm, ia, ca, ib, cb, dtiau, stream);
+  }
+  // Digital filter initialisation (run.f90:58-145): 2 ntdfi steps from t,
+  // the Lanczos-weighted average of the states (FP64 accumulator) becomes
+  // the state, valid at t + ntdfi dt; accumulated precipitation restarts
+  // (init_phydata).
+  void dfi(double t, int ntdfi) override {
+    if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
+    std::vector<double> wts(2 * ntdfi + 1);
+    dfi_weights(ntdfi, wts.data());
+    const int ncs = (3 + nt) * L;
+    double* acc = dalloc<double>(2L * nlm * (ncs + 1));
+    t_cur = t;
+    launch_dfi_acc<R>(acc, S, ldS, sc, ncs, nlm, wts[0], 1, stream);
+    for (int k = 1; k <= 2 * ntdfi; ++k) {
+      advance(1);
+      launch_dfi_acc<R>(acc, S, ldS, sc, ncs, nlm, wts[k], 0, stream);
+    }
+    launch_dfi_set<R>(S, ldS, sc, ncs, nlm, acc, stream);
+    launch_sc<R>(S, ldS, sc, L, nlm, lapv, (R)Phys::rerth, stream);
+    GD_CUDA(cudaMemsetAsync(apcp, 0, sizeof(R) * ng, stream));
+    GD_CUDA(cudaStreamSynchronize(stream));
+    release(acc);
+    t_cur = t + ntdfi * c.dt;
+  }
   // advance (run.f90:194-565)
   void step() {
     mark(-1);
@@ -873,6 +985,8 @@ class Dycore : public DycoreBase {
   void profile_step(double* ms, int n) override {
     if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
     for (int i = 0; i < n; ++i) ms[i] = 0;
+    if (iau_nf) iau_forcing(t_cur);
+    t_cur += c.dt;
     marks.clear();
     profiling = true;
     step();
@@ -890,6 +1004,8 @@ class Dycore : public DycoreBase {
   void advance(int nsteps) override {
     if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
     for (int i = 0; i < nsteps; ++i) {
+      if (iau_nf) iau_forcing(t_cur);  // outside the captured step: its coefficients change with time
+      t_cur += c.dt;
       // the legacy default stream cannot be captured: launch eagerly there
       const bool capturable = stream != nullptr && stream != cudaStreamLegacy && stream != cudaStreamPerThread;
       if (!capturable) {
@@ -1418,12 +1534,72 @@ int gd_getphytend(gd_ctx* ctx, double* dvrt, double* ddiv, double* dtv, double* 
   return guarded(ctx, [&] { ctx->d->getphytend(dvrt, ddiv, dtv, dtrc, dlnps); });
 }
 int gd_advance(gd_ctx* ctx, double t, int nsteps) {
-  (void)t;
   if (nsteps < 0) {
     if (ctx) ctx->err = "gd_advance: nsteps < 0";
     return GD_ERR_ARG;
   }
-  return guarded(ctx, [&] { ctx->d->advance(nsteps); });
+  return guarded(ctx, [&] {
+    ctx->d->t_cur = t;
+    ctx->d->advance(nsteps);
+  });
+}
+int gd_set_iau(gd_ctx* ctx, int nfiles, const double* fhrs, double delthrs, const double* vrt, const double* div,
+               const double* tv, const double* trc, const double* lnps) {
+  if (nfiles < 0 || (nfiles > 0 && !fhrs)) {
+    if (ctx) ctx->err = "gd_set_iau: bad nfiles or null times";
+    return GD_ERR_ARG;
+  }
+  return guarded(ctx, [&] { ctx->d->set_iau(nfiles, fhrs, delthrs, vrt, div, tv, trc, lnps); });
+}
+int gd_set_iau_files(gd_ctx* ctx, int nfiles, const double* fhrs, double delthrs, const char* const* fg,
+                     const char* const* anl) {
+  if (!ctx || !ctx->d) return GD_ERR_ARG;
+  if (nfiles < 2 || !fhrs || !fg || !anl) {
+    ctx->err = "gd_set_iau_files: need at least two first-guess / analysis pairs";
+    return GD_ERR_ARG;
+  }
+  const gd_config& c = ctx->cfg;
+  const size_t n2 = (size_t)(c.ntrunc + 1) * (c.ntrunc + 2), L = (size_t)c.nlev, nt = (size_t)c.ntrac;
+  std::vector<double> inc[5], tmp[5];
+  const size_t sz[5] = {n2 * L, n2 * L, n2 * L, n2 * L * nt, n2};
+  try {
+    for (int f = 0; f < 5; ++f) {
+      inc[f].assign(sz[f] * nfiles, 0.0);
+      tmp[f].assign(sz[f], 0.0);
+    }
+  } catch (const std::bad_alloc&) {
+    ctx->err = "gd_set_iau_files: host allocation failed";
+    return GD_ERR_NOMEM;
+  }
+  for (int n = 0; n < nfiles; ++n) {  // init_iau (iau_module.f90:57-78): analysis - first guess
+    gd_sighead h;
+    int rc = gd_sigio_read(fg[n], c.ntrunc, c.nlev, c.ntrac, &h, tmp[0].data(), tmp[1].data(), tmp[2].data(),
+                           nt ? tmp[3].data() : nullptr, tmp[4].data(), nullptr);
+    double* o[5];
+    for (int f = 0; f < 5; ++f) o[f] = inc[f].data() + n * sz[f];
+    if (rc == GD_OK)
+      rc = gd_sigio_read(anl[n], c.ntrunc, c.nlev, c.ntrac, &h, o[0], o[1], o[2], nt ? o[3] : nullptr, o[4], nullptr);
+    if (rc != GD_OK) {
+      ctx->err = gd_sigio_last_error();
+      return rc;
+    }
+    for (int f = 0; f < 5; ++f)
+      for (size_t i = 0; i < sz[f]; ++i) o[f][i] = o[f][i] - tmp[f][i];
+  }
+  return gd_set_iau(ctx, nfiles, fhrs, delthrs, inc[0].data(), inc[1].data(), inc[2].data(),
+                    nt ? inc[3].data() : nullptr, inc[4].data());
+}
+int gd_dfi(gd_ctx* ctx, double t, int ntdfi) {
+  if (ntdfi < 1) {
+    if (ctx) ctx->err = "gd_dfi: ntdfi must be >= 1";
+    return GD_ERR_ARG;
+  }
+  return guarded(ctx, [&] { ctx->d->dfi(t, ntdfi); });
+}
+int gd_dfi_weights(int ntdfi, double* w) {
+  if (ntdfi < 1 || !w) return GD_ERR_ARG;
+  gd::dfi_weights(ntdfi, w);
+  return GD_OK;
 }
 int gd_spectogrd(gd_ctx* ctx, int nb, const double* spec, double* grid) {
   if (nb < 0 || (nb > 0 && (!spec || !grid))) return GD_ERR_ARG;
@@ -1473,7 +1649,7 @@ int gd_ensemble_advance(gd_ctx** ctxs, int n, double t, int nsteps) {
   if (!ctxs || n < 1 || nsteps < 0) return GD_ERR_ARG;
   for (int i = 0; i < n; ++i)
     if (!ctxs[i] || !ctxs[i]->d) return GD_ERR_ARG;
-  (void)t;
+  for (int i = 0; i < n; ++i) ctxs[i]->d->t_cur = t;
   // members step in turn, each on its own stream: their steps overlap on the GPU
   for (int s = 0; s < nsteps; ++s)
     for (int i = 0; i < n; ++i) {

@@ -142,6 +142,13 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_stage(StageArgs
     const long idx = IDX(i);
     V dvrt, ddiv, dtv;
     raw_tend(a, idx, k, lap, dvrt, ddiv, dtv);
+    if (a.F) {  // IAU forcing, before the linear terms are taken out
+      const V fv = ldg2(a.F, idx, a.ldS, a.sc.vrt + k), fd = ldg2(a.F, idx, a.ldS, a.sc.div + k),
+              ft = ldg2(a.F, idx, a.ldS, a.sc.tv + k);
+      dvrt.x += fv.x, dvrt.y += fv.y;
+      ddiv.x += fd.x, ddiv.y += fd.y;
+      dtv.x += ft.x, dtv.y += ft.y;
+    }
     V ddl = vz<V>(), dtl = vz<V>();
     if (!a.explicit_) {
       ddl.x = -lap * (Y[i * L + k].x + a.tor[k] * LN[i].x);
@@ -200,6 +207,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_stage(StageArgs
     for (int iq = 0; iq < a.nt; ++iq) {  // tracers, always explicit
       const int col = iq * L + k;
       V dq = ldg2(a.AP, idx, a.ldAP, a.ap.qtend + col);
+      if (a.F) {
+        const V fq = ldg2(a.F, idx, a.ldS, a.sc.trc + col);
+        dq.x += fq.x, dq.y += fq.y;
+      }
       st2(TDs, idx, a.ldTD, a.tc.dtrc + col, dq);
       V q = ldg2(a.S0, idx, a.ldS, a.sc.trc + col);
       V sq = vz<V>();
@@ -221,6 +232,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_stage(StageArgs
   for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
     const long idx = IDX(i);
     V dl = ldg2(a.AP, idx, a.ldAP, a.ap.dlnps);
+    if (a.F) {
+      const V fl = ldg2(a.F, idx, a.ldS, a.sc.lnps);
+      dl.x += fl.x, dl.y += fl.y;
+    }
     V dpl = vz<V>();
     if (!a.explicit_) {
       dpl.x = -Y3[i].x;
@@ -478,6 +493,90 @@ template void launch_simple_update<double>(double*, long, const SpecCols&, int, 
                                            cudaStream_t);
 template void launch_simple_update<float>(float*, long, const SpecCols&, int, int, const float*, long, const float*,
                                           long, int, float, float, const float*, float, cudaStream_t);
+
+// prognostic column j of the state layout: the (3+nt) L columns from vrt, then lnps
+__device__ __forceinline__ int prog_col(const SpecCols& sc, int ncs, int j) { return j < ncs ? sc.vrt + j : sc.lnps; }
+
+template <typename R>
+__global__ void k_iau_forcing(R* F, const R* inc, long ldS, SpecCols sc, int ncs, int nlm, int ia, double ca, int ib,
+                              double cb, double dtiau) {
+  const long per = (long)nlm * ldS;
+  const long total = (long)nlm * (ncs + 1);
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const long idx = e / (ncs + 1);
+    const int col = prog_col(sc, ncs, (int)(e - idx * (ncs + 1)));
+    typename C2<R>::T f;
+    if (ca == 0.0 && cb == 0.0) {
+      f.x = f.y = R(0);
+    } else {
+      const typename C2<R>::T x = ld2(inc + ia * per, idx, ldS, col), y = ld2(inc + ib * per, idx, ldS, col);
+      f.x = (R(ca) * x.x + R(cb) * y.x) / R(dtiau);
+      f.y = (R(ca) * x.y + R(cb) * y.y) / R(dtiau);
+    }
+    st2(F, idx, ldS, col, f);
+  }
+}
+template <typename R>
+void launch_iau_forcing(R* F, const R* inc, long ldS, const SpecCols& sc, int ncs, int nlm, int ia, double ca,
+                        int ib, double cb, double dtiau, cudaStream_t s) {
+  const long total = (long)nlm * (ncs + 1);
+  k_iau_forcing<R><<<std::min(ceil_div(total, 256), 8192), 256, 0, s>>>(F, inc, ldS, sc, ncs, nlm, ia, ca, ib, cb,
+                                                                        dtiau);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template void launch_iau_forcing<double>(double*, const double*, long, const SpecCols&, int, int, int, double, int,
+                                         double, double, cudaStream_t);
+template void launch_iau_forcing<float>(float*, const float*, long, const SpecCols&, int, int, int, double, int,
+                                        double, double, cudaStream_t);
+
+template <typename R>
+__global__ void k_dfi_acc(double* acc, const R* S, long ldS, SpecCols sc, int ncs, int nlm, double w, int first) {
+  const long total = (long)nlm * (ncs + 1);
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const long idx = e / (ncs + 1);
+    const int j = (int)(e - idx * (ncs + 1));
+    const typename C2<R>::T x = ld2(S, idx, ldS, prog_col(sc, ncs, j));
+    double* o = acc + 2 * e;
+    if (first) {
+      o[0] = w * (double)x.x;
+      o[1] = w * (double)x.y;
+    } else {
+      o[0] = o[0] + w * (double)x.x;
+      o[1] = o[1] + w * (double)x.y;
+    }
+  }
+}
+template <typename R>
+void launch_dfi_acc(double* acc, const R* S, long ldS, const SpecCols& sc, int ncs, int nlm, double w, int first,
+                    cudaStream_t s) {
+  const long total = (long)nlm * (ncs + 1);
+  k_dfi_acc<R><<<std::min(ceil_div(total, 256), 8192), 256, 0, s>>>(acc, S, ldS, sc, ncs, nlm, w, first);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template void launch_dfi_acc<double>(double*, const double*, long, const SpecCols&, int, int, double, int,
+                                     cudaStream_t);
+template void launch_dfi_acc<float>(double*, const float*, long, const SpecCols&, int, int, double, int, cudaStream_t);
+
+template <typename R>
+__global__ void k_dfi_set(R* S, long ldS, SpecCols sc, int ncs, int nlm, const double* acc) {
+  const long total = (long)nlm * (ncs + 1);
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const long idx = e / (ncs + 1);
+    const int j = (int)(e - idx * (ncs + 1));
+    st2(S, idx, ldS, prog_col(sc, ncs, j), mk2<R>((R)acc[2 * e], (R)acc[2 * e + 1]));
+  }
+}
+template <typename R>
+void launch_dfi_set(R* S, long ldS, const SpecCols& sc, int ncs, int nlm, const double* acc, cudaStream_t s) {
+  const long total = (long)nlm * (ncs + 1);
+  k_dfi_set<R><<<std::min(ceil_div(total, 256), 8192), 256, 0, s>>>(S, ldS, sc, ncs, nlm, acc);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template void launch_dfi_set<double>(double*, long, const SpecCols&, int, int, const double*, cudaStream_t);
+template void launch_dfi_set<float>(float*, long, const SpecCols&, int, int, const double*, cudaStream_t);
 
 template <typename R>
 __global__ void k_sc(R* S, long ldS, SpecCols sc, int L, int nlm, const R* lapv, R rerth) {

@@ -49,6 +49,10 @@ struct StageArgs {
   const R* dmp_prof;
   R dt, ainv, ainv2, rerth;
   R ce[3], ci[3], cimp;
+  // IAU forcing in the state's columns (vrt, div, tv, trc, lnps), added to the
+  // explicit tendencies of every stage (run.f90:301-308, 362-369, 428-435);
+  // null without IAU
+  const R* F;
   SpecCols sc;
   TendCols tc;
   APCols ap;
@@ -79,6 +83,22 @@ void launch_phys_update(R* S, long ldS, const SpecCols& sc, int L, int nt, int n
 template <typename R>
 void launch_simple_update(R* S, long ldS, const SpecCols& sc, int L, int nlm, const R* AP, long ldAP, const R* AH,
                           long ldAH, int massfix, R dt, R ainv, const R* lapv, R rerth, cudaStream_t s);
+
+// IAU forcing of one step (iau_module.f90:88-135): F = (ca inc[ia] + cb
+// inc[ib]) / dtiau over the prognostic columns of the state layout (the
+// (3+nt) L columns from vrt and the lnps column); ca = cb = 0 gives zero.
+// inc holds nfiles arrays of nlm rows with the state's pitch.
+template <typename R>
+void launch_iau_forcing(R* F, const R* inc, long ldS, const SpecCols& sc, int ncs, int nlm, int ia, double ca,
+                        int ib, double cb, double dtiau, cudaStream_t s);
+// Digital filter (run.f90:58-91): acc = w S (first) or acc += w S, over the
+// prognostic columns, acc in FP64 [nlm][ncs+1] complex.
+template <typename R>
+void launch_dfi_acc(double* acc, const R* S, long ldS, const SpecCols& sc, int ncs, int nlm, double w, int first,
+                    cudaStream_t s);
+// S = acc over the prognostic columns (run.f90:116-117).
+template <typename R>
+void launch_dfi_set(R* S, long ldS, const SpecCols& sc, int ncs, int nlm, const double* acc, cudaStream_t s);
 
 // s = a invlap vrt, c = a invlap div for all coefficients.
 template <typename R>

@@ -39,7 +39,7 @@ API_FUNCTIONS = [
     "gd_pattern_launch_count", "gd_pattern_last_error", "gd_set_sppt", "gd_ensemble_advance",
     "gd_sigio_head_init", "gd_sigio_read_head", "gd_sigio_read", "gd_sigio_write", "gd_sigio_config",
     "gd_read_sig", "gd_write_sig", "gd_sigio_last_error", "gd_dcmip_ics",
-    "gd_dcmip_point",
+    "gd_dcmip_point", "gd_set_iau", "gd_set_iau_files", "gd_dfi", "gd_dfi_weights",
 ]
 PHASES = ["legendre_synth", "fft_synth", "columns", "fft_anal", "legendre_anal", "semi_implicit",
           "physics", "other", "column_physics"]
@@ -118,6 +118,10 @@ def load(build_if_missing=True):
     L.gd_sigio_last_error.argtypes = []
     L.gd_dcmip_ics.argtypes = [vp, i]
     L.gd_dcmip_point.argtypes = [i, i, d, d, d, vp]
+    L.gd_set_iau.argtypes = [vp, i, vp, d, vp, vp, vp, vp, vp]
+    L.gd_set_iau_files.argtypes = [vp, i, vp, d, ctypes.POINTER(cp), ctypes.POINTER(cp)]
+    L.gd_dfi.argtypes = [vp, d, i]
+    L.gd_dfi_weights.argtypes = [i, vp]
     _lib = L
     return L
 
@@ -134,6 +138,15 @@ def default_config(**kw):
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def dfi_weights(ntdfi):
+    """gd_dfi_weights: the Lanczos weights of the digital filter."""
+    w = np.zeros(2 * ntdfi + 1)
+    rc = load().gd_dfi_weights(int(ntdfi), _p(w))
+    if rc != GD_OK:
+        raise GdError(rc, "gd_dfi_weights: ntdfi must be >= 1")
+    return w
 
 
 def dcmip_point(testcase, lon, lat, p, moist=True):
@@ -200,6 +213,27 @@ class Dycore:
     def dcmip_ics(self, testcase):
         """DCMIP-2012 test 4x (baroclinic wave) or 5x (tropical cyclone) initial state (gd_dcmip_ics)."""
         self._chk(load().gd_dcmip_ics(self.h, int(testcase)))
+
+    def set_iau(self, fhrs, delthrs=6.0, vrt=None, div=None, tv=None, trc=None, lnps=None):
+        """gd_set_iau: increments with a leading file axis; fhrs=None detaches."""
+        if fhrs is None:
+            self._chk(load().gd_set_iau(self.h, 0, None, ctypes.c_double(delthrs), None, None, None, None, None))
+            return
+        fh = np.ascontiguousarray(fhrs, np.float64)
+        c = lambda a: None if a is None else np.ascontiguousarray(a, np.complex128)
+        self._iau = [fh] + [c(x) for x in (vrt, div, tv, trc, lnps)]
+        self._chk(load().gd_set_iau(self.h, len(fh), _p(fh), ctypes.c_double(delthrs),
+                                    *[_p(x) for x in self._iau[1:]]))
+
+    def set_iau_files(self, fhrs, fg, anl, delthrs=6.0):
+        """gd_set_iau_files: increments from first-guess / analysis sigma files."""
+        fh = np.ascontiguousarray(fhrs, np.float64)
+        arr = lambda names: (ctypes.c_char_p * len(names))(*[str(x).encode() for x in names])
+        self._chk(load().gd_set_iau_files(self.h, len(fh), _p(fh), ctypes.c_double(delthrs), arr(fg), arr(anl)))
+
+    def dfi(self, ntdfi, t=0.0):
+        """gd_dfi: the digital filter over 2 ntdfi steps from time t."""
+        self._chk(load().gd_dfi(self.h, ctypes.c_double(t), int(ntdfi)))
 
     def read_sig(self, path):
         """readin_sig + init_dyn's ln(ps) conversion (gd_read_sig); returns the header."""

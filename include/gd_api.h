@@ -110,9 +110,36 @@ int gd_getphytend(gd_ctx* ctx, double* dvrt, double* ddiv, double* dtv, double* 
 
 /* Replaces nsteps calls of advance(t) (src/run.f90:194-565): IMEX RK3 with
    the semi-implicit solve, implicit hyperdiffusion, time-split Held-Suarez
-   physics and the dry-mass fixer.  Runs asynchronously on the context
-   stream; the state stays on the device. */
+   physics and the dry-mass fixer.  t (s) is the model time of the first
+   step, t + k dt of the next ones; it matters only for the IAU forcing.
+   Runs asynchronously on the context stream; the state stays on the
+   device. */
 int gd_advance(gd_ctx* ctx, double t, int nsteps);
+
+/* Incremental analysis update (src/iau_module.f90, run.f90:250-258,
+   301-308): increments (analysis - first guess) at nfiles >= 2 equally
+   spaced forecast hours fhrs, in the state layouts with a leading nfiles
+   axis: vrt, div, tv [nfiles][nlev][nlm], trc [nfiles][ntrac][nlev][nlm],
+   lnps [nfiles][nlm].  Each step of gd_advance at time t adds the forcing
+   of getiauforcing (iau_module.f90:88-135) -- the increments interpolated
+   linearly in time between the bracketing files, divided by delthrs hours,
+   zero outside [fhrs[0], fhrs[nfiles-1]] -- to the explicit tendencies of
+   all three RK stages.  nfiles = 0 detaches. */
+int gd_set_iau(gd_ctx* ctx, int nfiles, const double* fhrs, double delthrs, const double* vrt, const double* div,
+               const double* tv, const double* trc, const double* lnps);
+/* init_iau (iau_module.f90:19-79): the increments from pairs of sigma files
+   (first guess fg[n], analysis anl[n], read as readin_sig reads them). */
+int gd_set_iau_files(gd_ctx* ctx, int nfiles, const double* fhrs, double delthrs, const char* const* fg,
+                     const char* const* anl);
+
+/* Digital filter initialisation (run.f90:58-145): advances 2 ntdfi steps
+   from time t, accumulating the Lanczos-weighted state (set_dfi_wts,
+   run.f90:567-588; FP64 accumulator), then replaces the state by that
+   average, valid at t + ntdfi dt; the accumulated precipitation restarts
+   at 0 (init_phydata).  Synchronous. */
+int gd_dfi(gd_ctx* ctx, double t, int ntdfi);
+/* The 2 ntdfi + 1 filter weights of gd_dfi (host only). */
+int gd_dfi_weights(int ntdfi, double* w);
 
 /* Transform facade of src/shtns.f90, batched over nb 2-D fields
    (spectral [nb][nlm], grid [nb][nlat][nlon]); rsphere = 6.3712e6 m.
@@ -152,8 +179,9 @@ int gd_diag(gd_ctx* ctx, double* out5);
    :506,:525).  ms[0..7] receive milliseconds spent in: 0 Legendre
    synthesis, 1 longitude FFT synthesis, 2 grid-space column kernels,
    3 longitude FFT analysis, 4 Legendre analysis, 5 semi-implicit / RK
-   stage updates, 6 physics grid work and update, 7 other.  The state
-   advances by one step.  nphase must be >= 8. */
+   stage updates, 6 physics grid work and update, 7 other, and with
+   nphase >= 9: 8 the DCMIP column-physics kernel alone (else counted in
+   6).  The state advances by one step.  nphase must be >= 8. */
 int gd_profile_step(gd_ctx* ctx, double* ms, int nphase);
 
 /* Allocation-free step diagnostics.  This entry point has no counterpart in

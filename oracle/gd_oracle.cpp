@@ -1149,9 +1149,102 @@ struct Dycore {
     for (long q = 0; q < (long)nt * L * NL; ++q) dtrc[q] = 0;
   }
 
-  // run.f90:194-565 (IAU, stochastic and DFI branches are out of scope)
-  void advance(double) {
+  // IAU (iau_module.f90): increments analysis - first guess at iau_nf times
+  int iau_nf = 0;
+  std::vector<double> iau_fh;
+  double iau_delthrs = 6.0;
+  std::vector<cplx> ivrt, idiv, itv, itrc, ilnps;  // [nf][...]
+  std::vector<cplx> fvrt, fdiv, ftv, ftrc, flnps;  // the forcing of the current step
+  // getiauforcing (iau_module.f90:88-135)
+  void getiauforcing(double t) {
+    const long NS = (long)L * nlm, NT = (long)nt * NS;
+    fvrt.assign(NS, 0);
+    fdiv.assign(NS, 0);
+    ftv.assign(NS, 0);
+    ftrc.assign(NT, 0);
+    flnps.assign(nlm, 0);
+    const int nf = iau_nf;
+    const double dt = iau_delthrs * 3600.;
+    if (t < iau_fh[0] * 3600. || t > iau_fh[nf - 1] * 3600.) return;
+    auto one = [&](int n) {
+      for (long q = 0; q < NS; ++q) {
+        fvrt[q] = ivrt[n * NS + q] / dt;
+        fdiv[q] = idiv[n * NS + q] / dt;
+        ftv[q] = itv[n * NS + q] / dt;
+      }
+      for (long q = 0; q < NT; ++q) ftrc[q] = itrc[n * NT + q] / dt;
+      for (long q = 0; q < nlm; ++q) flnps[q] = ilnps[n * nlm + q] / dt;
+    };
+    if (t == 3600. * iau_fh[nf - 1]) return one(nf - 1);
+    if (t == 3600. * iau_fh[0]) return one(0);
+    int n = 0;
+    while (n < nf && !(iau_fh[n] * 3600. > t)) ++n;
+    const double delt = (iau_fh[n] - (t / 3600.)) / (iau_fh[n] - iau_fh[n - 1]);
+    auto mix = [&](const std::vector<cplx>& v, long sz, long q) {
+      return ((1. - delt) * v[n * sz + q] + delt * v[(n - 1) * sz + q]) / dt;
+    };
+    for (long q = 0; q < NS; ++q) {
+      fvrt[q] = mix(ivrt, NS, q);
+      fdiv[q] = mix(idiv, NS, q);
+      ftv[q] = mix(itv, NS, q);
+    }
+    for (long q = 0; q < NT; ++q) ftrc[q] = mix(itrc, NT, q);
+    for (long q = 0; q < nlm; ++q) flnps[q] = mix(ilnps, nlm, q);
+  }
+  void add_iau(cplx* dvrt, cplx* ddiv, cplx* dtv, cplx* dtrc, cplx* dlnps) {
+    if (!iau_nf) return;
+    const long NS = (long)L * nlm, NT = (long)nt * NS;
+    for (long q = 0; q < NS; ++q) {
+      dvrt[q] += fvrt[q];
+      ddiv[q] += fdiv[q];
+      dtv[q] += ftv[q];
+    }
+    for (long q = 0; q < NT; ++q) dtrc[q] += ftrc[q];
+    for (long q = 0; q < nlm; ++q) dlnps[q] += flnps[q];
+  }
+
+  // set_dfi_wts (run.f90:567-588); the angles in single precision
+  static void dfi_wts(int n, double* w) {
+    const float pif = acosf(-1.0f);
+    double tot = 0;
+    for (int k = 0; k <= 2 * n; ++k) {
+      w[k] = 1.;
+      const double sx = pif * (float)(k - n) / (float)n;
+      const double wx = pif * (float)(k - n) / (float)(n + 1);
+      if (k != n) w[k] = sin(wx) / wx * sin(sx) / sx;
+      tot += w[k];
+    }
+    for (int k = 0; k <= 2 * n; ++k) w[k] = w[k] / tot;
+  }
+  // run.f90:58-145 without the file output: the state becomes the
+  // Lanczos-weighted average over 2 ntdfi steps; apcp restarts (init_phydata)
+  void dfi(double t, int ntdfi) {
+    std::vector<double> w(2 * ntdfi + 1);
+    dfi_wts(ntdfi, w.data());
+    std::vector<cplx> av(vrt.size()), ad(div.size()), at(tv.size()), aq(trc.size()), al(lnps.size());
+    auto acc = [&](double wk, bool first) {
+      for (size_t q = 0; q < vrt.size(); ++q) {
+        av[q] = first ? wk * vrt[q] : av[q] + wk * vrt[q];
+        ad[q] = first ? wk * div[q] : ad[q] + wk * div[q];
+        at[q] = first ? wk * tv[q] : at[q] + wk * tv[q];
+      }
+      for (size_t q = 0; q < trc.size(); ++q) aq[q] = first ? wk * trc[q] : aq[q] + wk * trc[q];
+      for (size_t q = 0; q < lnps.size(); ++q) al[q] = first ? wk * lnps[q] : al[q] + wk * lnps[q];
+    };
+    acc(w[0], true);
+    for (int k = 1; k <= 2 * ntdfi; ++k) {
+      advance(t);
+      t += c.dt;
+      acc(w[k], false);
+    }
+    vrt = av, div = ad, tv = at, trc = aq, lnps = al;
+    std::fill(apcp.begin(), apcp.end(), 0.0);
+  }
+
+  // run.f90:194-565 (the stochastic branches but SPPT are out of scope)
+  void advance(double t) {
     if (sppt) sppt_step();
+    if (iau_nf) getiauforcing(t);
     const long NS = (long)L * nlm, NT = (long)nt * L * nlm;
     const double dt = c.dt;
     std::vector<cplx> vrt0 = vrt, div0 = div, tv0 = tv, trc0 = trc, lnps0 = lnps;
@@ -1208,6 +1301,7 @@ struct Dycore {
 
     // stage 1 (run.f90:294-352)
     getdyntend(dvrt0.data(), ddiv0.data(), dtv0.data(), dtrc0.data(), dlnps0.data(), 1, false);
+    add_iau(dvrt0.data(), ddiv0.data(), dtv0.data(), dtrc0.data(), dlnps0.data());
     for (long q = 0; q < NS; ++q) vrt[q] = vrt0[q] + A21 * dt * dvrt0[q];
     for (long q = 0; q < NT; ++q) trc[q] = trc0[q] + A21 * dt * dtrc0[q];
     if (c.explicit_) {
@@ -1232,6 +1326,7 @@ struct Dycore {
     }
     // stage 2 (run.f90:354-418)
     getdyntend(dvrt1.data(), ddiv1.data(), dtv1.data(), dtrc1.data(), dlnps1.data(), 2, false);
+    add_iau(dvrt1.data(), ddiv1.data(), dtv1.data(), dtrc1.data(), dlnps1.data());
     for (long q = 0; q < NS; ++q) vrt[q] = vrt0[q] + dt * (A31 * dvrt0[q] + A32 * dvrt1[q]);
     for (long q = 0; q < NT; ++q) trc[q] = trc0[q] + dt * (A31 * dtrc0[q] + A32 * dtrc1[q]);
     if (c.explicit_) {
@@ -1256,6 +1351,7 @@ struct Dycore {
     }
     // stage 3 (run.f90:420-490)
     getdyntend(dvrt2.data(), ddiv2.data(), dtv2.data(), dtrc2.data(), dlnps2.data(), 3, false);
+    add_iau(dvrt2.data(), ddiv2.data(), dtv2.data(), dtrc2.data(), dlnps2.data());
     for (long q = 0; q < NS; ++q) vrt[q] = vrt0[q] + dt * (B1 * dvrt0[q] + B2 * dvrt1[q] + B3 * dvrt2[q]);
     for (long q = 0; q < NT; ++q) trc[q] = trc0[q] + dt * (B1 * dtrc0[q] + B2 * dtrc1[q] + B3 * dtrc2[q]);
     if (c.explicit_) {
@@ -1530,6 +1626,32 @@ void ora_damp(void* h, double* disspec, double* diff_prof, double* dmp_prof) {
 }
 
 void ora_diag(void* h, double* out5) { D(h)->diag(out5); }
+
+void ora_set_iau(void* h, int nf, const double* fhrs, double delthrs, const double* vrt, const double* div,
+                 const double* tv, const double* trc, const double* lnps) {
+  Dycore* d = D(h);
+  d->iau_nf = nf;
+  if (!nf) return;
+  const long NS = (long)d->L * d->nlm, NT = (long)d->nt * NS;
+  d->iau_fh.assign(fhrs, fhrs + nf);
+  d->iau_delthrs = delthrs;
+  d->ivrt.assign(C(vrt), C(vrt) + nf * NS);
+  d->idiv.assign(C(div), C(div) + nf * NS);
+  d->itv.assign(C(tv), C(tv) + nf * NS);
+  d->itrc.assign(NT ? C(trc) : nullptr, NT ? C(trc) + nf * NT : nullptr);
+  d->ilnps.assign(C(lnps), C(lnps) + nf * d->nlm);
+}
+void ora_getiauforcing(void* h, double t, double* dvrt, double* ddiv, double* dtv, double* dtrc, double* dlnps) {
+  Dycore* d = D(h);
+  d->getiauforcing(t);
+  std::copy(d->fvrt.begin(), d->fvrt.end(), C(dvrt));
+  std::copy(d->fdiv.begin(), d->fdiv.end(), C(ddiv));
+  std::copy(d->ftv.begin(), d->ftv.end(), C(dtv));
+  if (dtrc) std::copy(d->ftrc.begin(), d->ftrc.end(), C(dtrc));
+  std::copy(d->flnps.begin(), d->flnps.end(), C(dlnps));
+}
+void ora_dfi(void* h, double t, int ntdfi) { D(h)->dfi(t, ntdfi); }
+void ora_dfi_weights(int ntdfi, double* w) { Dycore::dfi_wts(ntdfi, w); }
 
 void ora_simple_columns(int ncol, int n, double dtime, const double* lat, double* t, double* q, double* u, double* v,
                         const double* pmid, const double* pint, const double* ps, double* precl, int test,

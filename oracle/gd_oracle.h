@@ -84,6 +84,13 @@ void ora_damp(void* h, double* disspec, double* diff_prof, double* dmp_prof);
 void ora_diag(void* h, double* out5);
 /* HS forcing tendencies from current grid state (phy_run_hs.f90:22) */
 void ora_getphytend(void* h, double* dvrt, double* ddiv, double* dtv, double* dtrc, double* dlnps);
+/* IAU increments [nf][...] (iau_module.f90), nf = 0 detaches; the forcing of time t;
+   digital filter over 2 ntdfi steps (run.f90:58-145) and its weights */
+void ora_set_iau(void* h, int nf, const double* fhrs, double delthrs, const double* vrt, const double* div,
+                 const double* tv, const double* trc, const double* lnps);
+void ora_getiauforcing(void* h, double t, double* dvrt, double* ddiv, double* dtv, double* dtrc, double* dlnps);
+void ora_dfi(void* h, double t, int ntdfi);
+void ora_dfi_weights(int ntdfi, double* w);
 /* simple_physics_v5_1.f90 on ncol independent columns [ncol][n] top to
    bottom (pint [ncol][n+1]); t, q, u, v updated in place, precl out (m/s) */
 void ora_simple_columns(int ncol, int n, double dtime, const double* lat, double* t, double* q, double* u, double* v,

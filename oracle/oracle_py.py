@@ -233,10 +233,43 @@ class Oracle:
         lib().ora_damp(self.h, _p(dis), _p(dp), _p(mp))
         return dict(disspec=dis, diff_prof=dp, dmp_prof=mp)
 
+    def set_iau(self, fhrs, delthrs=6.0, vrt=None, div=None, tv=None, trc=None, lnps=None):
+        """IAU increments with a leading file axis (iau_module.f90); fhrs=None detaches."""
+        L = lib()
+        L.ora_set_iau.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_double] + [
+            ctypes.c_void_p] * 5
+        if fhrs is None:
+            L.ora_set_iau(self.h, 0, None, delthrs, None, None, None, None, None)
+            return
+        c = lambda a: None if a is None else np.ascontiguousarray(a, np.complex128)
+        self._iau = [np.ascontiguousarray(fhrs, np.float64)] + [c(x) for x in (vrt, div, tv, trc, lnps)]
+        L.ora_set_iau(self.h, len(self._iau[0]), *[_p(self._iau[0])], delthrs, *[_p(x) for x in self._iau[1:]])
+
+    def getiauforcing(self, t):
+        L_, n = self.nlev, self.nlm
+        d = [np.zeros((L_, n), np.complex128) for _ in range(3)]
+        dtrc = np.zeros((max(self.ntrac, 1), L_, n), np.complex128)
+        dl = np.zeros(n, np.complex128)
+        L = lib()
+        L.ora_getiauforcing.argtypes = [ctypes.c_void_p, ctypes.c_double] + [ctypes.c_void_p] * 5
+        L.ora_getiauforcing(self.h, t, _p(d[0]), _p(d[1]), _p(d[2]), _p(dtrc) if self.ntrac else None, _p(dl))
+        return dict(dvrt=d[0], ddiv=d[1], dtv=d[2], dtrc=dtrc[: self.ntrac], dlnps=dl)
+
+    def dfi(self, ntdfi, t=0.0):
+        L = lib()
+        L.ora_dfi.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
+        L.ora_dfi(self.h, t, ntdfi)
+
     def diag(self):
         o = np.zeros(5)
         lib().ora_diag(self.h, _p(o))
         return dict(spdmax=o[0], psmin=o[1], psmax=o[2], pstend=o[3], pdryini=o[4])
+
+
+def dfi_weights(ntdfi):
+    w = np.zeros(2 * ntdfi + 1)
+    lib().ora_dfi_weights(int(ntdfi), _p(w))
+    return w
 
 
 def simple_columns(dtime, lat, t, q, u, v, pmid, pint, ps, test, turbflux):

@@ -131,8 +131,20 @@ def work_counts(T, nlon, nlat, L, nt, rsize):
         ((3 * L + 1) * ng * rsize + (3 * L + 1) * (T + 1) * nlat * cbytes)
     col_in = (7 + 3 * nt) * L + 3
     col_bytes = 3 * (col_in + r2c_rows) * ng * rsize + (5 * L + 3) * ng * rsize
+
+    # Legendre GEMM launches: each reads (synthesis) or writes (analysis) its
+    # real columns of the spectral array (nlm rows) and writes or reads them in
+    # the Fourier array ((T+1) orders x nlat), and reads the table (hi and lo
+    # copies in the split modes, nlm x nlat/2 each)
+    def leg(ncomplex, tables):
+        return 2 * ncomplex * (nlm + (T + 1) * nlat) * rsize + tables * nlm * (nlat // 2) * rsize
+
+    ntab = 2 if rsize == 4 else 1
+    legendre_launches = [ncolS, ncolS - 2 * L] * 4 + [(4 + nt) * L + 1, 2 * L] * 3 + [3 * L + 1]
+    legendre_bytes = sum(leg(c, ntab) for c in legendre_launches)
     return dict(legendre_flop=cols * scalar_flop, legendre_cols=cols, c2r_bytes=c2r_bytes, r2c_bytes=r2c_bytes,
-                col_bytes=col_bytes, scalar_flop=scalar_flop)
+                col_bytes=col_bytes, scalar_flop=scalar_flop, legendre_bytes=legendre_bytes,
+                legendre_launches=len(legendre_launches))
 
 
 def gpu_arm(args):
@@ -237,23 +249,33 @@ def gpu_arm(args):
     wc = work_counts(T, nlon, nlat, L, nt, rsize)
     dom = max(phases, key=phases.get)
     leg_ms = phases["legendre_synth"] + phases["legendre_anal"]
-    if dom in ("legendre_synth", "legendre_anal") or leg_ms >= max(phases.values()):
-        achieved = wc["legendre_flop"] / (leg_ms * 1e-3) / 1e12
-        roof = dict(kernel="legendre GEMMs (synthesis+analysis)", bound="tensor", achieved=achieved,
-                    peak=pk["bf16"], unit="TFLOP/s", frac=achieved / pk["bf16"], traffic=None,
-                    peak_source=pk["src"] + " bf16 burst",
-                    note="SIMT FMA path; tensor peak shown for scale" if args.precision in ("fp32", "fp64") else "")
-        if args.precision in ("tf32x3", "bf16x3"):
-            # three products are issued per algorithmic one
-            roof["issued_tflops"] = 3 * achieved
+    if args.precision in ("tf32x3", "bf16x3") and (dom in ("legendre_synth", "legendre_anal")
+                                                  or leg_ms >= max(phases.values())):
+        # The split-precision Legendre GEMM issues 3 products per algorithmic one: 6 flop per
+        # (coefficient, latitude pair) against ~4 bytes of array traffic per coefficient and column, an
+        # intensity (~140 flop/B at T574 with the tables) below this GPU's kind::tf32 balance point
+        # (1290 TFLOP/s / 6.8 TB/s ~ 190 flop/B): the HBM roof is the lower one.
+        nl = wc["legendre_launches"]
+        achieved = wc["legendre_bytes"] / (leg_ms * 1e-3) / 1e9
+        flops = wc["legendre_flop"] / (leg_ms * 1e-3) / 1e12
+        roof = dict(kernel="k_tc_gemm_f (Legendre synthesis+analysis, orders m >= 1)", bound="hbm",
+                    achieved=achieved, peak=pk["hbm"], unit="GB/s", frac=achieved / pk["hbm"], traffic=None,
+                    peak_source=pk["src"], algorithmic_bytes_per_launch=wc["legendre_bytes"] / nl,
+                    ms_per_launch=leg_ms / nl, algorithmic_tflops=flops, issued_tflops=3 * flops)
+        if args.precision == "tf32x3":
+            # the kind::tf32 rate measured on this GPU with a tcgen05.mma throughput probe
+            roof["tf32_tflops_measured"] = 1290.0
+            roof["tensor_frac_of_tf32"] = 3 * flops / 1290.0
         if args.precision == "tf32x3" and name == "T574L64":
             # DRAM bytes per k_tc_gemm_f launch, averaged over the four launches of a dynamics stage, from
             # a single-pass ncu capture of dram__bytes_read.sum + dram__bytes_write.sum on this workload
-            # (they equal the algorithmic bytes to within 2%)
             roof["traffic"] = 2.13e9
             roof["traffic_unit"] = "bytes per launch (ncu)"
-            # the kind::tf32 rate measured on this GPU with a tcgen05.mma throughput probe
-            roof["tf32_tflops_measured"] = 1290.0
+    elif dom in ("legendre_synth", "legendre_anal") or leg_ms >= max(phases.values()):
+        achieved = wc["legendre_flop"] / (leg_ms * 1e-3) / 1e12
+        roof = dict(kernel="legendre GEMMs (synthesis+analysis)", bound="tensor", achieved=achieved,
+                    peak=pk["bf16"], unit="TFLOP/s", frac=achieved / pk["bf16"], traffic=None,
+                    peak_source=pk["src"] + " bf16 burst", note="SIMT FMA path; tensor peak shown for scale")
     else:
         key = {"fft_synth": "c2r_bytes", "fft_anal": "r2c_bytes", "columns": "col_bytes"}.get(dom)
         byt = wc[key] if key else None

@@ -572,7 +572,7 @@ class Dycore : public DycoreBase {
     diagbuf = dalloc<double>(4 * nlat);
     diagout = dalloc<double>(8);
     GD_CUDA(cudaMemcpyAsync(pdryini, &c.pdryini, sizeof(double), cudaMemcpyHostToDevice, stream));
-    auto items = make_stage_items(T, 16);
+    auto items = make_stage_items(T, GD_STAGE_QC);
     nstage_items = (int)items.size();
     stage_items = upload(items);
   }

@@ -9,7 +9,7 @@
 
 namespace gd {
 
-constexpr int QC = 16;  // spectral coefficients (same degree n) per CTA
+constexpr int QC = GD_STAGE_QC;  // spectral coefficients (same degree n) per CTA
 static_assert(QC % 4 == 0, "the matvec works on groups of four coefficients");
 
 std::vector<int4> make_stage_items(int T, int qc) {
@@ -94,7 +94,7 @@ __device__ __forceinline__ void raw_tend(const StageArgs<R>& a, long idx, int k,
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_stage(StageArgs<R> a) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? GD_STAGE_MINB : 2) k_stage(StageArgs<R> a) {
   typedef typename C2<R>::T V;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int L = a.L;

@@ -58,6 +58,13 @@ struct StageArgs {
   APCols ap;
   AHCols ah;
 };
+// coefficients of one degree per stage CTA, and the FP32 stage kernel's resident CTAs per SM
+#ifndef GD_STAGE_QC
+#define GD_STAGE_QC 16
+#endif
+#ifndef GD_STAGE_MINB
+#define GD_STAGE_MINB 4
+#endif
 std::vector<int4> make_stage_items(int T, int qc);
 template <typename R>
 void launch_stage(const StageArgs<R>& a, cudaStream_t s);

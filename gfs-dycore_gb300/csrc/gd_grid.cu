@@ -322,6 +322,16 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_dyn_columns(Col
     R qm = Q(b0 - 1), q0 = Q(b0), q1 = Q(b0 + 1), q2 = Q(b0 + 2);
     // limited value at the bottom interface of level b0 (half[L] = q[0])
     R hb = (b0 == 0) ? q0 : half_at(L - b0, L, Q(b0 - 2), qm, q0, q1, ETA(L - b0));
+    // the horizontal gradients of the block's levels, loaded ahead of their use
+    R gqx[LB], gqy[LB];
+#pragma unroll
+    for (int i = 0; i < LB; ++i) {
+      gqx[i] = gqy[i] = R(0);
+      if (i < nb) {
+        gqx[i] = S(a.s.dqdx + iq * L + b0 + i);
+        gqy[i] = S(a.s.dqdy + iq * L + b0 + i);
+      }
+    }
 #pragma unroll
     for (int i = 0; i < LB; ++i) {
       if (i >= nb) continue;
@@ -330,7 +340,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_dyn_columns(Col
       const R ht = (t == 0) ? q0 : half_at(t, L, qm, q0, q1, q2, e0);
       const R idp = idpa[i];
       const R vadq = idp * ((hb * e1 - ht * e0) + (q0 * (e0 - e1)));
-      A(a.a.qtend + iq * L + b, -uu[i] * S(a.s.dqdx + iq * L + b) - vv[i] * S(a.s.dqdy + iq * L + b) - vadq);
+      A(a.a.qtend + iq * L + b, -uu[i] * gqx[i] - vv[i] * gqy[i] - vadq);
       hb = ht;
       qm = q0;
       q0 = q1;

@@ -1115,29 +1115,53 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
     sb = (long)nlat * ld;
   }
   V* brow = buf + r * RP;
-  for (int kk = kq; kk <= M / 2; kk += KS) {
+  // the gather issues the loads of CB consecutive orders of the thread
+  // before using any of them: the loads are latency-bound, not issue-bound
+  constexpr int CB = 4;
+  for (int kb = kq; kb <= M / 2; kb += CB * KS) {
+    const V zz = mk2<R>(R(0), R(0));
+    V la1[CB], la2[CB], lb1[CB], lb2[CB];
+#pragma unroll
+    for (int c = 0; c < CB; ++c) {
+      const int kk = kb + c * KS, k2 = M - kk;
+      la1[c] = la2[c] = lb1[c] = lb2[c] = zz;
+      if (kk <= M / 2 && live && kk <= T) {
+        if (pa) {
+          la1[c] = *reinterpret_cast<const V*>(pa + kk * sa);
+          if (kk > 0 && k2 <= T) la2[c] = *reinterpret_cast<const V*>(pa + k2 * sa);
+        }
+        if (pb) {
+          lb1[c] = *reinterpret_cast<const V*>(pb + kk * sb);
+          if (kk > 0 && k2 <= T) lb2[c] = *reinterpret_cast<const V*>(pb + k2 * sb);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < CB; ++c) {
+    const int kk = kb + c * KS;
+    if (kk > M / 2) break;
     const int k2 = M - kk;
     V z1 = mk2<R>(R(0), R(0)), z2 = z1;
     if (live && kk <= T) {  // kk > T: both orders above the truncation, z = 0
       // x_k = alpha A_k + beta (i k / cos) B_k, zero above the truncation
       V x1 = z1, x2 = z1;
       if (pa) {
-        const V v1 = *reinterpret_cast<const V*>(pa + kk * sa);
+        const V v1 = la1[c];
         x1.x = alpha * v1.x;
         x1.y = alpha * v1.y;
         if (kk > 0 && k2 <= T) {
-          const V v2 = *reinterpret_cast<const V*>(pa + k2 * sa);
+          const V v2 = la2[c];
           x2.x = alpha * v2.x;
           x2.y = alpha * v2.y;
         }
       }
       if (pb) {
-        const V v1 = *reinterpret_cast<const V*>(pb + kk * sb);
+        const V v1 = lb1[c];
         const R f1 = beta * (R)kk * rc;
         x1.x -= f1 * v1.y;
         x1.y += f1 * v1.x;
         if (kk > 0 && k2 <= T) {
-          const V v2 = *reinterpret_cast<const V*>(pb + k2 * sb);
+          const V v2 = lb2[c];
           const R f2 = beta * (R)k2 * rc;
           x2.x -= f2 * v2.y;
           x2.y += f2 * v2.x;
@@ -1157,6 +1181,7 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
     }
     brow[pad_addr<M, M1>(kk)] = z1;
     if (kk > 0 && k2 != kk) brow[pad_addr<M, M1>(k2)] = z2;
+    }
   }
   __syncthreads();
   fft4<R, M, M1, M2, NR, NT, +1>(buf, d.twM);

@@ -230,7 +230,7 @@ def gpu_arm(args):
         g.set_state(pinned["vrt"], pinned["div"], pinned["tv"], pinned["lnps"], trc=pinned.get("trc"))
         g.advance(1)
     barrier()
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = max(1, min(args.steps, 10))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         g._chk(lib.gd_set_state(g.h, P(pinned["vrt"]), P(pinned["div"]), P(pinned["tv"]),

@@ -41,42 +41,34 @@ __device__ __forceinline__ float clog(float a) { return __logf(a); }
 // Thuburn (1993) limited half-level value at interior interface k
 // (dyn_run.f90:574-590): qa = level above the interface, qb = level below,
 // dm = dd[k-1], d0 = dd[k], dp = dd[k+1], upwind by the sign of etadot.
+// Both upwind cases in one path: the columns of a warp differ in the sign.
 template <typename R>
 __device__ __forceinline__ R thuburn_half(R qa, R qb, R dm, R d0, R dp, R eta) {
-  R h = R(0.5) * (qb + qa);
-  if (eta > R(0)) {
-    const R phi = cdiv(dm, d0);
-    h = qa + cdiv(phi + fabs(phi), R(1) + fabs(phi)) * (h - qa);
-  } else {
-    const R phi = cdiv(dp, d0);
-    h = qb + cdiv(phi + fabs(phi), R(1) + fabs(phi)) * (h - qb);
-  }
-  return h;
+  const R h = R(0.5) * (qb + qa);
+  const bool up = eta > R(0);
+  const R qu = up ? qa : qb;
+  const R phi = cdiv(up ? dm : dp, d0);
+  return qu + cdiv(phi + fabs(phi), R(1) + fabs(phi)) * (h - qu);
 }
 
-// Limited tracer value at interior interface t (0 < t < L) whose level
-// below is b = L-1-t: qm = q[b-1], q0 = q[b], q1 = q[b+1], q2 = q[b+2].
-// dd[k] = q(level below k) - q(level above k), clamped away from zero;
-// the one-sided boundary differences of dyn_run.f90:507-518.
+// dd[k] = q(level below k) - q(level above k) at interior interface k,
+// clamped away from zero (dyn_run.f90:519-524)
 template <typename R>
-__device__ __forceinline__ R half_at(int t, int L, R qm, R q0, R q1, R q2, R eta) {
+__device__ __forceinline__ R dd_mid(R qbelow, R qabove) {
   const R eps = epstiny_of<R>();
-  R dm, d0, dp;
-  if (t == 1) {  // dd[0], top boundary
-    dm = (q1 >= R(0)) ? q1 - fmax(R(0), R(2) * q1 - q0) : q1 - fmin(R(0), R(2) * q1 - q0);
-  } else {
-    dm = q1 - q2;
-    if (fabs(dm) < eps) dm = copysign(eps, dm);
-  }
-  d0 = q0 - q1;
-  if (fabs(d0) < eps) d0 = copysign(eps, d0);
-  if (t + 1 == L) {  // dd[L], bottom boundary
-    dp = (q0 >= R(0)) ? fmax(R(0), R(2) * q0 - q1) - q0 : fmin(R(0), R(2) * q0 - q1) - q0;
-  } else {
-    dp = qm - q0;
-    if (fabs(dp) < eps) dp = copysign(eps, dp);
-  }
-  return thuburn_half(q1, q0, dm, d0, dp, eta);
+  const R d = qbelow - qabove;
+  return (fabs(d) < eps) ? copysign(eps, d) : d;
+}
+// one-sided boundary differences (dyn_run.f90:507-518): dd[0] from the top
+// level qt and the one below it, dd[L] from the bottom level qb and the one
+// above it
+template <typename R>
+__device__ __forceinline__ R dd_top(R qt, R qn) {
+  return (qt >= R(0)) ? qt - fmax(R(0), R(2) * qt - qn) : qt - fmin(R(0), R(2) * qt - qn);
+}
+template <typename R>
+__device__ __forceinline__ R dd_bottom(R qb, R qn) {
+  return (qb >= R(0)) ? fmax(R(0), R(2) * qb - qn) - qb : fmin(R(0), R(2) * qb - qn) - qb;
 }
 
 // Level-parallel column kernel.  A CTA owns 32 adjacent grid columns (one per
@@ -97,11 +89,16 @@ __device__ __forceinline__ R half_at(int t, int L, R qm, R q0, R q1, R q2, R eta
 //      (getvadv_tracers, :478-603) and horizontal advection.
 // Levels are indexed b bottom (0) to top; interface quantities t top (0)
 // to bottom; layer t = L-1-b.
-// at most 8 warps (LB is chosen so), and 4 resident CTAs per SM for the FP32 state
-template <typename R, int LB>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_dyn_columns(ColumnArgs<R> a, int inverse_only) {
+// at most NWM warps (LB is chosen so); 1024 resident threads per SM for the
+// FP32 state (64 registers), 512 for FP64
+template <typename R, int LB, int NWM>
+__global__ void __launch_bounds__(32 * NWM, (sizeof(R) == 4 ? 32 : 16) / NWM)
+    k_dyn_columns(ColumnArgs<R> a, int inverse_only) {
   extern __shared__ __align__(16) unsigned char smcol[];
-  const int lane = threadIdx.x, w = threadIdx.y, NW = blockDim.y;
+  // the warp's level block: the same for all its lanes (blockDim.x is 32);
+  // taken through a warp reduction so that the compiler knows it too, and
+  // every level index, row offset and branch on a level is warp-uniform
+  const int lane = threadIdx.x, w = (int)__reduce_min_sync(0xffffffffu, threadIdx.y), NW = blockDim.y;
   const int L = a.L;
   const long ng = (long)a.nlon * a.nlat;
   const long pq = (long)blockIdx.x * 32 + lane;
@@ -315,13 +312,12 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_dyn_columns(Col
   }
   if (inverse_only) return;
 
-  // phase 4: tracers
+  // phase 4: tracers, one at a time.  Interface t (top of level b = L-1-t)
+  // has dd[t] = q[b] - q[b+1]; the limited value at t uses dd[t-1], dd[t],
+  // dd[t+1], so each level computes one new difference and carries two.
   for (int iq = 0; iq < a.nt; ++iq) {
     const int r0 = a.s.trc + iq * L;
     auto Q = [&](int b) -> R { return (b >= 0 && b < L) ? S(r0 + b) : R(0); };
-    R qm = Q(b0 - 1), q0 = Q(b0), q1 = Q(b0 + 1), q2 = Q(b0 + 2);
-    // limited value at the bottom interface of level b0 (half[L] = q[0])
-    R hb = (b0 == 0) ? q0 : half_at(L - b0, L, Q(b0 - 2), qm, q0, q1, ETA(L - b0));
     // the horizontal gradients of the block's levels, loaded ahead of their use
     R gqx[LB], gqy[LB];
 #pragma unroll
@@ -332,17 +328,40 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_dyn_columns(Col
         gqy[i] = S(a.s.dqdy + iq * L + b0 + i);
       }
     }
+    const int t0 = L - 1 - b0;
+    R q0 = Q(b0), q1 = Q(b0 + 1), q2 = Q(b0 + 2);
+    // dA = dd[t], dB = dd[t+1] for the level about to be processed; hb =
+    // limited value at its bottom interface t+1 (half[L] = q[0])
+    R dA, dB, hb;
+    if (b0 == 0) {
+      hb = q0;
+      dA = dd_mid(q0, q1);  // unused when L = 1
+      dB = dd_bottom(q0, q1);
+    } else {
+      const R qm = Q(b0 - 1), qmm = Q(b0 - 2);
+      dA = (t0 == 0) ? dd_top(q0, qm) : dd_mid(q0, q1);
+      dB = dd_mid(qm, q0);
+      const R dC = (b0 == 1) ? dd_bottom(qm, q0) : dd_mid(qmm, qm);
+      hb = thuburn_half(q0, qm, dA, dB, dC, ETA(t0 + 1));
+    }
+    R e1 = ETA(t0 + 1);
 #pragma unroll
     for (int i = 0; i < LB; ++i) {
       if (i >= nb) continue;
       const int b = b0 + i, t = L - 1 - b;
-      const R e0 = ETA(t), e1 = ETA(t + 1);
-      const R ht = (t == 0) ? q0 : half_at(t, L, qm, q0, q1, q2, e0);
+      const R e0 = ETA(t);
+      R ht = q0;  // half[0] = q at the top level
+      if (t > 0) {
+        const R dN = (t == 1) ? dd_top(q1, q0) : dd_mid(q1, q2);  // dd[t-1]
+        ht = thuburn_half(q1, q0, dN, dA, dB, e0);
+        dB = dA;
+        dA = dN;
+      }
       const R idp = idpa[i];
       const R vadq = idp * ((hb * e1 - ht * e0) + (q0 * (e0 - e1)));
       A(a.a.qtend + iq * L + b, -uu[i] * gqx[i] - vv[i] * gqy[i] - vadq);
       hb = ht;
-      qm = q0;
+      e1 = e0;
       q0 = q1;
       q1 = q2;
       q2 = Q(b + 3);
@@ -350,26 +369,24 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_dyn_columns(Col
   }
 }
 
-template <typename R, int LB>
+template <typename R, int LB, int NWM>
 static void launch_cols_lb(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t s) {
   const long ng = (long)a.nlon * a.nlat;
   const int nw = ceil_div(a.L, LB);
   const size_t sm = (size_t)(5 * nw + a.L + 1) * 32 * sizeof(R);
   if (sm > 48 * 1024)
-    GD_CUDA(cudaFuncSetAttribute(k_dyn_columns<R, LB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  k_dyn_columns<R, LB><<<(unsigned)ceil_div(ng, 32), dim3(32, nw), sm, s>>>(a, inverse_only ? 1 : 0);
+    GD_CUDA(cudaFuncSetAttribute(k_dyn_columns<R, LB, NWM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_dyn_columns<R, LB, NWM><<<(unsigned)ceil_div(ng, 32), dim3(32, nw), sm, s>>>(a, inverse_only ? 1 : 0);
 }
 
 template <typename R>
 void launch_dyn_columns(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t s) {
   if (a.L < 1 || a.L > LMAX) throw std::runtime_error("nlev out of range for the column kernel");
-  // levels per warp: at most 8 warps per CTA
-  if (a.L <= 32)
-    launch_cols_lb<R, 4>(a, inverse_only, s);
-  else if (a.L <= 64)
-    launch_cols_lb<R, 8>(a, inverse_only, s);
+  // levels per warp: at most 16 warps per CTA
+  if (a.L <= 64)
+    launch_cols_lb<R, 4, 16>(a, inverse_only, s);
   else
-    launch_cols_lb<R, 16>(a, inverse_only, s);
+    launch_cols_lb<R, 8, 16>(a, inverse_only, s);
   count_launch();
   GD_LAUNCH_CHECK();
 }

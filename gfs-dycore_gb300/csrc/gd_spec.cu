@@ -30,35 +30,69 @@ __device__ __forceinline__ V vz() {
 // Y[i][k] = sum_j A[k][j] X[i][j] for i < cnt (complex X, real A).  AT
 // holds A transposed (AT[j][k] = A[k][j]) so a warp's loads of one j are
 // contiguous over k; the L x L matrices stay L1-resident.  X, Y index-major
-// with QC rows.  A thread owns one output level k of four coefficients, so
-// each matrix element it loads feeds eight FMAs; the X reads are warp
-// broadcasts.  Rows past cnt are computed from unused shared memory and
-// not stored.
+// with QC rows.  For even L a thread owns two adjacent output levels of four
+// coefficients: one paired matrix load and four broadcast reads of X feed
+// sixteen FMAs (the shared-memory pipe, not the FMA pipe, bounds this loop).
+// Odd L: one level per thread.  Rows past cnt are computed from unused
+// shared memory and not stored.  Every output sums over j in order, so both
+// forms give the same bits.
 template <typename R, typename V>
 __device__ __forceinline__ void smem_matvec(const R* __restrict__ AT, const V* X, V* Y, int L, int cnt) {
   const int nq = (cnt + 3) >> 2;
-  for (int e = threadIdx.x; e < L * nq; e += blockDim.x) {
-    const int q = e / L, k = e - q * L;
-    const int i0 = 4 * q;
-    R ax[4], ay[4];
+  if (L & 1) {
+    for (int e = threadIdx.x; e < L * nq; e += blockDim.x) {
+      const int q = e / L, k = e - q * L;
+      const int i0 = 4 * q;
+      R ax[4], ay[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) ax[u] = ay[u] = R(0);
+      for (int u = 0; u < 4; ++u) ax[u] = ay[u] = R(0);
+      const V* X0 = X + i0 * L;
+#pragma unroll 4
+      for (int j = 0; j < L; ++j) {
+        const R aj = __ldg(AT + j * L + k);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const V x = X0[u * L + j];
+          ax[u] += aj * x.x;
+          ay[u] += aj * x.y;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (i0 + u < cnt) {
+          Y[(i0 + u) * L + k].x = ax[u];
+          Y[(i0 + u) * L + k].y = ay[u];
+        }
+    }
+    return;
+  }
+  const int Lh = L >> 1;
+  for (int e = threadIdx.x; e < Lh * nq; e += blockDim.x) {
+    const int q = e / Lh, k = 2 * (e - q * Lh);
+    const int i0 = 4 * q;
+    R ax0[4], ay0[4], ax1[4], ay1[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) ax0[u] = ay0[u] = ax1[u] = ay1[u] = R(0);
     const V* X0 = X + i0 * L;
 #pragma unroll 4
     for (int j = 0; j < L; ++j) {
-      const R aj = __ldg(AT + j * L + k);
+      const V aj = __ldg(reinterpret_cast<const V*>(AT + j * L + k));  // A[k][j], A[k+1][j]
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const V x = X0[u * L + j];
-        ax[u] += aj * x.x;
-        ay[u] += aj * x.y;
+        ax0[u] += aj.x * x.x;
+        ay0[u] += aj.x * x.y;
+        ax1[u] += aj.y * x.x;
+        ay1[u] += aj.y * x.y;
       }
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u)
       if (i0 + u < cnt) {
-        Y[(i0 + u) * L + k].x = ax[u];
-        Y[(i0 + u) * L + k].y = ay[u];
+        Y[(i0 + u) * L + k].x = ax0[u];
+        Y[(i0 + u) * L + k].y = ay0[u];
+        Y[(i0 + u) * L + k + 1].x = ax1[u];
+        Y[(i0 + u) * L + k + 1].y = ay1[u];
       }
   }
 }

@@ -105,8 +105,8 @@ __global__ void __launch_bounds__(32 * NWM, (sizeof(R) == 4 ? 32 : 16) / NWM)
   const bool valid = pq < ng;
   const long p = valid ? pq : ng - 1;  // lanes past the end compute a copy and store nothing
   const int j = (int)(p / a.nlon);
-  R* part = reinterpret_cast<R*>(smcol);  // [5][NW][32] block sums
-  R* etas = part + 5 * NW * 32;            // [L+1][32] etadot
+  R* part = reinterpret_cast<R*>(smcol);  // [5][NW][32] block sums, then [2][32] column totals
+  R* etas = part + (5 * NW + 2) * 32;      // [L+1][32] etadot
   auto PART = [&](int q, int ww) -> R& { return part[(q * NW + ww) * 32 + lane]; };
   auto ETA = [&](int t) -> R& { return etas[t * 32 + lane]; };
   const R* gS = a.gS;
@@ -128,6 +128,19 @@ __global__ void __launch_bounds__(32 * NWM, (sizeof(R) == 4 ? 32 : 16) / NWM)
   // pressure and its reciprocal at the bottom interface of the current level,
   // carried upward (the top interface of level i is the bottom one of i + 1)
   R pkb = PK(L - b0), ipkb = crcp(pkb);
+  // the block's inputs, all loads issued before the arithmetic (levels past
+  // the block's end load its last level again and are not used)
+  R lu[LB], lv[LB], ldv[LB], ltv[LB], ltx[LB], lty[LB];
+#pragma unroll
+  for (int i = 0; i < LB; ++i) {
+    const int b = b0 + min(i, nb - 1);
+    lu[i] = S(a.s.u + b);
+    lv[i] = S(a.s.v + b);
+    ldv[i] = S(a.s.div + b);
+    ltv[i] = S(a.s.tv + b);
+    ltx[i] = S(a.s.dtvdx + b);
+    lty[i] = S(a.s.dtvdy + b);
+  }
 #pragma unroll
   for (int i = 0; i < LB; ++i) {
     xdb[i] = R(0);
@@ -138,14 +151,14 @@ __global__ void __launch_bounds__(32 * NWM, (sizeof(R) == 4 ? 32 : 16) / NWM)
       const R ipkt = t > 0 ? crcp(pkt) : R(0), ipk1 = ipkb;
       pkb = pkt;
       ipkb = ipkt;
-      const R cg = S(a.s.u + b) * dlx + S(a.s.v + b) * dly;
-      xdb[i] = S(a.s.div + b) * dp;
+      const R cg = lu[i] * dlx + lv[i] * dly;
+      xdb[i] = ldv[i] * dp;
       xcb[i] = cg * __ldg(dbk + t);
       if (t > 0) {  // terms of the sums over the layers below a layer
         const R rl = clog(cdiv(pkt1, pkt));
-        s2 += (__ldg(bk + t + 1) * ipk1 - __ldg(bk + t) * ipkt) * S(a.s.tv + b);
-        su += rl * S(a.s.dtvdx + b);
-        sv += rl * S(a.s.dtvdy + b);
+        s2 += (__ldg(bk + t + 1) * ipk1 - __ldg(bk + t) * ipkt) * ltv[i];
+        su += rl * ltx[i];
+        sv += rl * lty[i];
       }
       if (a.prs && valid)
         a.prs[(long)b * ng + p] =
@@ -169,23 +182,23 @@ __global__ void __launch_bounds__(32 * NWM, (sizeof(R) == 4 ? 32 : 16) / NWM)
   PART(4, w) = sv;
   __syncthreads();
 
-  // phase 2: offsets from the blocks above (DB, CB) and below (the rest)
-  R dbo = R(0), cbo = R(0), dbt = R(0), cbt = R(0);
-  for (int ww = NW - 1; ww >= 0; --ww) {
-    const R d = PART(0, ww), c = PART(1, ww);
-    if (ww == w) {
-      dbo = dbt;
-      cbo = cbt;
+  // phase 2: offsets from the blocks above (DB, CB) and below (the rest).
+  // Warp q scans quantity q over the blocks in place (exclusive sums; DB
+  // and CB also keep their column totals), then every warp reads its own.
+  for (int q = w; q < 5; q += NW) {
+    R run = R(0);
+    for (int k = 0; k < NW; ++k) {
+      const int ww = q < 2 ? NW - 1 - k : k;
+      const R v = PART(q, ww);
+      PART(q, ww) = run;
+      run += v;
     }
-    dbt += d;
-    cbt += c;
+    if (q < 2) part[(5 * NW + q) * 32 + lane] = run;
   }
-  R S2 = R(0), SU = R(0), SV = R(0);
-  for (int ww = 0; ww < w; ++ww) {
-    S2 += PART(2, ww);
-    SU += PART(3, ww);
-    SV += PART(4, ww);
-  }
+  __syncthreads();
+  const R dbo = PART(0, w), cbo = PART(1, w);
+  const R dbt = part[5 * NW * 32 + lane], cbt = part[(5 * NW + 1) * 32 + lane];
+  R S2 = PART(2, w), SU = PART(3, w), SV = PART(4, w);
   const R dlnpsdt = -dbt / ps - cbt;
 #pragma unroll
   for (int i = 0; i < LB; ++i) {
@@ -373,7 +386,7 @@ template <typename R, int LB, int NWM>
 static void launch_cols_lb(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t s) {
   const long ng = (long)a.nlon * a.nlat;
   const int nw = ceil_div(a.L, LB);
-  const size_t sm = (size_t)(5 * nw + a.L + 1) * 32 * sizeof(R);
+  const size_t sm = (size_t)(5 * nw + 2 + a.L + 1) * 32 * sizeof(R);
   if (sm > 48 * 1024)
     GD_CUDA(cudaFuncSetAttribute(k_dyn_columns<R, LB, NWM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   k_dyn_columns<R, LB, NWM><<<(unsigned)ceil_div(ng, 32), dim3(32, nw), sm, s>>>(a, inverse_only ? 1 : 0);

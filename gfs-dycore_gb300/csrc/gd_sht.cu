@@ -9,6 +9,7 @@
 // (shtns.f90:261,270,303,308,341,348).  Convention: orthonormal harmonics
 // without Condon-Shortley phase (shtns.f90:110), latitudes north to south.
 #include <cstdlib>
+#include <type_traits>
 #include <vector>
 
 #include "gd_kernels.h"
@@ -1032,18 +1033,30 @@ __device__ __forceinline__ void reg_fft(typename C2<R>::T* x, typename C2<R>::T*
   }
 }
 
-// four-step FFT of NR rows held in buf (padded addressing), sign SIGN
-template <typename R, int M, int M1, int M2, int NR, int NT, int SIGN>
-__device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R>::T* __restrict__ tw) {
+// four-step FFT of NR rows held in buf (padded addressing), sign SIGN.
+// LoadA(r, n1, x) fills x[n2] = row r's x[n1 + M1 n2] for step A: from buf
+// (nullptr: the rows are already there) or straight from global memory;
+// StoreB(r, k2, x) takes the outputs X[k2 + M2 k1] of step B (nullptr: back
+// into buf).  Going straight to or from global memory saves one pass over
+// shared memory and one barrier.
+struct Fft4InBuf {};
+template <typename R, int M, int M1, int M2, int NR, int NT, int SIGN, typename LoadA, typename StoreB>
+__device__ __forceinline__ void fft4x(typename C2<R>::T* buf, const typename C2<R>::T* __restrict__ tw, LoadA lda,
+                                      StoreB stb) {
   typedef typename C2<R>::T V;
   constexpr int RP = row_pitch4<M, M1>();
+  constexpr bool a_buf = std::is_same<LoadA, Fft4InBuf>::value, b_buf = std::is_same<StoreB, Fft4InBuf>::value;
   // step A: thread (r, n1) -> M2-point DFT over n2 of x[n1 + M1 n2], twiddle, store in place
   for (int e = threadIdx.x; e < NR * M1; e += NT) {
     const int r = e / M1, n1 = e - r * M1;
     V* row = buf + r * RP;
     V x[M2], y[M2];
+    if constexpr (a_buf) {
 #pragma unroll
-    for (int n2 = 0; n2 < M2; ++n2) x[n2] = row[n1 + (M1 + 1) * n2];  // pad_addr(n1 + M1 n2), n1 < M1
+      for (int n2 = 0; n2 < M2; ++n2) x[n2] = row[n1 + (M1 + 1) * n2];  // pad_addr(n1 + M1 n2), n1 < M1
+    } else {
+      lda(r, n1, x);
+    }
     reg_fft<R, M2, M, SIGN>(x, y);
 #pragma unroll
     for (int k2 = 1; k2 < M2; ++k2) {
@@ -1068,13 +1081,21 @@ __device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R
     for (int n1 = 0; n1 < M1; ++n1) x[n1] = row[n1];
     reg_fft<R, M1, M, SIGN>(x, y);
   }
-  __syncthreads();
-  if (e < NR * M2) {
-    V* row = buf + r * RP;
+  if constexpr (b_buf) {
+    __syncthreads();
+    if (e < NR * M2) {
+      V* row = buf + r * RP;
 #pragma unroll
-    for (int k1 = 0; k1 < M1; ++k1) row[pad_addr<M, M1>(k2 + M2 * k1)] = x[k1];
+      for (int k1 = 0; k1 < M1; ++k1) row[pad_addr<M, M1>(k2 + M2 * k1)] = x[k1];
+    }
+    __syncthreads();
+  } else {
+    if (e < NR * M2) stb(r, k2, x);
   }
-  __syncthreads();
+}
+template <typename R, int M, int M1, int M2, int NR, int NT, int SIGN>
+__device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R>::T* __restrict__ tw) {
+  fft4x<R, M, M1, M2, NR, NT, SIGN>(buf, tw, Fft4InBuf{}, Fft4InBuf{});
 }
 
 // Minimum resident CTAs per SM: these kernels are latency-bound and run
@@ -1184,25 +1205,17 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
     }
   }
   __syncthreads();
-  fft4<R, M, M1, M2, NR, NT, +1>(buf, d.twM);
-  // store: two complex values (n even, n + 1; adjacent in the padded row)
-  // per store, NR * M / 2 stores spread evenly over the threads
-  constexpr int NS = NR * M / 2;
-#pragma unroll 4
-  for (int it = 0; it < (NS + NT - 1) / NT; ++it) {
-    const int e = threadIdx.x + it * NT;
-    const int rr = e / (M / 2), q = e - rr * (M / 2);
-    if (e < NS && rr < nr) {
-      const int pn = rr * RP + pad_addr<M, M1>(2 * q);
-      const V u = buf[pn], w = buf[pn + 1];
-      V4 o;
-      o.x = u.x;
-      o.y = u.y;
-      o.z = w.x;
-      o.w = w.y;
-      *reinterpret_cast<V4*>(grid + ((long)(ds.dst + r0 + rr) * nlat + j) * nlon + 4 * q) = o;
+  // step B stores its outputs straight to the grid row: z[n] is the real
+  // pair (x[2n], x[2n+1]); a warp's lanes hold consecutive n of a row
+  R* const gout = grid + ((long)(ds.dst + r0) * nlat + j) * nlon;
+  const long rstride = (long)nlat * nlon;
+  fft4x<R, M, M1, M2, NR, NT, +1>(buf, d.twM, Fft4InBuf{}, [&](int rr, int k2, const V* x) {
+    if (rr < nr) {
+      V* o = reinterpret_cast<V*>(gout + rr * rstride) + k2;
+#pragma unroll
+      for (int k1 = 0; k1 < M1; ++k1) o[M2 * k1] = x[k1];
     }
-  }
+  });
 }
 
 template <typename R, int M, int M1, int M2>
@@ -1220,32 +1233,20 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
   const AnalDesc ds = descs[jb.x];
   const int j = blockIdx.y, r0 = jb.y;
   const int nr = min(NR, ds.count - r0);
-  // load: two complex values per load, NR * M / 2 loads spread evenly over
-  // the threads, in batches issued ahead of their use; rows past nr zero
-  constexpr int NE = NR * M / 2, NIT = (NE + NT - 1) / NT, GB = 3;
-  for (int it0 = 0; it0 < NIT; it0 += GB) {
-    V4 z[GB];
+  // step A loads its inputs straight from the grid row: x[n] is the real
+  // pair (g[2n], g[2n+1]); rows past nr are zero
+  const R* const gin = grid + ((long)(ds.src + r0) * nlat + j) * nlon;
+  const long rstride = (long)nlat * nlon;
+  fft4x<R, M, M1, M2, NR, NT, -1>(buf, d.twM, [&](int rr, int n1, V* x) {
+    if (rr < nr) {
+      const V* g = reinterpret_cast<const V*>(gin + rr * rstride) + n1;
 #pragma unroll
-    for (int u = 0; u < GB; ++u) {
-      const int e = threadIdx.x + (it0 + u) * NT;
-      z[u].x = z[u].y = z[u].z = z[u].w = R(0);
-      if (it0 + u < NIT && e < NE) {
-        const int rr = e / (M / 2), q = e - rr * (M / 2);
-        if (rr < nr) z[u] = *reinterpret_cast<const V4*>(grid + ((long)(ds.src + r0 + rr) * nlat + j) * nlon + 4 * q);
-      }
-    }
+      for (int n2 = 0; n2 < M2; ++n2) x[n2] = g[M1 * n2];
+    } else {
 #pragma unroll
-    for (int u = 0; u < GB; ++u) {
-      const int e = threadIdx.x + (it0 + u) * NT;
-      if (it0 + u >= NIT || e >= NE) continue;
-      const int rr = e / (M / 2), q = e - rr * (M / 2);
-      const int pn = rr * RP + pad_addr<M, M1>(2 * q);
-      buf[pn] = mk2<R>(z[u].x, z[u].y);
-      buf[pn + 1] = mk2<R>(z[u].z, z[u].w);
+      for (int n2 = 0; n2 < M2; ++n2) x[n2] = mk2<R>(R(0), R(0));
     }
-  }
-  __syncthreads();
-  fft4<R, M, M1, M2, NR, NT, -1>(buf, d.twM);
+  }, Fft4InBuf{});
   const R wn = d.wn[j] * R(0.5), rc = d.rcos[j];
   const int r = threadIdx.x % NR, kq = threadIdx.x / NR;
   if (r >= nr) return;

@@ -419,23 +419,40 @@ __global__ void __launch_bounds__(256) k_hs(HsArgs<R> a) {
   const R sl = a.sinlat[j], cl = a.coslat[j];
   const R s2 = sl * sl, c2 = cl * cl, c4 = c2 * c2;
   const R p0 = R(1.e5);
-  for (int b = 0; b < L; ++b) {
-    const int t = L - 1 - b;
-    const R pkt = a.ak[t] + a.bk[t] * ps, pkt1 = a.ak[t + 1] + a.bk[t + 1] * ps;
-    const R prs =
-        pow((pow(pkt1, a.kappa) * pkt1 - pow(pkt, a.kappa) * pkt) / ((a.kappa + R(1)) * (pkt1 - pkt)), R(1) / a.kappa);
-    R bl = prs / ps;
-    R teq = pow(prs / p0, a.expo) * (R(315) - R(60) * s2 - R(10) * log(prs / p0) * c2);
-    bl = (bl - a.sigbot) / (R(1) - a.sigbot);
-    if (bl < R(0)) bl = R(0);
-    if (teq < R(200)) teq = R(200);
-    const R tv = a.gS[(long)(a.s.tv + b) * ng + p];
-    const R vr = a.gS[(long)(a.s.vrt + b) * ng + p];
-    const R dv = a.gS[(long)(a.s.div + b) * ng + p];
-    const R f = a.sppt ? R(1) + a.vfact[b] * a.sppt[p] : R(1);
-    a.gA[(long)b * ng + p] = f * ((a.krada + (a.kradb - a.krada) * bl * c4) * (teq - tv));
-    a.gA[(long)(L + b) * ng + p] = f * (-(bl * a.kdrag) * vr);
-    a.gA[(long)(2 * L + b) * ng + p] = f * (-(bl * a.kdrag) * dv);
+  // levels in groups of four: the group's grid loads are issued before its
+  // arithmetic, and pk^kappa of an interface is carried from the level below
+  // (the bottom interface of a level is the top one of the level under it)
+  constexpr int G = 4;
+  R pw1 = pow(a.ak[L] + a.bk[L] * ps, a.kappa);
+  for (int b0 = 0; b0 < L; b0 += G) {
+    R tvv[G], vrv[G], dvv[G];
+#pragma unroll
+    for (int u = 0; u < G; ++u) {
+      const int b = min(b0 + u, L - 1);
+      tvv[u] = a.gS[(long)(a.s.tv + b) * ng + p];
+      vrv[u] = a.gS[(long)(a.s.vrt + b) * ng + p];
+      dvv[u] = a.gS[(long)(a.s.div + b) * ng + p];
+    }
+#pragma unroll
+    for (int u = 0; u < G; ++u) {
+      const int b = b0 + u;
+      if (b >= L) break;
+      const int t = L - 1 - b;
+      const R pkt = a.ak[t] + a.bk[t] * ps, pkt1 = a.ak[t + 1] + a.bk[t + 1] * ps;
+      const R pw0 = pow(pkt, a.kappa);
+      const R prs = pow((pw1 * pkt1 - pw0 * pkt) / ((a.kappa + R(1)) * (pkt1 - pkt)), R(1) / a.kappa);
+      pw1 = pw0;
+      R bl = prs / ps;
+      R teq = pow(prs / p0, a.expo) * (R(315) - R(60) * s2 - R(10) * log(prs / p0) * c2);
+      bl = (bl - a.sigbot) / (R(1) - a.sigbot);
+      if (bl < R(0)) bl = R(0);
+      if (teq < R(200)) teq = R(200);
+      const R tv = tvv[u], vr = vrv[u], dv = dvv[u];
+      const R f = a.sppt ? R(1) + a.vfact[b] * a.sppt[p] : R(1);
+      a.gA[(long)b * ng + p] = f * ((a.krada + (a.kradb - a.krada) * bl * c4) * (teq - tv));
+      a.gA[(long)(L + b) * ng + p] = f * (-(bl * a.kdrag) * vr);
+      a.gA[(long)(2 * L + b) * ng + p] = f * (-(bl * a.kdrag) * dv);
+    }
   }
 }
 template <typename R>

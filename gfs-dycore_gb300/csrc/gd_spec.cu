@@ -194,11 +194,13 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? GD_STAGE_MINB : 2) k_sta
       dtv.x -= dtl.x;
       dtv.y -= dtl.y;
     }
-    st2(TDs, idx, a.ldTD, a.tc.dvrt + k, dvrt);
-    st2(TDs, idx, a.ldTD, a.tc.ddiv + k, ddiv);
-    st2(TDs, idx, a.ldTD, a.tc.dtv + k, dtv);
-    st2(TDs, idx, a.ldTD, a.tc.ddl + k, ddl);
-    st2(TDs, idx, a.ldTD, a.tc.dtl + k, dtl);
+    if (!a.final_) {  // the last stage's tendencies feed no later stage
+      st2(TDs, idx, a.ldTD, a.tc.dvrt + k, dvrt);
+      st2(TDs, idx, a.ldTD, a.tc.ddiv + k, ddiv);
+      st2(TDs, idx, a.ldTD, a.tc.dtv + k, dtv);
+      st2(TDs, idx, a.ldTD, a.tc.ddl + k, ddl);
+      st2(TDs, idx, a.ldTD, a.tc.dtl + k, dtl);
+    }
     V vr = ldg2(a.S0, idx, a.ldS, a.sc.vrt + k), dv = ldg2(a.S0, idx, a.ldS, a.sc.div + k),
       tv = ldg2(a.S0, idx, a.ldS, a.sc.tv + k);
     V svr = vz<V>(), sdv = vz<V>(), stv = vz<V>();
@@ -245,7 +247,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? GD_STAGE_MINB : 2) k_sta
         const V fq = ldg2(a.F, idx, a.ldS, a.sc.trc + col);
         dq.x += fq.x, dq.y += fq.y;
       }
-      st2(TDs, idx, a.ldTD, a.tc.dtrc + col, dq);
+      if (!a.final_) st2(TDs, idx, a.ldTD, a.tc.dtrc + col, dq);
       V q = ldg2(a.S0, idx, a.ldS, a.sc.trc + col);
       V sq = vz<V>();
       for (int r = 0; r <= s; ++r) {
@@ -277,8 +279,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? GD_STAGE_MINB : 2) k_sta
       dl.x -= dpl.x;
       dl.y -= dpl.y;
     }
-    st2(TDs, idx, a.ldTD, a.tc.dlnps, dl);
-    st2(TDs, idx, a.ldTD, a.tc.dpl, dpl);
+    if (!a.final_) {
+      st2(TDs, idx, a.ldTD, a.tc.dlnps, dl);
+      st2(TDs, idx, a.ldTD, a.tc.dpl, dpl);
+    }
     V ln = ldg2(a.S0, idx, a.ldS, a.sc.lnps);
     V sl = vz<V>();
     for (int r = 0; r <= s; ++r) {

@@ -35,12 +35,13 @@ __device__ __forceinline__ V vz() {
 // sixteen FMAs (the shared-memory pipe, not the FMA pipe, bounds this loop).
 // Odd L: one level per thread.  Rows past cnt are computed from unused
 // shared memory and not stored.  Every output sums over j in order, so both
-// forms give the same bits.
+// forms give the same bits.  Threads t = 0 .. nt-1 of a group share the work
+// (two independent products run side by side on the two halves of a CTA).
 template <typename R, typename V>
-__device__ __forceinline__ void smem_matvec(const R* __restrict__ AT, const V* X, V* Y, int L, int cnt) {
+__device__ __forceinline__ void smem_matvec(const R* __restrict__ AT, const V* X, V* Y, int L, int cnt, int t, int nt) {
   const int nq = (cnt + 3) >> 2;
   if (L & 1) {
-    for (int e = threadIdx.x; e < L * nq; e += blockDim.x) {
+    for (int e = t; e < L * nq; e += nt) {
       const int q = e / L, k = e - q * L;
       const int i0 = 4 * q;
       R ax[4], ay[4];
@@ -67,14 +68,14 @@ __device__ __forceinline__ void smem_matvec(const R* __restrict__ AT, const V* X
     return;
   }
   const int Lh = L >> 1;
-  for (int e = threadIdx.x; e < Lh * nq; e += blockDim.x) {
+  for (int e = t; e < Lh * nq; e += nt) {
     const int q = e / Lh, k = 2 * (e - q * Lh);
     const int i0 = 4 * q;
     R ax0[4], ay0[4], ax1[4], ay1[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) ax0[u] = ay0[u] = ax1[u] = ay1[u] = R(0);
     const V* X0 = X + i0 * L;
-#pragma unroll 4
+#pragma unroll 16
     for (int j = 0; j < L; ++j) {
       const V aj = __ldg(reinterpret_cast<const V*>(AT + j * L + k));  // A[k][j], A[k+1][j]
 #pragma unroll
@@ -94,6 +95,33 @@ __device__ __forceinline__ void smem_matvec(const R* __restrict__ AT, const V* X
         Y[(i0 + u) * L + k + 1].x = ax1[u];
         Y[(i0 + u) * L + k + 1].y = ay1[u];
       }
+  }
+}
+
+// Y3[i] = sum_k w[k] X[i][k] for i < cnt: eight threads per coefficient, each
+// summing every eighth level, then a shuffle tree over the eight.  The group
+// (nt threads, a multiple of 32) runs whole warps, all of them to the end.
+template <typename R, typename V>
+__device__ __forceinline__ void smem_dot(const R* __restrict__ w, const V* X, V* Y3, int L, int cnt, int t, int nt) {
+  const int g = t & 7, per = nt >> 3;
+  for (int base = 0; base < cnt; base += per) {
+    const int i = base + (t >> 3);
+    R sx = R(0), sy = R(0);
+    if (i < cnt)
+      for (int k = g; k < L; k += 8) {
+        const R wk = __ldg(w + k);
+        sx += wk * X[i * L + k].x;
+        sy += wk * X[i * L + k].y;
+      }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+      sx += __shfl_xor_sync(0xffffffffu, sx, o);
+      sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    }
+    if (g == 0 && i < cnt) {
+      Y3[i].x = sx;
+      Y3[i].y = sy;
+    }
   }
 }
 
@@ -155,17 +183,13 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? GD_STAGE_MINB : 2) k_sta
   }
   for (int i = threadIdx.x; i < cnt; i += blockDim.x) LN[i] = ld2(a.S, IDX(i), a.ldS, a.sc.lnps);
   __syncthreads();
+  const int th = (int)blockDim.x >> 1;  // half of the CTA, whole warps
   if (!a.explicit_) {  // linear terms on the current state (run.f90:329-335)
-    smem_matvec<R, V>(a.amhyb, TV, Y, L, cnt);
-    smem_matvec<R, V>(a.bmhyb, DV, Y2, L, cnt);
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-      R sx = 0, sy = 0;
-      for (int k = 0; k < L; ++k) {
-        sx += a.svhyb[k] * DV[i * L + k].x;
-        sy += a.svhyb[k] * DV[i * L + k].y;
-      }
-      Y3[i].x = sx;
-      Y3[i].y = sy;
+    if ((int)threadIdx.x < th) {
+      smem_matvec<R, V>(a.amhyb, TV, Y, L, cnt, threadIdx.x, th);
+    } else {
+      smem_matvec<R, V>(a.bmhyb, DV, Y2, L, cnt, threadIdx.x - th, th);
+      smem_dot<R, V>(a.svhyb, DV, Y3, L, cnt, threadIdx.x - th, th);
     }
   }
   __syncthreads();
@@ -301,7 +325,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? GD_STAGE_MINB : 2) k_sta
   __syncthreads();
   if (!a.explicit_ && a.cimp != R(0)) {  // implicit solve for divergence
     const R c = a.cimp;
-    smem_matvec<R, V>(a.amhyb, TV, Y, L, cnt);
+    smem_matvec<R, V>(a.amhyb, TV, Y, L, cnt, threadIdx.x, blockDim.x);
     __syncthreads();
     for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {
       const int i = e / L, k = e - i * L;
@@ -312,18 +336,12 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? GD_STAGE_MINB : 2) k_sta
     }
     __syncthreads();
     const R* D = a.dhyb + ((long)s * (a.T + 1) + n) * L * L;
-    smem_matvec<R, V>(D, Y2, DV, L, cnt);
+    smem_matvec<R, V>(D, Y2, DV, L, cnt, threadIdx.x, blockDim.x);
     __syncthreads();
-    smem_matvec<R, V>(a.bmhyb, DV, Y, L, cnt);
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-      R sx = 0, sy = 0;
-      for (int k = 0; k < L; ++k) {
-        sx += a.svhyb[k] * DV[i * L + k].x;
-        sy += a.svhyb[k] * DV[i * L + k].y;
-      }
-      Y3[i].x = sx;
-      Y3[i].y = sy;
-    }
+    if ((int)threadIdx.x < th)
+      smem_matvec<R, V>(a.bmhyb, DV, Y, L, cnt, threadIdx.x, th);
+    else
+      smem_dot<R, V>(a.svhyb, DV, Y3, L, cnt, threadIdx.x - th, th);
     __syncthreads();
     for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {
       const int i = e / L, k = e - i * L;

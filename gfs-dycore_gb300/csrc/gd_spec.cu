@@ -27,12 +27,48 @@ __device__ __forceinline__ V vz() {
   return v;
 }
 
+// even-L product on two adjacent levels x Q coefficients per thread
+template <typename R, typename V, int Q>
+__device__ __forceinline__ void smem_matvec_even(const R* __restrict__ AT, const V* X, V* Y, int L, int cnt, int t,
+                                                 int nt) {
+  const int Lh = L >> 1, nqq = (cnt + Q - 1) / Q;
+  for (int e = t; e < Lh * nqq; e += nt) {
+    const int q = e / Lh, k = 2 * (e - q * Lh);
+    const int i0 = Q * q;
+    R ax0[Q], ay0[Q], ax1[Q], ay1[Q];
+#pragma unroll
+    for (int u = 0; u < Q; ++u) ax0[u] = ay0[u] = ax1[u] = ay1[u] = R(0);
+    const V* X0 = X + i0 * L;
+#pragma unroll 16
+    for (int j = 0; j < L; ++j) {
+      const V aj = __ldg(reinterpret_cast<const V*>(AT + j * L + k));  // A[k][j], A[k+1][j]
+#pragma unroll
+      for (int u = 0; u < Q; ++u) {
+        const V x = X0[u * L + j];
+        ax0[u] += aj.x * x.x;
+        ay0[u] += aj.x * x.y;
+        ax1[u] += aj.y * x.x;
+        ay1[u] += aj.y * x.y;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < Q; ++u)
+      if (i0 + u < cnt) {
+        Y[(i0 + u) * L + k].x = ax0[u];
+        Y[(i0 + u) * L + k].y = ay0[u];
+        Y[(i0 + u) * L + k + 1].x = ax1[u];
+        Y[(i0 + u) * L + k + 1].y = ay1[u];
+      }
+  }
+}
+
 // Y[i][k] = sum_j A[k][j] X[i][j] for i < cnt (complex X, real A).  AT
 // holds A transposed (AT[j][k] = A[k][j]) so a warp's loads of one j are
 // contiguous over k; the L x L matrices stay L1-resident.  X, Y index-major
 // with QC rows.  For even L a thread owns two adjacent output levels of four
 // coefficients: one paired matrix load and four broadcast reads of X feed
-// sixteen FMAs (the shared-memory pipe, not the FMA pipe, bounds this loop).
+// sixteen FMAs (the shared-memory pipe, not the FMA pipe, bounds this loop);
+// of two coefficients when four would leave threads of the group idle.
 // Odd L: one level per thread.  Rows past cnt are computed from unused
 // shared memory and not stored.  Every output sums over j in order, so both
 // forms give the same bits.  Threads t = 0 .. nt-1 of a group share the work
@@ -67,34 +103,13 @@ __device__ __forceinline__ void smem_matvec(const R* __restrict__ AT, const V* X
     }
     return;
   }
+  // four coefficients per thread while that leaves no thread of the group
+  // idle, else two (one more thread's worth of loads per FMA, twice the threads)
   const int Lh = L >> 1;
-  for (int e = t; e < Lh * nq; e += nt) {
-    const int q = e / Lh, k = 2 * (e - q * Lh);
-    const int i0 = 4 * q;
-    R ax0[4], ay0[4], ax1[4], ay1[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) ax0[u] = ay0[u] = ax1[u] = ay1[u] = R(0);
-    const V* X0 = X + i0 * L;
-#pragma unroll 16
-    for (int j = 0; j < L; ++j) {
-      const V aj = __ldg(reinterpret_cast<const V*>(AT + j * L + k));  // A[k][j], A[k+1][j]
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const V x = X0[u * L + j];
-        ax0[u] += aj.x * x.x;
-        ay0[u] += aj.x * x.y;
-        ax1[u] += aj.y * x.x;
-        ay1[u] += aj.y * x.y;
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (i0 + u < cnt) {
-        Y[(i0 + u) * L + k].x = ax0[u];
-        Y[(i0 + u) * L + k].y = ay0[u];
-        Y[(i0 + u) * L + k + 1].x = ax1[u];
-        Y[(i0 + u) * L + k + 1].y = ay1[u];
-      }
+  if (Lh * nq >= nt) {
+    smem_matvec_even<R, V, 4>(AT, X, Y, L, cnt, t, nt);
+  } else {
+    smem_matvec_even<R, V, 2>(AT, X, Y, L, cnt, t, nt);
   }
 }
 

@@ -28,8 +28,8 @@ __device__ __forceinline__ V vz() {
 }
 
 // even-L product on two adjacent levels x Q coefficients per thread
-template <typename R, typename V, int Q>
-__device__ __forceinline__ void smem_matvec_even(const R* __restrict__ AT, const V* X, V* Y, int L, int cnt, int t,
+template <typename R, typename V, int Q, typename St>
+__device__ __forceinline__ void smem_matvec_even(const R* __restrict__ AT, const V* X, St st, int L, int cnt, int t,
                                                  int nt) {
   const int Lh = L >> 1, nqq = (cnt + Q - 1) / Q;
   for (int e = t; e < Lh * nqq; e += nt) {
@@ -54,10 +54,13 @@ __device__ __forceinline__ void smem_matvec_even(const R* __restrict__ AT, const
 #pragma unroll
     for (int u = 0; u < Q; ++u)
       if (i0 + u < cnt) {
-        Y[(i0 + u) * L + k].x = ax0[u];
-        Y[(i0 + u) * L + k].y = ay0[u];
-        Y[(i0 + u) * L + k + 1].x = ax1[u];
-        Y[(i0 + u) * L + k + 1].y = ay1[u];
+        V y0, y1;
+        y0.x = ax0[u];
+        y0.y = ay0[u];
+        y1.x = ax1[u];
+        y1.y = ay1[u];
+        st(i0 + u, k, y0);
+        st(i0 + u, k + 1, y1);
       }
   }
 }
@@ -73,8 +76,16 @@ __device__ __forceinline__ void smem_matvec_even(const R* __restrict__ AT, const
 // shared memory and not stored.  Every output sums over j in order, so both
 // forms give the same bits.  Threads t = 0 .. nt-1 of a group share the work
 // (two independent products run side by side on the two halves of a CTA).
-template <typename R, typename V>
-__device__ __forceinline__ void smem_matvec(const R* __restrict__ AT, const V* X, V* Y, int L, int cnt, int t, int nt) {
+// st(i, k, y) takes output (i, k): stores it, or folds the step that uses it
+// into the product's epilogue
+template <typename V>
+struct MvStore {
+  V* Y;
+  int L;
+  __device__ __forceinline__ void operator()(int i, int k, V y) const { Y[i * L + k] = y; }
+};
+template <typename R, typename V, typename St>
+__device__ __forceinline__ void smem_matvec(const R* __restrict__ AT, const V* X, St st, int L, int cnt, int t, int nt) {
   const int nq = (cnt + 3) >> 2;
   if (L & 1) {
     for (int e = t; e < L * nq; e += nt) {
@@ -97,8 +108,10 @@ __device__ __forceinline__ void smem_matvec(const R* __restrict__ AT, const V* X
 #pragma unroll
       for (int u = 0; u < 4; ++u)
         if (i0 + u < cnt) {
-          Y[(i0 + u) * L + k].x = ax[u];
-          Y[(i0 + u) * L + k].y = ay[u];
+          V y;
+          y.x = ax[u];
+          y.y = ay[u];
+          st(i0 + u, k, y);
         }
     }
     return;
@@ -107,17 +120,17 @@ __device__ __forceinline__ void smem_matvec(const R* __restrict__ AT, const V* X
   // idle, else two (one more thread's worth of loads per FMA, twice the threads)
   const int Lh = L >> 1;
   if (Lh * nq >= nt) {
-    smem_matvec_even<R, V, 4>(AT, X, Y, L, cnt, t, nt);
+    smem_matvec_even<R, V, 4>(AT, X, st, L, cnt, t, nt);
   } else {
-    smem_matvec_even<R, V, 2>(AT, X, Y, L, cnt, t, nt);
+    smem_matvec_even<R, V, 2>(AT, X, st, L, cnt, t, nt);
   }
 }
 
 // Y3[i] = sum_k w[k] X[i][k] for i < cnt: eight threads per coefficient, each
 // summing every eighth level, then a shuffle tree over the eight.  The group
 // (nt threads, a multiple of 32) runs whole warps, all of them to the end.
-template <typename R, typename V>
-__device__ __forceinline__ void smem_dot(const R* __restrict__ w, const V* X, V* Y3, int L, int cnt, int t, int nt) {
+template <typename R, typename V, typename St>
+__device__ __forceinline__ void smem_dot(const R* __restrict__ w, const V* X, St st, int L, int cnt, int t, int nt) {
   const int g = t & 7, per = nt >> 3;
   for (int base = 0; base < cnt; base += per) {
     const int i = base + (t >> 3);
@@ -134,8 +147,10 @@ __device__ __forceinline__ void smem_dot(const R* __restrict__ w, const V* X, V*
       sy += __shfl_xor_sync(0xffffffffu, sy, o);
     }
     if (g == 0 && i < cnt) {
-      Y3[i].x = sx;
-      Y3[i].y = sy;
+      V y;
+      y.x = sx;
+      y.y = sy;
+      st(i, 0, y);
     }
   }
 }
@@ -201,10 +216,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? GD_STAGE_MINB : 2) k_sta
   const int th = (int)blockDim.x >> 1;  // half of the CTA, whole warps
   if (!a.explicit_) {  // linear terms on the current state (run.f90:329-335)
     if ((int)threadIdx.x < th) {
-      smem_matvec<R, V>(a.amhyb, TV, Y, L, cnt, threadIdx.x, th);
+      smem_matvec<R, V>(a.amhyb, TV, MvStore<V>{Y, L}, L, cnt, threadIdx.x, th);
     } else {
-      smem_matvec<R, V>(a.bmhyb, DV, Y2, L, cnt, threadIdx.x - th, th);
-      smem_dot<R, V>(a.svhyb, DV, Y3, L, cnt, threadIdx.x - th, th);
+      smem_matvec<R, V>(a.bmhyb, DV, MvStore<V>{Y2, L}, L, cnt, threadIdx.x - th, th);
+      smem_dot<R, V>(a.svhyb, DV, MvStore<V>{Y3, 1}, L, cnt, threadIdx.x - th, th);  // Y3[i]
     }
   }
   __syncthreads();
@@ -340,33 +355,38 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? GD_STAGE_MINB : 2) k_sta
   __syncthreads();
   if (!a.explicit_ && a.cimp != R(0)) {  // implicit solve for divergence
     const R c = a.cimp;
-    smem_matvec<R, V>(a.amhyb, TV, Y, L, cnt, threadIdx.x, blockDim.x);
-    __syncthreads();
-    for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {
-      const int i = e / L, k = e - i * L;
-      V r;
-      r.x = DV[i * L + k].x - c * lap * dt * (Y[i * L + k].x + a.tor[k] * LN[i].x);
-      r.y = DV[i * L + k].y - c * lap * dt * (Y[i * L + k].y + a.tor[k] * LN[i].y);
-      Y2[i * L + k] = r;
-    }
+    // right-hand side r = D - c lap dt (A T + tor ln ps), formed in the
+    // epilogue of the A T product
+    smem_matvec<R, V>(
+        a.amhyb, TV,
+        [&](int i, int k, V y) {
+          V r;
+          r.x = DV[i * L + k].x - c * lap * dt * (y.x + a.tor[k] * LN[i].x);
+          r.y = DV[i * L + k].y - c * lap * dt * (y.y + a.tor[k] * LN[i].y);
+          Y2[i * L + k] = r;
+        },
+        L, cnt, threadIdx.x, blockDim.x);
     __syncthreads();
     const R* D = a.dhyb + ((long)s * (a.T + 1) + n) * L * L;
-    smem_matvec<R, V>(D, Y2, DV, L, cnt, threadIdx.x, blockDim.x);
+    smem_matvec<R, V>(D, Y2, MvStore<V>{DV, L}, L, cnt, threadIdx.x, blockDim.x);
     __syncthreads();
+    // back-substitution into T and ln ps in the epilogues of B D and sv . D
     if ((int)threadIdx.x < th)
-      smem_matvec<R, V>(a.bmhyb, DV, Y, L, cnt, threadIdx.x, th);
+      smem_matvec<R, V>(
+          a.bmhyb, DV,
+          [&](int i, int k, V y) {
+            TV[i * L + k].x -= c * dt * y.x;
+            TV[i * L + k].y -= c * dt * y.y;
+          },
+          L, cnt, threadIdx.x, th);
     else
-      smem_dot<R, V>(a.svhyb, DV, Y3, L, cnt, threadIdx.x - th, th);
-    __syncthreads();
-    for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {
-      const int i = e / L, k = e - i * L;
-      TV[i * L + k].x -= c * dt * Y[i * L + k].x;
-      TV[i * L + k].y -= c * dt * Y[i * L + k].y;
-    }
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-      LN[i].x -= c * dt * Y3[i].x;
-      LN[i].y -= c * dt * Y3[i].y;
-    }
+      smem_dot<R, V>(
+          a.svhyb, DV,
+          [&](int i, int, V y) {
+            LN[i].x -= c * dt * y.x;
+            LN[i].y -= c * dt * y.y;
+          },
+          L, cnt, threadIdx.x - th, th);
     __syncthreads();
   }
   for (int e = threadIdx.x; e < L * cnt; e += blockDim.x) {

@@ -20,6 +20,7 @@
 #include "gd_pattern.cuh"
 #include "gd_dcmip.h"
 #include "gd_physics.cuh"
+#include "gd_mlp.cuh"
 #include "gd_spec.cuh"
 #include "gd_tc.cuh"
 #include <type_traits>
@@ -60,6 +61,8 @@ class DycoreBase {
   virtual void profile_step(double*, int) = 0;
   virtual void check() = 0;
   virtual void set_sppt(gd_pattern*, double, double) = 0;
+  virtual void set_closure(gd_mlp*) = 0;
+  virtual void closure_features(float*) = 0;
   virtual double get_pdryini() = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = true;
@@ -124,7 +127,7 @@ class Dycore : public DycoreBase {
   long ldS, ldTD, ldAP, ldAH, ldFP, ldFH, ldGP, ldGH;
   long nlm_rows = 0;  // allocated rows of the synthesis sources: nlm rounded up to even
   GemmPlan synP, synH, anaP, anaH, anaPhys, anaSimple;
-  FftPlan c2rFull, c2rInv, r2cDyn, r2cPhys, r2cSimple;
+  FftPlan c2rFull, c2rInv, r2cDyn, r2cPhys, r2cSimple, r2cClos;
   Tableau tb;
   // per-phase CUDA-event profiling of one eager step (gd_profile_step)
   enum { PH_LSYN, PH_FSYN, PH_COL, PH_FANA, PH_LANA, PH_SEMI, PH_PHYS, PH_OTHER, PH_CPHYS, PH_N };
@@ -271,6 +274,9 @@ class Dycore : public DycoreBase {
     free_fft_plan(c2rInv);
     free_fft_plan(r2cDyn);
     free_fft_plan(r2cPhys);
+    free_plan(anaSimple);
+    free_fft_plan(r2cSimple);
+    free_fft_plan(r2cClos);
     if (stream) cudaStreamSynchronize(stream);
     if (side) cudaStreamSynchronize(side);
     for (void* p : allocs) cudaFree(p);
@@ -816,7 +822,7 @@ class Dycore : public DycoreBase {
     inverse_pass(false);
     if (simple()) {
       simple_pass();
-      launch_simple_update<R>(S, ldS, sc, L, nlm, AP, ldAP, AH, ldAH, c.massfix, (R)c.dt, (R)(1.0 / Phys::rerth),
+      launch_simple_update<R>(S, ldS, sc, L, nlm, AP, ldAP, AH, ldAH, c.massfix, 1, (R)c.dt, (R)(1.0 / Phys::rerth),
                               lapv, (R)Phys::rerth, stream);
       mark(PH_PHYS);
       return;
@@ -836,6 +842,70 @@ class Dycore : public DycoreBase {
                             (R)Phys::rerth, stream);
       mark(PH_PHYS);
     }
+    if (closure) closure_pass();
+  }
+  // Learned closure: the attached net's tendencies from the grid columns of
+  // the step's inverse transform (the state before the forcing, as the
+  // forcing sees it), times dt, analysed as in the column-physics update (Tv
+  // scalar, u and v through the vector analysis) and added to the state.
+  gd_mlp* closure = nullptr;
+  float *clos_x = nullptr, *clos_y = nullptr;
+  void closure_pass() {
+    const float *imu, *isd, *omu, *osd;
+    mlp_norm(closure, &imu, &isd, &omu, &osd);
+    launch_closure_in<R>(gS, sr, L, ng, imu, isd, clos_x, stream);
+    mlp_forward_on(closure, clos_x, (int)ng, clos_y, stream);
+    launch_closure_out<R>(clos_y, L, ng, omu, osd, (R)c.dt, gA, stream);
+    mark(PH_PHYS);
+    launch_r2c<R>(sd, r2cClos, gA, FPb, ldGP, FHb, ldGH, stream);
+    mark(PH_FANA);
+    do_anal(false, anaSimple, FPb, ldGP, 2 * (4 * L + 1), AP, ldAP);
+    do_anal(true, anaH, FHb, ldGH, 2 * ah.ncol, AH, ldAH);
+    mark(PH_LANA);
+    launch_simple_update<R>(S, ldS, sc, L, nlm, AP, ldAP, AH, ldAH, 0, 0, (R)c.dt, (R)(1.0 / Phys::rerth), lapv,
+                            (R)Phys::rerth, stream);
+    mark(PH_PHYS);
+  }
+  void closure_buffers() {
+    if (!clos_x) clos_x = dalloc<float>((size_t)ng * (3 * L + 1));
+    if (!clos_y) clos_y = dalloc<float>((size_t)ng * 3 * L);
+  }
+  void set_closure(gd_mlp* net) override {
+    if (net) {
+      if (mlp_device(net) != c.device) throw std::invalid_argument("gd_set_closure: net on another device");
+      if (mlp_nin(net) != 3 * L + 1 || mlp_nout(net) != 3 * L)
+        throw std::invalid_argument("gd_set_closure: need nin = 3 nlev + 1 and nout = 3 nlev");
+      const float *a, *b, *d, *e;
+      if (!mlp_norm(net, &a, &b, &d, &e)) throw std::invalid_argument("gd_set_closure: net has no normalisation");
+      if (simple()) throw std::invalid_argument("gd_set_closure: not with the DCMIP simple physics");
+      GD_CUDA(cudaStreamSynchronize(stream));
+      closure_buffers();
+      mlp_reserve(net, (int)ng);
+      if (!r2cClos.jobs) {  // grid rows Tv [0,L), u [2L,3L), v [3L,4L) as in the column-physics update
+        std::vector<AnalDesc> cd = {
+            {L, 0, 0, 0, -1, 1.0, 0.0},
+            {L, 2 * L, 3 * L + 1, 1, 0, 1.0, 1.0},
+            {L, 3 * L, 2 * L + 1, 1, L, 1.0, -1.0},
+        };
+        r2cClos = make_r2c_plan<R>(cd.data(), (int)cd.size(), stream, M);
+      }
+      if (!anaSimple.items) anaSimple = make_anal_plan(T, 2 * (4 * L + 1), stream);
+      GD_CUDA(cudaStreamSynchronize(stream));
+    }
+    closure = net;
+    if (gexec) {  // the captured step changes
+      GD_CUDA(cudaStreamSynchronize(stream));
+      GD_CUDA(cudaGraphExecDestroy(gexec));
+      gexec = nullptr;
+    }
+  }
+  void closure_features(float* x) override {
+    if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
+    closure_buffers();
+    inverse_pass(false);
+    launch_closure_in<R>(gS, sr, L, ng, nullptr, nullptr, clos_x, stream);
+    GD_CUDA(cudaMemcpyAsync(x, clos_x, sizeof(float) * (size_t)ng * (3 * L + 1), cudaMemcpyDeviceToHost, stream));
+    GD_CUDA(cudaStreamSynchronize(stream));
   }
   // Stochastically perturbed physics: an attached pattern (gd_pattern) is
   // advanced one step at the start of every step and put on the grid with the
@@ -1644,6 +1714,13 @@ int gd_profile_step(gd_ctx* ctx, double* ms, int nphase) {
 }
 int gd_set_sppt(gd_ctx* ctx, gd_pattern* pattern, double sigtop, double sigbot) {
   return guarded(ctx, [&] { ctx->d->set_sppt(pattern, sigtop, sigbot); });
+}
+int gd_set_closure(gd_ctx* ctx, gd_mlp* net) {
+  return guarded(ctx, [&] { ctx->d->set_closure(net); });
+}
+int gd_closure_features(gd_ctx* ctx, float* x) {
+  if (!x) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->closure_features(x); });
 }
 int gd_ensemble_advance(gd_ctx** ctxs, int n, double t, int nsteps) {
   if (!ctxs || n < 1 || nsteps < 0) return GD_ERR_ARG;

@@ -1,0 +1,619 @@
+// gd_mlp.cu -- the learned per-column closure's network: a fully connected
+// net nin -> nh (GELU) -> ... -> nh (GELU) -> nout with BF16 weights and FP32
+// accumulation.  Forward and backward passes, the mean-squared-error loss and
+// Adam run as CUDA kernels on the net's stream; the dycore applies a trained
+// net to its grid columns once per step (gd_set_closure, gd_dycore.cu).
+//
+// Parameters are one FP32 master array, layer after layer: W_l [fout][fin]
+// row-major, then b_l [fout].  The forward and backward passes read the
+// weights from a BF16 copy made after every update (biases stay FP32), so a
+// trained net is exactly the BF16 net it is evaluated as.
+//
+// The products are small (nh = 256) and the batch is the grid's columns, so
+// one tiled SIMT GEMM serves every product: 64 x 64 output tiles, K in steps
+// of 16 through shared memory, 4 x 4 outputs per thread, operands addressed
+// through (row, column) strides so the same kernel forms X W^T, dZ^T X and
+// dZ W, with the bias/GELU or GELU-derivative epilogue fused.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstdint>
+#include <memory>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "gd_api.h"
+#include "gd_common.cuh"
+#include "gd_mlp.cuh"
+
+struct gd_mlp {
+  int device = 0;
+  int nin = 0, nh = 0, nl = 0, nout = 0;  // nl hidden layers
+  int nlayer = 0;                          // nl + 1 linear layers
+  std::vector<int> fin, fout;
+  std::vector<long> offw, offb;  // offsets of W_l and b_l in the parameter array
+  long np = 0;
+  float* p32 = nullptr;          // master parameters
+  __nv_bfloat16* w16 = nullptr;  // BF16 copy (all np entries; the bias slots are unused)
+  float* grad = nullptr;
+  float* am = nullptr;  // Adam moments
+  float* av = nullptr;
+  long adam_t = 0;
+  // normalisation of the closure's inputs and outputs (device, nin / nout)
+  float *in_mu = nullptr, *in_sd = nullptr, *out_mu = nullptr, *out_sd = nullptr;
+  bool has_norm = false;
+  // activations: Z_l (pre-activation) and A_l (GELU) of each hidden layer,
+  // the output and its gradient, two gradient buffers for the backward pass
+  int bcap = 0;
+  float *zb = nullptr, *ab = nullptr, *yb = nullptr, *gy = nullptr, *g0 = nullptr, *g1 = nullptr;
+  float* partial = nullptr;  // loss partial sums
+  float* lossd = nullptr;
+  cudaStream_t stream = nullptr;  // the stream the net's work runs on
+  cudaStream_t own = nullptr;     // the net's own stream (destroyed with it)
+  std::string err;
+  std::vector<void*> allocs;
+  void* alloc(size_t bytes) {
+    void* p = nullptr;
+    GD_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+    allocs.push_back(p);
+    return p;
+  }
+  void release(void* p) {
+    for (auto& a : allocs)
+      if (a == p) {
+        cudaFree(a);
+        a = nullptr;
+      }
+  }
+  ~gd_mlp() {
+    int cur = 0;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* p : allocs)
+      if (p) cudaFree(p);
+    if (own) cudaStreamDestroy(own);
+    if (cur != device) cudaSetDevice(cur);
+  }
+};
+
+namespace gd {
+namespace {
+
+constexpr int GM = 64, GN = 64, GK = 16;
+constexpr int KPART = 256;  // loss partial sums
+
+__device__ __forceinline__ float tofloat(float x) { return x; }
+__device__ __forceinline__ float tofloat(__nv_bfloat16 x) { return __bfloat162float(x); }
+
+// GELU with the exact normal CDF, and its derivative
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_d(float z) {
+  return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+}
+
+// C(m, n) = sum_k A(m, k) B(k, n) with A(m, k) = A[m sam + k sak], B(k, n) =
+// B[k sbk + n sbn]; epi(m, n, c) takes each output
+template <typename TA, typename TB, typename Epi>
+__global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const TA* __restrict__ A, long sam, long sak,
+                                              const TB* __restrict__ B, long sbk, long sbn, Epi epi) {
+  __shared__ float As[GK][GM + 4];
+  __shared__ float Bs[GK][GN + 4];
+  const int tid = threadIdx.x;
+  const int m0 = blockIdx.y * GM, n0 = blockIdx.x * GN;
+  const int tm = (tid >> 4) * 4, tn = (tid & 15) * 4;
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+  const bool a_kfast = sak == 1, b_nfast = sbn == 1;
+  for (int k0 = 0; k0 < K; k0 += GK) {
+    for (int e = tid; e < GM * GK; e += 256) {  // the unit-stride index fastest over the threads
+      const int mm = a_kfast ? e / GK : e % GM, kk = a_kfast ? e % GK : e / GM;
+      const int m = m0 + mm, k = k0 + kk;
+      As[kk][mm] = (m < M && k < K) ? tofloat(A[(long)m * sam + (long)k * sak]) : 0.f;
+    }
+    for (int e = tid; e < GK * GN; e += 256) {
+      const int nn = b_nfast ? e % GN : e / GK, kk = b_nfast ? e / GN : e % GK;
+      const int n = n0 + nn, k = k0 + kk;
+      Bs[kk][nn] = (n < N && k < K) ? tofloat(B[(long)k * sbk + (long)n * sbn]) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GK; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        a[i] = As[kk][tm + i];
+        b[i] = Bs[kk][tn + i];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int m = m0 + tm + i, n = n0 + tn + j;
+      if (m < M && n < N) epi(m, n, acc[i][j]);
+    }
+}
+
+struct EpiHidden {  // Z = acc + b, A = GELU(Z)
+  const float* b;
+  float* Z;
+  float* Aout;
+  int N;
+  __device__ void operator()(int m, int n, float c) const {
+    const float z = c + b[n];
+    Z[(long)m * N + n] = z;
+    Aout[(long)m * N + n] = gelu(z);
+  }
+};
+struct EpiLinear {  // Y = acc + b
+  const float* b;
+  float* Y;
+  int N;
+  __device__ void operator()(int m, int n, float c) const { Y[(long)m * N + n] = c + b[n]; }
+};
+struct EpiStore {  // G = acc
+  float* G;
+  int N;
+  __device__ void operator()(int m, int n, float c) const { G[(long)m * N + n] = c; }
+};
+struct EpiGeluD {  // dZ = acc * GELU'(Z)
+  const float* Z;
+  float* G;
+  int N;
+  __device__ void operator()(int m, int n, float c) const {
+    const long i = (long)m * N + n;
+    G[i] = c * gelu_d(Z[i]);
+  }
+};
+
+template <typename TA, typename TB, typename Epi>
+void gemm(int M, int N, int K, const TA* A, long sam, long sak, const TB* B, long sbk, long sbn, Epi epi,
+          cudaStream_t s) {
+  if (M <= 0 || N <= 0) return;
+  dim3 grid((unsigned)ceil_div(N, GN), (unsigned)ceil_div(M, GM));
+  k_gemm<TA, TB, Epi><<<grid, 256, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, epi);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+
+// db[n] = sum_m G[m][n] (fixed order: 8 strided partial sums, then a tree)
+__global__ void k_colsum(const float* __restrict__ G, int M, int N, float* db) {
+  __shared__ float red[8][33];
+  const int n = blockIdx.x * 32 + threadIdx.x;
+  float s = 0.f;
+  if (n < N)
+    for (int m = threadIdx.y; m < M; m += 8) s += G[(long)m * N + n];
+  red[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && n < N) {
+    float t = 0.f;
+#pragma unroll
+    for (int y = 0; y < 8; ++y) t += red[y][threadIdx.x];
+    db[n] = t;
+  }
+}
+
+// squared error: gy = 2 (y - t) / count, partial[block] = sum (y - t)^2
+__global__ void k_mse(const float* __restrict__ y, const float* __restrict__ t, long count, float* gy,
+                      float* partial) {
+  __shared__ float red[256];
+  float s = 0.f;
+  const float sc = 2.f / (float)count;
+  for (long i = (long)blockIdx.x * 256 + threadIdx.x; i < count; i += (long)gridDim.x * 256) {
+    const float d = y[i] - t[i];
+    s += d * d;
+    if (gy) gy[i] = sc * d;
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+__global__ void k_mse_final(const float* partial, int n, long count, float* loss) {
+  __shared__ float red[KPART];
+  red[threadIdx.x] = threadIdx.x < n ? partial[threadIdx.x] : 0.f;
+  __syncthreads();
+  for (int o = KPART / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *loss = red[0] / (float)count;
+}
+
+__global__ void k_adam(float* p, const float* g, float* m, float* v, __nv_bfloat16* w16, long n, float lr, float b1,
+                       float b2, float eps, float c1, float c2) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi, vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float pi = p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    p[i] = pi;
+    w16[i] = __float2bfloat16_rn(pi);
+  }
+}
+__global__ void k_to_bf16(const float* p, __nv_bfloat16* w16, long n) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    w16[i] = __float2bfloat16_rn(p[i]);
+}
+
+template <typename F>
+int mguard(gd_mlp* p, F f) {
+  if (!p) return GD_ERR_ARG;
+  try {
+    int cur = 0;
+    GD_CUDA(cudaGetDevice(&cur));
+    if (cur != p->device) GD_CUDA(cudaSetDevice(p->device));
+    f();
+    if (cur != p->device) GD_CUDA(cudaSetDevice(cur));
+    return GD_OK;
+  } catch (const CudaError& e) {
+    p->err = e.what();
+    return GD_ERR_CUDA;
+  } catch (const std::invalid_argument& e) {
+    p->err = e.what();
+    return GD_ERR_ARG;
+  } catch (const std::exception& e) {
+    p->err = e.what();
+    return GD_ERR_CUDA;
+  }
+}
+std::string g_mlp_init_error;
+
+void to_bf16(gd_mlp* p) {
+  k_to_bf16<<<std::min(ceil_div(p->np, 256), 4096), 256, 0, p->stream>>>(p->p32, p->w16, p->np);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+
+}  // namespace
+
+// --------------------------------------------------- shared with the dycore
+void mlp_reserve(gd_mlp* p, int ncols) {
+  if (ncols <= p->bcap) return;
+  GD_CUDA(cudaStreamSynchronize(p->stream));
+  for (float* b : {p->zb, p->ab, p->yb, p->gy, p->g0, p->g1})
+    if (b) p->release(b);
+  const long w = std::max(p->nh, std::max(p->nin, p->nout));
+  p->zb = (float*)p->alloc(sizeof(float) * (size_t)p->nl * ncols * p->nh);
+  p->ab = (float*)p->alloc(sizeof(float) * (size_t)p->nl * ncols * p->nh);
+  p->yb = (float*)p->alloc(sizeof(float) * (size_t)ncols * p->nout);
+  p->gy = (float*)p->alloc(sizeof(float) * (size_t)ncols * p->nout);
+  p->g0 = (float*)p->alloc(sizeof(float) * (size_t)ncols * w);
+  p->g1 = (float*)p->alloc(sizeof(float) * (size_t)ncols * w);
+  p->bcap = ncols;
+}
+
+// y [n][nout] = net(x [n][nin]) on stream s; the hidden activations stay in
+// the net's buffers for a backward pass.  No allocation when n <= bcap.
+void mlp_forward_on(gd_mlp* p, const float* x, int n, float* y, cudaStream_t s) {
+  if (n > p->bcap) throw std::invalid_argument("gd_mlp: batch above the reserved capacity");
+  const float* in = x;
+  for (int l = 0; l < p->nlayer; ++l) {
+    const int fi = p->fin[l], fo = p->fout[l];
+    const __nv_bfloat16* W = p->w16 + p->offw[l];
+    const float* b = p->p32 + p->offb[l];
+    if (l < p->nl) {
+      float* Z = p->zb + (size_t)l * p->bcap * p->nh;
+      float* A = p->ab + (size_t)l * p->bcap * p->nh;
+      gemm(n, fo, fi, in, (long)fi, 1L, W, 1L, (long)fi, EpiHidden{b, Z, A, fo}, s);
+      in = A;
+    } else {
+      gemm(n, fo, fi, in, (long)fi, 1L, W, 1L, (long)fi, EpiLinear{b, y, fo}, s);
+    }
+  }
+}
+
+int mlp_nin(const gd_mlp* p) { return p->nin; }
+int mlp_nout(const gd_mlp* p) { return p->nout; }
+int mlp_device(const gd_mlp* p) { return p->device; }
+bool mlp_norm(const gd_mlp* p, const float** in_mu, const float** in_sd, const float** out_mu,
+              const float** out_sd) {
+  *in_mu = p->in_mu;
+  *in_sd = p->in_sd;
+  *out_mu = p->out_mu;
+  *out_sd = p->out_sd;
+  return p->has_norm;
+}
+
+namespace {
+// loss and gradient of a batch into p->grad; the loss lands in p->lossd
+void loss_grad(gd_mlp* p, const float* x, const float* t, int n) {
+  cudaStream_t s = p->stream;
+  mlp_forward_on(p, x, n, p->yb, s);
+  const long cnt = (long)n * p->nout;
+  const int nb = std::min(KPART, ceil_div(cnt, 256));
+  k_mse<<<nb, 256, 0, s>>>(p->yb, t, cnt, p->gy, p->partial);
+  k_mse_final<<<1, KPART, 0, s>>>(p->partial, nb, cnt, p->lossd);
+  count_launch(2);
+  GD_LAUNCH_CHECK();
+  // backward: dZ of layer l in cur; dW_l = dZ^T A_{l-1}, db_l = colsum dZ,
+  // dZ_{l-1} = (dZ W_l) * GELU'(Z_{l-1})
+  const float* cur = p->gy;
+  for (int l = p->nlayer - 1; l >= 0; --l) {
+    const int fi = p->fin[l], fo = p->fout[l];
+    const float* Ain = l == 0 ? x : p->ab + (size_t)(l - 1) * p->bcap * p->nh;
+    gemm(fo, fi, n, cur, 1L, (long)fo, Ain, (long)fi, 1L, EpiStore{p->grad + p->offw[l], fi}, s);
+    k_colsum<<<ceil_div(fo, 32), dim3(32, 8), 0, s>>>(cur, n, fo, p->grad + p->offb[l]);
+    count_launch();
+    GD_LAUNCH_CHECK();
+    if (l > 0) {
+      float* nxt = (cur == p->g0) ? p->g1 : p->g0;
+      const float* Zp = p->zb + (size_t)(l - 1) * p->bcap * p->nh;
+      gemm(n, fi, fo, cur, (long)fo, 1L, p->w16 + p->offw[l], (long)fi, 1L, EpiGeluD{Zp, nxt, fi}, s);
+      cur = nxt;
+    }
+  }
+}
+}  // namespace
+
+}  // namespace gd
+
+using namespace gd;
+
+extern "C" {
+
+int gd_mlp_init(int nin, int nhidden, int nlayers, int nout, unsigned long long seed, int device, gd_mlp** out) {
+  if (!out) return GD_ERR_ARG;
+  *out = nullptr;
+  if (nin < 1 || nhidden < 1 || nlayers < 1 || nout < 1) {
+    g_mlp_init_error = "gd_mlp_init: need nin, nhidden, nlayers, nout >= 1";
+    return GD_ERR_ARG;
+  }
+  std::unique_ptr<gd_mlp> p(new gd_mlp());
+  p->device = device;
+  p->nin = nin;
+  p->nh = nhidden;
+  p->nl = nlayers;
+  p->nout = nout;
+  p->nlayer = nlayers + 1;
+  long off = 0;
+  for (int l = 0; l < p->nlayer; ++l) {
+    const int fi = l == 0 ? nin : nhidden, fo = l == nlayers ? nout : nhidden;
+    p->fin.push_back(fi);
+    p->fout.push_back(fo);
+    p->offw.push_back(off);
+    off += (long)fi * fo;
+    p->offb.push_back(off);
+    off += fo;
+  }
+  p->np = off;
+  // He-normal hidden weights, the output layer scaled by 0.1 (the net starts
+  // close to no correction), zero biases
+  std::vector<float> h(off, 0.f);
+  std::mt19937_64 rng(seed);
+  std::normal_distribution<double> nd(0.0, 1.0);
+  for (int l = 0; l < p->nlayer; ++l) {
+    const double sd = std::sqrt(2.0 / p->fin[l]) * (l == nlayers ? 0.1 : 1.0);
+    for (long i = 0; i < (long)p->fin[l] * p->fout[l]; ++i) h[p->offw[l] + i] = (float)(sd * nd(rng));
+  }
+  const int rc = mguard(p.get(), [&] {
+    GD_CUDA(cudaStreamCreateWithFlags(&p->own, cudaStreamNonBlocking));
+    p->stream = p->own;
+    p->p32 = (float*)p->alloc(sizeof(float) * off);
+    p->w16 = (__nv_bfloat16*)p->alloc(sizeof(__nv_bfloat16) * off);
+    p->grad = (float*)p->alloc(sizeof(float) * off);
+    p->am = (float*)p->alloc(sizeof(float) * off);
+    p->av = (float*)p->alloc(sizeof(float) * off);
+    p->partial = (float*)p->alloc(sizeof(float) * KPART);
+    p->lossd = (float*)p->alloc(sizeof(float));
+    p->in_mu = (float*)p->alloc(sizeof(float) * nin);
+    p->in_sd = (float*)p->alloc(sizeof(float) * nin);
+    p->out_mu = (float*)p->alloc(sizeof(float) * nout);
+    p->out_sd = (float*)p->alloc(sizeof(float) * nout);
+    GD_CUDA(cudaMemcpy(p->p32, h.data(), sizeof(float) * off, cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemset(p->am, 0, sizeof(float) * off));
+    GD_CUDA(cudaMemset(p->av, 0, sizeof(float) * off));
+    GD_CUDA(cudaMemset(p->grad, 0, sizeof(float) * off));
+    to_bf16(p.get());
+    GD_CUDA(cudaStreamSynchronize(p->stream));
+  });
+  if (rc != GD_OK) {
+    g_mlp_init_error = p->err;
+    return rc;
+  }
+  *out = p.release();
+  return GD_OK;
+}
+
+int gd_mlp_destroy(gd_mlp* p) {
+  if (!p) return GD_ERR_ARG;
+  delete p;
+  return GD_OK;
+}
+
+int gd_mlp_nparams(gd_mlp* p, long long* n) {
+  if (!p || !n) return GD_ERR_ARG;
+  *n = p->np;
+  return GD_OK;
+}
+
+int gd_mlp_get_params(gd_mlp* p, float* params) {
+  if (!params) return GD_ERR_ARG;
+  return mguard(p, [&] {
+    GD_CUDA(cudaStreamSynchronize(p->stream));
+    GD_CUDA(cudaMemcpy(params, p->p32, sizeof(float) * p->np, cudaMemcpyDeviceToHost));
+  });
+}
+
+int gd_mlp_set_params(gd_mlp* p, const float* params) {
+  if (!params) return GD_ERR_ARG;
+  return mguard(p, [&] {
+    GD_CUDA(cudaStreamSynchronize(p->stream));
+    GD_CUDA(cudaMemcpy(p->p32, params, sizeof(float) * p->np, cudaMemcpyHostToDevice));
+    to_bf16(p);
+    GD_CUDA(cudaStreamSynchronize(p->stream));
+  });
+}
+
+int gd_mlp_set_norm(gd_mlp* p, const float* in_mu, const float* in_sd, const float* out_mu, const float* out_sd) {
+  if (!in_mu || !in_sd || !out_mu || !out_sd) return GD_ERR_ARG;
+  return mguard(p, [&] {
+    for (int i = 0; i < p->nin; ++i)
+      if (!(in_sd[i] > 0)) throw std::invalid_argument("gd_mlp_set_norm: input scales must be > 0");
+    GD_CUDA(cudaStreamSynchronize(p->stream));
+    GD_CUDA(cudaMemcpy(p->in_mu, in_mu, sizeof(float) * p->nin, cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemcpy(p->in_sd, in_sd, sizeof(float) * p->nin, cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemcpy(p->out_mu, out_mu, sizeof(float) * p->nout, cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemcpy(p->out_sd, out_sd, sizeof(float) * p->nout, cudaMemcpyHostToDevice));
+    p->has_norm = true;
+  });
+}
+
+int gd_mlp_forward(gd_mlp* p, const float* x, int ncols, float* y) {
+  if (!x || !y || ncols < 0) return GD_ERR_ARG;
+  return mguard(p, [&] {
+    mlp_reserve(p, ncols);
+    mlp_forward_on(p, x, ncols, y, p->stream);
+  });
+}
+
+int gd_mlp_loss_grad(gd_mlp* p, const float* x, const float* t, int ncols, float* loss, float* grad) {
+  if (!x || !t || ncols < 1) return GD_ERR_ARG;
+  return mguard(p, [&] {
+    mlp_reserve(p, ncols);
+    loss_grad(p, x, t, ncols);
+    GD_CUDA(cudaStreamSynchronize(p->stream));
+    if (loss) GD_CUDA(cudaMemcpy(loss, p->lossd, sizeof(float), cudaMemcpyDeviceToHost));
+    if (grad) GD_CUDA(cudaMemcpy(grad, p->grad, sizeof(float) * p->np, cudaMemcpyDeviceToHost));
+  });
+}
+
+int gd_mlp_train_step(gd_mlp* p, const float* x, const float* t, int ncols, float lr, float* loss) {
+  if (!x || !t || ncols < 1 || !(lr > 0)) return GD_ERR_ARG;
+  return mguard(p, [&] {
+    mlp_reserve(p, ncols);
+    loss_grad(p, x, t, ncols);
+    ++p->adam_t;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - std::pow(b1, (float)p->adam_t), c2 = 1.f - std::pow(b2, (float)p->adam_t);
+    k_adam<<<std::min(ceil_div(p->np, 256), 4096), 256, 0, p->stream>>>(p->p32, p->grad, p->am, p->av, p->w16, p->np,
+                                                                         lr, b1, b2, 1e-8f, c1, c2);
+    count_launch();
+    GD_LAUNCH_CHECK();
+    if (loss) {
+      GD_CUDA(cudaMemcpyAsync(loss, p->lossd, sizeof(float), cudaMemcpyDeviceToHost, p->stream));
+      GD_CUDA(cudaStreamSynchronize(p->stream));
+    }
+  });
+}
+
+int gd_mlp_set_stream(gd_mlp* p, void* stream) {
+  return mguard(p, [&] {
+    GD_CUDA(cudaStreamSynchronize(p->stream));
+    p->stream = stream ? (cudaStream_t)stream : p->own;
+  });
+}
+
+int gd_mlp_sync(gd_mlp* p) {
+  return mguard(p, [&] { GD_CUDA(cudaStreamSynchronize(p->stream)); });
+}
+
+const char* gd_mlp_last_error(gd_mlp* p) { return p ? p->err.c_str() : g_mlp_init_error.c_str(); }
+
+}  // extern "C"
+
+// ------------------------------------------------------ closure columns --
+namespace gd {
+namespace {
+constexpr int CT = 32;  // grid columns per CTA of the transposes
+}
+
+// rows of gS (column index fastest) -> x [column][feature] through a shared
+// tile: the reads and the writes both run along contiguous memory
+template <typename R>
+__global__ void k_closure_in(const R* __restrict__ gS, SynthRows s, int L, long ng, const float* __restrict__ mu,
+                             const float* __restrict__ sd, float* __restrict__ x) {
+  extern __shared__ float tile[];  // [nf][CT + 1]
+  const int nf = 3 * L + 1;
+  const long p0 = (long)blockIdx.x * CT;
+  for (int e = threadIdx.x; e < nf * CT; e += blockDim.x) {
+    const int f = e / CT, c = e % CT;
+    const long p = p0 + c;
+    float v = 0.f;
+    if (p < ng) {
+      if (f < L)
+        v = (float)gS[(long)(s.u + f) * ng + p];
+      else if (f < 2 * L)
+        v = (float)gS[(long)(s.v + f - L) * ng + p];
+      else if (f < 3 * L)
+        v = (float)gS[(long)(s.tv + f - 2 * L) * ng + p];
+      else
+        v = (float)exp(gS[(long)s.lnps * ng + p]);
+      if (mu) v = (v - mu[f]) / sd[f];
+    }
+    tile[f * (CT + 1) + c] = v;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nf * CT; e += blockDim.x) {
+    const int c = e / nf, f = e % nf;
+    const long p = p0 + c;
+    if (p < ng) x[p * nf + f] = tile[f * (CT + 1) + c];
+  }
+}
+
+template <typename R>
+__global__ void k_closure_out(const float* __restrict__ y, int L, long ng, const float* __restrict__ mu,
+                              const float* __restrict__ sd, R dt, R* __restrict__ gA) {
+  extern __shared__ float tile[];  // [3L][CT + 1]
+  const int no = 3 * L;
+  const long p0 = (long)blockIdx.x * CT;
+  for (int e = threadIdx.x; e < no * CT; e += blockDim.x) {
+    const int c = e / no, f = e % no;
+    const long p = p0 + c;
+    tile[f * (CT + 1) + c] = p < ng ? y[p * no + f] * sd[f] + mu[f] : 0.f;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < 4 * L * CT; e += blockDim.x) {
+    const int r = e / CT, c = e % CT;
+    const long p = p0 + c;
+    if (p >= ng) continue;
+    // grid row r: Tv [0,L) <- y[2L, 3L); q [L,2L) <- 0; u [2L,3L) <- y[0,L); v [3L,4L) <- y[L,2L)
+    const int f = r < L ? 2 * L + r : r < 2 * L ? -1 : r - 2 * L;
+    gA[(long)r * ng + p] = f < 0 ? R(0) : dt * (R)tile[f * (CT + 1) + c];
+  }
+}
+
+template <typename R>
+void launch_closure_in(const R* gS, const SynthRows& s, int L, long ng, const float* mu, const float* sd, float* x,
+                       cudaStream_t st) {
+  const size_t sm = sizeof(float) * (size_t)(3 * L + 1) * (CT + 1);
+  if (sm > 48 * 1024) GD_CUDA(cudaFuncSetAttribute(k_closure_in<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_closure_in<R><<<ceil_div(ng, CT), 256, sm, st>>>(gS, s, L, ng, mu, sd, x);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template <typename R>
+void launch_closure_out(const float* y, int L, long ng, const float* mu, const float* sd, R dt, R* gA,
+                        cudaStream_t st) {
+  const size_t sm = sizeof(float) * (size_t)(3 * L) * (CT + 1);
+  if (sm > 48 * 1024)
+    GD_CUDA(cudaFuncSetAttribute(k_closure_out<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_closure_out<R><<<ceil_div(ng, CT), 256, sm, st>>>(y, L, ng, mu, sd, dt, gA);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template void launch_closure_in<double>(const double*, const SynthRows&, int, long, const float*, const float*,
+                                        float*, cudaStream_t);
+template void launch_closure_in<float>(const float*, const SynthRows&, int, long, const float*, const float*, float*,
+                                       cudaStream_t);
+template void launch_closure_out<double>(const float*, int, long, const float*, const float*, double, double*,
+                                         cudaStream_t);
+template void launch_closure_out<float>(const float*, int, long, const float*, const float*, float, float*,
+                                        cudaStream_t);
+
+}  // namespace gd

@@ -523,7 +523,7 @@ template void launch_phys_update<float>(float*, long, const SpecCols&, int, int,
 
 template <typename R>
 __global__ void k_simple_update(R* S, long ldS, SpecCols sc, int L, int nlm, const R* AP, long ldAP, const R* AH,
-                                long ldAH, int massfix, R dt, R ainv, const R* lapv, R rerth) {
+                                long ldAH, int massfix, int hasq, R dt, R ainv, const R* lapv, R rerth) {
   typedef typename C2<R>::T V;
   const long total = (long)nlm * (L + 1);
   for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
@@ -544,21 +544,25 @@ __global__ void k_simple_update(R* S, long ldS, SpecCols sc, int L, int nlm, con
     }
     const R lap = lapv[idx];
     const R il = (idx == 0) ? R(0) : R(1) / lap;
-    V tv = ld2(S, idx, ldS, sc.tv + k), q = ld2(S, idx, ldS, sc.trc + k);
+    V tv = ld2(S, idx, ldS, sc.tv + k);
     V vr = ld2(S, idx, ldS, sc.vrt + k), dv = ld2(S, idx, ldS, sc.div + k);
-    const V at = ld2(AP, idx, ldAP, k), aq = ld2(AP, idx, ldAP, L + k);
+    const V at = ld2(AP, idx, ldAP, k);
     const V pv = ld2(AP, idx, ldAP, 2 * L + 1 + k), pd = ld2(AP, idx, ldAP, 3 * L + 1 + k);
     const V hv = ld2(AH, idx, ldAH, k), hd = ld2(AH, idx, ldAH, L + k);
     tv.x += dt * (at.x / dt);
     tv.y += dt * (at.y / dt);
-    q.x += dt * (aq.x / dt);
-    q.y += dt * (aq.y / dt);
+    if (hasq) {  // the first tracer's increment (the learned closure has none)
+      V q = ld2(S, idx, ldS, sc.trc + k);
+      const V aq = ld2(AP, idx, ldAP, L + k);
+      q.x += dt * (aq.x / dt);
+      q.y += dt * (aq.y / dt);
+      st2(S, idx, ldS, sc.trc + k, q);
+    }
     vr.x += dt * ((pv.x + hv.x) * ainv / dt);
     vr.y += dt * ((pv.y + hv.y) * ainv / dt);
     dv.x += dt * ((pd.x + hd.x) * ainv / dt);
     dv.y += dt * ((pd.y + hd.y) * ainv / dt);
     st2(S, idx, ldS, sc.tv + k, tv);
-    st2(S, idx, ldS, sc.trc + k, q);
     st2(S, idx, ldS, sc.vrt + k, vr);
     st2(S, idx, ldS, sc.div + k, dv);
     V s_, c_;
@@ -572,18 +576,18 @@ __global__ void k_simple_update(R* S, long ldS, SpecCols sc, int L, int nlm, con
 }
 template <typename R>
 void launch_simple_update(R* S, long ldS, const SpecCols& sc, int L, int nlm, const R* AP, long ldAP, const R* AH,
-                          long ldAH, int massfix, R dt, R ainv, const R* lapv, R rerth, cudaStream_t s) {
+                          long ldAH, int massfix, int hasq, R dt, R ainv, const R* lapv, R rerth, cudaStream_t s) {
   long total = (long)nlm * (L + 1);
   k_simple_update<R><<<std::min(ceil_div(total, 256), 8192), 256, 0, s>>>(S, ldS, sc, L, nlm, AP, ldAP, AH, ldAH,
-                                                                         massfix, dt, ainv, lapv, rerth);
+                                                                         massfix, hasq, dt, ainv, lapv, rerth);
   count_launch();
   GD_LAUNCH_CHECK();
 }
 template void launch_simple_update<double>(double*, long, const SpecCols&, int, int, const double*, long,
-                                           const double*, long, int, double, double, const double*, double,
+                                           const double*, long, int, int, double, double, const double*, double,
                                            cudaStream_t);
 template void launch_simple_update<float>(float*, long, const SpecCols&, int, int, const float*, long, const float*,
-                                          long, int, float, float, const float*, float, cudaStream_t);
+                                          long, int, int, float, float, const float*, float, cudaStream_t);
 
 // prognostic column j of the state layout: the (3+nt) L columns from vrt, then lnps
 __device__ __forceinline__ int prog_col(const SpecCols& sc, int ncs, int j) { return j < ncs ? sc.vrt + j : sc.lnps; }

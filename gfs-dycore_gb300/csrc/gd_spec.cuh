@@ -85,11 +85,11 @@ void launch_phys_update(R* S, long ldS, const SpecCols& sc, int L, int nt, int n
 // Tv, [L,2L) q, 2L dry-mass fixer, [2L+1,3L+1) and [3L+1,4L+1) the
 // i m/cos parts of vorticity and divergence, AH columns [0,L) and [L,2L)
 // their d/dphi parts; tendency = analysis / dt (vorticity, divergence scaled
-// by 1/a), state += dt * tendency for Tv, tracer 1, vorticity, divergence;
+// by 1/a), state += dt * tendency for Tv, tracer 1 (hasq), vorticity, divergence;
 // lnps from the fixer (or unchanged); recomputes s, c.
 template <typename R>
 void launch_simple_update(R* S, long ldS, const SpecCols& sc, int L, int nlm, const R* AP, long ldAP, const R* AH,
-                          long ldAH, int massfix, R dt, R ainv, const R* lapv, R rerth, cudaStream_t s);
+                          long ldAH, int massfix, int hasq, R dt, R ainv, const R* lapv, R rerth, cudaStream_t s);
 
 // IAU forcing of one step (iau_module.f90:88-135): F = (ca inc[ia] + cb
 // inc[ib]) / dtiau over the prognostic columns of the state layout (the

@@ -15,7 +15,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libgdcore.so")
 SOURCES = ["gd_sht.cu", "gd_grid.cu", "gd_spec.cu", "gd_tc.cu", "gd_dycore.cu", "gd_noalloc.cu", "gd_pattern.cu",
-           "gd_physics.cu", "gd_sigio.cpp", "gd_dcmip.cpp"]
+           "gd_physics.cu", "gd_mlp.cu", "gd_sigio.cpp", "gd_dcmip.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no FMA contraction (the single-precision pattern set-up is
 # specified operation by operation)

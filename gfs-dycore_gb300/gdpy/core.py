@@ -40,6 +40,9 @@ API_FUNCTIONS = [
     "gd_sigio_head_init", "gd_sigio_read_head", "gd_sigio_read", "gd_sigio_write", "gd_sigio_config",
     "gd_read_sig", "gd_write_sig", "gd_sigio_last_error", "gd_dcmip_ics",
     "gd_dcmip_point", "gd_set_iau", "gd_set_iau_files", "gd_dfi", "gd_dfi_weights",
+    "gd_mlp_init", "gd_mlp_destroy", "gd_mlp_nparams", "gd_mlp_get_params", "gd_mlp_set_params",
+    "gd_mlp_set_norm", "gd_mlp_forward", "gd_mlp_loss_grad", "gd_mlp_train_step", "gd_mlp_set_stream",
+    "gd_mlp_sync", "gd_mlp_last_error", "gd_set_closure", "gd_closure_features",
 ]
 PHASES = ["legendre_synth", "fft_synth", "columns", "fft_anal", "legendre_anal", "semi_implicit",
           "physics", "other", "column_physics"]
@@ -122,6 +125,22 @@ def load(build_if_missing=True):
     L.gd_set_iau_files.argtypes = [vp, i, vp, d, ctypes.POINTER(cp), ctypes.POINTER(cp)]
     L.gd_dfi.argtypes = [vp, d, i]
     L.gd_dfi_weights.argtypes = [i, vp]
+    f = ctypes.c_float
+    L.gd_mlp_init.argtypes = [i, i, i, i, ctypes.c_ulonglong, i, ctypes.POINTER(vp)]
+    L.gd_mlp_destroy.argtypes = [vp]
+    L.gd_mlp_nparams.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+    L.gd_mlp_get_params.argtypes = [vp, vp]
+    L.gd_mlp_set_params.argtypes = [vp, vp]
+    L.gd_mlp_set_norm.argtypes = [vp, vp, vp, vp, vp]
+    L.gd_mlp_forward.argtypes = [vp, vp, i, vp]
+    L.gd_mlp_loss_grad.argtypes = [vp, vp, vp, i, vp, vp]
+    L.gd_mlp_train_step.argtypes = [vp, vp, vp, i, f, vp]
+    L.gd_mlp_set_stream.argtypes = [vp, vp]
+    L.gd_mlp_sync.argtypes = [vp]
+    L.gd_mlp_last_error.restype = ctypes.c_char_p
+    L.gd_mlp_last_error.argtypes = [vp]
+    L.gd_set_closure.argtypes = [vp, vp]
+    L.gd_closure_features.argtypes = [vp, vp]
     _lib = L
     return L
 
@@ -270,6 +289,18 @@ class Dycore:
         """Attach a Pattern as stochastically perturbed physics (None detaches)."""
         self._sppt = pattern  # keep the generator alive while attached
         self._chk(load().gd_set_sppt(self.h, pattern.h if pattern is not None else None, sigtop, sigbot))
+
+    def set_closure(self, net):
+        """Attach a trained Mlp as the learned per-column closure (None detaches)."""
+        self._closure = net  # keep the net alive while attached
+        self._chk(load().gd_set_closure(self.h, net.h if net is not None else None))
+
+    def closure_features(self):
+        """Raw closure inputs of the current state: float32 [nlat*nlon, 3 nlev + 1]
+        (u, v, Tv at the levels bottom to top, then ps in Pa)."""
+        out = np.zeros((self.nlat * self.nlon, 3 * self.nlev + 1), np.float32)
+        self._chk(load().gd_closure_features(self.h, _p(out)))
+        return out
 
     def advance(self, nsteps=1, t=0.0):
         self._chk(load().gd_advance(self.h, ctypes.c_double(t), int(nsteps)))
@@ -426,3 +457,83 @@ def ensemble_advance(members, nsteps=1):
     if rc != GD_OK:
         raise GdError(rc, "gd_ensemble_advance failed: " + "; ".join(
             load().gd_last_error(m.h).decode() for m in members))
+
+
+class Mlp:
+    """The learned closure's network (gd_mlp): nin -> nhidden (GELU) x nlayers
+    -> nout, BF16 weights with FP32 accumulation, trained by the library's own
+    forward/backward kernels.  Batches are torch CUDA float32 tensors
+    [ncols, nin] / [ncols, nout] on the net's device."""
+
+    def __init__(self, nin, nhidden, nlayers, nout, seed=1, device=0):
+        L = load()
+        h = ctypes.c_void_p()
+        rc = L.gd_mlp_init(nin, nhidden, nlayers, nout, seed, device, ctypes.byref(h))
+        if rc != GD_OK:
+            raise GdError(rc, L.gd_mlp_last_error(None).decode())
+        self.h = h
+        self.nin, self.nhidden, self.nlayers, self.nout, self.device = nin, nhidden, nlayers, nout, device
+        n = ctypes.c_longlong()
+        self._chk(L.gd_mlp_nparams(h, ctypes.byref(n)))
+        self.nparams = n.value
+
+    def _chk(self, rc):
+        if rc != GD_OK:
+            raise GdError(rc, load().gd_mlp_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().gd_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def layer_shapes(self):
+        """(fout, fin) of each linear layer, in the packed parameter order."""
+        sizes = [self.nin] + [self.nhidden] * self.nlayers + [self.nout]
+        return [(sizes[i + 1], sizes[i]) for i in range(len(sizes) - 1)]
+
+    def get_params(self):
+        out = np.zeros(self.nparams, np.float32)
+        self._chk(load().gd_mlp_get_params(self.h, _p(out)))
+        return out
+
+    def set_params(self, params):
+        a = np.ascontiguousarray(params, np.float32)
+        if a.size != self.nparams:
+            raise ValueError("parameter count")
+        self._chk(load().gd_mlp_set_params(self.h, _p(a)))
+
+    def set_norm(self, in_mu, in_sd, out_mu, out_sd):
+        arrs = [np.ascontiguousarray(x, np.float32) for x in (in_mu, in_sd, out_mu, out_sd)]
+        self._norm = arrs
+        self._chk(load().gd_mlp_set_norm(self.h, *[_p(x) for x in arrs]))
+
+    def forward(self, x):
+        import torch
+
+        y = torch.empty((x.shape[0], self.nout), dtype=torch.float32, device=x.device)
+        self._chk(load().gd_mlp_forward(self.h, ctypes.c_void_p(x.data_ptr()), int(x.shape[0]),
+                                        ctypes.c_void_p(y.data_ptr())))
+        self.sync()
+        return y
+
+    def loss_grad(self, x, t):
+        loss = np.zeros(1, np.float32)
+        g = np.zeros(self.nparams, np.float32)
+        self._chk(load().gd_mlp_loss_grad(self.h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(t.data_ptr()),
+                                          int(x.shape[0]), _p(loss), _p(g)))
+        return float(loss[0]), g
+
+    def train_step(self, x, t, lr, want_loss=False):
+        loss = np.zeros(1, np.float32)
+        self._chk(load().gd_mlp_train_step(self.h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(t.data_ptr()),
+                                           int(x.shape[0]), ctypes.c_float(lr), _p(loss) if want_loss else None))
+        return float(loss[0]) if want_loss else None
+
+    def sync(self):
+        self._chk(load().gd_mlp_sync(self.h))

@@ -379,6 +379,50 @@ int gd_write_sig(gd_ctx* ctx, const char* path, double fhour, gd_sighead* head);
 /* Text of the calling thread's last sigma-file failure. */
 const char* gd_sigio_last_error(void);
 
+/* ---- Learned per-column closure -----------------------------------------
+   A fully connected network nin -> nhidden (GELU) x nlayers -> nout with
+   BF16 weights and FP32 accumulation, trained on the GPU by the library's
+   own forward and backward kernels (mean-squared error, Adam).  The closure
+   configuration is a coarse run (T62L64) whose tendencies the network
+   corrects from each grid column's u, v, Tv (levels bottom to top) and ps:
+   nin = 3 nlev + 1, nout = 3 nlev (du/dt, dv/dt, dTv/dt).  It has no
+   counterpart in the reference, whose plain step stays the fallback and the
+   judge of its error.  x, t and y below are device pointers of float
+   [ncols][nin] / [ncols][nout]; parameters are host float arrays in the
+   packed layout (per layer W [fout][fin] row-major, then b [fout]). */
+typedef struct gd_mlp gd_mlp;
+/* A net with He-normal hidden weights from seed (output layer x 0.1). */
+int gd_mlp_init(int nin, int nhidden, int nlayers, int nout, unsigned long long seed, int device, gd_mlp** out);
+int gd_mlp_destroy(gd_mlp* net);
+int gd_mlp_nparams(gd_mlp* net, long long* n);
+int gd_mlp_get_params(gd_mlp* net, float* params);
+int gd_mlp_set_params(gd_mlp* net, const float* params);
+/* Normalisation of a closure's raw inputs ((x - in_mu) / in_sd) and outputs
+   (y out_sd + out_mu), host arrays of nin and nout. */
+int gd_mlp_set_norm(gd_mlp* net, const float* in_mu, const float* in_sd, const float* out_mu, const float* out_sd);
+/* y = net(x) on the net's stream (asynchronous). */
+int gd_mlp_forward(gd_mlp* net, const float* x, int ncols, float* y);
+/* Mean-squared error of net(x) against t and its gradient with respect to
+   the parameters (host float[nparams], may be NULL); synchronous. */
+int gd_mlp_loss_grad(gd_mlp* net, const float* x, const float* t, int ncols, float* loss, float* grad);
+/* One Adam step (beta 0.9, 0.999, eps 1e-8) on the batch (x, t); the loss
+   before the step to *loss when not NULL (then synchronous). */
+int gd_mlp_train_step(gd_mlp* net, const float* x, const float* t, int ncols, float lr, float* loss);
+/* Runs the net's own calls on an external CUDA stream (NULL: its own). */
+int gd_mlp_set_stream(gd_mlp* net, void* stream);
+int gd_mlp_sync(gd_mlp* net);
+/* Text of the last error on net (or of the last failed gd_mlp_init if NULL). */
+const char* gd_mlp_last_error(gd_mlp* net);
+/* Attaches a trained net (with its normalisation) to ctx: every step, after
+   the forcing, the net's tendencies times dt are added to Tv and, through
+   the vector analysis, to vorticity and divergence.  NULL detaches.  The net
+   must live on ctx's device with nin = 3 nlev + 1 and nout = 3 nlev; it
+   runs on ctx's stream while attached. */
+int gd_set_closure(gd_ctx* ctx, gd_mlp* net);
+/* The raw closure inputs of ctx's current state, host float[nlat nlon][3
+   nlev + 1]: u, v, Tv at the levels bottom to top and ps (Pa) per column. */
+int gd_closure_features(gd_ctx* ctx, float* x);
+
 /* Runs the context on an external CUDA stream (cudaStream_t as void*). */
 int gd_set_stream(gd_ctx* ctx, void* stream);
 /* Waits for all work of the context. */

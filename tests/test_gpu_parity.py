@@ -141,6 +141,27 @@ def test_steps_with_tracers_fp64(oracle_mod):
         assert rel(a[k], b[k]) < 1e-10, (k, rel(a[k], b[k]))
 
 
+@pytest.mark.parametrize("L", [7, 13])
+def test_steps_odd_levels(oracle_mod, L):
+    # odd L: the one-level-per-thread form of the stage's level products and
+    # a partial last block of levels in the column kernel
+    T = 21
+    g, o = pair(oracle_mod, T, L, ntrac=2, dt=900.0)
+    set_both(g, o, inputs.smooth_random_state(T, L, ntrac=2, seed=21))
+    g.advance(3)
+    o.advance(3)
+    a, b = g.get_state(), o.get_state()
+    for k in ("vrt", "div", "tv", "lnps", "trc"):
+        assert rel(a[k], b[k]) < 1e-10, (k, rel(a[k], b[k]))
+    g32, _ = pair(oracle_mod, T, L, ntrac=2, dt=900.0, precision="fp32")
+    st = inputs.smooth_random_state(T, L, ntrac=2, seed=21)
+    g32.set_state(st["vrt"], st["div"], st["tv"], st["lnps"], trc=st["trc"])
+    g32.advance(3)
+    c = g32.get_state()
+    for k in ("vrt", "tv", "lnps"):
+        assert rel(c[k], b[k]) < 1e-4, (k, rel(c[k], b[k]))
+
+
 def test_one_day_trajectory_t42l20(oracle_mod):
     g, o = pair(oracle_mod, 42, 20)
     set_both(g, o, inputs.hs_rest_state(42, 20, seed=0))

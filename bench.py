@@ -302,6 +302,8 @@ def gpu_arm(args):
         out["pattern_generator"] = pattern_generator_rate()
         if not args.no_dcmip:
             out["dcmip_simple_physics"] = dcmip_rate(args.precision)
+        if not args.no_closure:
+            out["learned_closure"] = closure_rate(args.precision)
         print(json.dumps(out))
     g.close()
     grp.close()
@@ -351,6 +353,62 @@ def dcmip_rate(precision, steps=10, warmup=3):
                 column_kernel=dict(kernel="k_simple_physics", bound="hbm", ms=cms, bytes=byt, achieved=achieved,
                                    peak=hbm["hbm"], unit="GB/s", frac=achieved / hbm["hbm"],
                                    peak_source=hbm["src"]))
+
+
+def closure_rate(precision, steps=20, warmup=3, train_steps=50):
+    """The learned per-column closure's configuration: a Held-Suarez T62L64
+    step (dt 1200 s) with and without a closure net of the configured shape
+    (193 -> 256 GELU x 3 -> 192, BF16 weights, FP32 accumulation; seeded
+    weights and a unit normalisation: the cost does not depend on the values),
+    and the training throughput of the library's forward + backward + Adam
+    kernels on minibatches of 4096 columns.  Flops: 2 x 230 592 per column
+    and inference, 6 x per column and training step."""
+    import torch
+
+    from gdpy import core, inputs
+
+    T, nlon, nlat, L, dt = 62, 192, 94, 64, 1200.0
+    ak, bk = inputs.hybrid_coords(L)
+    st = inputs.hs_rest_state(T, L, seed=3)
+    stream = torch.cuda.Stream()
+    res = {}
+    net = core.Mlp(3 * L + 1, 256, 3, 3 * L, seed=2)
+    net.set_norm(np.zeros(3 * L + 1), np.ones(3 * L + 1), np.zeros(3 * L), np.full(3 * L, 1e-6))
+    for name, use in (("plain", None), ("closure", net)):
+        g = core.Dycore(T, nlon, nlat, L, ak, bk, ntrac=0, dt=dt, precision=precision)
+        g.set_stream(stream.cuda_stream)
+        g.set_state(st["vrt"], st["div"], st["tv"], st["lnps"])
+        if use is not None:
+            g.set_closure(use)
+        g.advance(warmup)
+        g.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.advance(steps)
+        e1.record(stream)
+        g.sync()
+        res[name] = e0.elapsed_time(e1) / steps
+        if use is not None:
+            g.set_closure(None)
+        g.close()
+    ncol = nlon * nlat
+    x = torch.randn(4096, 3 * L + 1, device="cuda")
+    t = torch.randn(4096, 3 * L, device="cuda")
+    for _ in range(3):
+        net.train_step(x, t, 1e-4)
+    net.sync()
+    t0 = time.perf_counter()
+    for _ in range(train_steps):
+        net.train_step(x, t, 1e-4)
+    net.sync()
+    tr = (time.perf_counter() - t0) / train_steps
+    flop = 2.0 * net.nparams
+    return dict(workload="Held-Suarez T62L64 dt 1200 s, closure net 193-256x3-192", precision=precision,
+                ms_per_step_plain=res["plain"], ms_per_step_closure=res["closure"],
+                closure_ms_per_step=res["closure"] - res["plain"],
+                inference_tflops=flop * ncol / ((res["closure"] - res["plain"]) * 1e-3) / 1e12,
+                train_ms_per_batch4096=tr * 1e3, train_columns_per_s=4096 / tr,
+                train_tflops=3 * flop * 4096 / tr / 1e12)
 
 
 def pattern_generator_rate(steps=40, cpu_steps=3):
@@ -458,6 +516,7 @@ def main():
     ap.add_argument("--cpu-levels", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-dcmip", action="store_true", help="skip the DCMIP simple-physics side measurement")
+    ap.add_argument("--no-closure", action="store_true", help="skip the learned-closure side measurement")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gd":
         args.warmup = 3

@@ -198,7 +198,10 @@ class Dycore : public DycoreBase {
     }
     launch_anal<R>(sd, useH, plan, G, ldG, ncr, A, ldA, stream);
   }
-  void check() override { tc_status(); }
+  void check() override {
+    tc_status();
+    if (closure) mlp_check(closure, stream);
+  }
   void tc_status() {
     if (tcp && tc_check(*tcp, stream))
       throw CudaError("tensor-core Legendre pipeline: a bounded wait gave up (results invalid)");

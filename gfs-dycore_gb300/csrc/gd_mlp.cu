@@ -13,7 +13,11 @@
 // one tiled SIMT GEMM serves every product: 64 x 64 output tiles, K in steps
 // of 16 through shared memory, 4 x 4 outputs per thread, operands addressed
 // through (row, column) strides so the same kernel forms X W^T, dZ^T X and
-// dZ W, with the bias/GELU or GELU-derivative epilogue fused.
+// dZ W, with the bias/GELU or GELU-derivative epilogue fused.  Inference
+// (gd_mlp_forward and the closure in the step) runs on the tensor cores
+// instead (k_tc_mlp in gd_tc.cu): the weights are exact in TF32 and each
+// activation is split into TF32 hi + lo, so two MMAs per K step give the
+// FP32 products of the BF16 net.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -27,6 +31,7 @@
 #include "gd_api.h"
 #include "gd_common.cuh"
 #include "gd_mlp.cuh"
+#include "gd_tc.cuh"
 
 struct gd_mlp {
   int device = 0;
@@ -50,6 +55,17 @@ struct gd_mlp {
   float *zb = nullptr, *ab = nullptr, *yb = nullptr, *gy = nullptr, *g0 = nullptr, *g1 = nullptr;
   float* partial = nullptr;  // loss partial sums
   float* lossd = nullptr;
+  // tensor-core inference (gd_tc.cu, k_tc_mlp): weights exact in TF32, padded
+  // to [Np][Kp] per layer; the input and hidden activations split hi + lo
+  bool tc = false;
+  std::vector<int> kp, npd;
+  std::vector<long> tcoff;
+  float* wtc = nullptr;
+  uint32_t *xh = nullptr, *xl = nullptr;
+  uint32_t* hh[2] = {nullptr, nullptr};
+  uint32_t* hl[2] = {nullptr, nullptr};
+  std::vector<gd::TcMlpLayer> layers;
+  int* terr = nullptr;
   cudaStream_t stream = nullptr;  // the stream the net's work runs on
   cudaStream_t own = nullptr;     // the net's own stream (destroyed with it)
   std::string err;
@@ -251,6 +267,27 @@ __global__ void k_to_bf16(const float* p, __nv_bfloat16* w16, long n) {
     w16[i] = __float2bfloat16_rn(p[i]);
 }
 
+// a layer's BF16 weights as FP32 (exact in TF32), padded to [Np][Kp] with zeros
+__global__ void k_w_tc(const __nv_bfloat16* __restrict__ w, int fo, int fi, int Np, int Kp, float* __restrict__ o) {
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < (long)Np * Kp; e += (long)gridDim.x * blockDim.x) {
+    const int n = (int)(e / Kp), k = (int)(e % Kp);
+    o[e] = (n < fo && k < fi) ? __bfloat162float(w[(long)n * fi + k]) : 0.f;
+  }
+}
+// inputs x [n][nin] split to TF32 hi + lo rows of pitch Kp (the padding
+// columns stay zero from allocation)
+__global__ void k_split_in(const float* __restrict__ x, long n, int nin, int Kp, uint32_t* __restrict__ xh,
+                           uint32_t* __restrict__ xl) {
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n * nin; e += (long)gridDim.x * blockDim.x) {
+    const long m = e / nin;
+    const int k = (int)(e % nin);
+    const float v = x[e];
+    const uint32_t h = (__float_as_uint(v) + 0x1000u) & 0xFFFFE000u;  // nearest TF32, ties away
+    xh[m * Kp + k] = h;
+    xl[m * Kp + k] = __float_as_uint(v - __uint_as_float(h));
+  }
+}
+
 template <typename F>
 int mguard(gd_mlp* p, F f) {
   if (!p) return GD_ERR_ARG;
@@ -296,12 +333,83 @@ void mlp_reserve(gd_mlp* p, int ncols) {
   p->g0 = (float*)p->alloc(sizeof(float) * (size_t)ncols * w);
   p->g1 = (float*)p->alloc(sizeof(float) * (size_t)ncols * w);
   p->bcap = ncols;
+  if (p->tc) {  // tensor-core operands (zero padding) and the layers' tensor maps
+    for (uint32_t* b : {p->xh, p->xl, p->hh[0], p->hh[1], p->hl[0], p->hl[1]})
+      if (b) p->release(b);
+    const int ldh = p->kp.size() > 1 ? p->kp[1] : p->kp[0];
+    auto z = [&](size_t words) {
+      uint32_t* b = (uint32_t*)p->alloc(sizeof(uint32_t) * words);
+      GD_CUDA(cudaMemsetAsync(b, 0, sizeof(uint32_t) * words, p->stream));
+      return b;
+    };
+    p->xh = z((size_t)ncols * p->kp[0]);
+    p->xl = z((size_t)ncols * p->kp[0]);
+    for (int i = 0; i < 2; ++i) {
+      p->hh[i] = z((size_t)ncols * ldh);
+      p->hl[i] = z((size_t)ncols * ldh);
+    }
+    GD_CUDA(cudaStreamSynchronize(p->stream));
+    p->layers.assign(p->nlayer, TcMlpLayer{});
+    for (int l = 0; l < p->nlayer; ++l) {
+      TcMlpLayer& L = p->layers[l];
+      L.M = ncols;
+      L.N = p->fout[l];
+      L.Np = p->npd[l];
+      L.Kp = p->kp[l];
+      L.bias = p->p32 + p->offb[l];
+      L.gelu = l < p->nl;
+      L.err = p->terr;
+      const uint32_t* ah = l == 0 ? p->xh : p->hh[(l - 1) & 1];
+      const uint32_t* al = l == 0 ? p->xl : p->hl[(l - 1) & 1];
+      if (L.gelu) {
+        L.oh = p->hh[l & 1];
+        L.ol = p->hl[l & 1];
+        L.ldo = ldh;
+      }
+      tc_mlp_maps(L, ah, al, p->wtc + p->tcoff[l]);
+    }
+  }
 }
 
-// y [n][nout] = net(x [n][nin]) on stream s; the hidden activations stay in
-// the net's buffers for a backward pass.  No allocation when n <= bcap.
+namespace {
+void forward_simt(gd_mlp* p, const float* x, int n, float* y, cudaStream_t s);
+// the tensor-core forward: weights refreshed from the BF16 copy, inputs
+// split, one k_tc_mlp launch per layer
+void forward_tc(gd_mlp* p, const float* x, int n, float* y, cudaStream_t s) {
+  for (int l = 0; l < p->nlayer; ++l) {
+    const long cnt = (long)p->npd[l] * p->kp[l];
+    k_w_tc<<<std::min(ceil_div(cnt, 256), 1024), 256, 0, s>>>(p->w16 + p->offw[l], p->fout[l], p->fin[l], p->npd[l],
+                                                              p->kp[l], p->wtc + p->tcoff[l]);
+  }
+  k_split_in<<<std::min(ceil_div((long)n * p->nin, 256), 8192), 256, 0, s>>>(x, n, p->nin, p->kp[0], p->xh, p->xl);
+  count_launch(p->nlayer + 1);
+  GD_LAUNCH_CHECK();
+  for (int l = 0; l < p->nlayer; ++l) {
+    TcMlpLayer L = p->layers[l];
+    L.M = n;  // rows past n are neither needed nor stored
+    if (!L.gelu) {
+      L.y = y;
+      L.ldy = p->nout;
+    }
+    tc_mlp_layer(L, s);
+  }
+}
+}  // namespace
+
+// y [n][nout] = net(x [n][nin]) on stream s, on the tensor cores when the
+// shape allows (every layer at most 256 wide).  No allocation when n <= bcap.
 void mlp_forward_on(gd_mlp* p, const float* x, int n, float* y, cudaStream_t s) {
   if (n > p->bcap) throw std::invalid_argument("gd_mlp: batch above the reserved capacity");
+  if (p->tc)
+    forward_tc(p, x, n, y, s);
+  else
+    forward_simt(p, x, n, y, s);
+}
+
+namespace {
+// the SIMT forward; the hidden pre-activations and activations stay in the
+// net's buffers for a backward pass
+void forward_simt(gd_mlp* p, const float* x, int n, float* y, cudaStream_t s) {
   const float* in = x;
   for (int l = 0; l < p->nlayer; ++l) {
     const int fi = p->fin[l], fo = p->fout[l];
@@ -315,6 +423,20 @@ void mlp_forward_on(gd_mlp* p, const float* x, int n, float* y, cudaStream_t s) 
     } else {
       gemm(n, fo, fi, in, (long)fi, 1L, W, 1L, (long)fi, EpiLinear{b, y, fo}, s);
     }
+  }
+}
+}  // namespace
+
+// raises (and clears) a bounded wait's timeout in the tensor-core forward
+void mlp_check(gd_mlp* p, cudaStream_t s) {
+  if (!p->terr) return;
+  int e = 0;
+  GD_CUDA(cudaMemcpyAsync(&e, p->terr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GD_CUDA(cudaStreamSynchronize(s));
+  if (e) {
+    GD_CUDA(cudaMemsetAsync(p->terr, 0, sizeof(int), s));
+    GD_CUDA(cudaStreamSynchronize(s));
+    throw CudaError("closure net: a tensor-core wait timed out (code " + std::to_string(e) + ")");
   }
 }
 
@@ -334,7 +456,7 @@ namespace {
 // loss and gradient of a batch into p->grad; the loss lands in p->lossd
 void loss_grad(gd_mlp* p, const float* x, const float* t, int n) {
   cudaStream_t s = p->stream;
-  mlp_forward_on(p, x, n, p->yb, s);
+  forward_simt(p, x, n, p->yb, s);
   const long cnt = (long)n * p->nout;
   const int nb = std::min(KPART, ceil_div(cnt, 256));
   k_mse<<<nb, 256, 0, s>>>(p->yb, t, cnt, p->gy, p->partial);
@@ -392,6 +514,16 @@ int gd_mlp_init(int nin, int nhidden, int nlayers, int nout, unsigned long long 
     off += fo;
   }
   p->np = off;
+  // tensor-core inference when every layer is at most 256 wide
+  p->tc = true;
+  long toff = 0;
+  for (int l = 0; l < p->nlayer; ++l) {
+    p->kp.push_back((p->fin[l] + 31) / 32 * 32);
+    p->npd.push_back((p->fout[l] + 15) / 16 * 16);
+    if (p->npd[l] > 256) p->tc = false;
+    p->tcoff.push_back(toff);
+    toff += (long)p->npd[l] * p->kp[l];
+  }
   // He-normal hidden weights, the output layer scaled by 0.1 (the net starts
   // close to no correction), zero biases
   std::vector<float> h(off, 0.f);
@@ -415,6 +547,11 @@ int gd_mlp_init(int nin, int nhidden, int nlayers, int nout, unsigned long long 
     p->in_sd = (float*)p->alloc(sizeof(float) * nin);
     p->out_mu = (float*)p->alloc(sizeof(float) * nout);
     p->out_sd = (float*)p->alloc(sizeof(float) * nout);
+    if (p->tc) {
+      p->wtc = (float*)p->alloc(sizeof(float) * toff);
+      p->terr = (int*)p->alloc(sizeof(int));
+      GD_CUDA(cudaMemset(p->terr, 0, sizeof(int)));
+    }
     GD_CUDA(cudaMemcpy(p->p32, h.data(), sizeof(float) * off, cudaMemcpyHostToDevice));
     GD_CUDA(cudaMemset(p->am, 0, sizeof(float) * off));
     GD_CUDA(cudaMemset(p->av, 0, sizeof(float) * off));
@@ -479,6 +616,7 @@ int gd_mlp_forward(gd_mlp* p, const float* x, int ncols, float* y) {
   return mguard(p, [&] {
     mlp_reserve(p, ncols);
     mlp_forward_on(p, x, ncols, y, p->stream);
+    mlp_check(p, p->stream);
   });
 }
 
@@ -520,7 +658,9 @@ int gd_mlp_set_stream(gd_mlp* p, void* stream) {
 }
 
 int gd_mlp_sync(gd_mlp* p) {
-  return mguard(p, [&] { GD_CUDA(cudaStreamSynchronize(p->stream)); });
+  return mguard(p, [&] {
+    mlp_check(p, p->stream);
+  });
 }
 
 const char* gd_mlp_last_error(gd_mlp* p) { return p ? p->err.c_str() : g_mlp_init_error.c_str(); }

@@ -11,6 +11,8 @@ namespace gd {
 
 void mlp_reserve(gd_mlp* p, int ncols);
 void mlp_forward_on(gd_mlp* p, const float* x, int n, float* y, cudaStream_t s);
+// throws when a bounded wait of the tensor-core forward timed out
+void mlp_check(gd_mlp* p, cudaStream_t s);
 int mlp_nin(const gd_mlp* p);
 int mlp_nout(const gd_mlp* p);
 int mlp_device(const gd_mlp* p);

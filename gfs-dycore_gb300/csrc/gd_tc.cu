@@ -1350,4 +1350,163 @@ int tc_check(TcPlan& p, cudaStream_t s) {
   return h;
 }
 
+
+// ------------------------------------------- closure network layers --
+// One CTA per 128 rows (grid columns of the closure); warp 0's first thread
+// issues the TMA copies of A hi, A lo and W per 32-wide K chunk into a
+// 3-stage ring, warp 1's first thread issues two MMAs per K step (hi W and
+// lo W; W is exact in TF32), all four warps drain the accumulator (warp w
+// holds TMEM lanes 32w..32w+31 = rows).  Every wait is bounded.
+struct TcMlpArgs {
+  int M, N, Np, nk;
+  const float* bias;
+  int gelu;
+  uint32_t* oh;
+  uint32_t* ol;
+  int ldo;
+  float* y;
+  int ldy;
+  int* err;
+  uint32_t idesc, tmem_cols;
+};
+
+__device__ __forceinline__ float tc_gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_tc_mlp(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+             const __grid_constant__ CUtensorMap mW, TcMlpArgs a) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t)1023);
+  const uint32_t bytesA = TC_M * 128, bytesW = (uint32_t)a.Np * 128;
+  const uint32_t stage_bytes = 2 * bytesA + bytesW;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + TC_NS * stage_bytes);
+  uint64_t* empty = full + TC_NS;
+  uint64_t* done = empty + TC_NS;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * TC_M;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(a.tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < TC_NS; ++s) {
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&empty[s]), 1);
+    }
+    mbar_init(smem_u32(done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+
+  if (tid == 0) {  // ---- TMA producer
+    int fills[TC_NS] = {0, 0, 0};
+    for (int i = 0; i < a.nk; ++i) {
+      const int s = i % TC_NS, u = i / TC_NS;
+      if (u >= 1 && !mbar_wait(smem_u32(&empty[s]), (u - 1) & 1, a.err, 31)) break;
+      unsigned char* st = sm + s * stage_bytes;
+      const uint32_t fb = smem_u32(&full[s]);
+      mbar_expect_tx(fb, stage_bytes);
+      tma_2d(smem_u32(st), &mAh, i * 32, m0, fb);
+      tma_2d(smem_u32(st + bytesA), &mAl, i * 32, m0, fb);
+      tma_2d(smem_u32(st + 2 * bytesA), &mW, i * 32, 0, fb);
+      ++fills[s];
+    }
+    for (int s = 0; s < TC_NS; ++s)  // never leave with copies in flight
+      if (fills[s] > 0) mbar_wait(smem_u32(&full[s]), (fills[s] - 1) & 1, a.err, 32);
+  } else if (tid == 32) {  // ---- MMA issuer
+    for (int i = 0; i < a.nk; ++i) {
+      const int s = i % TC_NS, u = i / TC_NS;
+      if (!mbar_wait(smem_u32(&full[s]), u & 1, a.err, 33)) break;
+      tc_fence_after();
+      unsigned char* st = sm + s * stage_bytes;
+      const uint64_t dah = smem_desc(smem_u32(st)), dal = smem_desc(smem_u32(st + bytesA));
+      const uint64_t dw = smem_desc(smem_u32(st + 2 * bytesA));
+#pragma unroll
+      for (int k4 = 0; k4 < 4; ++k4) {  // 4 MMAs of K = 8 per 128-byte row
+        const uint64_t o = (uint64_t)(2 * k4);
+        mma<TC_TF32>(tbase, dah + o, dw + o, a.idesc, (i > 0 || k4 > 0) ? 1u : 0u);
+        mma<TC_TF32>(tbase, dal + o, dw + o, a.idesc, 1u);
+      }
+      mma_commit(smem_u32(&empty[s]));
+    }
+    mma_commit(smem_u32(done));  // every issued MMA has completed at done
+  }
+  __syncwarp();
+  // ---- epilogue
+  const bool ok = mbar_wait(smem_u32(done), 0, a.err, 34);
+  tc_fence_after();
+  const bool go = __all_sync(0xffffffffu, ok && *(volatile int*)a.err == 0);
+  if (go) {
+    const int m = m0 + warp * 32 + lane;
+    const uint32_t tw = tbase + ((uint32_t)(warp * 32) << 16);
+    for (int g = 0; g < a.Np; g += 16) {
+      float v[16];
+      tmem_ld16(tw + g, v);
+      if (m < a.M) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int n = g + q;
+          if (n < a.N) {
+            const float z = v[q] + a.bias[n];
+            if (a.gelu) {
+              uint32_t h, l;
+              Elem<TC_TF32>::splitf(tc_gelu(z), h, l);
+              a.oh[(long)m * a.ldo + n] = h;
+              a.ol[(long)m * a.ldo + n] = l;
+            } else {
+              a.y[(long)m * a.ldy + n] = z;
+            }
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(a.tmem_cols));
+}
+
+void tc_mlp_maps(TcMlpLayer& L, const uint32_t* ah, const uint32_t* al, const float* w) {
+  if (L.Kp % 32 || L.Np % 16 || L.Np < 16 || L.Np > 256 || L.N > L.Np || L.M < 1)
+    throw std::invalid_argument("tc_mlp_maps: bad layer shape");
+  const uint64_t da[2] = {(uint64_t)L.Kp, (uint64_t)L.M}, dw[2] = {(uint64_t)L.Kp, (uint64_t)L.Np};
+  make_map(&L.ah, const_cast<uint32_t*>(ah), TC_TF32, 2, da, 32, TC_M);
+  make_map(&L.al, const_cast<uint32_t*>(al), TC_TF32, 2, da, 32, TC_M);
+  make_map(&L.w, const_cast<float*>(w), TC_TF32, 2, dw, 32, L.Np);
+}
+
+void tc_mlp_layer(const TcMlpLayer& L, cudaStream_t s) {
+  TcMlpArgs a;
+  a.M = L.M;
+  a.N = L.N;
+  a.Np = L.Np;
+  a.nk = L.Kp / 32;
+  a.bias = L.bias;
+  a.gelu = L.gelu;
+  a.oh = L.oh;
+  a.ol = L.ol;
+  a.ldo = L.ldo;
+  a.y = L.y;
+  a.ldy = L.ldy;
+  a.err = L.err;
+  a.idesc = make_idesc(TC_TF32, L.Np);
+  a.tmem_cols = tmem_cols_for(L.Np / 2);  // a power of two >= Np (and >= 32)
+  const size_t sm = (size_t)TC_NS * (2 * TC_M * 128 + (size_t)L.Np * 128) + 1024 + 256;
+  static bool attr = false;
+  if (!attr) {
+    GD_CUDA(cudaFuncSetAttribute(k_tc_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    attr = true;
+  }
+  k_tc_mlp<<<ceil_div(L.M, TC_M), TC_THREADS, sm, s>>>(L.ah, L.al, L.w, a);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+
 }  // namespace gd

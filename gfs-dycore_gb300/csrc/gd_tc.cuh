@@ -60,4 +60,27 @@ void tc_anal(TcPlan& p, const long* d_moff, bool useH, const float* G, long ldG,
 // returns and clears the device error flag (nonzero: a bounded wait gave up)
 int tc_check(TcPlan& p, cudaStream_t s);
 
+// One dense layer of the closure network on the tensor cores: for m < M,
+// n < N, acc[m][n] = sum_k (Ah[m][k] + Al[m][k]) W[n][k], A split to TF32 hi +
+// lo (row pitch Kp, a multiple of 32 with zeros past the layer's inputs), W
+// exact in TF32 ([Np][Kp], Np = N rounded up to 16, zero rows past N), FP32
+// accumulation in TMEM.  The epilogue adds the bias, then either applies GELU
+// and writes the next layer's split operands (oh, ol, row pitch ldo) or
+// writes FP32 outputs y (row pitch ldy).  N <= 256.
+struct TcMlpLayer {
+  CUtensorMap ah, al, w;
+  int M = 0, N = 0, Np = 0, Kp = 0;
+  const float* bias = nullptr;
+  int gelu = 0;
+  uint32_t* oh = nullptr;
+  uint32_t* ol = nullptr;
+  int ldo = 0;
+  float* y = nullptr;
+  int ldy = 0;
+  int* err = nullptr;  // device flag: nonzero when a bounded wait gave up
+};
+// tensor maps of a layer over its operand buffers (rows M of A)
+void tc_mlp_maps(TcMlpLayer& L, const uint32_t* ah, const uint32_t* al, const float* w);
+void tc_mlp_layer(const TcMlpLayer& L, cudaStream_t s);
+
 }  // namespace gd

@@ -41,6 +41,24 @@ def test_forward_matches_oracle():
     np.testing.assert_array_equal(net.get_params(), p)
 
 
+def test_closure_shape_forward_on_tensor_cores_matches_oracle():
+    # the configured closure net (193 -> 256 x 3 -> 192): inference runs on the
+    # tensor cores (TF32 hi + lo activations, weights exact in TF32)
+    import mlp_oracle as mo
+    from gdpy import core
+
+    net = core.Mlp(193, 256, 3, 192, seed=11)
+    rng = np.random.default_rng(11)
+    shp = mo.shapes(193, 256, 3, 192)
+    p = np.concatenate([np.concatenate([rng.standard_normal(fo * fi) * np.sqrt(2.0 / fi),
+                                        rng.standard_normal(fo) * 0.1]) for fo, fi in shp]).astype(np.float32)
+    net.set_params(p)
+    x = rng.standard_normal((1000, 193)).astype(np.float32)
+    y = net.forward(torch.from_numpy(x).cuda()).cpu().numpy()
+    yo, _ = mo.forward(p, shp, x)
+    assert rel(y, yo) < 1e-5
+
+
 def test_gradient_matches_oracle():
     import mlp_oracle as mo
 

@@ -1443,28 +1443,49 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   tc_fence_after();
   const bool go = __all_sync(0xffffffffu, ok && *(volatile int*)a.err == 0);
   if (go) {
-    const int m = m0 + warp * 32 + lane;
+    // each lane finishes 64 columns of its row into the warp's part of the
+    // (now idle) ring, then the warp stores row after row: 128 contiguous
+    // bytes per store instead of 32 rows' scattered words
+    constexpr int TP = 65;  // tile pitch (words): conflict-free column writes
+    uint32_t* th = reinterpret_cast<uint32_t*>(sm) + warp * (2 * 32 * TP);
+    uint32_t* tl = th + 32 * TP;
     const uint32_t tw = tbase + ((uint32_t)(warp * 32) << 16);
-    for (int g = 0; g < a.Np; g += 16) {
-      float v[16];
-      tmem_ld16(tw + g, v);
-      if (m < a.M) {
+    const int mw = m0 + warp * 32;
+    for (int g0 = 0; g0 < a.Np; g0 += 64) {
+      for (int g = g0; g < g0 + 64 && g < a.Np; g += 16) {
+        float v[16];
+        tmem_ld16(tw + g, v);
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
           const int n = g + q;
+          const float z = v[q] + (n < a.N ? a.bias[n] : 0.f);
+          uint32_t h, l = 0;
+          if (a.gelu)
+            Elem<TC_TF32>::splitf(tc_gelu(z), h, l);
+          else
+            h = __float_as_uint(z);
+          th[lane * TP + (n - g0)] = h;
+          tl[lane * TP + (n - g0)] = l;
+        }
+      }
+      __syncwarp();
+      for (int r = 0; r < 32; ++r) {
+        const int m = mw + r;
+        if (m >= a.M) break;
+#pragma unroll
+        for (int c = 0; c < 64; c += 32) {
+          const int n = g0 + c + lane;
           if (n < a.N) {
-            const float z = v[q] + a.bias[n];
             if (a.gelu) {
-              uint32_t h, l;
-              Elem<TC_TF32>::splitf(tc_gelu(z), h, l);
-              a.oh[(long)m * a.ldo + n] = h;
-              a.ol[(long)m * a.ldo + n] = l;
+              a.oh[(long)m * a.ldo + n] = th[r * TP + c + lane];
+              a.ol[(long)m * a.ldo + n] = tl[r * TP + c + lane];
             } else {
-              a.y[(long)m * a.ldy + n] = z;
+              a.y[(long)m * a.ldy + n] = __uint_as_float(th[r * TP + c + lane]);
             }
           }
         }
       }
+      __syncwarp();
     }
   }
   tc_fence_before();

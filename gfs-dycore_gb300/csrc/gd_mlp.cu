@@ -54,6 +54,7 @@ struct gd_mlp {
   int bcap = 0;
   float *zb = nullptr, *ab = nullptr, *yb = nullptr, *gy = nullptr, *g0 = nullptr, *g1 = nullptr;
   float* partial = nullptr;  // loss partial sums
+  float* kpart = nullptr;    // split-K partial weight gradients
   float* lossd = nullptr;
   // tensor-core inference (gd_tc.cu, k_tc_mlp): weights exact in TF32, padded
   // to [Np][Kp] per layer; the input and hidden activations split hi + lo
@@ -112,8 +113,8 @@ __device__ __forceinline__ float gelu_d(float z) {
 // C(m, n) = sum_k A(m, k) B(k, n) with A(m, k) = A[m sam + k sak], B(k, n) =
 // B[k sbk + n sbn]; epi(m, n, c) takes each output
 template <typename TA, typename TB, typename Epi>
-__global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const TA* __restrict__ A, long sam, long sak,
-                                              const TB* __restrict__ B, long sbk, long sbn, Epi epi) {
+__global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, int kchunk, const TA* __restrict__ A, long sam,
+                                              long sak, const TB* __restrict__ B, long sbk, long sbn, Epi epi) {
   __shared__ float As[GK][GM + 4];
   __shared__ float Bs[GK][GN + 4];
   const int tid = threadIdx.x;
@@ -125,16 +126,18 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const TA* __r
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
   const bool a_kfast = sak == 1, b_nfast = sbn == 1;
-  for (int k0 = 0; k0 < K; k0 += GK) {
+  // split K: this CTA sums k in [kb, ke) (blockIdx.z-th chunk)
+  const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+  for (int k0 = kb; k0 < ke; k0 += GK) {
     for (int e = tid; e < GM * GK; e += 256) {  // the unit-stride index fastest over the threads
       const int mm = a_kfast ? e / GK : e % GM, kk = a_kfast ? e % GK : e / GM;
       const int m = m0 + mm, k = k0 + kk;
-      As[kk][mm] = (m < M && k < K) ? tofloat(A[(long)m * sam + (long)k * sak]) : 0.f;
+      As[kk][mm] = (m < M && k < ke) ? tofloat(A[(long)m * sam + (long)k * sak]) : 0.f;
     }
     for (int e = tid; e < GK * GN; e += 256) {
       const int nn = b_nfast ? e % GN : e / GK, kk = b_nfast ? e / GN : e % GK;
       const int n = n0 + nn, k = k0 + kk;
-      Bs[kk][nn] = (n < N && k < K) ? tofloat(B[(long)k * sbk + (long)n * sbn]) : 0.f;
+      Bs[kk][nn] = (n < N && k < ke) ? tofloat(B[(long)k * sbk + (long)n * sbn]) : 0.f;
     }
     __syncthreads();
 #pragma unroll
@@ -157,7 +160,7 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const TA* __r
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int m = m0 + tm + i, n = n0 + tn + j;
-      if (m < M && n < N) epi(m, n, acc[i][j]);
+      if (m < M && n < N) epi(m + blockIdx.z * M, n, acc[i][j]);  // split K: partial z at rows zM..
     }
 }
 
@@ -198,8 +201,32 @@ void gemm(int M, int N, int K, const TA* A, long sam, long sak, const TB* B, lon
           cudaStream_t s) {
   if (M <= 0 || N <= 0) return;
   dim3 grid((unsigned)ceil_div(N, GN), (unsigned)ceil_div(M, GM));
-  k_gemm<TA, TB, Epi><<<grid, 256, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, epi);
+  k_gemm<TA, TB, Epi><<<grid, 256, 0, s>>>(M, N, K, K, A, sam, sak, B, sbk, sbn, epi);
   count_launch();
+  GD_LAUNCH_CHECK();
+}
+// C = A B with K split into nsplit chunks: partial z goes to part[z][M][N],
+// then the partials are summed in order (deterministic) into out [M][N]
+constexpr int KSPLIT = 16;
+__global__ void k_sum_parts(const float* __restrict__ part, int nsplit, long count, float* __restrict__ out) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (long)gridDim.x * blockDim.x) {
+    float t = 0.f;
+    for (int z = 0; z < nsplit; ++z) t += part[z * count + i];
+    out[i] = t;
+  }
+}
+template <typename TA, typename TB>
+void gemm_splitk(int M, int N, int K, const TA* A, long sam, long sak, const TB* B, long sbk, long sbn, float* part,
+                 float* out, cudaStream_t s) {
+  if (M <= 0 || N <= 0) return;
+  const int nsplit = std::max(1, std::min(KSPLIT, K / 256));
+  const int kchunk = (ceil_div(K, nsplit) + GK - 1) / GK * GK;
+  const int ns = ceil_div(K, kchunk);
+  dim3 grid((unsigned)ceil_div(N, GN), (unsigned)ceil_div(M, GM), (unsigned)ns);
+  k_gemm<TA, TB, EpiStore><<<grid, 256, 0, s>>>(M, N, K, kchunk, A, sam, sak, B, sbk, sbn, EpiStore{part, N});
+  const long cnt = (long)M * N;
+  k_sum_parts<<<std::min(ceil_div(cnt, 256), 1024), 256, 0, s>>>(part, ns, cnt, out);
+  count_launch(2);
   GD_LAUNCH_CHECK();
 }
 
@@ -469,7 +496,7 @@ void loss_grad(gd_mlp* p, const float* x, const float* t, int n) {
   for (int l = p->nlayer - 1; l >= 0; --l) {
     const int fi = p->fin[l], fo = p->fout[l];
     const float* Ain = l == 0 ? x : p->ab + (size_t)(l - 1) * p->bcap * p->nh;
-    gemm(fo, fi, n, cur, 1L, (long)fo, Ain, (long)fi, 1L, EpiStore{p->grad + p->offw[l], fi}, s);
+    gemm_splitk(fo, fi, n, cur, 1L, (long)fo, Ain, (long)fi, 1L, p->kpart, p->grad + p->offw[l], s);
     k_colsum<<<ceil_div(fo, 32), dim3(32, 8), 0, s>>>(cur, n, fo, p->grad + p->offb[l]);
     count_launch();
     GD_LAUNCH_CHECK();
@@ -542,6 +569,9 @@ int gd_mlp_init(int nin, int nhidden, int nlayers, int nout, unsigned long long 
     p->am = (float*)p->alloc(sizeof(float) * off);
     p->av = (float*)p->alloc(sizeof(float) * off);
     p->partial = (float*)p->alloc(sizeof(float) * KPART);
+    long wmax = 0;
+    for (int l = 0; l < p->nlayer; ++l) wmax = std::max(wmax, (long)p->fin[l] * p->fout[l]);
+    p->kpart = (float*)p->alloc(sizeof(float) * KSPLIT * wmax);
     p->lossd = (float*)p->alloc(sizeof(float));
     p->in_mu = (float*)p->alloc(sizeof(float) * nin);
     p->in_sd = (float*)p->alloc(sizeof(float) * nin);

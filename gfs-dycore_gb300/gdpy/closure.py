@@ -12,7 +12,7 @@ higher truncation (T254L64), spectrally truncated to the coarse one every
     target_k = (truth_{k+1} - coarse_forecast_k) / (every_h h)   on the grid,
 
 and the closure adds dt * net(columns) every step.  The plain coarse step is
-the fallback (detach the net) and the judge: `evaluate` compares zonal-mean u
+the fallback (detach the net) and the yardstick: `climate` compares zonal-mean u
 and T against the coarse-grained truth with and without the net.
 
 Run the experiment on a GPU with

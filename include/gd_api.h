@@ -386,8 +386,8 @@ const char* gd_sigio_last_error(void);
    configuration is a coarse run (T62L64) whose tendencies the network
    corrects from each grid column's u, v, Tv (levels bottom to top) and ps:
    nin = 3 nlev + 1, nout = 3 nlev (du/dt, dv/dt, dTv/dt).  It has no
-   counterpart in the reference, whose plain step stays the fallback and the
-   judge of its error.  x, t and y below are device pointers of float
+   counterpart in the reference; the plain step stays the fallback and the
+   measure of its error.  x, t and y below are device pointers of float
    [ncols][nin] / [ncols][nout]; parameters are host float arrays in the
    packed layout (per layer W [fout][fin] row-major, then b [fout]). */
 typedef struct gd_mlp gd_mlp;

@@ -1,4 +1,4 @@
-// gd_oracle.cpp -- TEST INFRASTRUCTURE ONLY (parity checker + timed CPU
+// gd_oracle.cpp -- TEST INFRASTRUCTURE ONLY (parity oracle + timed CPU
 // baseline).  FP64 CPU restatement of the GFS spectral dycore time step of
 // jswhit/gfs-dycore.  Each routine cites the reference file:line it follows.
 //

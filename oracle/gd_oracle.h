@@ -5,7 +5,7 @@
  * dycore time step of jswhit/gfs-dycore (src/shtns.f90, src/dyn_run.f90,
  * src/pressure_data.f90, src/semimp_data.f90, src/run.f90::advance,
  * src/phy_run_hs.f90, src/dyn_init.f90::setdampspec) in plain C++ with
- * OpenMP over levels.  It is the parity checker for the CUDA library and
+ * OpenMP over levels.  It is the parity oracle for the CUDA library and
  * the timed CPU baseline; nothing in the product links or calls it.
  *
  * Parity status: the reference cannot be built here (no Fortran compiler,

@@ -1,4 +1,4 @@
-// gd_pattern_oracle.cpp -- TEST INFRASTRUCTURE ONLY (the checker, never the
+// gd_pattern_oracle.cpp -- TEST INFRASTRUCTURE ONLY (the oracle, never the
 // product path): CPU restatement of the reference's stochastic pattern
 // generator, src/patterngenerator.f90, and of the Mersenne twister it draws
 // from, src/w3lib/mersenne_twister.f.

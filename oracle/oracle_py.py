@@ -1,6 +1,6 @@
 """ctypes wrapper of the FP64 CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
-Used by tests/, by ``__graft_entry__.smoke()`` as the checker and by
+Used by tests/, by ``__graft_entry__.smoke()`` as the oracle and by
 ``bench.py``'s CPU-baseline leg; the product never imports it.  The oracle
 restates the jswhit/gfs-dycore time step (src/shtns.f90, src/dyn_run.f90,
 src/run.f90, src/semimp_data.f90, src/pressure_data.f90,

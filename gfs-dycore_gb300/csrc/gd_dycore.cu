@@ -8,6 +8,7 @@
 // src/shtns.f90.  All state lives on one GPU; one context owns one stream,
 // and every step is one CUDA graph replay.
 #include <algorithm>
+#include <functional>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -62,6 +63,7 @@ class DycoreBase {
   virtual void check() = 0;
   virtual void set_sppt(gd_pattern*, double, double) = 0;
   virtual void set_closure(gd_mlp*) = 0;
+  virtual void autotune(int*) = 0;
   virtual void closure_features(float*) = 0;
   virtual double get_pdryini() = 0;
   cudaStream_t stream = nullptr;
@@ -687,7 +689,7 @@ class Dycore : public DycoreBase {
   // getdyntend: transforms to the grid, column physics, transforms back
   void dyn_pass(int stage, bool want_extra) {
     synthesis(c2rFull);
-    launch_dyn_columns<R>(column_args(want_extra), false, stream);
+    launch_dyn_columns<R>(column_args(want_extra), false, stream, col_lb);
     if (stage == 0) {  // pdry on stage 1 (dyn_run.f90:135-153)
       launch_area_mean_ps<R>(psg, w, nlat, nlon, rowsum, pmean, stream);
       const bool moist = !c.dry && nt > 0;
@@ -705,7 +707,7 @@ class Dycore : public DycoreBase {
   }
   void inverse_pass(bool want_extra) {
     synthesis(c2rInv);
-    launch_dyn_columns<R>(column_args(want_extra), true, stream);
+    launch_dyn_columns<R>(column_args(want_extra), true, stream, col_lb);
     mark(PH_COL);
   }
   StageArgs<R> stage_args(int s) {
@@ -847,6 +849,65 @@ class Dycore : public DycoreBase {
     }
     if (closure) closure_pass();
   }
+  // Autotuning: the synthesis GEMM's latitude tile (split modes) and the
+  // column kernel's levels per warp, each chosen by timing its candidates on
+  // this context's own buffers (the transform rows of the current state).
+  // The choices hold for the context's later steps.
+  int col_lb = 0;
+  void autotune(int* out) override {
+    if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
+    GD_CUDA(cudaStreamSynchronize(stream));
+    cudaEvent_t e0, e1;
+    GD_CUDA(cudaEventCreate(&e0));
+    GD_CUDA(cudaEventCreate(&e1));
+    auto timed = [&](const std::function<void()>& f) {
+      f();  // warm-up
+      GD_CUDA(cudaEventRecord(e0, stream));
+      for (int r = 0; r < 3; ++r) f();
+      GD_CUDA(cudaEventRecord(e1, stream));
+      GD_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      GD_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      return ms;
+    };
+    synthesis(c2rFull);  // the grid rows the column kernel reads
+    float best = 1e30f;
+    int blb = 4;
+    for (int lb : {4, 8}) {
+      if (lb == 4 && L > 64) continue;
+      const float ms = timed([&] { launch_dyn_columns<R>(column_args(false), false, stream, lb); });
+      if (ms < best) best = ms, blb = lb;
+    }
+    col_lb = blb;
+    if (tcp) {
+      std::vector<int> tiles;
+      for (int cap : {48, 64, 80, 96}) {
+        const int n = tc_tile_n(nh, cap);
+        if (std::find(tiles.begin(), tiles.end(), n) == tiles.end()) tiles.push_back(n);
+      }
+      best = 1e30f;
+      int bn = tcp->nsyn;
+      for (int n : tiles) {
+        tc_set_nsyn(*tcp, n);
+        const float ms = timed([&] {
+          do_synth(false, synP, S, ldS, 2 * sc.ncol, FPb, ldFP);
+          do_synth(true, synH, S + 2 * (2 * L), ldS, 2 * (sc.ncol - 2 * L), FHb, ldFH);
+        });
+        if (ms < best) best = ms, bn = n;
+      }
+      tc_set_nsyn(*tcp, bn);
+      tc_status();
+    }
+    GD_CUDA(cudaEventDestroy(e0));
+    GD_CUDA(cudaEventDestroy(e1));
+    out[0] = tcp ? tcp->nsyn : 0;
+    out[1] = col_lb;
+    if (gexec) {  // the captured step changes
+      GD_CUDA(cudaGraphExecDestroy(gexec));
+      gexec = nullptr;
+    }
+    steps_done = 0;  // the next step runs eagerly (new work lists), the one after is captured
+  }
   // Learned closure: the attached net's tendencies from the grid columns of
   // the step's inverse transform (the state before the forcing, as the
   // forcing sees it), times dt, analysed as in the column-physics update (Tv
@@ -901,6 +962,7 @@ class Dycore : public DycoreBase {
       GD_CUDA(cudaGraphExecDestroy(gexec));
       gexec = nullptr;
     }
+    steps_done = 0;  // the next step runs eagerly (the net's kernels set their attributes), then is captured
   }
   void closure_features(float* x) override {
     if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
@@ -1717,6 +1779,10 @@ int gd_profile_step(gd_ctx* ctx, double* ms, int nphase) {
 }
 int gd_set_sppt(gd_ctx* ctx, gd_pattern* pattern, double sigtop, double sigbot) {
   return guarded(ctx, [&] { ctx->d->set_sppt(pattern, sigtop, sigbot); });
+}
+int gd_autotune(gd_ctx* ctx, int* choices) {
+  if (!choices) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->autotune(choices); });
 }
 int gd_set_closure(gd_ctx* ctx, gd_mlp* net) {
   return guarded(ctx, [&] { ctx->d->set_closure(net); });

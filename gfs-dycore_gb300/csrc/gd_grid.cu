@@ -393,18 +393,18 @@ static void launch_cols_lb(const ColumnArgs<R>& a, bool inverse_only, cudaStream
 }
 
 template <typename R>
-void launch_dyn_columns(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t s) {
+void launch_dyn_columns(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t s, int lb) {
   if (a.L < 1 || a.L > LMAX) throw std::runtime_error("nlev out of range for the column kernel");
-  // levels per warp: at most 16 warps per CTA
-  if (a.L <= 64)
+  // levels per warp (at most 16 warps per CTA): 4, or 8 when asked or above 64 levels
+  if (a.L <= 64 && lb != 8)
     launch_cols_lb<R, 4, 16>(a, inverse_only, s);
   else
     launch_cols_lb<R, 8, 16>(a, inverse_only, s);
   count_launch();
   GD_LAUNCH_CHECK();
 }
-template void launch_dyn_columns<double>(const ColumnArgs<double>&, bool, cudaStream_t);
-template void launch_dyn_columns<float>(const ColumnArgs<float>&, bool, cudaStream_t);
+template void launch_dyn_columns<double>(const ColumnArgs<double>&, bool, cudaStream_t, int);
+template void launch_dyn_columns<float>(const ColumnArgs<float>&, bool, cudaStream_t, int);
 
 // Held-Suarez forcing on the grid (phy_run_hs.f90:42-77); prs and psg are
 // recomputed from ln(ps) as in calc_pressdata.

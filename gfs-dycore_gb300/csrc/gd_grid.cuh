@@ -37,7 +37,8 @@ struct ColumnArgs {
 };
 
 template <typename R>
-void launch_dyn_columns(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t s);
+// lb: levels per warp, 4 or 8 (0: 4 up to 64 levels, else 8)
+void launch_dyn_columns(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t s, int lb = 0);
 
 template <typename R>
 struct HsArgs {

@@ -1061,6 +1061,23 @@ void tc_init(TcPlan& p, int kind, int T, int nh, int nlat, int ncap, const long*
   GD_CUDA(cudaStreamSynchronize(s));
 }
 
+int tc_tile_n(int n, int cap) { return tile_n(n, cap); }
+
+// a new latitude tile of the synthesis GEMM: the tables keep their layout,
+// the tensor maps take the new box and the cached work lists are dropped
+void tc_set_nsyn(TcPlan& p, int nsyn) {
+  if (nsyn < 16 || nsyn % 16 || nsyn > (p.persistent ? 96 : 160))
+    throw std::invalid_argument("tc_set_nsyn: N tile must be a multiple of 16 within the TMEM budget");
+  p.nsyn = nsyn;
+  const int kind = p.kind;
+  for (int t = 0; t < 2; ++t)
+    for (int h = 0; h < 2; ++h) {
+      uint64_t ds[3] = {(uint64_t)2 * p.kepad, (uint64_t)p.nh, (uint64_t)p.T + 1};
+      make_map(&p.m_tsyn[t][h], p.tsyn[t][h], kind, 3, ds, p.kc, p.nsyn);
+    }
+  p.item_cache.clear();  // the lists depend on the tile; their device arrays are freed with the plan
+}
+
 void tc_free(TcPlan& p) {
   for (void* d : p.allocs) cudaFree(d);
   p.allocs.clear();

@@ -47,6 +47,10 @@ struct TcPlan {
 void tc_init(TcPlan& p, int kind, int T, int nh, int nlat, int ncap, const long* d_toff, const double* P64,
              const double* H64, cudaStream_t s);
 void tc_free(TcPlan& p);
+// the balanced tile at most cap wide over n rows (a multiple of 16)
+int tc_tile_n(int n, int cap);
+// switches the synthesis GEMM to latitude tile nsyn (autotuning)
+void tc_set_nsyn(TcPlan& p, int nsyn);
 
 // F[m][j][c] (real columns c0.. of the GEMM) = Legendre synthesis of the
 // real columns [0, ncols) of B[idx][.] (row pitch ldB, nrowsB rows

@@ -42,7 +42,7 @@ API_FUNCTIONS = [
     "gd_dcmip_point", "gd_set_iau", "gd_set_iau_files", "gd_dfi", "gd_dfi_weights",
     "gd_mlp_init", "gd_mlp_destroy", "gd_mlp_nparams", "gd_mlp_get_params", "gd_mlp_set_params",
     "gd_mlp_set_norm", "gd_mlp_forward", "gd_mlp_loss_grad", "gd_mlp_train_step", "gd_mlp_set_stream",
-    "gd_mlp_sync", "gd_mlp_last_error", "gd_set_closure", "gd_closure_features",
+    "gd_mlp_sync", "gd_mlp_last_error", "gd_set_closure", "gd_closure_features", "gd_autotune",
 ]
 PHASES = ["legendre_synth", "fft_synth", "columns", "fft_anal", "legendre_anal", "semi_implicit",
           "physics", "other", "column_physics"]
@@ -141,6 +141,7 @@ def load(build_if_missing=True):
     L.gd_mlp_last_error.argtypes = [vp]
     L.gd_set_closure.argtypes = [vp, vp]
     L.gd_closure_features.argtypes = [vp, vp]
+    L.gd_autotune.argtypes = [vp, vp]
     _lib = L
     return L
 
@@ -289,6 +290,14 @@ class Dycore:
         """Attach a Pattern as stochastically perturbed physics (None detaches)."""
         self._sppt = pattern  # keep the generator alive while attached
         self._chk(load().gd_set_sppt(self.h, pattern.h if pattern is not None else None, sigtop, sigbot))
+
+    def autotune(self):
+        """Times the candidate tile shapes on this context and keeps the fastest;
+        returns {"synth_tile": latitude tile of the synthesis GEMM (0 without the
+        tensor-core path), "column_levels_per_warp": ...}."""
+        out = np.zeros(2, np.int32)
+        self._chk(load().gd_autotune(self.h, _p(out)))
+        return {"synth_tile": int(out[0]), "column_levels_per_warp": int(out[1])}
 
     def set_closure(self, net):
         """Attach a trained Mlp as the learned per-column closure (None detaches)."""

@@ -8,6 +8,8 @@ n = 40), in split precision.  The members are advanced one by one
 (gd_advance + sync per member) and together (gd_ensemble_advance: every
 member's captured step graph on its own stream, overlapping on the GPU); the
 rate is the sum over members of simulated time per wall time, member-days/day.
+Each member's tile shapes are chosen by the autotuner (gd_autotune) at set-up
+unless --no-autotune is given.
 
 Usage (from the repository root):
 
@@ -30,7 +32,10 @@ MEMBERS = [  # (count, T, nlon, nlat, nlev, ntrac, dt)
 PATTERN = dict(lscale=500e3, tau=6 * 3600.0, stdev=0.5, jcap=40)
 
 
-def build(precision="tf32x3", members=MEMBERS, sppt=True, seed0=0):
+def build(precision="tf32x3", members=MEMBERS, sppt=True, seed0=0, autotune=True):
+    """The members, each with its state and pattern set; with autotune every
+    member's tile shapes are chosen by gd_autotune on its own buffers (the
+    best tiles differ between truncations)."""
     out = []
     i = 0
     for count, T, nlon, nlat, L, nt, dt in members:
@@ -45,13 +50,16 @@ def build(precision="tf32x3", members=MEMBERS, sppt=True, seed0=0):
                 p.start()
                 g.set_sppt(p)
             g.dt_s = dt
+            g.tiles = g.autotune() if autotune else None
             out.append(g)
             i += 1
     return out
 
 
-def measure(steps=10, warmup=3, precision="tf32x3"):
-    ms = build(precision)
+def measure(steps=10, warmup=3, precision="tf32x3", autotune=True):
+    t0 = time.perf_counter()
+    ms = build(precision, autotune=autotune)
+    setup = time.perf_counter() - t0
     for g in ms:  # first step eager, second captures the graph
         g.advance(warmup)
     for g in ms:
@@ -69,7 +77,8 @@ def measure(steps=10, warmup=3, precision="tf32x3"):
                members=len(ms), steps=steps,
                one_by_one=dict(seconds=one_by_one, member_days_per_day=sim / one_by_one),
                together=dict(seconds=together, member_days_per_day=sim / together),
-               speedup=one_by_one / together)
+               speedup=one_by_one / together, setup_seconds=setup,
+               tiles={f"T{g.ntrunc}L{g.nlev}": g.tiles for g in ms} if autotune else None)
     finite = all(np.isfinite(g.get_state()["vrt"]).all() for g in ms)
     res["states_finite"] = bool(finite)
     for g in ms:
@@ -83,8 +92,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--precision", default="tf32x3", choices=["fp32", "tf32x3", "bf16x3", "fp64"])
     ap.add_argument("--out", default=None)
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default tile shapes")
     a = ap.parse_args()
-    res = measure(a.steps, a.warmup, a.precision)
+    res = measure(a.steps, a.warmup, a.precision, autotune=not a.no_autotune)
     js = json.dumps(res)
     if a.out:
         os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)

@@ -379,6 +379,14 @@ int gd_write_sig(gd_ctx* ctx, const char* path, double fhour, gd_sighead* head);
 /* Text of the calling thread's last sigma-file failure. */
 const char* gd_sigio_last_error(void);
 
+/* Autotuner: times the candidate tile shapes of this context's kernels on
+   its own buffers (a state must be set) and keeps the fastest for the later
+   steps: choices[0] = the synthesis Legendre GEMM's latitude tile (split
+   precision modes; 0 otherwise), choices[1] = the column kernel's levels per
+   warp.  Results do not depend on the tile; the levels per warp change the
+   order of the column sums (last-bit differences). */
+int gd_autotune(gd_ctx* ctx, int* choices);
+
 /* ---- Learned per-column closure -----------------------------------------
    A fully connected network nin -> nhidden (GELU) x nlayers -> nout with
    BF16 weights and FP32 accumulation, trained on the GPU by the library's

@@ -14,8 +14,10 @@ SMALL = [(2, 21, 64, 32, 8, 1, 1200.0), (1, 42, 128, 64, 20, 2, 900.0)]
 def test_together_equals_one_by_one(precision, sppt):
     from gdpy import core, ensemble
 
-    a = ensemble.build(precision, SMALL, sppt=sppt, seed0=5)
-    b = ensemble.build(precision, SMALL, sppt=sppt, seed0=5)
+    # the default tiles on both sides: autotuning may pick different levels
+    # per warp for the two builds, which changes the last bits
+    a = ensemble.build(precision, SMALL, sppt=sppt, seed0=5, autotune=False)
+    b = ensemble.build(precision, SMALL, sppt=sppt, seed0=5, autotune=False)
     core.ensemble_advance(a, 4)
     for g in b:
         g.advance(4)

@@ -254,3 +254,32 @@ def test_step_split_close_to_fp64(oracle_mod, prec):
     assert rel(a["tv"], b["tv"]) < 1e-5
     assert rel(a["vrt"], b["vrt"]) < (2e-3 if prec == "tf32x3" else 2e-2)
     assert rel(a["lnps"], b["lnps"]) < 2e-6
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "fp64"])
+def test_autotune_keeps_the_step(prec):
+    # the tuned context steps like the untuned one: the latitude tile does not
+    # enter the sums, the levels per warp only their order
+    T, L = 126, 64
+    nlon, nlat = GRIDS[T]
+    ak, bk = inputs.hybrid_coords(L)
+    st = inputs.smooth_random_state(T, L, ntrac=2, seed=12)
+    out = []
+    for tune in (False, True):
+        g = core.Dycore(T, nlon, nlat, L, ak, bk, ntrac=2, dt=600.0, precision=prec)
+        g.set_state(st["vrt"], st["div"], st["tv"], st["lnps"], trc=st["trc"])
+        g.advance(2)  # a captured step graph exists before tuning
+        g.set_state(st["vrt"], st["div"], st["tv"], st["lnps"], trc=st["trc"])
+        if tune:
+            ch = g.autotune()
+            assert ch["column_levels_per_warp"] in (4, 8)
+            if prec == "tf32x3":
+                assert ch["synth_tile"] % 16 == 0 and 16 <= ch["synth_tile"] <= 96
+            else:
+                assert ch["synth_tile"] == 0
+            g.set_state(st["vrt"], st["div"], st["tv"], st["lnps"], trc=st["trc"])
+        g.advance(2)
+        out.append(g.get_state())
+    tol = 1e-6 if prec == "tf32x3" else 1e-12
+    for k in ("vrt", "tv", "lnps", "trc"):
+        assert rel(out[1][k], out[0][k]) < tol, k

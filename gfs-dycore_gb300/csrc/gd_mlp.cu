@@ -77,13 +77,6 @@ struct gd_mlp {
     allocs.push_back(p);
     return p;
   }
-  void release(void* p) {
-    for (auto& a : allocs)
-      if (a == p) {
-        cudaFree(a);
-        a = nullptr;
-      }
-  }
   ~gd_mlp() {
     int cur = 0;
     if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
@@ -347,11 +340,12 @@ void to_bf16(gd_mlp* p) {
 }  // namespace
 
 // --------------------------------------------------- shared with the dycore
+// Grows the activation buffers to ncols columns.  The old buffers are kept
+// until the net is destroyed: a context's captured step may still address
+// them (a step graph holds the buffers and tensor maps of its capture).
 void mlp_reserve(gd_mlp* p, int ncols) {
   if (ncols <= p->bcap) return;
   GD_CUDA(cudaStreamSynchronize(p->stream));
-  for (float* b : {p->zb, p->ab, p->yb, p->gy, p->g0, p->g1})
-    if (b) p->release(b);
   const long w = std::max(p->nh, std::max(p->nin, p->nout));
   p->zb = (float*)p->alloc(sizeof(float) * (size_t)p->nl * ncols * p->nh);
   p->ab = (float*)p->alloc(sizeof(float) * (size_t)p->nl * ncols * p->nh);
@@ -361,8 +355,6 @@ void mlp_reserve(gd_mlp* p, int ncols) {
   p->g1 = (float*)p->alloc(sizeof(float) * (size_t)ncols * w);
   p->bcap = ncols;
   if (p->tc) {  // tensor-core operands (zero padding) and the layers' tensor maps
-    for (uint32_t* b : {p->xh, p->xl, p->hh[0], p->hh[1], p->hl[0], p->hl[1]})
-      if (b) p->release(b);
     const int ldh = p->kp.size() > 1 ? p->kp[1] : p->kp[0];
     auto z = [&](size_t words) {
       uint32_t* b = (uint32_t*)p->alloc(sizeof(uint32_t) * words);

@@ -425,7 +425,8 @@ const char* gd_mlp_last_error(gd_mlp* net);
    the forcing, the net's tendencies times dt are added to Tv and, through
    the vector analysis, to vorticity and divergence.  NULL detaches.  The net
    must live on ctx's device with nin = 3 nlev + 1 and nout = 3 nlev; it
-   runs on ctx's stream while attached. */
+   runs on ctx's stream while attached and must outlive the attachment
+   (detach before gd_mlp_destroy). */
 int gd_set_closure(gd_ctx* ctx, gd_mlp* net);
 /* The raw closure inputs of ctx's current state, host float[nlat nlon][3
    nlev + 1]: u, v, Tv at the levels bottom to top and ps (Pa) per column. */

@@ -8,10 +8,12 @@
 // src/shtns.f90.  All state lives on one GPU; one context owns one stream,
 // and every step is one CUDA graph replay.
 #include <algorithm>
+#include <atomic>
 #include <functional>
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -64,6 +66,17 @@ class DycoreBase {
   virtual void set_sppt(gd_pattern*, double, double) = 0;
   virtual void set_closure(gd_mlp*) = 0;
   virtual void autotune(int*) = 0;
+  // For gd_ensemble_advance's one launch over all members: the captured step
+  // graph and its capture epoch, when this context can take part (a step has
+  // been captured, no per-step host work such as the IAU forcing); and the
+  // host bookkeeping of one step taken inside the ensemble graph.
+  virtual bool ensemble_step_graph(cudaGraph_t* g, unsigned long long* epoch) = 0;
+  virtual void ensemble_step_done() = 0;
+  const unsigned long long uid = next_uid();  // unique over the process (addresses are reused)
+  static unsigned long long next_uid() {
+    static std::atomic<unsigned long long> n{0};
+    return ++n;
+  }
   virtual void closure_features(float*) = 0;
   virtual double get_pdryini() = 0;
   cudaStream_t stream = nullptr;
@@ -149,6 +162,20 @@ class Dycore : public DycoreBase {
   }
   bool state_set = false;
   cudaGraphExec_t gexec = nullptr;
+  cudaGraph_t gstep = nullptr;  // the captured step (kept for gd_ensemble_advance's ensemble graph)
+  unsigned long long graph_epoch = 0;  // counts captures: an ensemble graph built on an older one is stale
+  void drop_graph() {
+    if (gexec) {
+      GD_CUDA(cudaStreamSynchronize(stream));
+      GD_CUDA(cudaGraphExecDestroy(gexec));
+      gexec = nullptr;
+    }
+    if (gstep) {
+      GD_CUDA(cudaGraphDestroy(gstep));
+      gstep = nullptr;
+    }
+    ++graph_epoch;
+  }
   int steps_done = 0;
   long long launches_per_step = 0;
   std::map<int, GemmPlan> synth_cache, anal_cache;
@@ -264,6 +291,7 @@ class Dycore : public DycoreBase {
   }
   ~Dycore() override {
     if (gexec) cudaGraphExecDestroy(gexec);
+    if (gstep) cudaGraphDestroy(gstep);
     if (tcp) tc_free(*tcp);
     for (auto e : evpool) cudaEventDestroy(e);
     free_plan(synP);
@@ -902,10 +930,7 @@ class Dycore : public DycoreBase {
     GD_CUDA(cudaEventDestroy(e1));
     out[0] = tcp ? tcp->nsyn : 0;
     out[1] = col_lb;
-    if (gexec) {  // the captured step changes
-      GD_CUDA(cudaGraphExecDestroy(gexec));
-      gexec = nullptr;
-    }
+    drop_graph();  // the captured step changes
     steps_done = 0;  // the next step runs eagerly (new work lists), the one after is captured
   }
   // Learned closure: the attached net's tendencies from the grid columns of
@@ -957,11 +982,7 @@ class Dycore : public DycoreBase {
       GD_CUDA(cudaStreamSynchronize(stream));
     }
     closure = net;
-    if (gexec) {  // the captured step changes
-      GD_CUDA(cudaStreamSynchronize(stream));
-      GD_CUDA(cudaGraphExecDestroy(gexec));
-      gexec = nullptr;
-    }
+    drop_graph();  // the captured step changes
     steps_done = 0;  // the next step runs eagerly (the net's kernels set their attributes), then is captured
   }
   void closure_features(float* x) override {
@@ -1002,11 +1023,7 @@ class Dycore : public DycoreBase {
       GD_CUDA(cudaStreamSynchronize(stream));
     }
     sppt = p;
-    if (gexec) {  // the captured step changes
-      GD_CUDA(cudaStreamSynchronize(stream));
-      GD_CUDA(cudaGraphExecDestroy(gexec));
-      gexec = nullptr;
-    }
+    drop_graph();  // the captured step changes
   }
   // IAU (iau_module.f90): increments analysis - first guess at nf times,
   // a forcing interpolated in time, constant over the RK stages of a step
@@ -1050,11 +1067,7 @@ class Dycore : public DycoreBase {
       iau_delthrs = delthrs;
       iau_nf = nf;
     }
-    if (gexec) {  // the captured step changes
-      GD_CUDA(cudaStreamSynchronize(stream));
-      GD_CUDA(cudaGraphExecDestroy(gexec));
-      gexec = nullptr;
-    }
+    drop_graph();  // the captured step changes
   }
   // getiauforcing (iau_module.f90:88-135) at time t into iau_F
   void iau_forcing(double t) {
@@ -1136,6 +1149,18 @@ class Dycore : public DycoreBase {
     }
     ++steps_done;
   }
+  bool ensemble_step_graph(cudaGraph_t* g, unsigned long long* epoch) override {
+    const bool capturable = stream != nullptr && stream != cudaStreamLegacy && stream != cudaStreamPerThread;
+    if (!state_set || !capturable || !gexec || !gstep || steps_done == 0 || iau_nf) return false;
+    *g = gstep;
+    *epoch = graph_epoch;
+    return true;
+  }
+  void ensemble_step_done() override {
+    t_cur += c.dt;
+    g_launches += launches_per_step;
+    ++steps_done;
+  }
   void advance(int nsteps) override {
     if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
     for (int i = 0; i < nsteps; ++i) {
@@ -1156,7 +1181,9 @@ class Dycore : public DycoreBase {
           step();
           GD_CUDA(cudaStreamEndCapture(stream, &g));
           GD_CUDA(cudaGraphInstantiate(&gexec, g, 0));
-          GD_CUDA(cudaGraphDestroy(g));
+          if (gstep) GD_CUDA(cudaGraphDestroy(gstep));
+          gstep = g;
+          ++graph_epoch;
           g_launches -= launches_per_step;  // counted once per replay below
           GD_CUDA(cudaGraphLaunch(gexec, stream));
           g_launches += launches_per_step;
@@ -1791,13 +1818,81 @@ int gd_closure_features(gd_ctx* ctx, float* x) {
   if (!x) return GD_ERR_ARG;
   return guarded(ctx, [&] { ctx->d->closure_features(x); });
 }
+// The ensemble graph: one child node per member's captured step, no edges
+// between them, so one launch runs every member's step and the graph
+// executor overlaps them.  Cached for the last member set (by the members'
+// unique ids and capture epochs); rebuilt when either changes.
+struct EnsembleGraph {
+  std::vector<unsigned long long> key;
+  cudaGraphExec_t exec = nullptr;
+};
+static std::mutex g_ens_mutex;
+static EnsembleGraph g_ens;
+
 int gd_ensemble_advance(gd_ctx** ctxs, int n, double t, int nsteps) {
   if (!ctxs || n < 1 || nsteps < 0) return GD_ERR_ARG;
   for (int i = 0; i < n; ++i)
     if (!ctxs[i] || !ctxs[i]->d) return GD_ERR_ARG;
   for (int i = 0; i < n; ++i) ctxs[i]->d->t_cur = t;
-  // members step in turn, each on its own stream: their steps overlap on the GPU
-  for (int s = 0; s < nsteps; ++s)
+  const int dev = ctxs[0]->cfg.device;
+  bool one_device = true;  // and no member twice (its step would run twice at once)
+  for (int i = 1; i < n; ++i) {
+    one_device = one_device && ctxs[i]->cfg.device == dev;
+    for (int j = 0; j < i; ++j) one_device = one_device && ctxs[j] != ctxs[i];
+  }
+  int s = 0;
+  while (s < nsteps) {
+    // one launch over all members once every member has a captured step
+    std::vector<cudaGraph_t> gs(n);
+    std::vector<unsigned long long> key;
+    bool ready = one_device && n > 1;
+    for (int i = 0; i < n && ready; ++i) {
+      unsigned long long ep = 0;
+      ready = ctxs[i]->d->ensemble_step_graph(&gs[i], &ep);
+      key.push_back(ctxs[i]->d->uid);
+      key.push_back(ep);
+    }
+    if (ready) {
+      const int rest = nsteps - s;
+      const int rc = guarded(ctxs[0], [&] {
+        GD_CUDA(cudaSetDevice(dev));
+        std::lock_guard<std::mutex> lk(g_ens_mutex);
+        if (!g_ens.exec || g_ens.key != key) {
+          if (g_ens.exec) GD_CUDA(cudaGraphExecDestroy(g_ens.exec));
+          g_ens.exec = nullptr;
+          cudaGraph_t parent;
+          GD_CUDA(cudaGraphCreate(&parent, 0));
+          for (int i = 0; i < n; ++i) {
+            cudaGraphNode_t node;
+            GD_CUDA(cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, gs[i]));
+          }
+          GD_CUDA(cudaGraphInstantiate(&g_ens.exec, parent, 0));
+          GD_CUDA(cudaGraphDestroy(parent));
+          g_ens.key = key;
+        }
+        // order: every member's earlier work before the launch, the launch
+        // before every member's later work
+        cudaStream_t s0 = ctxs[0]->d->stream;
+        cudaEvent_t ev;
+        GD_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        for (int i = 1; i < n; ++i) {
+          GD_CUDA(cudaEventRecord(ev, ctxs[i]->d->stream));
+          GD_CUDA(cudaStreamWaitEvent(s0, ev, 0));
+        }
+        for (int k = 0; k < rest; ++k) {
+          GD_CUDA(cudaGraphLaunch(g_ens.exec, s0));
+          for (int i = 0; i < n; ++i) ctxs[i]->d->ensemble_step_done();
+        }
+        GD_CUDA(cudaEventRecord(ev, s0));
+        for (int i = 1; i < n; ++i) GD_CUDA(cudaStreamWaitEvent(ctxs[i]->d->stream, ev, 0));
+        GD_CUDA(cudaEventDestroy(ev));
+      });
+      if (rc != GD_OK) return rc;
+      s = nsteps;
+      break;
+    }
+    // otherwise one step per member, each on its own stream (the first steps
+    // of a context run eagerly, then capture its step)
     for (int i = 0; i < n; ++i) {
       const int rc = guarded(ctxs[i], [&] {
         GD_CUDA(cudaSetDevice(ctxs[i]->cfg.device));
@@ -1805,6 +1900,8 @@ int gd_ensemble_advance(gd_ctx** ctxs, int n, double t, int nsteps) {
       });
       if (rc != GD_OK) return rc;
     }
+    ++s;
+  }
   for (int i = 0; i < n; ++i) {
     const int rc = guarded(ctxs[i], [&] {
       GD_CUDA(cudaSetDevice(ctxs[i]->cfg.device));

@@ -259,10 +259,14 @@ const char* gd_pattern_last_error(gd_pattern* p);
    ctx's; it is advanced on ctx's stream. */
 int gd_set_sppt(gd_ctx* ctx, gd_pattern* pattern, double sigtop, double sigbot);
 /* Advances n independent contexts (ensemble members, any mix of
-   truncations) by nsteps steps each: the members step in turn, each on its
-   own stream and captured step graph, so their steps overlap on the GPU;
-   returns when all are done.  No counterpart in the reference, which runs one
-   member per process. */
+   truncations, one device) by nsteps steps each.  Once every member has a
+   captured step graph (after its first two steps, taken member by member on
+   the members' streams), each ensemble step is one launch of a graph holding
+   every member's step as an independent child, so the members' steps
+   overlap on the GPU.  Members with per-step host work (the IAU forcing)
+   step member by member.  Returns when all are done.  Members must not share
+   a closure net (their steps run at once).  No counterpart in the reference,
+   which runs one member per process. */
 int gd_ensemble_advance(gd_ctx** ctxs, int n, double t, int nsteps);
 
 /* DCMIP-2012 initial state (dcmip_ics, src/dyn_init.f90:330-416) on ctx's grid:

@@ -331,6 +331,18 @@ int mguard(gd_mlp* p, F f) {
 }
 std::string g_mlp_init_error;
 
+// x, t and y of the batch entry points must be device memory of the net's
+// device (a host pointer would fault the kernels)
+void need_device(const gd_mlp* p, const void* ptr, const char* what) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    throw std::invalid_argument(std::string("gd_mlp: ") + what + " is not a device pointer");
+  }
+  if ((a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) || a.device != p->device)
+    throw std::invalid_argument(std::string("gd_mlp: ") + what + " is not device memory of the net's device");
+}
+
 void to_bf16(gd_mlp* p) {
   k_to_bf16<<<std::min(ceil_div(p->np, 256), 4096), 256, 0, p->stream>>>(p->p32, p->w16, p->np);
   count_launch();
@@ -419,6 +431,7 @@ void forward_tc(gd_mlp* p, const float* x, int n, float* y, cudaStream_t s) {
 // shape allows (every layer at most 256 wide).  No allocation when n <= bcap.
 void mlp_forward_on(gd_mlp* p, const float* x, int n, float* y, cudaStream_t s) {
   if (n > p->bcap) throw std::invalid_argument("gd_mlp: batch above the reserved capacity");
+  if (n <= 0) return;
   if (p->tc)
     forward_tc(p, x, n, y, s);
   else
@@ -636,6 +649,9 @@ int gd_mlp_set_norm(gd_mlp* p, const float* in_mu, const float* in_sd, const flo
 int gd_mlp_forward(gd_mlp* p, const float* x, int ncols, float* y) {
   if (!x || !y || ncols < 0) return GD_ERR_ARG;
   return mguard(p, [&] {
+    if (ncols == 0) return;
+    need_device(p, x, "x");
+    need_device(p, y, "y");
     mlp_reserve(p, ncols);
     mlp_forward_on(p, x, ncols, y, p->stream);
     mlp_check(p, p->stream);
@@ -645,6 +661,8 @@ int gd_mlp_forward(gd_mlp* p, const float* x, int ncols, float* y) {
 int gd_mlp_loss_grad(gd_mlp* p, const float* x, const float* t, int ncols, float* loss, float* grad) {
   if (!x || !t || ncols < 1) return GD_ERR_ARG;
   return mguard(p, [&] {
+    need_device(p, x, "x");
+    need_device(p, t, "t");
     mlp_reserve(p, ncols);
     loss_grad(p, x, t, ncols);
     GD_CUDA(cudaStreamSynchronize(p->stream));
@@ -656,6 +674,8 @@ int gd_mlp_loss_grad(gd_mlp* p, const float* x, const float* t, int ncols, float
 int gd_mlp_train_step(gd_mlp* p, const float* x, const float* t, int ncols, float lr, float* loss) {
   if (!x || !t || ncols < 1 || !(lr > 0)) return GD_ERR_ARG;
   return mguard(p, [&] {
+    need_device(p, x, "x");
+    need_device(p, t, "t");
     mlp_reserve(p, ncols);
     loss_grad(p, x, t, ncols);
     ++p->adam_t;

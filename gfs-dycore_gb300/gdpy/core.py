@@ -522,9 +522,18 @@ class Mlp:
         self._norm = arrs
         self._chk(load().gd_mlp_set_norm(self.h, *[_p(x) for x in arrs]))
 
+    def _batch(self, x, width, name):
+        import torch
+
+        if not (isinstance(x, torch.Tensor) and x.is_cuda and x.dtype == torch.float32 and x.is_contiguous()
+                and x.dim() == 2 and x.shape[1] == width and x.device.index == self.device):
+            raise ValueError(f"{name}: a contiguous float32 CUDA tensor [ncols, {width}] on device {self.device}")
+        return x
+
     def forward(self, x):
         import torch
 
+        self._batch(x, self.nin, "x")
         y = torch.empty((x.shape[0], self.nout), dtype=torch.float32, device=x.device)
         self._chk(load().gd_mlp_forward(self.h, ctypes.c_void_p(x.data_ptr()), int(x.shape[0]),
                                         ctypes.c_void_p(y.data_ptr())))
@@ -532,6 +541,8 @@ class Mlp:
         return y
 
     def loss_grad(self, x, t):
+        self._batch(x, self.nin, "x")
+        self._batch(t, self.nout, "t")
         loss = np.zeros(1, np.float32)
         g = np.zeros(self.nparams, np.float32)
         self._chk(load().gd_mlp_loss_grad(self.h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(t.data_ptr()),
@@ -539,6 +550,8 @@ class Mlp:
         return float(loss[0]), g
 
     def train_step(self, x, t, lr, want_loss=False):
+        self._batch(x, self.nin, "x")
+        self._batch(t, self.nout, "t")
         loss = np.zeros(1, np.float32)
         self._chk(load().gd_mlp_train_step(self.h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(t.data_ptr()),
                                            int(x.shape[0]), ctypes.c_float(lr), _p(loss) if want_loss else None))

@@ -63,6 +63,15 @@ def test_null_arguments_are_rejected():
     assert lib.gd_finalize(None) == core.GD_ERR_ARG
     assert lib.gd_advance(None, ctypes.c_double(0.0), 1) == core.GD_ERR_ARG
     assert lib.gd_sync(None) == core.GD_ERR_ARG
+    assert lib.gd_autotune(None, None) == core.GD_ERR_ARG
+    assert lib.gd_set_closure(None, None) == core.GD_ERR_ARG
+    assert lib.gd_closure_features(None, None) == core.GD_ERR_ARG
+    assert lib.gd_ensemble_advance(None, 1, ctypes.c_double(0.0), 1) == core.GD_ERR_ARG
+    for f in ("gd_mlp_destroy", "gd_mlp_sync"):
+        assert getattr(lib, f)(None) == core.GD_ERR_ARG
+    assert lib.gd_mlp_forward(None, None, 0, None) == core.GD_ERR_ARG
+    assert lib.gd_mlp_train_step(None, None, None, 1, ctypes.c_float(1e-3), None) == core.GD_ERR_ARG
+    assert lib.gd_mlp_init(4, 8, 1, 2, 0, 0, None) == core.GD_ERR_ARG
 
 
 def test_hybrid_coordinate_is_valid():

@@ -331,6 +331,12 @@ def dcmip_rate(precision, steps=10, warmup=3):
     t0 = time.perf_counter()
     g.dcmip_ics(43)
     ics_s = time.perf_counter() - t0
+    # The analytic state is subsaturated everywhere; humidity x1.6 (as in the parity tests) makes the
+    # large-scale condensation branch act from the first step, so the timed column kernel runs it.
+    x = g.get_state()
+    trc = x["trc"].copy()
+    trc[0] *= 1.6
+    g.set_state(x["vrt"], x["div"], x["tv"], x["lnps"], trc=trc, topo=g.get_topo())
     g.advance(warmup)
     g.sync()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -347,7 +353,8 @@ def dcmip_rate(precision, steps=10, warmup=3):
     achieved = byt / (cms * 1e-3) / 1e9
     apcp = g.get_grid("apcp")
     g.close()
-    return dict(workload="DCMIP-2012 4-3 moist baroclinic wave, simple physics, T574L64 ntrac 3 dt 150 s",
+    return dict(workload="DCMIP-2012 4-3 moist baroclinic wave (humidity x1.6, condensing), simple physics, "
+                         "T574L64 ntrac 3 dt 150 s",
                 precision=precision, ms_per_step=ms, days_per_day=dt / (ms * 1e-3), initial_state_s=ics_s,
                 phases_ms=ph, max_accumulated_precip_mm=float(apcp.max()),
                 column_kernel=dict(kernel="k_simple_physics", bound="hbm", ms=cms, bytes=byt, achieved=achieved,

@@ -1680,6 +1680,13 @@ int gd_set_state(gd_ctx* ctx, const double* vrt, const double* div, const double
 int gd_get_state(gd_ctx* ctx, double* vrt, double* div, double* tv, double* trc, double* lnps) {
   return guarded(ctx, [&] { ctx->d->get_state(vrt, div, tv, trc, lnps); });
 }
+int gd_get_topo(gd_ctx* ctx, double* topo) {
+  if (!ctx || !ctx->d || !topo) return GD_ERR_ARG;
+  const size_t n2 = 2 * (size_t)(ctx->cfg.ntrunc + 1) * (ctx->cfg.ntrunc + 2) / 2;
+  if (ctx->topo.size() == n2) std::copy(ctx->topo.begin(), ctx->topo.end(), topo);
+  else std::fill(topo, topo + n2, 0.0);
+  return GD_OK;
+}
 int gd_getdyntend(gd_ctx* ctx, int rkstage, int inverse_only, double* dvrt, double* ddiv, double* dtv, double* dtrc,
                   double* dlnps) {
   if (rkstage < 1 || rkstage > 3) {

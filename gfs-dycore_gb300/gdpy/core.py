@@ -29,7 +29,7 @@ GD_ERR_IO = -7
 PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3}
 
 API_FUNCTIONS = [
-    "gd_default_config", "gd_init", "gd_finalize", "gd_set_state", "gd_get_state",
+    "gd_default_config", "gd_init", "gd_finalize", "gd_set_state", "gd_get_state", "gd_get_topo",
     "gd_getdyntend", "gd_getphytend", "gd_advance", "gd_spectogrd", "gd_grdtospec",
     "gd_getuv", "gd_getvrtdivspec", "gd_getgrad", "gd_grid_info", "gd_get_grid", "gd_diag",
     "gd_set_stream", "gd_sync", "gd_launch_count", "gd_last_error", "gd_profile_step",
@@ -89,7 +89,7 @@ def load(build_if_missing=True):
     L.gd_launch_count.argtypes = [vp]
     L.gd_advance.argtypes = [vp, ctypes.c_double, ctypes.c_int]
     L.gd_set_stream.argtypes = [vp, vp]
-    for f in ["gd_set_state", "gd_get_state", "gd_getdyntend", "gd_getphytend", "gd_spectogrd",
+    for f in ["gd_set_state", "gd_get_state", "gd_get_topo", "gd_getdyntend", "gd_getphytend", "gd_spectogrd",
               "gd_grdtospec", "gd_getuv", "gd_getvrtdivspec", "gd_getgrad", "gd_grid_info",
               "gd_get_grid", "gd_diag", "gd_sync", "gd_profile_step"]:
         getattr(L, f).restype = ctypes.c_int
@@ -229,6 +229,12 @@ class Dycore:
         lnps = np.zeros(n, np.complex128)
         self._chk(load().gd_get_state(self.h, _p(vrt), _p(div), _p(tv), _p(trc), _p(lnps)))
         return dict(vrt=vrt, div=div, tv=tv, trc=trc[: self.ntrac], lnps=lnps)
+
+    def get_topo(self):
+        """Orography (complex [nlm], m) of the last set_state."""
+        out = np.zeros(self.nlm, np.complex128)
+        self._chk(load().gd_get_topo(self.h, _p(out)))
+        return out
 
     def dcmip_ics(self, testcase):
         """DCMIP-2012 test 4x (baroclinic wave) or 5x (tropical cyclone) initial state (gd_dcmip_ics)."""

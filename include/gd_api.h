@@ -95,6 +95,12 @@ int gd_set_state(gd_ctx* ctx, const double* vrt, const double* div, const double
 int gd_get_state(gd_ctx* ctx, double* vrt, double* div, double* tv, double* trc,
                  double* lnps);
 
+/* Reads the orography of the last gd_set_state (complex [nlm], metres; zero
+   when it was given as NULL), the reference's topodataspec
+   (spectral_data.f90, set at dyn_init.f90:76), so a caller can set a
+   modified state again over the same surface. */
+int gd_get_topo(gd_ctx* ctx, double* topo);
+
 /* Replaces getdyntend (src/dyn_run.f90:33-305) on the current state.
    inverse_only != 0 is the just_do_inverse_transform form (grid fields,
    pressure data and getomega only; no tendencies are written). */
@@ -197,8 +203,10 @@ int gd_profile_step(gd_ctx* ctx, double* ms, int nphase);
    loading the library holds until exit; nlat above that limit is rejected
    with GD_ERR_ARG.  The first call on a device looks up that array's
    address with the device current; make that first call before any stream
-   capture.  All calls share the array, so calls that overlap on the GPU
-   race.  Work is enqueued on stream (cudaStream_t as void*, NULL = legacy
+   capture.  The address is kept with the id of the CUDA context it belongs
+   to: after a cudaDeviceReset the next call (under the new context) looks
+   it up again, and that call too should come before any stream capture.
+   All calls share the array, so calls that overlap on the GPU race.  Work is enqueued on stream (cudaStream_t as void*, NULL = legacy
    default stream) and is complete when the stream is. */
 #define GD_DIAG_STATIC_MAX_NLAT 4096
 int gd_diag_static(const double* ug, const double* vg, int nlev, const double* psg,

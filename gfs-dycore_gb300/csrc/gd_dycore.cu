@@ -179,10 +179,50 @@ class Dycore : public DycoreBase {
   int steps_done = 0;
   long long launches_per_step = 0;
   std::map<int, GemmPlan> synth_cache, anal_cache;
-  // tensor-core split-precision Legendre path (FP32 state only)
+  // tensor-core split-precision Legendre path: FP32 state (TF32x3, BF16x3)
+  // or FP64 state with FP32 staging copies around the GEMM (F64_TF32X3)
   std::unique_ptr<TcPlan> tcp;
   double *P64keep = nullptr, *H64keep = nullptr;
-  bool split_mode() const { return c.precision == GD_PREC_TF32X3 || c.precision == GD_PREC_BF16X3; }
+  bool split_mode() const {
+    return c.precision == GD_PREC_TF32X3 || c.precision == GD_PREC_BF16X3 || c.precision == GD_PREC_F64_TF32X3 ||
+           c.precision == GD_PREC_F64_EDDY;
+  }
+  // FP32 staging of the FP64-state split modes: spectral side (GEMM operand
+  // of the synthesis, result of the analysis) and the Fourier side of the P
+  // and H buffers (FPb, FHb)
+  float *stSpec = nullptr, *stFourP = nullptr, *stFourH = nullptr;
+  float* stFour(const R* F) const { return (const void*)F == (const void*)FHb ? stFourH : stFourP; }
+  // eddy FFTs (GD_PREC_F64_EDDY on a four-step grid): FP32 tables of the
+  // longitude stage and the FP64 row means of the analysis
+  bool eddy_ = false;
+  ShtDev<float> sdf;
+  double* rmean = nullptr;
+  template <typename D>
+  FftPlan mk_c2r(const D* descs, int n) {
+    return eddy_ ? make_c2r_plan<float>(descs, n, stream, M) : make_c2r_plan<R>(descs, n, stream, M);
+  }
+  template <typename D>
+  FftPlan mk_r2c(const D* descs, int n) {
+    return eddy_ ? make_r2c_plan<float>(descs, n, stream, M) : make_r2c_plan<R>(descs, n, stream, M);
+  }
+  void c2r(const FftPlan& plan, const R* FP, long ldP, const R* FH, long ldH, R* grid) {
+    if constexpr (std::is_same<R, double>::value) {
+      if (eddy_) {
+        launch_c2r_eddy(sdf, plan, stFour(FP), FP, ldP, stFour(FH), FH, ldH, grid, stream);
+        return;
+      }
+    }
+    launch_c2r<R>(sd, plan, FP, ldP, FH, ldH, grid, stream);
+  }
+  void r2c(const FftPlan& plan, const R* grid, R* GP, long ldP, R* GH, long ldH) {
+    if constexpr (std::is_same<R, double>::value) {
+      if (eddy_) {
+        launch_r2c_eddy(sdf, plan, grid, rmean, wn, stFour(GP), GP, ldP, stFour(GH), GH, ldH, stream);
+        return;
+      }
+    }
+    launch_r2c<R>(sd, plan, grid, GP, ldP, GH, ldH, stream);
+  }
   std::map<int, GemmPlan> synth0_cache, anal0_cache;  // order-0-only SIMT work lists
   // Side stream of the split modes: order 0 runs on the SIMT path beside the
   // tensor-core GEMM of orders m >= 1 (disjoint output rows; the small SIMT
@@ -200,30 +240,55 @@ class Dycore : public DycoreBase {
     GD_CUDA(cudaStreamWaitEvent(stream, ev_join, 0));
   }
   void do_synth(bool useH, const GemmPlan& plan, const R* B, long ldB, int ncr, R* F, long ldF) {
-    if constexpr (std::is_same<R, float>::value) {
-      if (tcp) {
-        auto it = synth0_cache.find(ncr);
-        if (it == synth0_cache.end()) it = synth0_cache.emplace(ncr, make_synth_plan(T, nh, ncr, stream, 0, 0)).first;
+    if (tcp) {
+      auto it = synth0_cache.find(ncr);
+      if (it == synth0_cache.end()) it = synth0_cache.emplace(ncr, make_synth_plan(T, nh, ncr, stream, 0, 0)).first;
+      if constexpr (std::is_same<R, float>::value) {
         fork();
         tc_synth(*tcp, moff, useH, B, ldB, nlm_rows, ncr, F, ldF, stream);
         launch_synth<R>(sd, useH, it->second, B, ldB, ncr, F, ldF, side);
         join();
-        return;
+      } else {
+        // FP64 state: the GEMM of orders m >= 1 reads an FP32 copy of the
+        // spectral columns and writes FP32 Fourier rows, widened after it;
+        // order 0 runs on the FP64 SIMT path straight into F
+        // (the eddy FFT reads the FP32 rows where the GEMM left them)
+        launch_convert2d<double, float>(B, ldB, stSpec, ldB, nlm_rows, ncr, stream);
+        fork();
+        tc_synth(*tcp, moff, useH, stSpec, ldB, nlm_rows, ncr, stFour(F), ldF, stream);
+        launch_synth<R>(sd, useH, it->second, B, ldB, ncr, F, ldF, side);
+        join();
+        if (!eddy_)
+          launch_convert2d<float, double>(stFour(F) + (long)nlat * ldF, ldF, F + (long)nlat * ldF, ldF,
+                                          (long)T * nlat, ncr, stream);
       }
+      return;
     }
     launch_synth<R>(sd, useH, plan, B, ldB, ncr, F, ldF, stream);
   }
   void do_anal(bool useH, const GemmPlan& plan, const R* G, long ldG, int ncr, R* A, long ldA) {
-    if constexpr (std::is_same<R, float>::value) {
-      if (tcp) {
-        auto it = anal0_cache.find(ncr);
-        if (it == anal0_cache.end()) it = anal0_cache.emplace(ncr, make_anal_plan(T, ncr, stream, 0, 0)).first;
+    if (tcp) {
+      auto it = anal0_cache.find(ncr);
+      if (it == anal0_cache.end()) it = anal0_cache.emplace(ncr, make_anal_plan(T, ncr, stream, 0, 0)).first;
+      if constexpr (std::is_same<R, float>::value) {
         fork();
         tc_anal(*tcp, moff, useH, G, ldG, ncr, A, ldA, stream);
         launch_anal<R>(sd, useH, it->second, G, ldG, ncr, A, ldA, side);
         join();
-        return;
+      } else {
+        // FP64 state: FP32 copy of every Fourier row (order 0 included, so the
+        // GEMM reads no stale staging), FP32 result rows of orders m >= 1
+        // (spectral rows T+1.. in the m-major order) widened after it
+        // (the eddy FFT already wrote the FP32 rows, with zeros for order 0)
+        if (!eddy_) launch_convert2d<double, float>(G, ldG, stFour(G), ldG, (long)(T + 1) * nlat, ncr, stream);
+        fork();
+        tc_anal(*tcp, moff, useH, stFour(G), ldG, ncr, stSpec, ldA, stream);
+        launch_anal<R>(sd, useH, it->second, G, ldG, ncr, A, ldA, side);
+        join();
+        launch_convert2d<float, double>(stSpec + (long)(T + 1) * ldA, ldA, A + (long)(T + 1) * ldA, ldA,
+                                        (long)nlm - (T + 1), ncr, stream);
       }
+      return;
     }
     launch_anal<R>(sd, useH, plan, G, ldG, ncr, A, ldA, stream);
   }
@@ -269,19 +334,32 @@ class Dycore : public DycoreBase {
     ng = (long)nlon * nlat;
     GD_CUDA(cudaSetDevice(c.device));
     GD_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    eddy_ = sizeof(R) == 8 && c.precision == GD_PREC_F64_EDDY && fft_eddy_supported(M);
     init_grid();
     init_vertical(ak_, bk_);
     init_buffers();
     init_plans();
     if (split_mode()) {
+      GD_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+      GD_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+      GD_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+      tcp.reset(new TcPlan());
+      const int ncap = 2 * std::max(sc.ncol, ap.ncol);
       if constexpr (std::is_same<R, float>::value) {
-        GD_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-        GD_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
-        GD_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
-        tcp.reset(new TcPlan());
-        const int ncap = 2 * std::max(sc.ncol, ap.ncol);
         tc_init(*tcp, c.precision == GD_PREC_TF32X3 ? TC_TF32 : TC_BF16, T, nh, nlat, ncap, toff, P64keep, H64keep,
                 stream);
+      } else {
+        // the FP64 tables are the state precision's own; the staging copies
+        // take the widest row pitch any synthesis or analysis call uses
+        tc_init(*tcp, TC_TF32, T, nh, nlat, ncap, toff, P, H, stream);
+        const long ldmax = std::max(std::max(std::max(ldS, ldAP), std::max(ldAH, ldFP)), std::max(ldGP, ldGH));
+        const size_t nfour = (size_t)(T + 1) * nlat * ldmax;
+        stSpec = dalloc<float>((size_t)nlm_rows * ldmax);
+        stFourP = dalloc<float>(nfour);
+        stFourH = dalloc<float>(nfour);
+        GD_CUDA(cudaMemsetAsync(stSpec, 0, sizeof(float) * nlm_rows * ldmax, stream));
+        GD_CUDA(cudaMemsetAsync(stFourP, 0, sizeof(float) * nfour, stream));
+        GD_CUDA(cudaMemsetAsync(stFourH, 0, sizeof(float) * nfour, stream));
       }
       release(P64keep);
       release(H64keep);
@@ -400,6 +478,20 @@ class Dycore : public DycoreBase {
     sd.twM = twM;
     sd.twN = twN;
     fft_radix_plan(M, &sd.nrad, sd.rad);
+    if (eddy_) {
+      std::vector<float> rcf(nlat), wnf(nlat);
+      for (int j = 0; j < nlat; ++j) rcf[j] = (float)rc[j], wnf[j] = (float)wnv[j];
+      sdf.T = T, sdf.nlon = nlon, sdf.nlat = nlat, sdf.nh = nh, sdf.nlm = nlm, sdf.M = M;
+      sdf.moff = moff, sdf.toff = toff, sdf.P = nullptr, sdf.H = nullptr;
+      sdf.rcos = upload(rcf);
+      sdf.wn = upload(wnf);
+      float2* tmf = dalloc<float2>(M);
+      float2* tnf = dalloc<float2>(M + 1);
+      fft_init_tables<float>(nlon, tmf, tnf, stream);
+      sdf.twM = tmf, sdf.twN = tnf;
+      sdf.nrad = sd.nrad;
+      for (int i = 0; i < 12; ++i) sdf.rad[i] = sd.rad[i];
+    }
   }
 
   // --- pressure_data / setdampspec / init_semimpdata ---
@@ -590,6 +682,7 @@ class Dycore : public DycoreBase {
     FHb = dalloc<R>((size_t)nf * std::max(std::max(ldFH, ldGH), ldS));
     gS = dalloc<R>((size_t)sr.total * ng);
     gA = dalloc<R>((size_t)ar.total * ng);
+    if (eddy_) rmean = dalloc<double>((size_t)ar.total * nlat);  // one mean per analysed (row, latitude)
     psg = dalloc<R>(ng);
     dlnpsdt = dalloc<R>(ng);
     dlnpdtg = dalloc<R>((size_t)L * ng);
@@ -641,12 +734,12 @@ class Dycore : public DycoreBase {
       full.push_back({nt * L, sr.dqdx, -1, 0, 0, sc.trc, 0.0, ai});
       full.push_back({nt * L, sr.dqdy, 1, sc.trc - h0, -1, 0, ai, 0.0});
     }
-    c2rFull = make_c2r_plan<R>(full.data(), (int)full.size(), stream, M);
+    c2rFull = mk_c2r(full.data(), (int)full.size());
     std::vector<SynthDesc> inv = {
         full[0], full[1], full[2], full[3], full[4], full[7], full[8], full[9],
     };
     if (nt > 0) inv.push_back(full[10]);
-    c2rInv = make_c2r_plan<R>(inv.data(), (int)inv.size(), stream, M);
+    c2rInv = mk_c2r(inv.data(), (int)inv.size());
     std::vector<AnalDesc> an = {
         {L, ar.ttend, ap.ttend, 0, -1, 1.0, 0.0},
         {L, ar.ke, ap.ke, 0, -1, 1.0, 0.0},
@@ -655,9 +748,9 @@ class Dycore : public DycoreBase {
         {L, ar.fv, ap.imfv, 1, ah.mfv, 1.0, -1.0},
     };
     if (nt > 0) an.push_back({nt * L, ar.qtend, ap.qtend, 0, -1, 1.0, 0.0});
-    r2cDyn = make_r2c_plan<R>(an.data(), (int)an.size(), stream, M);
+    r2cDyn = mk_r2c(an.data(), (int)an.size());
     AnalDesc ph = {3 * L + 1, 0, 0, 0, -1, 1.0, 0.0};
-    r2cPhys = make_r2c_plan<R>(&ph, 1, stream, M);
+    r2cPhys = mk_r2c(&ph, 1);
     if (simple()) {
       // grid rows: Tv [0,L), q [L,2L), u [2L,3L), v [3L,4L), fixer 4L.  As in
       // getvrtdivspec: GP gets i m/cos V (vorticity) and i m/cos U
@@ -669,7 +762,7 @@ class Dycore : public DycoreBase {
           {L, 3 * L, 2 * L + 1, 1, L, 1.0, -1.0},
       };
       if (c.massfix) sd_.push_back({1, 4 * L, 2 * L, 0, -1, 1.0, 0.0});
-      r2cSimple = make_r2c_plan<R>(sd_.data(), (int)sd_.size(), stream, M);
+      r2cSimple = mk_r2c(sd_.data(), (int)sd_.size());
       anaSimple = make_anal_plan(T, 2 * (4 * L + 1), stream);
     }
   }
@@ -679,7 +772,7 @@ class Dycore : public DycoreBase {
     do_synth(false, synP, S, ldS, 2 * sc.ncol, FPb, ldFP);
     do_synth(true, synH, S + 2 * (2 * L), ldS, 2 * (sc.ncol - 2 * L), FHb, ldFH);
     mark(PH_LSYN);
-    launch_c2r<R>(sd, plan, FPb, ldFP, FHb, ldFH, gS, stream);
+    c2r(plan, FPb, ldFP, FHb, ldFH, gS);
     mark(PH_FSYN);
   }
   ColumnArgs<R> column_args(bool want_extra) {
@@ -727,7 +820,7 @@ class Dycore : public DycoreBase {
       launch_pdry_init(pmean, moist ? pmoist : nullptr, pdryini, stream);
     }
     mark(PH_COL);
-    launch_r2c<R>(sd, r2cDyn, gA, FPb, ldGP, FHb, ldGH, stream);
+    r2c(r2cDyn, gA, FPb, ldGP, FHb, ldGH);
     mark(PH_FANA);
     do_anal(false, anaP, FPb, ldGP, 2 * ap.ncol, AP, ldAP);
     do_anal(true, anaH, FHb, ldGH, 2 * ah.ncol, AH, ldAH);
@@ -845,7 +938,7 @@ class Dycore : public DycoreBase {
       launch_massfix_grid<R>(psg, pdryini, pmean, pwatg, Phys::grav, (int)ng, gA + (long)4 * L * ng, stream);
     }
     mark(PH_PHYS);
-    launch_r2c<R>(sd, r2cSimple, gA, FPb, ldGP, FHb, ldGH, stream);
+    r2c(r2cSimple, gA, FPb, ldGP, FHb, ldGH);
     mark(PH_FANA);
     do_anal(false, anaSimple, FPb, ldGP, 2 * (4 * L + 1), AP, ldAP);
     do_anal(true, anaH, FHb, ldGH, 2 * ah.ncol, AH, ldAH);
@@ -867,7 +960,7 @@ class Dycore : public DycoreBase {
     }
     mark(PH_PHYS);
     if (c.heldsuarez || c.massfix) {
-      launch_r2c<R>(sd, r2cPhys, gA, FPb, ldGP, FHb, ldGH, stream);
+      r2c(r2cPhys, gA, FPb, ldGP, FHb, ldGH);
       mark(PH_FANA);
       do_anal(false, anaPhys, FPb, ldGP, 2 * (3 * L + 1), AP, ldAP);
       mark(PH_LANA);
@@ -946,7 +1039,7 @@ class Dycore : public DycoreBase {
     mlp_forward_on(closure, clos_x, (int)ng, clos_y, stream);
     launch_closure_out<R>(clos_y, L, ng, omu, osd, (R)c.dt, gA, stream);
     mark(PH_PHYS);
-    launch_r2c<R>(sd, r2cClos, gA, FPb, ldGP, FHb, ldGH, stream);
+    r2c(r2cClos, gA, FPb, ldGP, FHb, ldGH);
     mark(PH_FANA);
     do_anal(false, anaSimple, FPb, ldGP, 2 * (4 * L + 1), AP, ldAP);
     do_anal(true, anaH, FHb, ldGH, 2 * ah.ncol, AH, ldAH);
@@ -976,7 +1069,7 @@ class Dycore : public DycoreBase {
             {L, 2 * L, 3 * L + 1, 1, 0, 1.0, 1.0},
             {L, 3 * L, 2 * L + 1, 1, L, 1.0, -1.0},
         };
-        r2cClos = make_r2c_plan<R>(cd.data(), (int)cd.size(), stream, M);
+        r2cClos = mk_r2c(cd.data(), (int)cd.size());
       }
       if (!anaSimple.items) anaSimple = make_anal_plan(T, 2 * (4 * L + 1), stream);
       GD_CUDA(cudaStreamSynchronize(stream));
@@ -1291,7 +1384,7 @@ class Dycore : public DycoreBase {
     if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
     if (simple()) {  // phy_run_simple.f90:145-160 on the grid of the last getdyntend
       launch_simple_physics<R>(simple_args(), stream);
-      launch_r2c<R>(sd, r2cSimple, gA, FPb, ldGP, FHb, ldGH, stream);
+      r2c(r2cSimple, gA, FPb, ldGP, FHb, ldGH);
       do_anal(false, anaSimple, FPb, ldGP, 2 * (4 * L + 1), AP, ldAP);
       do_anal(true, anaH, FHb, ldGH, 2 * ah.ncol, AH, ldAH);
       const R ai = (R)(1.0 / Phys::rerth);
@@ -1323,7 +1416,7 @@ class Dycore : public DycoreBase {
       return;
     }
     launch_hs_forcing<R>(hs_args(), stream);
-    launch_r2c<R>(sd, r2cPhys, gA, FPb, ldGP, FHb, ldGH, stream);
+    r2c(r2cPhys, gA, FPb, ldGP, FHb, ldGH);
     do_anal(false, anaPhys, FPb, ldGP, 2 * (3 * L + 1), AP, ldAP);
     double* tmp = dalloc<double>(2L * nlm * L);
     spec_out(AP, ldAP, 0, L, dtv, tmp);
@@ -1350,8 +1443,8 @@ class Dycore : public DycoreBase {
   void api_synth(const R* X, int ncs, bool needH, const std::vector<SynthDesc>& ds, int nrows, double* out) {
     do_synth(false, synth_plan(2 * ncs), X, ldS, 2 * ncs, FPb, ldS);
     if (needH) do_synth(true, synth_plan(2 * ncs), X, ldS, 2 * ncs, FHb, ldS);
-    FftPlan p = make_c2r_plan<R>(ds.data(), (int)ds.size(), stream, M);
-    launch_c2r<R>(sd, p, FPb, ldS, FHb, ldS, gS, stream);
+    FftPlan p = mk_c2r(ds.data(), (int)ds.size());
+    c2r(p, FPb, ldS, FHb, ldS, gS);
     grid_out(gS, nrows, out);
     free_fft_plan(p);
   }
@@ -1440,8 +1533,8 @@ class Dycore : public DycoreBase {
     }
   }
   void api_anal(const std::vector<AnalDesc>& ds, int ncP, int ncH) {
-    FftPlan p = make_r2c_plan<R>(ds.data(), (int)ds.size(), stream, M);
-    launch_r2c<R>(sd, p, gA, FPb, ldS, FHb, ldS, stream);
+    FftPlan p = mk_r2c(ds.data(), (int)ds.size());
+    r2c(p, gA, FPb, ldS, FHb, ldS);
     do_anal(false, anal_plan(2 * ncP), FPb, ldS, 2 * ncP, AP, ldAP);
     if (ncH > 0) do_anal(true, anal_plan(2 * ncH), FHb, ldS, 2 * ncH, AH, ldAH);
     free_fft_plan(p);
@@ -1627,7 +1720,7 @@ int gd_init(const gd_config* cfg, const double* ak, const double* bk, gd_ctx** o
   else if (c.nlev < 3 || c.nlev > 126) why = "nlev must be in [3, 126]";
   else if (c.ntrac < 0) why = "ntrac must be >= 0";
   else if (!(c.dt > 0)) why = "dt must be positive";
-  else if (c.precision < GD_PREC_FP64 || c.precision > GD_PREC_BF16X3) why = "unknown precision";
+  else if (c.precision < GD_PREC_FP64 || c.precision > GD_PREC_F64_EDDY) why = "unknown precision";
   else if (c.dcmip >= 0 && c.heldsuarez) why = "heldsuarez and dcmip cannot both be set";
   else if (c.dcmip >= 0 && c.dcmip / 10 != 4 && c.dcmip / 10 != 5) why = "dcmip must be 4x or 5x (or -1)";
   else if (c.dcmip >= 0 && !c.dry && c.ntrac < 1) why = "moist DCMIP physics needs ntrac >= 1 (humidity)";
@@ -1641,7 +1734,7 @@ int gd_init(const gd_config* cfg, const double* ak, const double* bk, gd_ctx** o
   ctx->ak.assign(ak, ak + c.nlev + 1);
   ctx->bk.assign(bk, bk + c.nlev + 1);
   try {
-    if (c.precision == GD_PREC_FP64)
+    if (c.precision == GD_PREC_FP64 || c.precision == GD_PREC_F64_TF32X3 || c.precision == GD_PREC_F64_EDDY)
       ctx->d.reset(new gd::Dycore<double>(c, ak, bk));
     else
       ctx->d.reset(new gd::Dycore<float>(c, ak, bk));

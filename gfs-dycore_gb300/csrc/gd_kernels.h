@@ -33,6 +33,9 @@ void launch_legendre_tables(int T, int nh, const double* mu, const long* toff, d
                             cudaStream_t s);
 template <typename R>
 void launch_convert(const double* src, R* dst, long n, cudaStream_t s);
+// strided 2-D copy with a type change (rows x cols, row pitches lds / ldd)
+template <typename S, typename D>
+void launch_convert2d(const S* src, long lds, D* dst, long ldd, long rows, int cols, cudaStream_t s);
 
 // Legendre stage, per-order SIMT GEMMs with the even/odd split.
 // synthesis: F[m][j][c] = sum_{n} T[m][j][n-m] B[idx(n,m)][c]   (real columns)
@@ -87,6 +90,18 @@ void launch_r2c(const ShtDev<R>& d, const FftPlan& plan, const R* grid, R* GP, l
                 cudaStream_t s);
 template <typename R>
 void fft_init_tables(int nlon, typename C2<R>::T* twM, typename C2<R>::T* twN, cudaStream_t s);
+// Eddy FFTs of the FP64-state mode (four-step lengths only, see
+// fft_eddy_supported): orders m >= 1 in FP32 from / to the FP32 Fourier rows
+// FP, FH (or GP, GH); order 0 in FP64 from / to FP0, FH0 (GP0, GH0), same
+// pitches; FP64 grid.  Plans come from make_c2r_plan<float> /
+// make_r2c_plan<float>.  rmean holds one double per (grid row, latitude)
+// the r2c plan reads.
+bool fft_eddy_supported(int M);
+void launch_c2r_eddy(const ShtDev<float>& d, const FftPlan& plan, const float* FP, const double* FP0, long ldP,
+                     const float* FH, const double* FH0, long ldH, double* grid, cudaStream_t s);
+void launch_r2c_eddy(const ShtDev<float>& d, const FftPlan& plan, const double* grid, double* rmean,
+                     const double* wn64, float* GP, double* GP0, long ldP, float* GH, double* GH0, long ldH,
+                     cudaStream_t s);
 void fft_radix_plan(int M, int* nrad, int* rad);
 
 }  // namespace gd

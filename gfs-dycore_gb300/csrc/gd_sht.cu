@@ -132,6 +132,30 @@ void launch_convert(const double* src, R* dst, long n, cudaStream_t s) {
 template void launch_convert<double>(const double*, double*, long, cudaStream_t);
 template void launch_convert<float>(const double*, float*, long, cudaStream_t);
 
+// dst[r][c] = src[r][c] for r < rows, c < cols (row pitches lds, ldd), with
+// the type change round-to-nearest; the staging copies of the FP64-state
+// split-precision mode around the FP32 tensor-core Legendre GEMMs
+template <typename S, typename D>
+__global__ void k_convert2d(const S* __restrict__ src, long lds, D* __restrict__ dst, long ldd, long rows,
+                            int cols) {
+  const long n = rows * cols;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const long r = i / cols;
+    const int c = (int)(i - r * cols);
+    dst[r * ldd + c] = (D)src[r * lds + c];
+  }
+}
+template <typename S, typename D>
+void launch_convert2d(const S* src, long lds, D* dst, long ldd, long rows, int cols, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return;
+  int blocks = (int)std::min<long>(ceil_div(rows * cols, 256), 152L * 16);
+  k_convert2d<S, D><<<blocks, 256, 0, s>>>(src, lds, dst, ldd, rows, cols);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+template void launch_convert2d<double, float>(const double*, long, float*, long, long, int, cudaStream_t);
+template void launch_convert2d<float, double>(const float*, long, double*, long, long, int, cudaStream_t);
+
 // --------------------------------------------------------- Legendre GEMMs --
 // Tiles: synthesis 32 latitude pairs x 64 real columns, analysis 32 degrees
 // x 64 real columns; 256 threads, each 2 rows x 4 columns (columns strided
@@ -1103,16 +1127,23 @@ __device__ __forceinline__ void fft4(typename C2<R>::T* buf, const typename C2<R
 // r2c with 4 CTAs of 8 FP32 rows of 576 points; without a bound the
 // compiler takes more registers and fewer CTAs fit).
 constexpr int C2R4_MINB = 5, R2C4_MINB = 4;
-template <typename R, int M, int M1, int M2>
+// G (the grid type) differs from R in the eddy form of the FP64-state mode:
+// the FFT of orders m >= 1 runs in R = float from FP32 Fourier rows, order 0
+// (the zonal mean alpha Re F_0) is read in FP64 from FP0/FH0 (same pitches)
+// and added in FP64 to every FP64 grid value of its row.
+template <typename R, int M, int M1, int M2, typename G = R>
 __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, C2R4_MINB)
     k_c2r_4(const int2* __restrict__ jobs, const SynthDesc* __restrict__ descs, ShtDev<R> d,
-            const R* __restrict__ FP, long ldP, const R* __restrict__ FH, long ldH, R* __restrict__ grid) {
+            const R* __restrict__ FP, long ldP, const R* __restrict__ FH, long ldH, G* __restrict__ grid,
+            const double* __restrict__ FP0, const double* __restrict__ FH0) {
   typedef typename C2<R>::T V;
   typedef typename C4<R>::T V4;
+  constexpr bool kEddy = !std::is_same<G, R>::value;
   constexpr int NR = nr4_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = row_pitch4<M, M1>();
   constexpr int KS = NT / NR;  // order stride of one thread in the gather
   static_assert(NT % NR == 0 && M1 % 2 == 0, "thread maps of the four-step kernels");
   __shared__ V buf[NR * RP];
+  __shared__ double mean_s[kEddy ? NR : 1];
   const int T = d.T, nlat = d.nlat, nlon = d.nlon;
   const int2 jb = jobs[blockIdx.x];
   const SynthDesc ds = descs[jb.x];
@@ -1136,6 +1167,16 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
     sb = (long)nlat * ld;
   }
   V* brow = buf + r * RP;
+  if constexpr (kEddy) {
+    if (kq == 0) {  // one thread per row: the FP64 zonal mean of the row
+      double mv = 0.0;
+      if (live && ds.srcA >= 0) {
+        const long ld = ds.srcA == 0 ? ldP : ldH;
+        mv = ds.alpha * (ds.srcA == 0 ? FP0 : FH0)[(long)j * ld + 2 * (ds.colA + r0 + r)];
+      }
+      mean_s[r] = mv;
+    }
+  }
   // the gather issues the loads of CB consecutive orders of the thread
   // before using any of them: the loads are latency-bound, not issue-bound
   constexpr int CB = 4;
@@ -1189,6 +1230,9 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
         }
       }
       if (kk == 0) x1.y = R(0);
+      if constexpr (kEddy) {
+        if (kk == 0) x1.x = R(0);  // order 0 is added in FP64 at the store
+      }
       V A = cadd(x1, cconj(x2)), B = csub(x1, cconj(x2));
       V Bw = cmul(B, cconj(d.twN[kk]));
       z1.x = A.x - Bw.y;
@@ -1207,23 +1251,37 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
   __syncthreads();
   // step B stores its outputs straight to the grid row: z[n] is the real
   // pair (x[2n], x[2n+1]); a warp's lanes hold consecutive n of a row
-  R* const gout = grid + ((long)(ds.dst + r0) * nlat + j) * nlon;
+  G* const gout = grid + ((long)(ds.dst + r0) * nlat + j) * nlon;
   const long rstride = (long)nlat * nlon;
   fft4x<R, M, M1, M2, NR, NT, +1>(buf, d.twM, Fft4InBuf{}, [&](int rr, int k2, const V* x) {
     if (rr < nr) {
-      V* o = reinterpret_cast<V*>(gout + rr * rstride) + k2;
+      if constexpr (kEddy) {
+        const double mv = mean_s[rr];
+        double2* o = reinterpret_cast<double2*>(gout + rr * rstride) + k2;
 #pragma unroll
-      for (int k1 = 0; k1 < M1; ++k1) o[M2 * k1] = x[k1];
+        for (int k1 = 0; k1 < M1; ++k1) o[M2 * k1] = make_double2((double)x[k1].x + mv, (double)x[k1].y + mv);
+      } else {
+        V* o = reinterpret_cast<V*>(gout + rr * rstride) + k2;
+#pragma unroll
+        for (int k1 = 0; k1 < M1; ++k1) o[M2 * k1] = x[k1];
+      }
     }
   });
 }
 
-template <typename R, int M, int M1, int M2>
+// Eddy form (G = double, R = float): the row's FP64 zonal mean rmean (from
+// k_rowmean) is subtracted in FP64 before the values are rounded to FP32, the
+// FFT of the remainder gives orders m >= 1 in FP32 (GP, GH), and order 0 is
+// written in FP64 to GP0 / GH0 (same pitches): 2 pi w_j times the mean.
+template <typename R, int M, int M1, int M2, typename G = R>
 __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, R2C4_MINB)
     k_r2c_4(const int2* __restrict__ jobs, const AnalDesc* __restrict__ descs, ShtDev<R> d,
-            const R* __restrict__ grid, R* __restrict__ GP, long ldP, R* __restrict__ GH, long ldH) {
+            const G* __restrict__ grid, R* __restrict__ GP, long ldP, R* __restrict__ GH, long ldH,
+            const double* __restrict__ rmean, const double* __restrict__ wn64, double* __restrict__ GP0,
+            double* __restrict__ GH0) {
   typedef typename C2<R>::T V;
   typedef typename C4<R>::T V4;
+  constexpr bool kEddy = !std::is_same<G, R>::value;
   constexpr int NR = nr4_of<R>(), NT = ((NR * (M1 > M2 ? M1 : M2) + 31) / 32) * 32, RP = row_pitch4<M, M1>();
   constexpr int KS = NT / NR;
   static_assert(NT % NR == 0 && M1 % 2 == 0, "thread maps of the four-step kernels");
@@ -1235,13 +1293,23 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
   const int nr = min(NR, ds.count - r0);
   // step A loads its inputs straight from the grid row: x[n] is the real
   // pair (g[2n], g[2n+1]); rows past nr are zero
-  const R* const gin = grid + ((long)(ds.src + r0) * nlat + j) * nlon;
+  const G* const gin = grid + ((long)(ds.src + r0) * nlat + j) * nlon;
   const long rstride = (long)nlat * nlon;
   fft4x<R, M, M1, M2, NR, NT, -1>(buf, d.twM, [&](int rr, int n1, V* x) {
     if (rr < nr) {
-      const V* g = reinterpret_cast<const V*>(gin + rr * rstride) + n1;
+      if constexpr (kEddy) {
+        const double mv = rmean[(long)(ds.src + r0 + rr) * nlat + j];
+        const double2* g = reinterpret_cast<const double2*>(gin + rr * rstride) + n1;
 #pragma unroll
-      for (int n2 = 0; n2 < M2; ++n2) x[n2] = g[M1 * n2];
+        for (int n2 = 0; n2 < M2; ++n2) {
+          const double2 t = g[M1 * n2];
+          x[n2] = mk2<R>((R)(t.x - mv), (R)(t.y - mv));
+        }
+      } else {
+        const V* g = reinterpret_cast<const V*>(gin + rr * rstride) + n1;
+#pragma unroll
+        for (int n2 = 0; n2 < M2; ++n2) x[n2] = g[M1 * n2];
+      }
     } else {
 #pragma unroll
       for (int n2 = 0; n2 < M2; ++n2) x[n2] = mk2<R>(R(0), R(0));
@@ -1262,6 +1330,24 @@ __global__ void __launch_bounds__(((nr4_of<R>() * (M1 > M2 ? M1 : M2) + 31) / 32
     for (int h = 0; h < 2; ++h) {
       const int k = h ? M - kk : kk;
       if (k > T || (h && (kk == 0 || M - kk == kk))) continue;
+      if constexpr (kEddy) {
+        if (k == 0) {  // order 0 in FP64 from the row mean; zeros in the FP32 rows
+          const double x0 = wn64[j] * (double)nlon * rmean[(long)(ds.src + col) * nlat + j];
+          if (pP) {
+            *reinterpret_cast<V*>(pP) = mk2<R>(R(0), R(0));
+            double* q = GP0 + (long)j * ldP + 2 * (ds.dstP + col);
+            q[0] = ds.imcosP ? 0.0 : x0 * ds.scaleP;
+            q[1] = 0.0;
+          }
+          if (pH) {
+            *reinterpret_cast<V*>(pH) = mk2<R>(R(0), R(0));
+            double* q = GH0 + (long)j * ldH + 2 * (ds.dstH + col);
+            q[0] = x0 * ds.scaleH;
+            q[1] = 0.0;
+          }
+          continue;
+        }
+      }
       const V za = h ? Z2 : Z1, zb = h ? Z1 : Z2;
       V E = cadd(za, cconj(zb)), O = csub(za, cconj(zb));
       V Oi;
@@ -1310,7 +1396,8 @@ static bool launch_c2r_fixed(const ShtDev<R>& d, const FftPlan& plan, const R* F
     switch (d.M) {
 #define GD_C2R4(MM, A, B)                                                                         \
   case MM:                                                                                        \
-    k_c2r_4<R, MM, A, B><<<grd, nt4<MM, A, B>(NR), 0, s>>>(plan.jobs, ds, d, FP, ldP, FH, ldH, grid); \
+    k_c2r_4<R, MM, A, B><<<grd, nt4<MM, A, B>(NR), 0, s>>>(plan.jobs, ds, d, FP, ldP, FH, ldH, grid, nullptr, \
+                                                            nullptr);                                        \
     return true;
       GD_C2R4(64, 8, 8)
       GD_C2R4(96, 8, 12)
@@ -1352,7 +1439,8 @@ static bool launch_r2c_fixed(const ShtDev<R>& d, const FftPlan& plan, const R* g
     switch (d.M) {
 #define GD_R2C4(MM, A, B)                                                                         \
   case MM:                                                                                        \
-    k_r2c_4<R, MM, A, B><<<grd, nt4<MM, A, B>(NR), 0, s>>>(plan.jobs, ds, d, grid, GP, ldP, GH, ldH); \
+    k_r2c_4<R, MM, A, B><<<grd, nt4<MM, A, B>(NR), 0, s>>>(plan.jobs, ds, d, grid, GP, ldP, GH, ldH, nullptr, \
+                                                            nullptr, nullptr, nullptr);                      \
     return true;
       GD_R2C4(64, 8, 8)
       GD_R2C4(96, 8, 12)
@@ -1477,5 +1565,83 @@ template void launch_r2c<double>(const ShtDev<double>&, const FftPlan&, const do
                                  long, cudaStream_t);
 template void launch_r2c<float>(const ShtDev<float>&, const FftPlan&, const float*, float*, long, float*, long,
                                 cudaStream_t);
+
+// ------------------------------------------------- eddy FFTs (FP64 state) --
+// FP64 zonal mean of every (grid row, latitude) a r2c plan reads, one warp
+// per row in a fixed summation order (lane-strided partial sums, then the
+// xor butterfly; lane 0 writes), so the result does not depend on the launch.
+// The job list is the FP32 four-step plan's: NR rows per job.
+template <int NR>
+__global__ void __launch_bounds__(32 * NR) k_rowmean(const int2* __restrict__ jobs, const AnalDesc* __restrict__ descs,
+                                                     int nlat, int nlon, const double* __restrict__ grid,
+                                                     double* __restrict__ rmean) {
+  const int2 jb = jobs[blockIdx.x];
+  const AnalDesc ds = descs[jb.x];
+  const int j = blockIdx.y, rr = threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (rr >= min(NR, ds.count - jb.y)) return;
+  const long row = (long)ds.src + jb.y + rr;
+  const double* g = grid + (row * nlat + j) * nlon;
+  double sum = 0.0;
+  for (int i = lane; i < nlon; i += 32) sum += g[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) rmean[row * nlat + j] = sum / (double)nlon;
+}
+
+bool fft_eddy_supported(int M) { return four_step_len(M) && !getenv("GD_FFT_STOCKHAM"); }
+
+void launch_c2r_eddy(const ShtDev<float>& d, const FftPlan& plan, const float* FP, const double* FP0, long ldP,
+                     const float* FH, const double* FH0, long ldH, double* grid, cudaStream_t s) {
+  if (plan.njobs == 0) return;
+  dim3 grd(plan.njobs, d.nlat);
+  const SynthDesc* ds = (const SynthDesc*)plan.descs;
+  constexpr int NR = nr4_of<float>();
+  switch (d.M) {
+#define GD_C2RE(MM, A, B)                                                                                    \
+  case MM:                                                                                                   \
+    k_c2r_4<float, MM, A, B, double><<<grd, nt4<MM, A, B>(NR), 0, s>>>(plan.jobs, ds, d, FP, ldP, FH, ldH, grid, \
+                                                                       FP0, FH0);                            \
+    break;
+    GD_C2RE(64, 8, 8)
+    GD_C2RE(96, 8, 12)
+    GD_C2RE(192, 12, 16)
+    GD_C2RE(384, 16, 24)
+    GD_C2RE(576, 24, 24)
+#undef GD_C2RE
+    default:
+      throw CudaError("eddy FFT: no four-step kernel for this longitude count");
+  }
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+
+void launch_r2c_eddy(const ShtDev<float>& d, const FftPlan& plan, const double* grid, double* rmean,
+                     const double* wn64, float* GP, double* GP0, long ldP, float* GH, double* GH0, long ldH,
+                     cudaStream_t s) {
+  if (plan.njobs == 0) return;
+  dim3 grd(plan.njobs, d.nlat);
+  const AnalDesc* ds = (const AnalDesc*)plan.descs;
+  constexpr int NR = nr4_of<float>();
+  k_rowmean<NR><<<grd, 32 * NR, 0, s>>>(plan.jobs, ds, d.nlat, d.nlon, grid, rmean);
+  count_launch();
+  GD_LAUNCH_CHECK();
+  switch (d.M) {
+#define GD_R2CE(MM, A, B)                                                                                     \
+  case MM:                                                                                                    \
+    k_r2c_4<float, MM, A, B, double><<<grd, nt4<MM, A, B>(NR), 0, s>>>(plan.jobs, ds, d, grid, GP, ldP, GH, ldH, \
+                                                                       rmean, wn64, GP0, GH0);                \
+    break;
+    GD_R2CE(64, 8, 8)
+    GD_R2CE(96, 8, 12)
+    GD_R2CE(192, 12, 16)
+    GD_R2CE(384, 16, 24)
+    GD_R2CE(576, 24, 24)
+#undef GD_R2CE
+    default:
+      throw CudaError("eddy FFT: no four-step kernel for this longitude count");
+  }
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
 
 }  // namespace gd

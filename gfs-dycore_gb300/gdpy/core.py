@@ -26,7 +26,7 @@ GD_ERR_UNSUPPORTED = -5
 GD_ERR_NUMERIC = -6
 GD_ERR_IO = -7
 
-PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3}
+PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3, "f64_tf32x3": 4, "f64_eddy": 5}
 
 API_FUNCTIONS = [
     "gd_default_config", "gd_init", "gd_finalize", "gd_set_state", "gd_get_state", "gd_get_topo",

@@ -45,6 +45,18 @@ extern "C" {
 #define GD_PREC_FP32 1        /* FP32 state and SIMT FP32 Legendre GEMMs          */
 #define GD_PREC_TF32X3 2      /* FP32 state, Legendre as TF32x3 tcgen05 products  */
 #define GD_PREC_BF16X3 3      /* FP32 state, Legendre as BF16x3 tcgen05 products  */
+#define GD_PREC_F64_TF32X3 4  /* FP64 state, FFTs, column kernels and stage; the
+                                 Legendre orders m >= 1 as TF32x3 tcgen05
+                                 products of FP32-rounded operands, order 0
+                                 on the FP64 SIMT path                           */
+#define GD_PREC_F64_EDDY 5    /* FP64 state, column kernels and stage; every zonal
+                                 mean (order 0) transformed in FP64; the eddy
+                                 orders m >= 1 in FP32: longitude FFTs in FP32
+                                 (the FP64 row mean taken out before rounding)
+                                 and Legendre as TF32x3 tcgen05 products.  On
+                                 grids whose nlon/2 has no four-step FFT kernel
+                                 (64, 96, 192, 384, 576) the FFTs stay FP64, as
+                                 in GD_PREC_F64_TF32X3                           */
 
 typedef struct gd_config {
   int ntrunc;          /* triangular truncation T (params.f90 ntrunc)       */

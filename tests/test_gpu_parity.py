@@ -336,3 +336,44 @@ def test_autotune_keeps_the_step(prec):
     tol = 1e-6 if prec == "tf32x3" else 1e-12
     for k in ("vrt", "tv", "lnps", "trc"):
         assert rel(out[1][k], out[0][k]) < tol, k
+
+
+# ---- FP64 state with the split-precision Legendre GEMM (f64_tf32x3) ----
+@pytest.mark.parametrize("prec", ["f64_tf32x3", "f64_eddy"])
+@pytest.mark.parametrize("T", [21, 42, 126])
+def test_transforms_f64_split(oracle_mod, T, prec):
+    """The GEMM of orders m >= 1 sees FP32-rounded operands and accumulates in
+    FP32 on the tensor cores; order 0 and everything else stay FP64 (f64_eddy:
+    the longitude FFTs of orders m >= 1 also run in FP32; T21's 64-point rows
+    have no four-step kernel, so there it runs the FP64 FFTs)."""
+    g, o = pair(oracle_mod, T, 4, precision=prec)
+    a = rand_spec(T, 5, seed=T + 17, slope=-1.0)
+    b = rand_spec(T, 5, seed=T + 18, slope=-1.0)
+    e = {"spectogrd": rel(g.spectogrd(a), o.spectogrd(a))}
+    grid = o.spectogrd(a)
+    e["grdtospec"] = rel(g.grdtospec(grid), o.grdtospec(grid))
+    ug, vg = g.getuv(a, b)
+    uo, vo = o.getuv(a, b)
+    e["getuv"] = max(rel(ug, uo), rel(vg, vo))
+    vr, dv = g.getvrtdivspec(uo, vo)
+    vro, dvo = o.getvrtdivspec(uo, vo)
+    e["getvrtdivspec"] = max(rel(vr, vro), rel(dv, dvo))
+    print(f"T{T} {prec}", {k: f"{v:.2e}" for k, v in e.items()})
+    for k, v in e.items():
+        assert v < 1e-5, (k, v)
+    # order 0 alone (zonal means) is exact to FP64 rounding
+    z = np.zeros_like(a)
+    z[:, : T + 1] = a[:, : T + 1].real
+    assert rel(g.spectogrd(z), o.spectogrd(z)) < 1e-12
+
+
+@pytest.mark.parametrize("prec", ["f64_tf32x3", "f64_eddy"])
+def test_steps_f64_split(oracle_mod, prec):
+    g, o = pair(oracle_mod, 42, 20, precision=prec)
+    set_both(g, o, inputs.hs_rest_state(42, 20, seed=2))
+    g.advance(2)
+    o.advance(2)
+    a, b = g.get_state(), o.get_state()
+    e = {k: rel(a[k], b[k]) for k in ("vrt", "div", "tv", "lnps")}
+    print(f"T42L20 2 steps {prec}", {k: f"{v:.2e}" for k, v in e.items()})
+    assert e["tv"] < 1e-5 and e["lnps"] < 2e-6 and e["vrt"] < 2e-3

@@ -46,6 +46,9 @@ class DycoreBase {
   virtual void set_state(const double*, const double*, const double*, const double*, const double*,
                          const double*) = 0;
   virtual void get_state(double*, double*, double*, double*, double*) = 0;
+  // single-precision host arrays (the reference's default complex(4) / real(4))
+  virtual void set_state(const float*, const float*, const float*, const float*, const float*, const float*) = 0;
+  virtual void get_state(float*, float*, float*, float*, float*) = 0;
   virtual void getdyntend(int, int, double*, double*, double*, double*, double*) = 0;
   virtual void getphytend(double*, double*, double*, double*, double*) = 0;
   virtual void advance(int nsteps) = 0;
@@ -58,6 +61,11 @@ class DycoreBase {
   virtual void getuv(int, const double*, const double*, double*, double*) = 0;
   virtual void getvrtdivspec(int, const double*, const double*, double*, double*) = 0;
   virtual void getgrad(int, const double*, double*, double*) = 0;
+  virtual void spectogrd(int, const float*, float*) = 0;
+  virtual void grdtospec(int, const float*, float*) = 0;
+  virtual void getuv(int, const float*, const float*, float*, float*) = 0;
+  virtual void getvrtdivspec(int, const float*, const float*, float*, float*) = 0;
+  virtual void getgrad(int, const float*, float*, float*) = 0;
   virtual void grid_info(double*, double*, double*, int*, int*, double*, double*) = 0;
   virtual int get_grid(const char*, double*) = 0;
   virtual void diag(double*) = 0;
@@ -1299,12 +1307,31 @@ class Dycore : public DycoreBase {
   }
   void set_state(const double* vrt, const double* div, const double* tv, const double* trc, const double* lnps,
                  const double* topo) override {
+    set_state_t(vrt, div, tv, trc, lnps, topo);
+  }
+  void set_state(const float* vrt, const float* div, const float* tv, const float* trc, const float* lnps,
+                 const float* topo) override {
+    std::vector<double> t64;
+    if (topo) t64.assign(topo, topo + 2 * (size_t)nlm);
+    set_state_t(vrt, div, tv, trc, lnps, topo ? t64.data() : nullptr);
+  }
+  void get_state(double* vrt, double* div, double* tv, double* trc, double* lnps) override {
+    get_state_t(vrt, div, tv, trc, lnps);
+  }
+  void get_state(float* vrt, float* div, float* tv, float* trc, float* lnps) override {
+    get_state_t(vrt, div, tv, trc, lnps);
+  }
+  // H: the host element type (double, or float for the single-precision
+  // entry points); host arrays are copied as they are and converted on the
+  // device, so a float caller moves half the bytes
+  template <typename H>
+  void set_state_t(const H* vrt, const H* div, const H* tv, const H* trc, const H* lnps, const double* topo) {
     if (nt > 0 && !trc) throw std::invalid_argument("trc is NULL but ntrac > 0");
-    double* st = staging();
+    H* st = reinterpret_cast<H*>(staging());
     long off = 0;
-    auto put = [&](const double* h, int nb, int col) {
-      double* d = st + off;
-      GD_CUDA(cudaMemcpyAsync(d, h, sizeof(double) * 2 * (long)nb * nlm, cudaMemcpyHostToDevice, stream));
+    auto put = [&](const H* h, int nb, int col) {
+      H* d = st + off;
+      GD_CUDA(cudaMemcpyAsync(d, h, sizeof(H) * 2 * (long)nb * nlm, cudaMemcpyHostToDevice, stream));
       launch_ref2int<R>(d, nb, nlm, S, ldS, col, stream);
       off += 2L * nb * nlm;
     };
@@ -1337,15 +1364,16 @@ class Dycore : public DycoreBase {
     cudaFree(p);
     allocs.erase(std::remove(allocs.begin(), allocs.end(), p), allocs.end());
   }
-  void get_state(double* vrt, double* div, double* tv, double* trc, double* lnps) override {
-    double* st = staging();
+  template <typename H>
+  void get_state_t(H* vrt, H* div, H* tv, H* trc, H* lnps) {
+    H* st = reinterpret_cast<H*>(staging());
     long off = 0;
-    auto get = [&](double* h, int nb, int col) {
-      double* d = st + off;
+    auto get = [&](H* h, int nb, int col) {
+      H* d = st + off;
       off += 2L * nb * nlm;
       if (!h) return;
       launch_int2ref<R>(S, ldS, col, nb, nlm, d, stream);
-      GD_CUDA(cudaMemcpyAsync(h, d, sizeof(double) * 2 * (long)nb * nlm, cudaMemcpyDeviceToHost, stream));
+      GD_CUDA(cudaMemcpyAsync(h, d, sizeof(H) * 2 * (long)nb * nlm, cudaMemcpyDeviceToHost, stream));
     };
     get(vrt, L, sc.vrt);
     get(div, L, sc.div);
@@ -1440,7 +1468,8 @@ class Dycore : public DycoreBase {
   }
   int chunk_cols() const { return std::max(1, std::min(sc.ncol / 2, ar.total / 2)); }
   // synthesis of ncs complex columns X[nlm][ldS] with descriptors -> host grids
-  void api_synth(const R* X, int ncs, bool needH, const std::vector<SynthDesc>& ds, int nrows, double* out) {
+  template <typename H>
+  void api_synth(const R* X, int ncs, bool needH, const std::vector<SynthDesc>& ds, int nrows, H* out) {
     do_synth(false, synth_plan(2 * ncs), X, ldS, 2 * ncs, FPb, ldS);
     if (needH) do_synth(true, synth_plan(2 * ncs), X, ldS, 2 * ncs, FHb, ldS);
     FftPlan p = mk_c2r(ds.data(), (int)ds.size());
@@ -1448,26 +1477,34 @@ class Dycore : public DycoreBase {
     grid_out(gS, nrows, out);
     free_fft_plan(p);
   }
-  void grid_out(const R* g, int nrows, double* out) {
+  // device grid rows (R) -> host (H), converted on the device when the types differ
+  template <typename H>
+  void grid_out(const R* g, int nrows, H* out) {
     long n = (long)nrows * ng;
-    if (sizeof(R) == 8) {
-      GD_CUDA(cudaMemcpyAsync(out, g, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+    if constexpr (std::is_same<R, H>::value) {
+      GD_CUDA(cudaMemcpyAsync(out, g, sizeof(H) * n, cudaMemcpyDeviceToHost, stream));
     } else {
-      double* tmp = dalloc<double>(n);
-      launch_to_double<R>(g, tmp, n, stream);
-      GD_CUDA(cudaMemcpyAsync(out, tmp, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+      H* tmp = dalloc<H>(n);
+      launch_convert2d<R, H>(g, ng, tmp, ng, nrows, (int)ng, stream);
+      GD_CUDA(cudaMemcpyAsync(out, tmp, sizeof(H) * n, cudaMemcpyDeviceToHost, stream));
       GD_CUDA(cudaStreamSynchronize(stream));
       release(tmp);
     }
     GD_CUDA(cudaStreamSynchronize(stream));
   }
-  void grid_in(const double* in, int nrows, R* g) {
+  template <typename H>
+  void grid_in(const H* in, int nrows, R* g) {
     long n = (long)nrows * ng;
-    double* tmp = dalloc<double>(n);
-    GD_CUDA(cudaMemcpyAsync(tmp, in, sizeof(double) * n, cudaMemcpyHostToDevice, stream));
-    launch_convert<R>(tmp, g, n, stream);
-    GD_CUDA(cudaStreamSynchronize(stream));
-    release(tmp);
+    if constexpr (std::is_same<R, H>::value) {
+      GD_CUDA(cudaMemcpyAsync(g, in, sizeof(H) * n, cudaMemcpyHostToDevice, stream));
+      GD_CUDA(cudaStreamSynchronize(stream));
+    } else {
+      H* tmp = dalloc<H>(n);
+      GD_CUDA(cudaMemcpyAsync(tmp, in, sizeof(H) * n, cudaMemcpyHostToDevice, stream));
+      launch_convert2d<H, R>(tmp, ng, g, ng, nrows, (int)ng, stream);
+      GD_CUDA(cudaStreamSynchronize(stream));
+      release(tmp);
+    }
   }
   R* X_ = nullptr;
   R* scratchX() {
@@ -1477,14 +1514,30 @@ class Dycore : public DycoreBase {
     }
     return X_;
   }
-  void spec_in(const double* h, int nb, R* X, int col) {
-    double* tmp = dalloc<double>(2L * nb * nlm);
-    GD_CUDA(cudaMemcpyAsync(tmp, h, sizeof(double) * 2 * (long)nb * nlm, cudaMemcpyHostToDevice, stream));
+  template <typename H>
+  void spec_in(const H* h, int nb, R* X, int col) {
+    H* tmp = dalloc<H>(2L * nb * nlm);
+    GD_CUDA(cudaMemcpyAsync(tmp, h, sizeof(H) * 2 * (long)nb * nlm, cudaMemcpyHostToDevice, stream));
     launch_ref2int<R>(tmp, nb, nlm, X, ldS, col, stream);
     GD_CUDA(cudaStreamSynchronize(stream));
     release(tmp);
   }
-  void spectogrd(int nb, const double* spec, double* grid) override {
+  void spectogrd(int nb, const double* spec, double* grid) override { spectogrd_t(nb, spec, grid); }
+  void spectogrd(int nb, const float* spec, float* grid) override { spectogrd_t(nb, spec, grid); }
+  void getuv(int nb, const double* vrt, const double* div, double* u, double* v) override { getuv_t(nb, vrt, div, u, v); }
+  void getuv(int nb, const float* vrt, const float* div, float* u, float* v) override { getuv_t(nb, vrt, div, u, v); }
+  void getgrad(int nb, const double* spec, double* gx, double* gy) override { getgrad_t(nb, spec, gx, gy); }
+  void getgrad(int nb, const float* spec, float* gx, float* gy) override { getgrad_t(nb, spec, gx, gy); }
+  void grdtospec(int nb, const double* grid, double* spec) override { grdtospec_t(nb, grid, spec); }
+  void grdtospec(int nb, const float* grid, float* spec) override { grdtospec_t(nb, grid, spec); }
+  void getvrtdivspec(int nb, const double* u, const double* v, double* vrt, double* div) override {
+    getvrtdivspec_t(nb, u, v, vrt, div);
+  }
+  void getvrtdivspec(int nb, const float* u, const float* v, float* vrt, float* div) override {
+    getvrtdivspec_t(nb, u, v, vrt, div);
+  }
+  template <typename H>
+  void spectogrd_t(int nb, const H* spec, H* grid) {
     R* X = scratchX();
     for (int b0 = 0; b0 < nb; b0 += chunk_cols()) {
       int k = std::min(chunk_cols(), nb - b0);
@@ -1493,7 +1546,8 @@ class Dycore : public DycoreBase {
       api_synth(X, k, false, ds, k, grid + (long)b0 * ng);
     }
   }
-  void getuv(int nb, const double* vrt, const double* div, double* u, double* v) override {
+  template <typename H>
+  void getuv_t(int nb, const H* vrt, const H* div, H* u, H* v) {
     R* X = scratchX();
     const int ch = chunk_cols();
     for (int b0 = 0; b0 < nb; b0 += ch) {
@@ -1503,10 +1557,10 @@ class Dycore : public DycoreBase {
       // s = a invlap vrt, c = a invlap div (shtns.f90:259-260)
       launch_scale_cols<R>(X, ldS, 0, 2 * k, nlm, invlap_a(), R(1), stream);
       std::vector<SynthDesc> ds = {{k, 0, 1, 0, 0, k, -1.0, 1.0}, {k, k, 1, k, 0, 0, 1.0, 1.0}};
-      std::vector<double> out(2L * k * ng);
+      std::vector<H> out(2L * k * ng);
       api_synth(X, 2 * k, true, ds, 2 * k, out.data());
-      memcpy(u + (long)b0 * ng, out.data(), sizeof(double) * k * ng);
-      memcpy(v + (long)b0 * ng, out.data() + (long)k * ng, sizeof(double) * k * ng);
+      memcpy(u + (long)b0 * ng, out.data(), sizeof(H) * k * ng);
+      memcpy(v + (long)b0 * ng, out.data() + (long)k * ng, sizeof(H) * k * ng);
     }
   }
   R* invlap_ = nullptr;
@@ -1518,7 +1572,8 @@ class Dycore : public DycoreBase {
     }
     return invlap_;
   }
-  void getgrad(int nb, const double* spec, double* gx, double* gy) override {
+  template <typename H>
+  void getgrad_t(int nb, const H* spec, H* gx, H* gy) {
     R* X = scratchX();
     const double ai = 1.0 / Phys::rerth;
     const int ch = chunk_cols();
@@ -1526,10 +1581,10 @@ class Dycore : public DycoreBase {
       int k = std::min(ch, nb - b0);
       spec_in(spec + 2L * b0 * nlm, k, X, 0);
       std::vector<SynthDesc> ds = {{k, 0, -1, 0, 0, 0, 0.0, ai}, {k, k, 1, 0, -1, 0, ai, 0.0}};
-      std::vector<double> out(2L * k * ng);
+      std::vector<H> out(2L * k * ng);
       api_synth(X, k, true, ds, 2 * k, out.data());
-      memcpy(gx + (long)b0 * ng, out.data(), sizeof(double) * k * ng);
-      memcpy(gy + (long)b0 * ng, out.data() + (long)k * ng, sizeof(double) * k * ng);
+      memcpy(gx + (long)b0 * ng, out.data(), sizeof(H) * k * ng);
+      memcpy(gy + (long)b0 * ng, out.data() + (long)k * ng, sizeof(H) * k * ng);
     }
   }
   void api_anal(const std::vector<AnalDesc>& ds, int ncP, int ncH) {
@@ -1540,23 +1595,25 @@ class Dycore : public DycoreBase {
     free_fft_plan(p);
   }
   int achunk() const { return std::max(1, std::min(ap.ncol / 2, ar.total / 2)); }
-  void grdtospec(int nb, const double* grid, double* spec) override {
+  template <typename H>
+  void grdtospec_t(int nb, const H* grid, H* spec) {
     const int ch = achunk();
-    double* tmp = dalloc<double>(2L * ch * nlm);
+    H* tmp = dalloc<H>(2L * ch * nlm);
     for (int b0 = 0; b0 < nb; b0 += ch) {
       int k = std::min(ch, nb - b0);
       grid_in(grid + (long)b0 * ng, k, gA);
       api_anal({{k, 0, 0, 0, -1, 1.0, 0.0}}, k, 0);
       launch_int2ref<R>(AP, ldAP, 0, k, nlm, tmp, stream);
-      GD_CUDA(cudaMemcpyAsync(spec + 2L * b0 * nlm, tmp, sizeof(double) * 2 * (long)k * nlm, cudaMemcpyDeviceToHost,
+      GD_CUDA(cudaMemcpyAsync(spec + 2L * b0 * nlm, tmp, sizeof(H) * 2 * (long)k * nlm, cudaMemcpyDeviceToHost,
                               stream));
       GD_CUDA(cudaStreamSynchronize(stream));
     }
     release(tmp);
   }
-  void getvrtdivspec(int nb, const double* u, const double* v, double* vrt, double* div) override {
+  template <typename H>
+  void getvrtdivspec_t(int nb, const H* u, const H* v, H* vrt, H* div) {
     const int ch = std::max(1, std::min(ah.ncol / 2, achunk()));
-    double* tmp = dalloc<double>(2L * ch * nlm);
+    H* tmp = dalloc<H>(2L * ch * nlm);
     const R ai = (R)(1.0 / Phys::rerth);
     for (int b0 = 0; b0 < nb; b0 += ch) {
       int k = std::min(ch, nb - b0);
@@ -1568,11 +1625,11 @@ class Dycore : public DycoreBase {
       // vrt = (AP[0:k] + AH[0:k]) / a, div = (AP[k:2k] + AH[k:2k]) / a
       launch_combine<R>(AP, ldAP, 0, AH, ldAH, 0, AP, ldAP, 0, 2 * k, nlm, ai, stream);
       launch_int2ref<R>(AP, ldAP, 0, k, nlm, tmp, stream);
-      GD_CUDA(cudaMemcpyAsync(vrt + 2L * b0 * nlm, tmp, sizeof(double) * 2 * (long)k * nlm, cudaMemcpyDeviceToHost,
+      GD_CUDA(cudaMemcpyAsync(vrt + 2L * b0 * nlm, tmp, sizeof(H) * 2 * (long)k * nlm, cudaMemcpyDeviceToHost,
                               stream));
       GD_CUDA(cudaStreamSynchronize(stream));
       launch_int2ref<R>(AP, ldAP, k, k, nlm, tmp, stream);
-      GD_CUDA(cudaMemcpyAsync(div + 2L * b0 * nlm, tmp, sizeof(double) * 2 * (long)k * nlm, cudaMemcpyDeviceToHost,
+      GD_CUDA(cudaMemcpyAsync(div + 2L * b0 * nlm, tmp, sizeof(H) * 2 * (long)k * nlm, cudaMemcpyDeviceToHost,
                               stream));
       GD_CUDA(cudaStreamSynchronize(stream));
     }
@@ -1773,6 +1830,22 @@ int gd_set_state(gd_ctx* ctx, const double* vrt, const double* div, const double
 int gd_get_state(gd_ctx* ctx, double* vrt, double* div, double* tv, double* trc, double* lnps) {
   return guarded(ctx, [&] { ctx->d->get_state(vrt, div, tv, trc, lnps); });
 }
+int gd_set_state_f(gd_ctx* ctx, const float* vrt, const float* div, const float* tv, const float* trc,
+                   const float* lnps, const float* topo) {
+  if (!vrt || !div || !tv || !lnps) {
+    if (ctx) ctx->err = "gd_set_state_f: null state array";
+    return GD_ERR_ARG;
+  }
+  return guarded(ctx, [&] {
+    ctx->d->set_state(vrt, div, tv, trc, lnps, topo);
+    const long n2 = (long)(ctx->cfg.ntrunc + 1) * (ctx->cfg.ntrunc + 2);
+    if (topo) ctx->topo.assign(topo, topo + n2);
+    else ctx->topo.assign((size_t)n2, 0.0);
+  });
+}
+int gd_get_state_f(gd_ctx* ctx, float* vrt, float* div, float* tv, float* trc, float* lnps) {
+  return guarded(ctx, [&] { ctx->d->get_state(vrt, div, tv, trc, lnps); });
+}
 int gd_get_topo(gd_ctx* ctx, double* topo) {
   if (!ctx || !ctx->d || !topo) return GD_ERR_ARG;
   const size_t n2 = 2 * (size_t)(ctx->cfg.ntrunc + 1) * (ctx->cfg.ntrunc + 2) / 2;
@@ -1880,6 +1953,26 @@ int gd_getvrtdivspec(gd_ctx* ctx, int nb, const double* u, const double* v, doub
   return guarded(ctx, [&] { ctx->d->getvrtdivspec(nb, u, v, vrt, div); });
 }
 int gd_getgrad(gd_ctx* ctx, int nb, const double* spec, double* gx, double* gy) {
+  if (nb < 0 || (nb > 0 && (!spec || !gx || !gy))) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->getgrad(nb, spec, gx, gy); });
+}
+int gd_spectogrd_f(gd_ctx* ctx, int nb, const float* spec, float* grid) {
+  if (nb < 0 || (nb > 0 && (!spec || !grid))) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->spectogrd(nb, spec, grid); });
+}
+int gd_grdtospec_f(gd_ctx* ctx, int nb, const float* grid, float* spec) {
+  if (nb < 0 || (nb > 0 && (!spec || !grid))) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->grdtospec(nb, grid, spec); });
+}
+int gd_getuv_f(gd_ctx* ctx, int nb, const float* vrt, const float* div, float* u, float* v) {
+  if (nb < 0 || (nb > 0 && (!vrt || !div || !u || !v))) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->getuv(nb, vrt, div, u, v); });
+}
+int gd_getvrtdivspec_f(gd_ctx* ctx, int nb, const float* u, const float* v, float* vrt, float* div) {
+  if (nb < 0 || (nb > 0 && (!vrt || !div || !u || !v))) return GD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->d->getvrtdivspec(nb, u, v, vrt, div); });
+}
+int gd_getgrad_f(gd_ctx* ctx, int nb, const float* spec, float* gx, float* gy) {
   if (nb < 0 || (nb > 0 && (!spec || !gx || !gy))) return GD_ERR_ARG;
   return guarded(ctx, [&] { ctx->d->getgrad(nb, spec, gx, gy); });
 }

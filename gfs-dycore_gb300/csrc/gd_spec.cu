@@ -702,13 +702,32 @@ template void launch_sc<double>(double*, long, const SpecCols&, int, int, const 
 template void launch_sc<float>(float*, long, const SpecCols&, int, int, const float*, float, cudaStream_t);
 
 // ---------------------------------------------------------------- layout --
-template <typename R>
-__global__ void k_ref2int(const double* __restrict__ ref, int nb, int nlm, R* __restrict__ dst, long ld, int col0) {
+// Reference layout H[nb][nlm] complex (H = double, or float for the
+// single-precision host entry points) <-> the internal [nlm][ld] columns.
+template <typename H>
+__device__ __forceinline__ double2 ld_ref(const H* p) {
+  if constexpr (sizeof(H) == 8) {
+    return *reinterpret_cast<const double2*>(p);
+  } else {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    return make_double2((double)v.x, (double)v.y);
+  }
+}
+template <typename H>
+__device__ __forceinline__ void st_ref(H* p, double2 v) {
+  if constexpr (sizeof(H) == 8) {
+    *reinterpret_cast<double2*>(p) = v;
+  } else {
+    *reinterpret_cast<float2*>(p) = make_float2((float)v.x, (float)v.y);
+  }
+}
+template <typename H, typename R>
+__global__ void k_ref2int(const H* __restrict__ ref, int nb, int nlm, R* __restrict__ dst, long ld, int col0) {
   __shared__ double2 tile[32][33];
   const int q0 = blockIdx.x * 32, b0 = blockIdx.y * 32;
   for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
     int b = b0 + yy, q = q0 + threadIdx.x;
-    if (b < nb && q < nlm) tile[yy][threadIdx.x] = reinterpret_cast<const double2*>(ref)[(long)b * nlm + q];
+    if (b < nb && q < nlm) tile[yy][threadIdx.x] = ld_ref<H>(ref + 2 * ((long)b * nlm + q));
   }
   __syncthreads();
   for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
@@ -720,8 +739,8 @@ __global__ void k_ref2int(const double* __restrict__ ref, int nb, int nlm, R* __
     }
   }
 }
-template <typename R>
-__global__ void k_int2ref(const R* __restrict__ src, long ld, int col0, int nb, int nlm, double* __restrict__ ref) {
+template <typename R, typename H>
+__global__ void k_int2ref(const R* __restrict__ src, long ld, int col0, int nb, int nlm, H* __restrict__ ref) {
   __shared__ double2 tile[32][33];
   const int q0 = blockIdx.x * 32, b0 = blockIdx.y * 32;
   for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
@@ -733,29 +752,33 @@ __global__ void k_int2ref(const R* __restrict__ src, long ld, int col0, int nb, 
   __syncthreads();
   for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
     int b = b0 + yy, q = q0 + threadIdx.x;
-    if (b < nb && q < nlm) reinterpret_cast<double2*>(ref)[(long)b * nlm + q] = tile[threadIdx.x][yy];
+    if (b < nb && q < nlm) st_ref<H>(ref + 2 * ((long)b * nlm + q), tile[threadIdx.x][yy]);
   }
 }
-template <typename R>
-void launch_ref2int(const double* ref, int nb, int nlm, R* dst, long ld, int col0, cudaStream_t s) {
+template <typename R, typename H>
+void launch_ref2int(const H* ref, int nb, int nlm, R* dst, long ld, int col0, cudaStream_t s) {
   if (nb <= 0) return;
   dim3 g(ceil_div(nlm, 32), ceil_div(nb, 32)), b(32, 8);
-  k_ref2int<R><<<g, b, 0, s>>>(ref, nb, nlm, dst, ld, col0);
+  k_ref2int<H, R><<<g, b, 0, s>>>(ref, nb, nlm, dst, ld, col0);
   count_launch();
   GD_LAUNCH_CHECK();
 }
-template <typename R>
-void launch_int2ref(const R* src, long ld, int col0, int nb, int nlm, double* ref, cudaStream_t s) {
+template <typename R, typename H>
+void launch_int2ref(const R* src, long ld, int col0, int nb, int nlm, H* ref, cudaStream_t s) {
   if (nb <= 0) return;
   dim3 g(ceil_div(nlm, 32), ceil_div(nb, 32)), b(32, 8);
-  k_int2ref<R><<<g, b, 0, s>>>(src, ld, col0, nb, nlm, ref);
+  k_int2ref<R, H><<<g, b, 0, s>>>(src, ld, col0, nb, nlm, ref);
   count_launch();
   GD_LAUNCH_CHECK();
 }
-template void launch_ref2int<double>(const double*, int, int, double*, long, int, cudaStream_t);
-template void launch_ref2int<float>(const double*, int, int, float*, long, int, cudaStream_t);
-template void launch_int2ref<double>(const double*, long, int, int, int, double*, cudaStream_t);
-template void launch_int2ref<float>(const float*, long, int, int, int, double*, cudaStream_t);
+template void launch_ref2int<double, double>(const double*, int, int, double*, long, int, cudaStream_t);
+template void launch_ref2int<float, double>(const double*, int, int, float*, long, int, cudaStream_t);
+template void launch_ref2int<double, float>(const float*, int, int, double*, long, int, cudaStream_t);
+template void launch_ref2int<float, float>(const float*, int, int, float*, long, int, cudaStream_t);
+template void launch_int2ref<double, double>(const double*, long, int, int, int, double*, cudaStream_t);
+template void launch_int2ref<float, double>(const float*, long, int, int, int, double*, cudaStream_t);
+template void launch_int2ref<double, float>(const double*, long, int, int, int, float*, cudaStream_t);
+template void launch_int2ref<float, float>(const float*, long, int, int, int, float*, cudaStream_t);
 
 template <typename R>
 __global__ void k_combine(const R* X, long ldX, int cx, const R* Y, long ldY, int cy, R* O, long ldO, int co, int nb,

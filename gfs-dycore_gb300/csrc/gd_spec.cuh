@@ -111,11 +111,12 @@ void launch_dfi_set(R* S, long ldS, const SpecCols& sc, int ncs, int nlm, const 
 template <typename R>
 void launch_sc(R* S, long ldS, const SpecCols& sc, int L, int nlm, const R* lapv, R rerth, cudaStream_t s);
 
-// Layout conversion: ref [nb][nlm] complex double <-> internal [nlm][ld] R.
-template <typename R>
-void launch_ref2int(const double* ref, int nb, int nlm, R* dst, long ld, int col0, cudaStream_t s);
-template <typename R>
-void launch_int2ref(const R* src, long ld, int col0, int nb, int nlm, double* ref, cudaStream_t s);
+// Layout conversion: ref [nb][nlm] complex H (double, or float for the
+// single-precision host entry points) <-> internal [nlm][ld] R.
+template <typename R, typename H = double>
+void launch_ref2int(const H* ref, int nb, int nlm, R* dst, long ld, int col0, cudaStream_t s);
+template <typename R, typename H = double>
+void launch_int2ref(const R* src, long ld, int col0, int nb, int nlm, H* ref, cudaStream_t s);
 // out[c] = scale * (X[c] + Y[c]) on [nlm][nb] complex columns
 template <typename R>
 void launch_combine(const R* X, long ldX, int cx, const R* Y, long ldY, int cy, R* O, long ldO, int co, int nb,

@@ -30,6 +30,8 @@ PREC = {"fp64": 0, "fp32": 1, "tf32x3": 2, "bf16x3": 3, "f64_tf32x3": 4, "f64_ed
 
 API_FUNCTIONS = [
     "gd_default_config", "gd_init", "gd_finalize", "gd_set_state", "gd_get_state", "gd_get_topo",
+    "gd_set_state_f", "gd_get_state_f", "gd_spectogrd_f", "gd_grdtospec_f", "gd_getuv_f", "gd_getvrtdivspec_f",
+    "gd_getgrad_f",
     "gd_getdyntend", "gd_getphytend", "gd_advance", "gd_spectogrd", "gd_grdtospec",
     "gd_getuv", "gd_getvrtdivspec", "gd_getgrad", "gd_grid_info", "gd_get_grid", "gd_diag",
     "gd_set_stream", "gd_sync", "gd_launch_count", "gd_last_error", "gd_profile_step",
@@ -89,6 +91,9 @@ def load(build_if_missing=True):
     L.gd_launch_count.argtypes = [vp]
     L.gd_advance.argtypes = [vp, ctypes.c_double, ctypes.c_int]
     L.gd_set_stream.argtypes = [vp, vp]
+    for f in ["gd_set_state_f", "gd_get_state_f", "gd_spectogrd_f", "gd_grdtospec_f", "gd_getuv_f",
+              "gd_getvrtdivspec_f", "gd_getgrad_f"]:
+        getattr(L, f).restype = ctypes.c_int
     for f in ["gd_set_state", "gd_get_state", "gd_get_topo", "gd_getdyntend", "gd_getphytend", "gd_spectogrd",
               "gd_grdtospec", "gd_getuv", "gd_getvrtdivspec", "gd_getgrad", "gd_grid_info",
               "gd_get_grid", "gd_diag", "gd_sync", "gd_profile_step"]:
@@ -216,18 +221,25 @@ class Dycore:
 
     # ---- state ----
     def set_state(self, vrt, div, tv, lnps, trc=None, topo=None):
-        c = lambda a: None if a is None else np.ascontiguousarray(a, np.complex128)
+        """complex64 arrays go through gd_set_state_f (single-precision host
+        layout), anything else through gd_set_state."""
+        f = self._single(vrt)
+        ct = np.complex64 if f else np.complex128
+        c = lambda a: None if a is None else np.ascontiguousarray(a, ct)
         arr = [c(x) for x in (vrt, div, tv, trc, lnps, topo)]
-        self._chk(load().gd_set_state(self.h, *[_p(x) for x in arr]))
+        fn = load().gd_set_state_f if f else load().gd_set_state
+        self._chk(fn(self.h, *[_p(x) for x in arr]))
 
-    def get_state(self):
+    def get_state(self, single=False):
         L, n = self.nlev, self.nlm
-        vrt = np.zeros((L, n), np.complex128)
+        ct = np.complex64 if single else np.complex128
+        vrt = np.zeros((L, n), ct)
         div = np.zeros_like(vrt)
         tv = np.zeros_like(vrt)
-        trc = np.zeros((max(self.ntrac, 1), L, n), np.complex128)
-        lnps = np.zeros(n, np.complex128)
-        self._chk(load().gd_get_state(self.h, _p(vrt), _p(div), _p(tv), _p(trc), _p(lnps)))
+        trc = np.zeros((max(self.ntrac, 1), L, n), ct)
+        lnps = np.zeros(n, ct)
+        fn = load().gd_get_state_f if single else load().gd_get_state
+        self._chk(fn(self.h, _p(vrt), _p(div), _p(tv), _p(trc), _p(lnps)))
         return dict(vrt=vrt, div=div, tv=tv, trc=trc[: self.ntrac], lnps=lnps)
 
     def get_topo(self):
@@ -336,40 +348,59 @@ class Dycore:
         return load().gd_launch_count(self.h)
 
     # ---- transforms ----
-    def _g(self, nb):
-        return np.zeros((nb, self.nlat, self.nlon))
+    # Transforms: complex128 / float64 arrays use the double entry points;
+    # complex64 / float32 arrays the single-precision ones (gd_*_f), which
+    # copy the float arrays as they are and convert on the device.
+    @staticmethod
+    def _single(a):
+        return np.asarray(a).dtype in (np.complex64, np.float32)
+
+    def _g(self, nb, single=False):
+        return np.zeros((nb, self.nlat, self.nlon), np.float32 if single else np.float64)
 
     def spectogrd(self, spec):
-        spec = np.ascontiguousarray(np.atleast_2d(spec), np.complex128)
-        g = self._g(spec.shape[0])
-        self._chk(load().gd_spectogrd(self.h, spec.shape[0], _p(spec), _p(g)))
+        f = self._single(spec)
+        spec = np.ascontiguousarray(np.atleast_2d(spec), np.complex64 if f else np.complex128)
+        g = self._g(spec.shape[0], f)
+        fn = load().gd_spectogrd_f if f else load().gd_spectogrd
+        self._chk(fn(self.h, spec.shape[0], _p(spec), _p(g)))
         return g
 
     def grdtospec(self, grid):
-        grid = np.ascontiguousarray(grid, np.float64).reshape(-1, self.nlat, self.nlon)
-        s = np.zeros((grid.shape[0], self.nlm), np.complex128)
-        self._chk(load().gd_grdtospec(self.h, grid.shape[0], _p(grid), _p(s)))
+        f = self._single(grid)
+        grid = np.ascontiguousarray(grid, np.float32 if f else np.float64).reshape(-1, self.nlat, self.nlon)
+        s = np.zeros((grid.shape[0], self.nlm), np.complex64 if f else np.complex128)
+        fn = load().gd_grdtospec_f if f else load().gd_grdtospec
+        self._chk(fn(self.h, grid.shape[0], _p(grid), _p(s)))
         return s
 
     def getuv(self, vrt, div):
-        vrt = np.ascontiguousarray(np.atleast_2d(vrt), np.complex128)
-        div = np.ascontiguousarray(np.atleast_2d(div), np.complex128)
-        u, v = self._g(vrt.shape[0]), self._g(vrt.shape[0])
-        self._chk(load().gd_getuv(self.h, vrt.shape[0], _p(vrt), _p(div), _p(u), _p(v)))
+        f = self._single(vrt)
+        ct = np.complex64 if f else np.complex128
+        vrt = np.ascontiguousarray(np.atleast_2d(vrt), ct)
+        div = np.ascontiguousarray(np.atleast_2d(div), ct)
+        u, v = self._g(vrt.shape[0], f), self._g(vrt.shape[0], f)
+        fn = load().gd_getuv_f if f else load().gd_getuv
+        self._chk(fn(self.h, vrt.shape[0], _p(vrt), _p(div), _p(u), _p(v)))
         return u, v
 
     def getvrtdivspec(self, u, v):
-        u = np.ascontiguousarray(u, np.float64).reshape(-1, self.nlat, self.nlon)
-        v = np.ascontiguousarray(v, np.float64).reshape(-1, self.nlat, self.nlon)
-        vrt = np.zeros((u.shape[0], self.nlm), np.complex128)
+        f = self._single(u)
+        rt = np.float32 if f else np.float64
+        u = np.ascontiguousarray(u, rt).reshape(-1, self.nlat, self.nlon)
+        v = np.ascontiguousarray(v, rt).reshape(-1, self.nlat, self.nlon)
+        vrt = np.zeros((u.shape[0], self.nlm), np.complex64 if f else np.complex128)
         div = np.zeros_like(vrt)
-        self._chk(load().gd_getvrtdivspec(self.h, u.shape[0], _p(u), _p(v), _p(vrt), _p(div)))
+        fn = load().gd_getvrtdivspec_f if f else load().gd_getvrtdivspec
+        self._chk(fn(self.h, u.shape[0], _p(u), _p(v), _p(vrt), _p(div)))
         return vrt, div
 
     def getgrad(self, spec):
-        spec = np.ascontiguousarray(np.atleast_2d(spec), np.complex128)
-        gx, gy = self._g(spec.shape[0]), self._g(spec.shape[0])
-        self._chk(load().gd_getgrad(self.h, spec.shape[0], _p(spec), _p(gx), _p(gy)))
+        f = self._single(spec)
+        spec = np.ascontiguousarray(np.atleast_2d(spec), np.complex64 if f else np.complex128)
+        gx, gy = self._g(spec.shape[0], f), self._g(spec.shape[0], f)
+        fn = load().gd_getgrad_f if f else load().gd_getgrad
+        self._chk(fn(self.h, spec.shape[0], _p(spec), _p(gx), _p(gy)))
         return gx, gy
 
     def grid_info(self):

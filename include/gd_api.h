@@ -107,6 +107,16 @@ int gd_set_state(gd_ctx* ctx, const double* vrt, const double* div, const double
 int gd_get_state(gd_ctx* ctx, double* vrt, double* div, double* tv, double* trc,
                  double* lnps);
 
+/* gd_set_state / gd_get_state with single-precision host arrays (float
+   _Complex, interleaved re, im floats, same layouts): the spectral state of
+   the reference's default build (complex(r_kind), r_kind = 4,
+   src/kinds.f90:100; spectral_data.f90:11-21), bound without a host-side
+   widening copy.  Conversion to and from the context's state precision
+   runs on the device; topo (may be NULL) is complex(r_kind) too. */
+int gd_set_state_f(gd_ctx* ctx, const float* vrt, const float* div, const float* tv, const float* trc,
+                   const float* lnps, const float* topo);
+int gd_get_state_f(gd_ctx* ctx, float* vrt, float* div, float* tv, float* trc, float* lnps);
+
 /* Reads the orography of the last gd_set_state (complex [nlm], metres; zero
    when it was given as NULL), the reference's topodataspec
    (spectral_data.f90, set at dyn_init.f90:76), so a caller can set a
@@ -172,6 +182,20 @@ int gd_getuv(gd_ctx* ctx, int nb, const double* vrt, const double* div, double* 
 int gd_getvrtdivspec(gd_ctx* ctx, int nb, const double* u, const double* v, double* vrt,
                      double* div);
 int gd_getgrad(gd_ctx* ctx, int nb, const double* spec, double* gx, double* gy);
+
+/* The same five transforms with single-precision host arrays: the
+   reference's default build passes complex(r_kind) / real(r_kind) with
+   r_kind = 4 (src/kinds.f90:100) to the shtns.f90 wrappers, which widen
+   them to double on the host before SHTns (shtns.f90:192-197, 222-229).
+   Here the float arrays are copied as they are and converted on the device
+   (half the bytes over the host link); the arithmetic is the context's
+   precision mode.  Spectral arrays are float _Complex (interleaved re, im
+   floats) [nb][nlm], grids float [nb][nlat][nlon]. */
+int gd_spectogrd_f(gd_ctx* ctx, int nb, const float* spec, float* grid);
+int gd_grdtospec_f(gd_ctx* ctx, int nb, const float* grid, float* spec);
+int gd_getuv_f(gd_ctx* ctx, int nb, const float* vrt, const float* div, float* u, float* v);
+int gd_getvrtdivspec_f(gd_ctx* ctx, int nb, const float* u, const float* v, float* vrt, float* div);
+int gd_getgrad_f(gd_ctx* ctx, int nb, const float* spec, float* gx, float* gy);
 
 /* Module data of src/shtns.f90:58-60: lats (radians, nlat), gauwts (nlat),
    areawts per latitude (nlat; sum over the grid is 1), degree, order (nlm),

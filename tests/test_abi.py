@@ -72,6 +72,15 @@ def test_null_arguments_are_rejected():
     assert lib.gd_mlp_forward(None, None, 0, None) == core.GD_ERR_ARG
     assert lib.gd_mlp_train_step(None, None, None, 1, ctypes.c_float(1e-3), None) == core.GD_ERR_ARG
     assert lib.gd_mlp_init(4, 8, 1, 2, 0, 0, None) == core.GD_ERR_ARG
+    # single-precision host entry points
+    assert lib.gd_set_state_f(None, None, None, None, None, None, None) == core.GD_ERR_ARG
+    assert lib.gd_get_state_f(None, None, None, None, None, None) == core.GD_ERR_ARG
+    for f in ("gd_spectogrd_f", "gd_grdtospec_f"):
+        assert getattr(lib, f)(None, 1, None, None) == core.GD_ERR_ARG
+    assert lib.gd_getuv_f(None, 1, None, None, None, None) == core.GD_ERR_ARG
+    assert lib.gd_getvrtdivspec_f(None, 1, None, None, None, None) == core.GD_ERR_ARG
+    assert lib.gd_getgrad_f(None, 1, None, None, None) == core.GD_ERR_ARG
+    assert lib.gd_get_topo(None, None) == core.GD_ERR_ARG
 
 
 def test_hybrid_coordinate_is_valid():
@@ -80,3 +89,30 @@ def test_hybrid_coordinate_is_valid():
         assert ak[0] == 0 and bk[0] == 0 and bk[-1] == 1 and ak[-1] == 0
         p = ak + bk * 1e5
         assert np.all(np.diff(p) > 0) and np.all(ak >= 0)
+
+
+def test_fortran_module_binds_every_declared_symbol():
+    """include/gd_api.f90 has one bind(c) interface per entry point of
+    include/gd_api.h (no Fortran compiler here: the check is textual)."""
+    f90 = open(os.path.join(ROOT, "include", "gd_api.f90")).read()
+    bound = set(re.findall(r"bind\(c, name='(gd_\w+)'\)", f90))
+    assert bound == declared()
+
+
+def test_shtns_module_has_the_reference_interface():
+    """include/gd_shtns.f90 is module shtns with the public routines and
+    module data of src/shtns.f90:58-60, each transform generic over the
+    single- and double-precision kinds."""
+    f90 = open(os.path.join(ROOT, "include", "gd_shtns.f90")).read()
+    assert re.search(r"^module shtns$", f90, re.M)
+    joined = re.sub(r"&\s*\n\s*", " ", f90)  # Fortran continuation lines
+    public = set()
+    for m in re.finditer(r"^\s*public ::(.*)$", joined, re.M):
+        public |= {w.strip() for w in m.group(1).split(",") if w.strip()}
+    assert public == {"shtns_init", "grdtospec", "spectogrd", "getuv", "getvrtdivspec", "getgrad",
+                      "shtns_destroy", "gauwts", "lats", "lons", "nlm", "degree", "order", "lap", "invlap",
+                      "current_nlon", "current_nlat", "current_ntrunc", "areawts"}
+    for name in ("grdtospec", "spectogrd", "getuv", "getvrtdivspec", "getgrad"):
+        assert re.search(rf"module procedure {name}_r4, {name}_r8", f90), name
+        for k in ("r4", "r8"):
+            assert re.search(rf"subroutine {name}_{k}\(", f90), (name, k)

@@ -1,0 +1,53 @@
+"""Each precision mode's stated error after one simulated day, against the
+plain FP64 GPU step (which the FP64 tests pin to the oracle).
+
+Workload: T62L64 (192x94 grid, 3 tracers, dt 1200 s, 72 steps), the
+balanced-jet state (zonal jet of 35 m/s plus 1 K seeded temperature noise)
+with Held-Suarez forcing.  Errors are max-norm relative per spectral field;
+the measured values (one GB300) are in the comments, the bounds about three
+times them.
+
+  fp64_ulp    the FP64 step from a state moved by one ulp: the floor
+  f64_eddy    FP64 state, zonal means FP64, eddy FFTs FP32, TF32x3 Legendre
+  f64_tf32x3  FP64 state and FFTs, TF32x3 Legendre
+  tf32x3, bf16x3, fp32   FP32 state
+"""
+import os
+
+import pytest
+
+from gdpy import error_study
+
+pytestmark = pytest.mark.gpu
+
+BOUNDS = {
+    # measured after 24 h: vrt 1.5e-12, div 5.0e-11, tv 2.1e-14, lnps 3.7e-16
+    "fp64_ulp": dict(vrt=1e-11, div=3e-10, tv=1e-13, lnps=1e-14),
+    # measured: vrt 1.1e-6, div 3.6e-5, tv 1.5e-8, lnps 6.8e-11
+    "f64_eddy": dict(vrt=3e-6, div=1e-4, tv=5e-8, lnps=3e-10),
+    # measured: vrt 1.0e-6, div 3.2e-5, tv 1.3e-8, lnps 6.0e-11
+    "f64_tf32x3": dict(vrt=3e-6, div=1e-4, tv=5e-8, lnps=3e-10),
+    # measured: vrt 7.9e-4, div 3.3e-2, tv 8.3e-6, lnps 2.7e-7
+    "tf32x3": dict(vrt=3e-3, div=1e-1, tv=3e-5, lnps=1e-6),
+    # measured: vrt 9.3e-4, div 1.7e-2, tv 8.0e-6, lnps 1.9e-7
+    "bf16x3": dict(vrt=3e-3, div=1e-1, tv=3e-5, lnps=1e-6),
+    # measured: vrt 8.9e-4, div 2.2e-2, tv 1.1e-5, lnps 2.5e-7
+    "fp32": dict(vrt=3e-3, div=1e-1, tv=3e-5, lnps=1e-6),
+}
+
+
+def test_one_day_error_bounds_t62l64():
+    with open(os.devnull, "w") as null:
+        res = error_study.run("T62L64", 24.0, list(BOUNDS), checkpoints=[72], seed=0, log=null)
+    errs = res["checkpoints"][-1]["errors"]
+    for mode, bound in BOUNDS.items():
+        got = {k: errs[mode][k]["max_rel"] for k in bound}
+        print(mode, {k: f"{v:.2e}" for k, v in got.items()})
+        for k, b in bound.items():
+            assert got[k] < b, (mode, k, got[k])
+    # the FP64-state modes beat every FP32-state mode by at least 100x in
+    # vorticity and temperature
+    for k in ("vrt", "tv"):
+        worst64 = max(errs[m][k]["max_rel"] for m in ("f64_eddy", "f64_tf32x3"))
+        best32 = min(errs[m][k]["max_rel"] for m in ("tf32x3", "bf16x3", "fp32"))
+        assert worst64 * 100 < best32, k

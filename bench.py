@@ -328,6 +328,11 @@ def gpu_arm(args):
             out["dcmip_simple_physics"] = dcmip_rate(args.precision if args.precision in SIMPLE_PREC else "tf32x3")
         if not args.no_closure:
             out["learned_closure"] = closure_rate("tf32x3")
+        if not args.no_ensemble:
+            # the batching workload: 32 mixed-truncation members with SPPT, stepped one by one and together
+            from gdpy import ensemble
+
+            out["ensemble"] = ensemble.measure(steps=10, warmup=3, precision="tf32x3")
         print(json.dumps(out))
     grp.close()
 
@@ -663,6 +668,7 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=3, help="full CPU steps the reference arm times (>= 3)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the T42L20 / T126L64 days/day rows")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the 32-member ensemble side measurement")
     ap.add_argument("--config-cpu", action="store_true",
                     help="time the CPU rows over the full runs (T42L20 10 days, T126L64 one day)")
     ap.add_argument("--no-dcmip", action="store_true", help="skip the DCMIP simple-physics side measurement")

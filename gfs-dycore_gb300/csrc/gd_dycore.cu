@@ -360,6 +360,7 @@ class Dycore : public DycoreBase {
         // the FP64 tables are the state precision's own; the staging copies
         // take the widest row pitch any synthesis or analysis call uses
         tc_init(*tcp, TC_TF32, T, nh, nlat, ncap, toff, P, H, stream);
+        tcp->sepx = true;
         const long ldmax = std::max(std::max(std::max(ldS, ldAP), std::max(ldAH, ldFP)), std::max(ldGP, ldGH));
         const size_t nfour = (size_t)(T + 1) * nlat * ldmax;
         stSpec = dalloc<float>((size_t)nlm_rows * ldmax);

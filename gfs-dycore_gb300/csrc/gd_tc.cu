@@ -290,6 +290,10 @@ struct TcArgs {
   int* err;
   uint32_t idesc;
   uint32_t tmem_cols;
+  // fused kernel only: accumulate the hi*lo and lo*hi products in their own
+  // TMEM accumulator (single-buffered tiles), so the main accumulator takes
+  // a third of the truncating FP32 accumulation steps
+  int sepx;
 };
 
 template <int KIND>
@@ -764,7 +768,9 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
     bool bad = false;
     for (int idx = blockIdx.x; idx < nitems && !bad; idx += gridDim.x, ++titem) {
       const TcItem t = tc_item(a, idx);
-      const int b = titem & 1, u = titem >> 1;
+      // accumulator buffer b of this item (two, or one when the cross
+      // products have their own accumulator) and its use count u
+      const int b = a.sepx ? 0 : (titem & 1), u = a.sepx ? titem : (titem >> 1);
       if (u >= 1 && !mbar_wait(smem_u32(&tempty[b]), (uint32_t)((u - 1) & 1), a.err, 23)) break;
       tc_fence_after();
       const int total = t.nk0 + t.nk1;
@@ -781,13 +787,26 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
         const uint32_t ah = tbase + acol + 64u * (uint32_t)cs, al = ah + 32u;
         const uint64_t dbh = smem_desc(smem_u32(st)), dbl = smem_desc(smem_u32(st + tab_bytes));
         const uint32_t d = tbase + (uint32_t)(b * 2 * N + acc * N);
+        if (a.sepx) {  // the cross products into their own accumulator, 2N columns on
+          const uint32_t dx = d + 2u * (uint32_t)N;
 #pragma unroll
-        for (int k4 = 0; k4 < 4; ++k4) {  // K = 8 TF32 per MMA: 8 TMEM columns of A, 32 bytes of B
-          const uint64_t o = (uint64_t)(2 * k4);
-          const uint32_t ka = 8u * (uint32_t)k4;
-          mma_tf32_ta(d, ah + ka, dbh + o, a.idesc, (kk > 0 || k4 > 0) ? 1u : 0u);
-          mma_tf32_ta(d, ah + ka, dbl + o, a.idesc, 1u);
-          mma_tf32_ta(d, al + ka, dbh + o, a.idesc, 1u);
+          for (int k4 = 0; k4 < 4; ++k4) {
+            const uint64_t o = (uint64_t)(2 * k4);
+            const uint32_t ka = 8u * (uint32_t)k4;
+            const uint32_t first = (kk > 0 || k4 > 0) ? 1u : 0u;
+            mma_tf32_ta(d, ah + ka, dbh + o, a.idesc, first);
+            mma_tf32_ta(dx, ah + ka, dbl + o, a.idesc, first);
+            mma_tf32_ta(dx, al + ka, dbh + o, a.idesc, 1u);
+          }
+        } else {
+#pragma unroll
+          for (int k4 = 0; k4 < 4; ++k4) {  // K = 8 TF32 per MMA: 8 TMEM columns of A, 32 bytes of B
+            const uint64_t o = (uint64_t)(2 * k4);
+            const uint32_t ka = 8u * (uint32_t)k4;
+            mma_tf32_ta(d, ah + ka, dbh + o, a.idesc, (kk > 0 || k4 > 0) ? 1u : 0u);
+            mma_tf32_ta(d, ah + ka, dbl + o, a.idesc, 1u);
+            mma_tf32_ta(d, al + ka, dbh + o, a.idesc, 1u);
+          }
         }
         mma_commit(smem_u32(&used[s]));
       }
@@ -859,7 +878,7 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
     int titem = 0;
     for (int idx = blockIdx.x; idx < nitems; idx += gridDim.x, ++titem) {
       const TcItem t = tc_item(a, idx);
-      const int b = titem & 1, u = titem >> 1;
+      const int b = a.sepx ? 0 : (titem & 1), u = a.sepx ? titem : (titem >> 1);
       const bool ok = mbar_wait(smem_u32(&tfull[b]), (uint32_t)(u & 1), a.err, 28);
       if (!__all_sync(0xffffffffu, ok)) break;
       tc_fence_after();
@@ -873,6 +892,20 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
         else
 #pragma unroll
           for (int q = 0; q < 16; ++q) o[q] = 0.f;
+        if (a.sepx) {  // add the cross products' accumulator (round to nearest)
+          float xe[16], xo[16];
+          tmem_ld16(tw + 2 * N + g, xe);
+          if (t.nk1 > 0)
+            tmem_ld16(tw + 3 * N + g, xo);
+          else
+#pragma unroll
+            for (int q = 0; q < 16; ++q) xo[q] = 0.f;
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            e[q] += xe[q];
+            o[q] += xo[q];
+          }
+        }
         if (c < a.ncols) {
           if (a.mode == 0) {
 #pragma unroll
@@ -1152,10 +1185,13 @@ static void launch_fused(const TcPlan& p, const CUtensorMap& raw, const CUtensor
   const uint32_t stage = (uint32_t)round_up(2 * args.N * 128 + (int)raw_bytes, 1024);
   const size_t avail = 227 * 1024 - 1024 - 256;
   const int ns = (int)std::min<size_t>(TCF_MAXNS, avail / stage);
-  // TMEM: two E|O accumulator buffers (4N columns) + two A slots (128 columns)
+  // TMEM: two E|O accumulator buffers, or one buffer and the cross products'
+  // E|O accumulator (4N columns either way) + two A slots (128 columns)
   if (ns < 2 || args.N > 96 || args.N % 16) throw std::runtime_error("tc fused gemm: bad tile");
   const size_t sm = (size_t)ns * stage + 1024 + 256;
   args.tmem_cols = 512;
+  // the separate cross accumulator takes the second buffer's 2N columns
+  args.sepx = p.sepx ? 1 : 0;
   static bool attr = false;
   if (!attr) {
     GD_CUDA(cudaFuncSetAttribute(k_tc_gemm_f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
@@ -1178,7 +1214,7 @@ void tc_synth(TcPlan& p, const long* d_moff, bool useH, const float* B, long ldB
       for (int a = 0; a < ct; ++a)
         for (int b2 = 0; b2 < nt; ++b2) it.push_back(make_int4(m, a, b2, 0));
     if (it.empty()) return;
-    TcArgs args;
+    TcArgs args{};
     args.items = cached_items(p, ((long)ncols << 2) | 0, it);
     args.mode = 0;
     args.T = p.T;
@@ -1240,7 +1276,7 @@ void tc_synth(TcPlan& p, const long* d_moff, bool useH, const float* B, long ldB
       for (int b2 = 0; b2 < nt; ++b2) it.push_back(make_int4(m, a, b2, 0));
   if (it.empty()) return;
   int4* dit = cached_items(p, ((long)ncols << 2) | 0, it);
-  TcArgs args;
+  TcArgs args{};
   args.items = dit;
   args.mode = 0;
   args.T = p.T;
@@ -1281,7 +1317,7 @@ void tc_anal(TcPlan& p, const long* d_moff, bool useH, const float* G, long ldG,
         for (int b2 = 0; b2 < (ke + p.nana - 1) / p.nana; ++b2) it.push_back(make_int4(m, a, b2, 0));
     }
     if (it.empty()) return;
-    TcArgs args;
+    TcArgs args{};
     args.items = cached_items(p, ((long)ncols << 2) | 1, it);
     args.mode = 1;
     args.T = p.T;
@@ -1329,7 +1365,7 @@ void tc_anal(TcPlan& p, const long* d_moff, bool useH, const float* G, long ldG,
   }
   if (it.empty()) return;
   int4* dit = cached_items(p, ((long)ncols << 2) | 1, it);
-  TcArgs args;
+  TcArgs args{};
   args.items = dit;
   args.mode = 1;
   args.T = p.T;

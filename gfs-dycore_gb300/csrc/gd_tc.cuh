@@ -24,6 +24,10 @@ struct TcPlan {
   int kirows = 0;   // rows per parity of the analysis tables
   int ncap = 0;     // real-column capacity of the staging buffers
   bool persistent = true;  // persistent warp-specialised GEMM (N <= 128)
+  // fused TF32x3 GEMM: the hi*lo and lo*hi products in their own accumulator
+  // (a third of the truncating accumulation steps in the main one; tiles
+  // single-buffered); set by the FP64-state modes
+  bool sepx = false;
   int nsm = 0;             // SMs of the device (persistent grid size)
   long xlen = 0;    // padded spectral length of the synthesis operand
   std::vector<long> xbase;  // [T+1] start of order m in the padded layout

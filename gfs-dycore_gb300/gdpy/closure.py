@@ -11,9 +11,18 @@ higher truncation (T254L64), spectrally truncated to the coarse one every
 
     target_k = (truth_{k+1} - coarse_forecast_k) / (every_h h)   on the grid,
 
-and the closure adds dt * net(columns) every step.  The plain coarse step is
-the fallback (detach the net) and the yardstick: `climate` compares zonal-mean u
-and T against the coarse-grained truth with and without the net.
+and the closure adds dt * net(columns) every step.  Alternatively
+(target="tendency") the target is the truncation error of the tendencies
+themselves, a deterministic function of the high-resolution state:
+
+    target_k = trunc(tend_hi(truth_hi_k)) - tend_lo(trunc(truth_hi_k))   on the grid,
+
+the dynamics (getdyntend, src/dyn_run.f90:33-305) plus the Held-Suarez
+forcing (getphytend, src/phy_run_hs.f90:22-84) at each resolution, u and v
+tendencies from the vorticity and divergence tendencies through getuv.  The
+plain coarse step is the fallback (detach the net) and the yardstick:
+`climate` compares zonal-mean u and T against the coarse-grained truth with
+and without the net.
 
 Run the experiment on a GPU with
     PYTHONPATH=gfs-dycore_gb300 python -m gdpy.closure --help
@@ -47,9 +56,20 @@ def _ctx(T, L, dt, precision, **kw):
     return core.Dycore(T, nlon, nlat, L, ak, bk, ntrac=0, dt=dt, precision=precision, **kw)
 
 
-def coarse_truth(T_hi, T_lo, L, dt_hi, spin_days, days, every_h, seed=0, precision="tf32x3", log=print):
+def full_tendency(g):
+    """Spectral dynamics + Held-Suarez tendencies (dvrt, ddiv, dtv) of g's
+    current state (getphytend reads the grids of the getdyntend pass)."""
+    d = g.getdyntend(1)
+    p = g.getphytend()
+    return {k: d["d" + k] + p["d" + k] for k in ("vrt", "div", "tv")}
+
+
+def coarse_truth(T_hi, T_lo, L, dt_hi, spin_days, days, every_h, seed=0, precision="tf32x3", log=print,
+                 tendencies=False):
     """Held-Suarez run at T_hi from rest (seeded noise), sampled every `every_h`
-    hours after `spin_days`, each sample truncated to T_lo."""
+    hours after `spin_days`, each sample truncated to T_lo.  With tendencies,
+    each sample also carries the T_hi tendencies of its full state, truncated
+    to T_lo (keys dvrt, ddiv, dtv)."""
     g = _ctx(T_hi, L, dt_hi, precision)
     st = inputs.hs_rest_state(T_hi, L, seed=seed)
     g.set_state(st["vrt"], st["div"], st["tv"], st["lnps"])
@@ -64,7 +84,11 @@ def coarse_truth(T_hi, T_lo, L, dt_hi, spin_days, days, every_h, seed=0, precisi
         if k:
             g.advance(per)
         s = g.get_state()
-        out.append({f: truncate(s[f], T_hi, T_lo) for f in ("vrt", "div", "tv", "lnps")})
+        rec = {f: truncate(s[f], T_hi, T_lo) for f in ("vrt", "div", "tv", "lnps")}
+        if tendencies:
+            td = full_tendency(g)
+            rec.update({"d" + f: truncate(td[f], T_hi, T_lo) for f in ("vrt", "div", "tv")})
+        out.append(rec)
     log(f"truth T{T_hi}L{L}: {spin_days} + {days} days in {time.time() - t0:.1f} s, {len(out)} samples")
     return out
 
@@ -102,6 +126,28 @@ def training_pairs(truth, T_lo, L, dt_lo, every_h, precision="tf32x3", net=None,
         E.append(e)
         Y.append(e / (every_h * 3600.0))
     return np.concatenate(X), np.concatenate(Y), np.concatenate(E)
+
+
+def tendency_pairs(truth, T_lo, L, dt_lo, precision="tf32x3", col_frac=1.0, seed=0):
+    """(X, Y): closure inputs of every coarse-grained sample and the targets
+    trunc(tend_hi) - tend_lo(trunc state) on the coarse grid, columns [ncols,
+    3L] (du/dt, dv/dt, dTv/dt at the levels bottom to top)."""
+    g = _ctx(T_lo, L, dt_lo, precision)
+    rng = np.random.default_rng(seed)
+    X, Y = [], []
+    for s in truth:
+        x = features(g, s)
+        lo = full_tendency(g)
+        dvrt, ddiv, dtv = (s["d" + f] - lo[f] for f in ("vrt", "div", "tv"))
+        du, dv = g.getuv(dvrt, ddiv)
+        dt = g.spectogrd(dtv)
+        y = np.concatenate([a.reshape(L, -1).T for a in (du, dv, dt)], axis=1)
+        if col_frac < 1.0:
+            keep = rng.random(x.shape[0]) < col_frac
+            x, y = x[keep], y[keep]
+        X.append(x)
+        Y.append(y)
+    return np.concatenate(X), np.concatenate(Y)
 
 
 def train(X, Y, nhidden=256, nlayers=3, steps=3000, batch=4096, lr=1e-3, seed=1, device=0, log=print):
@@ -220,13 +266,20 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--precision", default="tf32x3")
+    ap.add_argument("--target", default="error6h", choices=["error6h", "tendency"],
+                    help="error6h: the coarse model's every_h-hour error; tendency: the truncation error of the "
+                         "tendencies")
     ap.add_argument("--out", default=None, help="write the results (JSON) and the trained parameters (.npz) here")
     a = ap.parse_args(argv)
     L = a.nlev
     truth = coarse_truth(a.t_hi, a.t_lo, L, a.dt_hi, a.spin_days, a.train_days + a.eval_days, a.every_h,
-                         precision=a.precision)
+                         precision=a.precision, tendencies=a.target == "tendency")
     ntrain = int(round(a.train_days * 24 / a.every_h))
-    X, Y, E = training_pairs(truth[:ntrain + 1], a.t_lo, L, a.dt_lo, a.every_h, a.precision, col_frac=a.col_frac)
+    if a.target == "tendency":
+        X, Y = tendency_pairs(truth[:ntrain + 1], a.t_lo, L, a.dt_lo, a.precision, col_frac=a.col_frac)
+    else:
+        X, Y, E = training_pairs(truth[:ntrain + 1], a.t_lo, L, a.dt_lo, a.every_h, a.precision,
+                                 col_frac=a.col_frac)
     net, losses = train(X, Y, steps=a.steps, batch=a.batch, lr=a.lr)
     # the first evaluation week: 6-hour errors without and with the closure
     week = truth[ntrain:ntrain + int(round(7 * 24 / a.every_h)) + 1]

@@ -195,6 +195,11 @@ class Dycore : public DycoreBase {
     return c.precision == GD_PREC_TF32X3 || c.precision == GD_PREC_BF16X3 || c.precision == GD_PREC_F64_TF32X3 ||
            c.precision == GD_PREC_F64_EDDY;
   }
+  // K segments of the tensor-core analysis in the FP64-state modes: each
+  // accumulates a quarter of the latitude sum in FP32, the quarters are added
+  // in FP64 (the truncating FP32 accumulation over all 288 latitudes of T574
+  // was the modes' largest error)
+  static constexpr int kAnalSegments = 4;
   // FP32 staging of the FP64-state split modes: spectral side (GEMM operand
   // of the synthesis, result of the analysis) and the Fourier side of the P
   // and H buffers (FPb, FHb)
@@ -293,8 +298,9 @@ class Dycore : public DycoreBase {
         tc_anal(*tcp, moff, useH, stFour(G), ldG, ncr, stSpec, ldA, stream);
         launch_anal<R>(sd, useH, it->second, G, ldG, ncr, A, ldA, side);
         join();
-        launch_convert2d<float, double>(stSpec + (long)(T + 1) * ldA, ldA, A + (long)(T + 1) * ldA, ldA,
-                                        (long)nlm - (T + 1), ncr, stream);
+        // the analysis GEMM's K segments are added here in FP64
+        launch_sumconvert(stSpec + (long)(T + 1) * ldA, ldA, (long)nlm * ldA, tc_anal_segments(*tcp),
+                          A + (long)(T + 1) * ldA, ldA, (long)nlm - (T + 1), ncr, stream);
       }
       return;
     }
@@ -361,12 +367,13 @@ class Dycore : public DycoreBase {
         // take the widest row pitch any synthesis or analysis call uses
         tc_init(*tcp, TC_TF32, T, nh, nlat, ncap, toff, P, H, stream);
         tcp->sepx = true;
+        tcp->aseg = kAnalSegments;
         const long ldmax = std::max(std::max(std::max(ldS, ldAP), std::max(ldAH, ldFP)), std::max(ldGP, ldGH));
         const size_t nfour = (size_t)(T + 1) * nlat * ldmax;
-        stSpec = dalloc<float>((size_t)nlm_rows * ldmax);
+        stSpec = dalloc<float>((size_t)tc_anal_segments(*tcp) * nlm_rows * ldmax);
         stFourP = dalloc<float>(nfour);
         stFourH = dalloc<float>(nfour);
-        GD_CUDA(cudaMemsetAsync(stSpec, 0, sizeof(float) * nlm_rows * ldmax, stream));
+        GD_CUDA(cudaMemsetAsync(stSpec, 0, sizeof(float) * tc_anal_segments(*tcp) * nlm_rows * ldmax, stream));
         GD_CUDA(cudaMemsetAsync(stFourP, 0, sizeof(float) * nfour, stream));
         GD_CUDA(cudaMemsetAsync(stFourH, 0, sizeof(float) * nfour, stream));
       }

@@ -36,6 +36,9 @@ void launch_convert(const double* src, R* dst, long n, cudaStream_t s);
 // strided 2-D copy with a type change (rows x cols, row pitches lds / ldd)
 template <typename S, typename D>
 void launch_convert2d(const S* src, long lds, D* dst, long ldd, long rows, int cols, cudaStream_t s);
+// dst[r][c] = sum_q src[q seg_stride + r lds + c] (q < nseg, FP64 sum in order q)
+void launch_sumconvert(const float* src, long lds, long seg_stride, int nseg, double* dst, long ldd, long rows,
+                       int cols, cudaStream_t s);
 
 // Legendre stage, per-order SIMT GEMMs with the even/odd split.
 // synthesis: F[m][j][c] = sum_{n} T[m][j][n-m] B[idx(n,m)][c]   (real columns)

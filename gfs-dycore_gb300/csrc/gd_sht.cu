@@ -156,6 +156,30 @@ void launch_convert2d(const S* src, long lds, D* dst, long ldd, long rows, int c
 template void launch_convert2d<double, float>(const double*, long, float*, long, long, int, cudaStream_t);
 template void launch_convert2d<float, double>(const float*, long, double*, long, long, int, cudaStream_t);
 
+// dst[r][c] = sum over q < nseg of src[q seg_stride + r lds + c], summed in
+// FP64 in the order q = 0, 1, ...: the K-segmented tensor-core analysis's
+// partial sums of the FP64-state modes
+__global__ void k_sumconvert(const float* __restrict__ src, long lds, long seg_stride, int nseg,
+                             double* __restrict__ dst, long ldd, long rows, int cols) {
+  const long n = rows * cols;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const long r = i / cols;
+    const int c = (int)(i - r * cols);
+    const float* p = src + r * lds + c;
+    double v = 0.0;
+    for (int q = 0; q < nseg; ++q) v += (double)p[q * seg_stride];
+    dst[r * ldd + c] = v;
+  }
+}
+void launch_sumconvert(const float* src, long lds, long seg_stride, int nseg, double* dst, long ldd, long rows,
+                       int cols, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return;
+  int blocks = (int)std::min<long>(ceil_div(rows * cols, 256), 152L * 16);
+  k_sumconvert<<<blocks, 256, 0, s>>>(src, lds, seg_stride, nseg, dst, ldd, rows, cols);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+
 // --------------------------------------------------------- Legendre GEMMs --
 // Tiles: synthesis 32 latitude pairs x 64 real columns, analysis 32 degrees
 // x 64 real columns; 256 threads, each 2 rows x 4 columns (columns strided

@@ -294,6 +294,10 @@ struct TcArgs {
   // TMEM accumulator (single-buffered tiles), so the main accumulator takes
   // a third of the truncating FP32 accumulation steps
   int sepx;
+  // analysis only: the latitude (K) range split into nseg segments, item.w
+  // the segment; segment q writes its FP32 partial sums at out + q * seg_stride
+  int nseg;
+  long seg_stride;
 };
 
 template <int KIND>
@@ -457,6 +461,7 @@ constexpr int TCP_THREADS = 192;
 struct TcItem {
   int m, c0, n0, nk0, nk1, kp, K;
   long xb;
+  int kb, seg;  // first K chunk of both parities, K segment (analysis with nseg > 1)
 };
 __device__ __forceinline__ TcItem tc_item(const TcArgs& a, int idx) {
   const int4 it = a.items[idx];
@@ -475,6 +480,14 @@ __device__ __forceinline__ TcItem tc_item(const TcArgs& a, int idx) {
     t.kp = 0;
     t.nk0 = t.nk1 = (a.nh + a.kc - 1) / a.kc;
     t.xb = 0;
+  }
+  t.kb = 0;
+  t.seg = 0;
+  if (a.mode == 1 && a.nseg > 1) {  // segment it.w of the latitude chunks (nseg <= chunks)
+    const int nk = t.nk0;
+    t.seg = it.w;
+    t.kb = t.seg * nk / a.nseg;
+    t.nk0 = t.nk1 = (t.seg + 1) * nk / a.nseg - t.kb;
   }
   return t;
 }
@@ -737,7 +750,7 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
           bad = true;
           break;
         }
-        const int acc = (i < t.nk0) ? 0 : 1, kk = acc ? i - t.nk0 : i;
+        const int acc = (i < t.nk0) ? 0 : 1, kk = t.kb + (acc ? i - t.nk0 : i);
         unsigned char* st = sm + (size_t)s * stage_bytes;
         const uint32_t fb = smem_u32(&full[s]);
         mbar_expect_tx(fb, 2 * tab_bytes + raw_bytes);
@@ -782,7 +795,7 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
           break;
         }
         tc_fence_after();
-        const int acc = (i < t.nk0) ? 0 : 1, kk = acc ? i - t.nk0 : i;
+        const int acc = (i < t.nk0) ? 0 : 1, kk = t.kb + (acc ? i - t.nk0 : i);
         unsigned char* st = sm + (size_t)s * stage_bytes;
         const uint32_t ah = tbase + acol + 64u * (uint32_t)cs, al = ah + 32u;
         const uint64_t dbh = smem_desc(smem_u32(st)), dbl = smem_desc(smem_u32(st + tab_bytes));
@@ -793,7 +806,7 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
           for (int k4 = 0; k4 < 4; ++k4) {
             const uint64_t o = (uint64_t)(2 * k4);
             const uint32_t ka = 8u * (uint32_t)k4;
-            const uint32_t first = (kk > 0 || k4 > 0) ? 1u : 0u;
+            const uint32_t first = (kk > t.kb || k4 > 0) ? 1u : 0u;  // a segment starts afresh
             mma_tf32_ta(d, ah + ka, dbh + o, a.idesc, first);
             mma_tf32_ta(dx, ah + ka, dbl + o, a.idesc, first);
             mma_tf32_ta(dx, al + ka, dbh + o, a.idesc, 1u);
@@ -803,7 +816,7 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
           for (int k4 = 0; k4 < 4; ++k4) {  // K = 8 TF32 per MMA: 8 TMEM columns of A, 32 bytes of B
             const uint64_t o = (uint64_t)(2 * k4);
             const uint32_t ka = 8u * (uint32_t)k4;
-            mma_tf32_ta(d, ah + ka, dbh + o, a.idesc, (kk > 0 || k4 > 0) ? 1u : 0u);
+            mma_tf32_ta(d, ah + ka, dbh + o, a.idesc, (kk > t.kb || k4 > 0) ? 1u : 0u);
             mma_tf32_ta(d, ah + ka, dbl + o, a.idesc, 1u);
             mma_tf32_ta(d, al + ka, dbh + o, a.idesc, 1u);
           }
@@ -830,7 +843,7 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
           bad = true;
           break;
         }
-        const int acc = (i < t.nk0) ? 0 : 1, kk = acc ? i - t.nk0 : i;
+        const int acc = (i < t.nk0) ? 0 : 1, kk = t.kb + (acc ? i - t.nk0 : i);
         const float* raw = reinterpret_cast<const float*>(sm + (size_t)s * stage_bytes + raw_off);
         int nv;  // valid K entries of this chunk: ii < nv
         bool plus = true;
@@ -918,11 +931,12 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
             }
           } else {
             const long base = a.moff[t.m];
+            float* const out = a.out + (long)t.seg * a.seg_stride;
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               const int qe = 2 * (t.n0 + g + q), qo = qe + 1;
-              if (qe < t.K) a.out[(base + qe) * a.ldout + c] = e[q];
-              if (qo < t.K) a.out[(base + qo) * a.ldout + c] = o[q];
+              if (qe < t.K) out[(base + qe) * a.ldout + c] = e[q];
+              if (qo < t.K) out[(base + qo) * a.ldout + c] = o[q];
             }
           }
         }
@@ -1305,20 +1319,28 @@ void tc_synth(TcPlan& p, const long* d_moff, bool useH, const float* B, long ldB
                          (int)it.size(), s);
 }
 
+int tc_anal_segments(const TcPlan& p) {  // K segments of the latitude sum: at most one per chunk
+  return std::max(1, std::min(p.aseg, (p.nh + p.kc - 1) / p.kc));
+}
+
 void tc_anal(TcPlan& p, const long* d_moff, bool useH, const float* G, long ldG, int ncols, float* A, long ldA,
              cudaStream_t s) {
   if (ncols > p.ncap) throw std::runtime_error("tc_anal: too many columns");
   if (fused_ok(p, G, ldG)) {
     const int ct = (ncols + TC_M - 1) / TC_M;
     std::vector<int4> it;
+    const int nseg = tc_anal_segments(p);
     for (int m = 1; m <= p.T; ++m) {  // order 0 runs on the IEEE SIMT path
       const int ke = (p.T - m + 2) / 2;
       for (int a = 0; a < ct; ++a)
-        for (int b2 = 0; b2 < (ke + p.nana - 1) / p.nana; ++b2) it.push_back(make_int4(m, a, b2, 0));
+        for (int b2 = 0; b2 < (ke + p.nana - 1) / p.nana; ++b2)
+          for (int q = 0; q < nseg; ++q) it.push_back(make_int4(m, a, b2, q));
     }
     if (it.empty()) return;
     TcArgs args{};
-    args.items = cached_items(p, ((long)ncols << 2) | 1, it);
+    args.items = cached_items(p, ((long)ncols << 8) | ((long)nseg << 2) | 1, it);
+    args.nseg = nseg;
+    args.seg_stride = (long)(p.T + 1) * (p.T + 2) / 2 * ldA;
     args.mode = 1;
     args.T = p.T;
     args.nh = p.nh;

@@ -28,6 +28,10 @@ struct TcPlan {
   // (a third of the truncating accumulation steps in the main one; tiles
   // single-buffered); set by the FP64-state modes
   bool sepx = false;
+  // fused TF32x3 analysis: the latitude sum in aseg segments, each written as
+  // FP32 partial sums to its own copy of the output (nlm x ldA floats apart),
+  // to be added in the caller's precision; set by the FP64-state modes
+  int aseg = 1;
   int nsm = 0;             // SMs of the device (persistent grid size)
   long xlen = 0;    // padded spectral length of the synthesis operand
   std::vector<long> xbase;  // [T+1] start of order m in the padded layout
@@ -65,6 +69,8 @@ void tc_synth(TcPlan& p, const long* d_moff, bool useH, const float* B, long ldB
 // A[idx][c] = Legendre analysis of G[m][j][c] (real columns [0, ncols)).
 void tc_anal(TcPlan& p, const long* d_moff, bool useH, const float* G, long ldG, int ncols, float* A, long ldA,
              cudaStream_t s);
+// the K segments tc_anal uses (the plan's aseg, at most one per latitude chunk)
+int tc_anal_segments(const TcPlan& p);
 // returns and clears the device error flag (nonzero: a bounded wait gave up)
 int tc_check(TcPlan& p, cudaStream_t s);
 

@@ -73,6 +73,33 @@ def test_gradient_matches_oracle():
             o += sz
 
 
+def test_closure_shape_gradient_matches_oracle():
+    # the configured closure net (193 -> 256 x 3 -> 192): loss and every
+    # layer's weight and bias gradients of the library's backward kernels
+    # against the float64 oracle, on 512 columns
+    import mlp_oracle as mo
+    from gdpy import core
+
+    nin, nh, nl, nout = 193, 256, 3, 192
+    net = core.Mlp(nin, nh, nl, nout, seed=12)
+    rng = np.random.default_rng(12)
+    shp = mo.shapes(nin, nh, nl, nout)
+    p = np.concatenate([np.concatenate([rng.standard_normal(fo * fi) * np.sqrt(2.0 / fi),
+                                        rng.standard_normal(fo) * 0.1]) for fo, fi in shp]).astype(np.float32)
+    net.set_params(p)
+    x = rng.standard_normal((512, nin)).astype(np.float32)
+    t = rng.standard_normal((512, nout)).astype(np.float32)
+    loss, g = net.loss_grad(torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda())
+    lo, go = mo.loss_grad(p, shp, x, t)
+    assert abs(loss - lo) <= 1e-5 * lo
+    o = 0
+    for fo, fi in shp:
+        for sz in (fo * fi, fo):
+            assert rel(g[o:o + sz], go[o:o + sz]) < 1e-4, (fo, fi, sz)
+            o += sz
+    assert o == net.nparams
+
+
 def test_training_fits_a_smooth_map():
     from gdpy import core
 

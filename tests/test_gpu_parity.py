@@ -238,7 +238,7 @@ def test_transforms_split(oracle_mod, T, prec):
     assert rel(gx, ox) < tol and rel(gy, oy) < tol
 
 
-@pytest.mark.parametrize("prec", ["tf32x3", "bf16x3"])
+@pytest.mark.parametrize("prec", ["tf32x3", "bf16x3", "f64_eddy"])
 def test_transforms_split_t574(oracle_mod, prec):
     T, nlon, nlat = 574, 1152, 576
     ak, bk = inputs.hybrid_coords(4)
@@ -248,8 +248,8 @@ def test_transforms_split_t574(oracle_mod, prec):
     # vector analysis, 3.7e-4: its 16-bit operands (hi + lo, no lo*lo product)
     # lose ~2^-17 per product, and the curl/divergence postscale n(n+1)/a
     # weights the high degrees of T574 where u and v cancel most
-    tol = {"tf32x3": 1e-5, "bf16x3": 2e-5}[prec]
-    vec_tol = {"tf32x3": 1e-5, "bf16x3": 1e-3}[prec]
+    tol = {"tf32x3": 1e-5, "bf16x3": 2e-5, "f64_eddy": 1e-5}[prec]
+    vec_tol = {"tf32x3": 1e-5, "bf16x3": 1e-3, "f64_eddy": 1e-5}[prec]
     a = rand_spec(T, 2, seed=5, slope=-1.0)
     b = rand_spec(T, 2, seed=6, slope=-1.0)
     e = {}

@@ -258,8 +258,10 @@ def gpu_arm(args):
     wc = work_counts(T, nlon, nlat, L, nt, rsize)
     dom = max(phases, key=phases.get)
     leg_ms = phases["legendre_synth"] + phases["legendre_anal"]
-    if args.precision in ("tf32x3", "bf16x3") and (dom in ("legendre_synth", "legendre_anal")
-                                                  or leg_ms >= max(phases.values())):
+    if args.precision in ("tf32x3", "bf16x3", "f64_tf32x3", "f64_eddy") and \
+            (dom in ("legendre_synth", "legendre_anal") or leg_ms >= max(phases.values())):
+        if args.precision.startswith("f64"):  # the GEMM runs on FP32 staging copies of the FP64 operands
+            wc = work_counts(T, nlon, nlat, L, nt, 4)
         # The split-precision Legendre GEMM issues 3 products per algorithmic one: 6 flop per
         # (coefficient, latitude pair) against ~4 bytes of array traffic per coefficient and column, an
         # intensity (~140 flop/B at T574 with the tables) below this GPU's tensor balance point: the HBM

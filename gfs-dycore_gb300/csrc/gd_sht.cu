@@ -134,21 +134,36 @@ template void launch_convert<float>(const double*, float*, long, cudaStream_t);
 
 // dst[r][c] = src[r][c] for r < rows, c < cols (row pitches lds, ldd), with
 // the type change round-to-nearest; the staging copies of the FP64-state
-// split-precision mode around the FP32 tensor-core Legendre GEMMs
+// split-precision modes around the FP32 tensor-core Legendre GEMMs.  Rows
+// hold real/imaginary pairs (even cols and pitches, pair-aligned bases), so
+// each thread moves whole pairs; a CTA walks rows with a stride over the grid.
+constexpr int kConvChunk = 1024;  // pairs per tile of the staging conversions
 template <typename S, typename D>
-__global__ void k_convert2d(const S* __restrict__ src, long lds, D* __restrict__ dst, long ldd, long rows,
-                            int cols) {
-  const long n = rows * cols;
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const long r = i / cols;
-    const int c = (int)(i - r * cols);
-    dst[r * ldd + c] = (D)src[r * lds + c];
+__global__ void __launch_bounds__(256) k_convert2d(const S* __restrict__ src, long lds, D* __restrict__ dst,
+                                                   long ldd, long rows, int cols) {
+  typedef typename C2<S>::T VS;
+  typedef typename C2<D>::T VD;
+  const int np = cols >> 1, nchunk = (np + kConvChunk - 1) / kConvChunk;
+  for (long t = blockIdx.x; t < rows * nchunk; t += gridDim.x) {  // tiles of (row, chunk of kConvChunk pairs)
+    const long r = t / nchunk;
+    const int q0 = (int)(t - r * nchunk) * kConvChunk, q1 = min(np, q0 + kConvChunk);
+    const VS* sp = reinterpret_cast<const VS*>(src + r * lds);
+    VD* dp = reinterpret_cast<VD*>(dst + r * ldd);
+    for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+      const VS v = sp[q];
+      VD w;
+      w.x = (D)v.x;
+      w.y = (D)v.y;
+      dp[q] = w;
+    }
   }
 }
 template <typename S, typename D>
 void launch_convert2d(const S* src, long lds, D* dst, long ldd, long rows, int cols, cudaStream_t s) {
   if (rows <= 0 || cols <= 0) return;
-  int blocks = (int)std::min<long>(ceil_div(rows * cols, 256), 152L * 16);
+  if ((cols | lds | ldd) & 1) throw CudaError("launch_convert2d: columns and pitches must be even");
+  const long tiles = rows * (((cols >> 1) + kConvChunk - 1) / kConvChunk);
+  const int blocks = (int)std::min<long>(tiles, 152L * 32);
   k_convert2d<S, D><<<blocks, 256, 0, s>>>(src, lds, dst, ldd, rows, cols);
   count_launch();
   GD_LAUNCH_CHECK();
@@ -158,23 +173,33 @@ template void launch_convert2d<float, double>(const float*, long, double*, long,
 
 // dst[r][c] = sum over q < nseg of src[q seg_stride + r lds + c], summed in
 // FP64 in the order q = 0, 1, ...: the K-segmented tensor-core analysis's
-// partial sums of the FP64-state modes
-__global__ void k_sumconvert(const float* __restrict__ src, long lds, long seg_stride, int nseg,
-                             double* __restrict__ dst, long ldd, long rows, int cols) {
-  const long n = rows * cols;
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const long r = i / cols;
-    const int c = (int)(i - r * cols);
-    const float* p = src + r * lds + c;
-    double v = 0.0;
-    for (int q = 0; q < nseg; ++q) v += (double)p[q * seg_stride];
-    dst[r * ldd + c] = v;
+// partial sums of the FP64-state modes (pairs per thread, rows per CTA)
+__global__ void __launch_bounds__(256) k_sumconvert(const float* __restrict__ src, long lds, long seg_stride,
+                                                    int nseg, double* __restrict__ dst, long ldd, long rows,
+                                                    int cols) {
+  const int np = cols >> 1, nchunk = (np + kConvChunk - 1) / kConvChunk;
+  for (long t = blockIdx.x; t < rows * nchunk; t += gridDim.x) {
+    const long r = t / nchunk;
+    const int q0 = (int)(t - r * nchunk) * kConvChunk, q1 = min(np, q0 + kConvChunk);
+    const float* sp = src + r * lds;
+    double2* dp = reinterpret_cast<double2*>(dst + r * ldd);
+    for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+      double2 v = make_double2(0.0, 0.0);
+      for (int k = 0; k < nseg; ++k) {
+        const float2 f = reinterpret_cast<const float2*>(sp + k * seg_stride)[q];
+        v.x += (double)f.x;
+        v.y += (double)f.y;
+      }
+      dp[q] = v;
+    }
   }
 }
 void launch_sumconvert(const float* src, long lds, long seg_stride, int nseg, double* dst, long ldd, long rows,
                        int cols, cudaStream_t s) {
   if (rows <= 0 || cols <= 0) return;
-  int blocks = (int)std::min<long>(ceil_div(rows * cols, 256), 152L * 16);
+  if ((cols | lds | ldd | seg_stride) & 1) throw CudaError("launch_sumconvert: columns and pitches must be even");
+  const long tiles = rows * (((cols >> 1) + kConvChunk - 1) / kConvChunk);
+  const int blocks = (int)std::min<long>(tiles, 152L * 32);
   k_sumconvert<<<blocks, 256, 0, s>>>(src, lds, seg_stride, nseg, dst, ldd, rows, cols);
   count_launch();
   GD_LAUNCH_CHECK();

@@ -377,3 +377,48 @@ def test_steps_f64_split(oracle_mod, prec):
     e = {k: rel(a[k], b[k]) for k in ("vrt", "div", "tv", "lnps")}
     print(f"T42L20 2 steps {prec}", {k: f"{v:.2e}" for k, v in e.items()})
     assert e["tv"] < 1e-5 and e["lnps"] < 2e-6 and e["vrt"] < 2e-3
+
+
+_UNFUSED_SCRIPT = r"""
+import sys
+import numpy as np
+from gdpy import core, inputs
+sys.path.insert(0, sys.argv[2])
+from helpers import rand_spec
+T, nlon, nlat = 126, 384, 190
+ak, bk = inputs.hybrid_coords(4)
+g = core.Dycore(T, nlon, nlat, 4, ak, bk, precision="tf32x3")
+a = rand_spec(T, 5, seed=41, slope=-1.0)
+b = rand_spec(T, 5, seed=42, slope=-1.0)
+grid = g.spectogrd(a)
+u, v = g.getuv(a, b)
+vr, dv = g.getvrtdivspec(u, v)
+np.savez(sys.argv[1], grid=grid, spec=g.grdtospec(grid), u=u, v=v, vr=vr, dv=dv)
+"""
+
+
+def test_fused_gemm_matches_unfused_bitwise(tmp_path):
+    """The fused TF32x3 GEMM (raw tiles split by converter warps straight
+    into tensor memory) against the unfused one (hi/lo arrays from the split
+    kernels, staged in shared memory by TMA): the same split and the same
+    products in the same order, so bit for bit the same transforms.  The
+    unfused run is a child process with GD_TC_FUSED=0."""
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, GD_TC_FUSED="0")
+    env["PYTHONPATH"] = os.pathsep.join([os.path.join(root, "gfs-dycore_gb300"), env.get("PYTHONPATH", "")])
+    out_u = str(tmp_path / "unfused.npz")
+    r = subprocess.run([sys.executable, "-c", _UNFUSED_SCRIPT, out_u, os.path.join(root, "tests")], env=env,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out_f = str(tmp_path / "fused.npz")
+    env.pop("GD_TC_FUSED")
+    r = subprocess.run([sys.executable, "-c", _UNFUSED_SCRIPT, out_f, os.path.join(root, "tests")], env=env,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    zu, zf = np.load(out_u), np.load(out_f)
+    for k in zu.files:
+        np.testing.assert_array_equal(zf[k], zu[k], err_msg=k)

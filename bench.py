@@ -190,8 +190,12 @@ def gpu_arm(args):
         ms = grp.max_over_ranks(e0.elapsed_time(e1))
         return ms, g.launch_count() - n0, ck.summary()
 
-    # fast-precision step (the headline)
+    # fast-precision step (the headline), its tile shapes chosen by the library's autotuner on this context
     g = ctx(args.precision)
+    tuned = None
+    if not args.no_autotune:
+        tuned = g.autotune()
+        g.set_state(st["vrt"], st["div"], st["tv"], st["lnps"], trc=trc)
     ms, launches, clocks = timed(g, args.steps, args.warmup)
     ms_step = ms / args.steps
     # simulated seconds per wall second == simulated days per day, summed over ranks
@@ -307,7 +311,7 @@ def gpu_arm(args):
         "scaling": "weak", "vs_baseline": None, "dtype": DTYPES[args.precision],
         "data": "synthetic (seeded balanced jet, Held-Suarez forcing)",
         "config": {"workload": name, "ntrunc": T, "grid": f"{nlon}x{nlat}", "nlev": L, "ntrac": nt, "dt_s": dt,
-                   "precision": args.precision, "parallelism": f"replicas x{world}",
+                   "precision": args.precision, "parallelism": f"replicas x{world}", "autotune": tuned,
                    "l2": "inputs larger than L2 (resident state and grids are GBs)"},
         "precision_modes": modes, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
         "phases_ms": phases, "clocks": clocks,
@@ -675,6 +679,8 @@ def main():
                     help="time the CPU rows over the full runs (T42L20 10 days, T126L64 one day)")
     ap.add_argument("--no-dcmip", action="store_true", help="skip the DCMIP simple-physics side measurement")
     ap.add_argument("--no-closure", action="store_true", help="skip the learned-closure side measurement")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="step the headline context with the default tile shapes instead of the autotuner's")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gd":
         args.warmup = 3

@@ -10,6 +10,8 @@
 #include <algorithm>
 #include <atomic>
 #include <functional>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -195,11 +197,19 @@ class Dycore : public DycoreBase {
     return c.precision == GD_PREC_TF32X3 || c.precision == GD_PREC_BF16X3 || c.precision == GD_PREC_F64_TF32X3 ||
            c.precision == GD_PREC_F64_EDDY;
   }
-  // K segments of the tensor-core analysis in the FP64-state modes: each
-  // accumulates a quarter of the latitude sum in FP32, the quarters are added
-  // in FP64 (the truncating FP32 accumulation over all 288 latitudes of T574
-  // was the modes' largest error)
+  // K segments of the tensor-core GEMMs in the FP64-state modes (the
+  // truncating FP32 accumulation in tensor memory over all 288 degrees or
+  // latitudes of T574 was the modes' largest error): segments of
+  // kFoldChunks K chunks, each accumulated afresh and folded in FP32 (round
+  // to nearest) by the GEMM's epilogue.  Without folding (GD_TC_FOLD_CHUNKS=0)
+  // the analysis' latitude sum goes in kAnalSegments segments to global
+  // memory, added in FP64.  Both are read from the environment at init.
+  static constexpr int kFoldChunks = 1;
   static constexpr int kAnalSegments = 4;
+  static int env_int(const char* name, int dflt) {
+    const char* e = getenv(name);
+    return (e && *e) ? atoi(e) : dflt;
+  }
   // FP32 staging of the FP64-state split modes: spectral side (GEMM operand
   // of the synthesis, result of the analysis) and the Fourier side of the P
   // and H buffers (FPb, FHb)
@@ -365,9 +375,10 @@ class Dycore : public DycoreBase {
       } else {
         // the FP64 tables are the state precision's own; the staging copies
         // take the widest row pitch any synthesis or analysis call uses
+        tcp->sepx = true;  // these choose the N tiles: set before tc_init
+        tcp->cps = std::max(0, env_int("GD_TC_FOLD_CHUNKS", kFoldChunks));
+        tcp->aseg = std::max(1, env_int("GD_TC_ANAL_SEGMENTS", tcp->cps > 0 ? 1 : kAnalSegments));
         tc_init(*tcp, TC_TF32, T, nh, nlat, ncap, toff, P, H, stream);
-        tcp->sepx = true;
-        tcp->aseg = kAnalSegments;
         const long ldmax = std::max(std::max(std::max(ldS, ldAP), std::max(ldAH, ldFP)), std::max(ldGP, ldGH));
         const size_t nfour = (size_t)(T + 1) * nlat * ldmax;
         stSpec = dalloc<float>((size_t)tc_anal_segments(*tcp) * nlm_rows * ldmax);
@@ -986,10 +997,13 @@ class Dycore : public DycoreBase {
     }
     if (closure) closure_pass();
   }
-  // Autotuning: the synthesis GEMM's latitude tile (split modes) and the
-  // column kernel's levels per warp, each chosen by timing its candidates on
-  // this context's own buffers (the transform rows of the current state).
-  // The choices hold for the context's later steps.
+  // Autotuning: the column kernel's levels per warp, and (split modes) the
+  // synthesis GEMM's latitude tile together with the tensor-memory A slots of
+  // both GEMMs, each chosen by timing its candidates on this context's own
+  // buffers (the transform rows of the current state; a tile and slot count
+  // by one synthesis and one analysis of the step).  The choices hold for the
+  // context's later steps.  GD_AUTOTUNE_VERBOSE=1 prints every candidate's
+  // time to stderr.
   int col_lb = 0;
   void autotune(int* out) override {
     if (!state_set) throw std::runtime_error("state not set (gd_set_state)");
@@ -1019,19 +1033,32 @@ class Dycore : public DycoreBase {
     if (tcp) {
       std::vector<int> tiles;
       for (int cap : {48, 64, 80, 96}) {
+        if (cap > tc_max_n(*tcp)) continue;  // beyond the GEMM kernel's TMEM budget
         const int n = tc_tile_n(nh, cap);
         if (std::find(tiles.begin(), tiles.end(), n) == tiles.end()) tiles.push_back(n);
       }
+      const bool verbose = env_int("GD_AUTOTUNE_VERBOSE", 0) != 0;
       best = 1e30f;
-      int bn = tcp->nsyn;
-      for (int n : tiles) {
-        tc_set_nsyn(*tcp, n);
-        const float ms = timed([&] {
-          do_synth(false, synP, S, ldS, 2 * sc.ncol, FPb, ldFP);
-          do_synth(true, synH, S + 2 * (2 * L), ldS, 2 * (sc.ncol - 2 * L), FHb, ldFH);
-        });
-        if (ms < best) best = ms, bn = n;
+      int bn = tcp->nsyn, bs = tcp->aslots;
+      for (int na : {2, 3, 4}) {
+        tcp->aslots = na;
+        for (int n : tiles) {
+          // a count that fits neither GEMM's tile is a candidate already timed
+          if (na > 2 && tc_slots(*tcp, n) < na && tc_slots(*tcp, tcp->nana) < na) continue;
+          tc_set_nsyn(*tcp, n);
+          const float ms = timed([&] {
+            do_synth(false, synP, S, ldS, 2 * sc.ncol, FPb, ldFP);
+            do_synth(true, synH, S + 2 * (2 * L), ldS, 2 * (sc.ncol - 2 * L), FHb, ldFH);
+            do_anal(false, anaP, FPb, ldGP, 2 * ap.ncol, AP, ldAP);
+            do_anal(true, anaH, FHb, ldGH, 2 * ah.ncol, AH, ldAH);
+          });
+          if (verbose)
+            fprintf(stderr, "autotune: synthesis tile %d, A slots %d/%d (synthesis/analysis): %.3f ms\n", n,
+                    tc_slots(*tcp, n), tc_slots(*tcp, tcp->nana), ms / 3);
+          if (ms < best) best = ms, bn = n, bs = na;
+        }
       }
+      tcp->aslots = bs;
       tc_set_nsyn(*tcp, bn);
       tc_status();
     }
@@ -1039,6 +1066,7 @@ class Dycore : public DycoreBase {
     GD_CUDA(cudaEventDestroy(e1));
     out[0] = tcp ? tcp->nsyn : 0;
     out[1] = col_lb;
+    out[2] = tcp ? tcp->aslots : 0;
     drop_graph();  // the captured step changes
     steps_done = 0;  // the next step runs eagerly (new work lists), the one after is captured
   }

@@ -42,13 +42,19 @@ __device__ __forceinline__ float clog(float a) { return __logf(a); }
 // (dyn_run.f90:574-590): qa = level above the interface, qb = level below,
 // dm = dd[k-1], d0 = dd[k], dp = dd[k+1], upwind by the sign of etadot.
 // Both upwind cases in one path: the columns of a warp differ in the sign.
+// The limiter (phi + |phi|) / (1 + |phi|) of phi = r / d0 (r = dm or dp) is
+// 2 phi / (1 + phi) = 2 r / (d0 + r) when r and d0 have one sign and 0
+// otherwise: one division instead of two, and finite where r / d0 would
+// overflow (d0 is clamped to the smallest normal, not to zero).
 template <typename R>
 __device__ __forceinline__ R thuburn_half(R qa, R qb, R dm, R d0, R dp, R eta) {
   const R h = R(0.5) * (qb + qa);
   const bool up = eta > R(0);
   const R qu = up ? qa : qb;
-  const R phi = cdiv(up ? dm : dp, d0);
-  return qu + cdiv(phi + fabs(phi), R(1) + fabs(phi)) * (h - qu);
+  const R r = up ? dm : dp;
+  const bool same = (r > R(0)) == (d0 > R(0)) && r != R(0);
+  const R lim = same ? cdiv(R(2) * r, d0 + r) : R(0);
+  return qu + lim * (h - qu);
 }
 
 // dd[k] = q(level below k) - q(level above k) at interior interface k,
@@ -107,6 +113,13 @@ __global__ void __launch_bounds__(32 * NWM, (sizeof(R) == 4 ? 32 : 16) / NWM)
   const int j = (int)(p / a.nlon);
   R* part = reinterpret_cast<R*>(smcol);  // [5][NW][32] block sums, then [2][32] column totals
   R* etas = part + (5 * NW + 2) * 32;      // [L+1][32] etadot
+  // FP64: ln(p(t+1)/p(t)) and 1/p(t) of every layer from phase 1 for phase 3
+  // (each thread reads back only what it wrote: no barrier).  Its log and
+  // reciprocals are the costly FP64 operations of the level loop; the FP32
+  // kernel recomputes them (hardware approximations).
+  constexpr bool kKeep = sizeof(R) == 8;
+  R* rls = etas + (L + 1) * 32;  // [L][32] (FP64 only)
+  R* ipks = rls + L * 32;        // [L][32] (FP64 only)
   auto PART = [&](int q, int ww) -> R& { return part[(q * NW + ww) * 32 + lane]; };
   auto ETA = [&](int t) -> R& { return etas[t * 32 + lane]; };
   const R* gS = a.gS;
@@ -159,7 +172,11 @@ __global__ void __launch_bounds__(32 * NWM, (sizeof(R) == 4 ? 32 : 16) / NWM)
         s2 += (__ldg(bk + t + 1) * ipk1 - __ldg(bk + t) * ipkt) * ltv[i];
         su += rl * ltx[i];
         sv += rl * lty[i];
+        if (kKeep) rls[t * 32 + lane] = rl;
+      } else if (kKeep) {
+        rls[lane] = a.rlnp_top;
       }
+      if (kKeep) ipks[t * 32 + lane] = ipkt;
       if (a.prs && valid)
         a.prs[(long)b * ng + p] =
             pow((pow(pkt1, a.kappa) * pkt1 - pow(pkt, a.kappa) * pkt) / ((a.kappa + R(1)) * dp), R(1) / a.kappa);
@@ -258,11 +275,12 @@ __global__ void __launch_bounds__(32 * NWM, (sizeof(R) == 4 ? 32 : 16) / NWM)
       tp = S(a.s.tv + b + 1);
     }
     const R pkt = PK(t), pkt1 = pkb3, dp = pkt1 - pkt, idp = crcp(dp);
-    const R ipkt = t > 0 ? crcp(pkt) : R(0), ipk1 = ipkb3;  // 1/pk(t) is unused at the model top (pk = 0)
+    // 1/pk(t) is unused at the model top (pk = 0)
+    const R ipkt = kKeep ? ipks[t * 32 + lane] : (t > 0 ? crcp(pkt) : R(0)), ipk1 = ipkb3;
     pkb3 = pkt;
     ipkb3 = ipkt;
     idpa[i] = idp;
-    const R rl = RLN(t, pkt, pkt1);
+    const R rl = kKeep ? rls[t * 32 + lane] : RLN(t, pkt, pkt1);
     const R al = (t == 0) ? a.log2sp : R(1) - (pkt * idp) * rl;
     const R cg = uc * dlx + vc * dly;
     const R dv = S(a.s.div + b);
@@ -386,7 +404,7 @@ template <typename R, int LB, int NWM>
 static void launch_cols_lb(const ColumnArgs<R>& a, bool inverse_only, cudaStream_t s) {
   const long ng = (long)a.nlon * a.nlat;
   const int nw = ceil_div(a.L, LB);
-  const size_t sm = (size_t)(5 * nw + 2 + a.L + 1) * 32 * sizeof(R);
+  const size_t sm = (size_t)(5 * nw + 2 + a.L + 1 + (sizeof(R) == 8 ? 2 * a.L : 0)) * 32 * sizeof(R);
   if (sm > 48 * 1024)
     GD_CUDA(cudaFuncSetAttribute(k_dyn_columns<R, LB, NWM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   k_dyn_columns<R, LB, NWM><<<(unsigned)ceil_div(ng, 32), dim3(32, nw), sm, s>>>(a, inverse_only ? 1 : 0);
@@ -418,7 +436,7 @@ __global__ void __launch_bounds__(256) k_hs(HsArgs<R> a) {
   const R ps = exp(a.gS[(long)a.s.lnps * ng + p]);
   const R sl = a.sinlat[j], cl = a.coslat[j];
   const R s2 = sl * sl, c2 = cl * cl, c4 = c2 * c2;
-  const R p0 = R(1.e5);
+  const R p0 = R(1.e5), logp0 = log(p0);
   // levels in groups of four: the group's grid loads are issued before its
   // arithmetic, and pk^kappa of an interface is carried from the level below
   // (the bottom interface of a level is the top one of the level under it)
@@ -440,10 +458,16 @@ __global__ void __launch_bounds__(256) k_hs(HsArgs<R> a) {
       const int t = L - 1 - b;
       const R pkt = a.ak[t] + a.bk[t] * ps, pkt1 = a.ak[t + 1] + a.bk[t + 1] * ps;
       const R pw0 = pow(pkt, a.kappa);
-      const R prs = pow((pw1 * pkt1 - pw0 * pkt) / ((a.kappa + R(1)) * (pkt1 - pkt)), R(1) / a.kappa);
+      // Phillips layer pressure prs = X^(1/kappa) and ln(prs/p0) from one
+      // logarithm of X: three logarithms and two powers fewer per level than
+      // pow(X, 1/kappa), pow(prs/p0, expo) and log(prs/p0) (the level loop's
+      // FP64 cost; the results agree to ~1e-14 relative)
+      const R lx = log((pw1 * pkt1 - pw0 * pkt) / ((a.kappa + R(1)) * (pkt1 - pkt))) / a.kappa;
+      const R prs = exp(lx);
+      const R lp = lx - logp0;
       pw1 = pw0;
       R bl = prs / ps;
-      R teq = pow(prs / p0, a.expo) * (R(315) - R(60) * s2 - R(10) * log(prs / p0) * c2);
+      R teq = exp(a.expo * lp) * (R(315) - R(60) * s2 - R(10) * lp * c2);
       bl = (bl - a.sigbot) / (R(1) - a.sigbot);
       if (bl < R(0)) bl = R(0);
       if (teq < R(200)) teq = R(200);

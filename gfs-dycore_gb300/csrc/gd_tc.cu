@@ -291,9 +291,16 @@ struct TcArgs {
   uint32_t idesc;
   uint32_t tmem_cols;
   // fused kernel only: accumulate the hi*lo and lo*hi products in their own
-  // TMEM accumulator (single-buffered tiles), so the main accumulator takes
-  // a third of the truncating FP32 accumulation steps
+  // TMEM accumulator beside the main one, so the main accumulator takes a
+  // third of the truncating FP32 accumulation steps
   int sepx;
+  // fused kernel only: K segments of cps chunks per parity, each accumulated
+  // afresh and folded by the epilogue into running FP32 sums in TMEM (round
+  // to nearest); 0: one accumulation per parity
+  int cps;
+  // fused kernel only: A slots in tensor memory (the converters run up to na
+  // chunks ahead of the MMAs)
+  int na;
   // analysis only: the latitude (K) range split into nseg segments, item.w
   // the segment; segment q writes its FP32 partial sums at out + q * seg_stride
   int nseg;
@@ -680,6 +687,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
 // k_tc_split_x/g, so results match the unfused path bit for bit.
 constexpr int TCF_THREADS = 448;  // producer, MMA, 4 epilogue, 8 converter warps
 constexpr int TCF_MAXNS = 6;
+constexpr int TCF_MAXA = 4;  // A slots in tensor memory at most (64 columns each)
 
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* v) {
   asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};" ::"r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]) : "memory");
@@ -691,9 +699,24 @@ __device__ __forceinline__ void mma_tf32_ta(uint32_t dtmem, uint32_t atmem, uint
       "r"(atmem), "l"(b), "r"(idesc), "r"(acc));
 }
 
+// Position of K chunk g in a ring of n slots, advanced once per chunk: the
+// slot g mod n and the parity (g / n) & 1 of its use count, without the
+// 64-bit division per chunk on the single-thread issue paths.
+struct TcRing {
+  int slot = 0;
+  uint32_t ph = 0;
+  __device__ __forceinline__ void next(int n) {
+    if (++slot == n) {
+      slot = 0;
+      ph ^= 1u;
+    }
+  }
+};
+
 __global__ void __launch_bounds__(TCF_THREADS, 1)
     k_tc_gemm_f(const __grid_constant__ CUtensorMap mRaw, const __grid_constant__ CUtensorMap mBh,
                 const __grid_constant__ CUtensorMap mBl, TcArgs a, int nitems, int ns, uint32_t raw_bytes) {
+  const int na = a.na;  // A slots (2 <= na <= min(ns, TCF_MAXA))
   extern __shared__ __align__(1024) unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t)1023);
   const int N = a.N, kc = a.kc;
@@ -702,16 +725,24 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
   const uint32_t stage_bytes = (raw_off + raw_bytes + 1023) & ~1023u;
   // full[s]: the TMA copies of a chunk landed; used[s]: the MMAs of the chunk
   // in stage s completed (frees the stage for the producer and, two chunks
-  // later, the A slot for the converters); afull[2]: an A slot is written
+  // na chunks later, the A slot for the converters); afull[na]: an A slot is
+  // written
   uint64_t* full = reinterpret_cast<uint64_t*>(sm + (size_t)ns * stage_bytes);
   uint64_t* used = full + ns;
   uint64_t* afull = used + ns;
-  uint64_t* tfull = afull + 2;   // [2] accumulator buffer ready
+  uint64_t* tfull = afull + TCF_MAXA;  // [2] accumulator buffer ready
   uint64_t* tempty = tfull + 2;  // [2] accumulator buffer drained
   uint64_t* done = tempty + 2;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t acol = 4u * (uint32_t)N;  // TMEM column of A slot 0 (hi 32 columns, lo 32 columns)
+  // TMEM: two accumulator buffers of bw columns, the running sums' E|O when
+  // K segments are folded, then the na A slots (hi 32, lo 32 columns each).
+  // A buffer holds E|O of an item, or one parity's K segment when folding,
+  // and with sepx the cross products' accumulator beside each
+  const bool fold = a.cps > 0;
+  const uint32_t bw = (fold ? 1u : 2u) * (a.sepx ? 2u : 1u) * (uint32_t)N;
+  const uint32_t rcol = 2u * bw;
+  const uint32_t acol = rcol + (fold ? 2u * (uint32_t)N : 0u);
 
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
@@ -724,10 +755,10 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
       mbar_init(smem_u32(&used[s]), 1);
     }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(smem_u32(&afull[b]), 8);  // one arrive per converter warp
       mbar_init(smem_u32(&tfull[b]), 1);
       mbar_init(smem_u32(&tempty[b]), 4);
     }
+    for (int q = 0; q < na; ++q) mbar_init(smem_u32(&afull[q]), 8);  // one arrive per converter warp
     mbar_init(smem_u32(done), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -739,14 +770,15 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
   if (tid == 0) {  // ------------------------------------------- producer
     int fills[TCF_MAXNS] = {0, 0, 0, 0, 0, 0};
     long g = 0;
+    TcRing rs;  // chunk g's stage
     bool bad = false;
     for (int idx = blockIdx.x; idx < nitems && !bad; idx += gridDim.x) {
       const TcItem t = tc_item(a, idx);
       const int total = t.nk0 + t.nk1;
       for (int i = 0; i < total; ++i, ++g) {
-        const int s = (int)(g % ns);
-        const long u = g / ns;
-        if (u >= 1 && !mbar_wait(smem_u32(&used[s]), (uint32_t)((u - 1) & 1), a.err, 21)) {
+        const int s = rs.slot;
+        // the stage's previous chunk, g - ns, must have been consumed
+        if (g >= ns && !mbar_wait(smem_u32(&used[s]), rs.ph ^ 1u, a.err, 21)) {
           bad = true;
           break;
         }
@@ -771,42 +803,53 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
           tma_3d(smem_u32(st + raw_off + raw_bytes / 2), &mRaw, t.c0, a.nlat - x - kc, t.m, fb);
         }
         ++fills[s];
+        rs.next(ns);
       }
     }
     for (int s = 0; s < ns; ++s)  // no copies left in flight at exit
       if (fills[s] > 0) mbar_wait(smem_u32(&full[s]), (fills[s] - 1) & 1, a.err, 22);
   } else if (tid == 32) {  // ------------------------------------ MMA issuer
     long g = 0;
-    int titem = 0;
+    int titem = 0;  // accumulator hand-offs so far: items, or K segments when folding
     bool bad = false;
-    for (int idx = blockIdx.x; idx < nitems && !bad; idx += gridDim.x, ++titem) {
+    const int cps = fold ? a.cps : (1 << 30);
+    TcRing rs, ra;  // chunk g's stage and A slot
+    for (int idx = blockIdx.x; idx < nitems && !bad; idx += gridDim.x) {
       const TcItem t = tc_item(a, idx);
-      // accumulator buffer b of this item (two, or one when the cross
-      // products have their own accumulator) and its use count u
-      const int b = a.sepx ? 0 : (titem & 1), u = a.sepx ? titem : (titem >> 1);
-      if (u >= 1 && !mbar_wait(smem_u32(&tempty[b]), (uint32_t)((u - 1) & 1), a.err, 23)) break;
-      tc_fence_after();
       const int total = t.nk0 + t.nk1;
+      int b = 0;   // accumulator buffer of the current hand-off
+      int sc = 0;  // chunk of the current K segment (segments restart with each parity)
       for (int i = 0; i < total; ++i, ++g) {
-        const int s = (int)(g % ns), cs = (int)(g & 1);
-        if (!mbar_wait(smem_u32(&full[s]), (uint32_t)((g / ns) & 1), a.err, 24) ||
-            !mbar_wait(smem_u32(&afull[cs]), (uint32_t)((g >> 1) & 1), a.err, 25)) {
+        const int acc = (i < t.nk0) ? 0 : 1, ip = acc ? i - t.nk0 : i;  // chunk ip of parity acc
+        const bool sfirst = sc == 0;  // a K segment starts: its accumulators start afresh
+        const bool slast = sc == cps - 1 || ip == (acc ? t.nk1 : t.nk0) - 1;
+        sc = slast ? 0 : sc + 1;
+        if (fold ? sfirst : i == 0) {  // wait until the epilogue drained the buffer
+          b = titem & 1;
+          const int u = titem >> 1;
+          if (u >= 1 && !mbar_wait(smem_u32(&tempty[b]), (uint32_t)((u - 1) & 1), a.err, 23)) {
+            bad = true;
+            break;
+          }
+          tc_fence_after();
+        }
+        const int s = rs.slot, cs = ra.slot;
+        if (!mbar_wait(smem_u32(&full[s]), rs.ph, a.err, 24) || !mbar_wait(smem_u32(&afull[cs]), ra.ph, a.err, 25)) {
           bad = true;
           break;
         }
         tc_fence_after();
-        const int acc = (i < t.nk0) ? 0 : 1, kk = t.kb + (acc ? i - t.nk0 : i);
         unsigned char* st = sm + (size_t)s * stage_bytes;
         const uint32_t ah = tbase + acol + 64u * (uint32_t)cs, al = ah + 32u;
         const uint64_t dbh = smem_desc(smem_u32(st)), dbl = smem_desc(smem_u32(st + tab_bytes));
-        const uint32_t d = tbase + (uint32_t)(b * 2 * N + acc * N);
-        if (a.sepx) {  // the cross products into their own accumulator, 2N columns on
-          const uint32_t dx = d + 2u * (uint32_t)N;
+        const uint32_t d = tbase + (uint32_t)b * bw + (fold ? 0u : (uint32_t)(acc * N));
+        if (a.sepx) {  // the cross products into their own accumulator, beside the E|O (or segment) one
+          const uint32_t dx = d + (fold ? 1u : 2u) * (uint32_t)N;
 #pragma unroll
           for (int k4 = 0; k4 < 4; ++k4) {
             const uint64_t o = (uint64_t)(2 * k4);
             const uint32_t ka = 8u * (uint32_t)k4;
-            const uint32_t first = (kk > t.kb || k4 > 0) ? 1u : 0u;  // a segment starts afresh
+            const uint32_t first = (!sfirst || k4 > 0) ? 1u : 0u;
             mma_tf32_ta(d, ah + ka, dbh + o, a.idesc, first);
             mma_tf32_ta(dx, ah + ka, dbl + o, a.idesc, first);
             mma_tf32_ta(dx, al + ka, dbh + o, a.idesc, 1u);
@@ -816,14 +859,19 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
           for (int k4 = 0; k4 < 4; ++k4) {  // K = 8 TF32 per MMA: 8 TMEM columns of A, 32 bytes of B
             const uint64_t o = (uint64_t)(2 * k4);
             const uint32_t ka = 8u * (uint32_t)k4;
-            mma_tf32_ta(d, ah + ka, dbh + o, a.idesc, (kk > t.kb || k4 > 0) ? 1u : 0u);
+            mma_tf32_ta(d, ah + ka, dbh + o, a.idesc, (!sfirst || k4 > 0) ? 1u : 0u);
             mma_tf32_ta(d, ah + ka, dbl + o, a.idesc, 1u);
             mma_tf32_ta(d, al + ka, dbh + o, a.idesc, 1u);
           }
         }
         mma_commit(smem_u32(&used[s]));
+        rs.next(ns);
+        ra.next(na);
+        if (fold ? slast : i == total - 1) {  // hand the buffer to the epilogue
+          mma_commit(smem_u32(&tfull[b]));
+          ++titem;
+        }
       }
-      if (!bad) mma_commit(smem_u32(&tfull[b]));
     }
     mma_commit(smem_u32(done));
   } else if (warp >= 6) {  // ----------------------------------- converters
@@ -832,13 +880,14 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
     const int k0 = ((warp - 6) >> 2) * 16;  // this thread's half of the chunk's K entries
     const uint32_t arow = tbase + ((uint32_t)(q4 * 32) << 16) + acol + (uint32_t)k0;
     long g = 0;
+    TcRing rs, ra, rp;  // chunk g's stage and A slot; chunk g - na's stage
     bool bad = false;
     for (int idx = blockIdx.x; idx < nitems && !bad; idx += gridDim.x) {
       const TcItem t = tc_item(a, idx);
       const int total = t.nk0 + t.nk1;
       for (int i = 0; i < total; ++i, ++g) {
-        const int s = (int)(g % ns), cs = (int)(g & 1);
-        const bool okf = mbar_wait(smem_u32(&full[s]), (uint32_t)((g / ns) & 1), a.err, 26);
+        const int s = rs.slot, cs = ra.slot;
+        const bool okf = mbar_wait(smem_u32(&full[s]), rs.ph, a.err, 26);
         if (!__all_sync(0xffffffffu, okf)) {
           bad = true;
           break;
@@ -868,14 +917,14 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
           if (ii >= nv) v = 0.f;
           Elem<TC_TF32>::splitf(v, h[e], l[e]);
         }
-        // the slot's previous contents fed chunk g - 2
-        if (g >= 2) {
-          const long gp = g - 2;
-          const bool oku = mbar_wait(smem_u32(&used[gp % ns]), (uint32_t)((gp / ns) & 1), a.err, 27);
+        // the slot's previous contents fed chunk g - na
+        if (g >= na) {
+          const bool oku = mbar_wait(smem_u32(&used[rp.slot]), rp.ph, a.err, 27);
           if (!__all_sync(0xffffffffu, oku)) {
             bad = true;
             break;
           }
+          rp.next(ns);
         }
         tc_fence_after();
         tmem_st16(arow + 64u * (uint32_t)cs, h);
@@ -884,19 +933,69 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
         tc_fence_before();
         __syncwarp();
         if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&afull[cs])) : "memory");
+        rs.next(ns);
+        ra.next(na);
       }
     }
   } else if (warp >= 2) {  // ------------------------------------- epilogue
     const int q4 = warp & 3;
+    const uint32_t lw = tbase + ((uint32_t)(q4 * 32) << 16);  // this warp's TMEM lane quadrant
     int titem = 0;
-    for (int idx = blockIdx.x; idx < nitems; idx += gridDim.x, ++titem) {
+    bool bad = false;
+    for (int idx = blockIdx.x; idx < nitems && !bad; idx += gridDim.x) {
       const TcItem t = tc_item(a, idx);
-      const int b = a.sepx ? 0 : (titem & 1), u = a.sepx ? titem : (titem >> 1);
-      const bool ok = mbar_wait(smem_u32(&tfull[b]), (uint32_t)(u & 1), a.err, 28);
-      if (!__all_sync(0xffffffffu, ok)) break;
-      tc_fence_after();
+      int bt = -1;       // the buffer holding the item's sums (without folding)
+      uint32_t tw = lw;  // TMEM columns of the item's E|O sums
+      if (fold) {
+        // each K segment, main + cross products, folded into the running sums
+        // of its parity (FP32, round to nearest)
+        const int nsE = (t.nk0 + a.cps - 1) / a.cps, nsub = nsE + (t.nk1 + a.cps - 1) / a.cps;
+        for (int j = 0; j < nsub; ++j, ++titem) {
+          const int b = titem & 1, u = titem >> 1;
+          const bool ok = mbar_wait(smem_u32(&tfull[b]), (uint32_t)(u & 1), a.err, 28);
+          if (!__all_sync(0xffffffffu, ok)) {
+            bad = true;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t ts = lw + (uint32_t)b * bw, tr = lw + rcol + (j < nsE ? 0u : (uint32_t)N);
+          const bool first = j == 0 || j == nsE;
+          for (int g = 0; g < N; g += 16) {
+            float v[16];
+            uint32_t w[16];
+            tmem_ld16(ts + g, v);
+            if (a.sepx) {
+              float x[16];
+              tmem_ld16(ts + N + g, x);
+#pragma unroll
+              for (int q = 0; q < 16; ++q) v[q] += x[q];
+            }
+            if (!first) {
+              float r[16];
+              tmem_ld16(tr + g, r);
+#pragma unroll
+              for (int q = 0; q < 16; ++q) v[q] = r[q] + v[q];
+            }
+#pragma unroll
+            for (int q = 0; q < 16; ++q) w[q] = __float_as_uint(v[q]);
+            tmem_st16(tr + g, w);
+          }
+          asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+        }
+        if (bad) break;
+        tw = lw + rcol;
+      } else {
+        bt = titem & 1;
+        const bool ok = mbar_wait(smem_u32(&tfull[bt]), (uint32_t)((titem >> 1) & 1), a.err, 28);
+        if (!__all_sync(0xffffffffu, ok)) break;
+        tc_fence_after();
+        tw = lw + (uint32_t)bt * bw;
+        ++titem;
+      }
       const int c = t.c0 + q4 * 32 + lane;
-      const uint32_t tw = tbase + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(b * 2 * N);
       for (int g = 0; g < N; g += 16) {
         float e[16], o[16];
         tmem_ld16(tw + g, e);
@@ -905,7 +1004,7 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
         else
 #pragma unroll
           for (int q = 0; q < 16; ++q) o[q] = 0.f;
-        if (a.sepx) {  // add the cross products' accumulator (round to nearest)
+        if (a.sepx && !fold) {  // add the cross products' accumulator (round to nearest)
           float xe[16], xo[16];
           tmem_ld16(tw + 2 * N + g, xe);
           if (t.nk1 > 0)
@@ -941,9 +1040,11 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
           }
         }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+      if (bt >= 0) {
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[bt])) : "memory");
+      }
     }
   }
   __syncwarp();
@@ -1021,6 +1122,31 @@ static void* tc_alloc(TcPlan& p, size_t bytes) {
   return d;
 }
 
+// TMEM columns of the fused kernel at N tile n: two accumulator buffers (E|O
+// of an item, or one parity's K segment when folding; doubled by the cross
+// products' accumulator), the running E|O sums when folding, na A slots
+static int tcf_tmem_cols(int n, bool sepx, bool fold, int na) {
+  const int bw = (fold ? 1 : 2) * (sepx ? 2 : 1) * n;
+  return 2 * bw + (fold ? 2 * n : 0) + 64 * na;
+}
+// A slots the fused kernel gets at N tile n: the plan's request, as far as
+// tensor memory holds them (at least two)
+static int tcf_slots(const TcPlan& p, int n) {
+  int na = std::max(2, std::min(p.aslots, TCF_MAXA));
+  while (na > 2 && tcf_tmem_cols(n, p.sepx, p.cps > 0, na) > 512) --na;
+  return na;
+}
+
+int tc_slots(const TcPlan& p, int n) { return tcf_slots(p, n); }
+
+int tc_max_n(const TcPlan& p) {
+  if (!p.persistent) return 160;
+  if (p.kind != TC_TF32) return 128;
+  int n = 96;
+  while (n > 16 && tcf_tmem_cols(n, p.sepx, p.cps > 0, 2) > 512) n -= 16;
+  return n;
+}
+
 void tc_init(TcPlan& p, int kind, int T, int nh, int nlat, int ncap, const long* d_toff, const double* P64,
              const double* H64, cudaStream_t s) {
   p.kind = kind;
@@ -1040,8 +1166,9 @@ void tc_init(TcPlan& p, int kind, int T, int nh, int nlat, int ncap, const long*
     GD_CUDA(cudaDeviceGetAttribute(&p.nsm, cudaDevAttrMultiProcessorCount, dev));
   }
   // persistent: two E|O accumulator buffers (4N TMEM columns) -> N <= 128;
-  // the fused TF32 path also keeps two A slots in TMEM -> N <= 96
-  const int ncap_n = !p.persistent ? 160 : kind == TC_TF32 ? 96 : 128;
+  // the fused TF32 path also keeps two A slots in TMEM and, as configured,
+  // cross-product accumulators and running sums
+  const int ncap_n = !p.persistent ? 160 : kind == TC_TF32 ? tc_max_n(p) : 128;
   p.nsyn = tile_n(nh, ncap_n);
   p.nana = tile_n(kemax, ncap_n);
   p.kirows = round_up(kemax, p.nana);
@@ -1113,7 +1240,7 @@ int tc_tile_n(int n, int cap) { return tile_n(n, cap); }
 // a new latitude tile of the synthesis GEMM: the tables keep their layout,
 // the tensor maps take the new box and the cached work lists are dropped
 void tc_set_nsyn(TcPlan& p, int nsyn) {
-  if (nsyn < 16 || nsyn % 16 || nsyn > (p.persistent ? 96 : 160))
+  if (nsyn < 16 || nsyn % 16 || nsyn > (!p.persistent ? 160 : p.kind == TC_TF32 ? tc_max_n(p) : 128))
     throw std::invalid_argument("tc_set_nsyn: N tile must be a multiple of 16 within the TMEM budget");
   p.nsyn = nsyn;
   const int kind = p.kind;
@@ -1199,13 +1326,13 @@ static void launch_fused(const TcPlan& p, const CUtensorMap& raw, const CUtensor
   const uint32_t stage = (uint32_t)round_up(2 * args.N * 128 + (int)raw_bytes, 1024);
   const size_t avail = 227 * 1024 - 1024 - 256;
   const int ns = (int)std::min<size_t>(TCF_MAXNS, avail / stage);
-  // TMEM: two E|O accumulator buffers, or one buffer and the cross products'
-  // E|O accumulator (4N columns either way) + two A slots (128 columns)
-  if (ns < 2 || args.N > 96 || args.N % 16) throw std::runtime_error("tc fused gemm: bad tile");
+  args.na = tcf_slots(p, args.N);
+  if (ns < args.na || args.N > 96 || args.N % 16 || tcf_tmem_cols(args.N, p.sepx, p.cps > 0, args.na) > 512)
+    throw std::runtime_error("tc fused gemm: bad tile");
   const size_t sm = (size_t)ns * stage + 1024 + 256;
   args.tmem_cols = 512;
-  // the separate cross accumulator takes the second buffer's 2N columns
   args.sepx = p.sepx ? 1 : 0;
+  args.cps = p.cps;
   static bool attr = false;
   if (!attr) {
     GD_CUDA(cudaFuncSetAttribute(k_tc_gemm_f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));

@@ -25,9 +25,16 @@ struct TcPlan {
   int ncap = 0;     // real-column capacity of the staging buffers
   bool persistent = true;  // persistent warp-specialised GEMM (N <= 128)
   // fused TF32x3 GEMM: the hi*lo and lo*hi products in their own accumulator
-  // (a third of the truncating accumulation steps in the main one; tiles
-  // single-buffered); set by the FP64-state modes
+  // (a third of the truncating accumulation steps in the main one); set by
+  // the FP64-state modes before tc_init (it bounds the N tile)
   bool sepx = false;
+  // fused TF32x3 GEMM: K segments of cps chunks per parity, accumulated afresh
+  // and folded in FP32 (round to nearest) by the epilogue; 0 = none; set
+  // before tc_init (it bounds the N tile)
+  int cps = 0;
+  // fused TF32x3 GEMM: A-operand slots in tensor memory requested (2..4; a
+  // launch gets as many as fit beside its accumulators)
+  int aslots = 2;
   // fused TF32x3 analysis: the latitude sum in aseg segments, each written as
   // FP32 partial sums to its own copy of the output (nlm x ldA floats apart),
   // to be added in the caller's precision; set by the FP64-state modes
@@ -57,6 +64,10 @@ void tc_init(TcPlan& p, int kind, int T, int nh, int nlat, int ncap, const long*
 void tc_free(TcPlan& p);
 // the balanced tile at most cap wide over n rows (a multiple of 16)
 int tc_tile_n(int n, int cap);
+// largest N tile the plan's GEMM kernel takes (TMEM budget)
+int tc_max_n(const TcPlan& p);
+// A slots a fused launch at N tile n gets (the request, as far as TMEM holds)
+int tc_slots(const TcPlan& p, int n);
 // switches the synthesis GEMM to latitude tile nsyn (autotuning)
 void tc_set_nsyn(TcPlan& p, int nsyn);
 

@@ -312,10 +312,11 @@ class Dycore:
     def autotune(self):
         """Times the candidate tile shapes on this context and keeps the fastest;
         returns {"synth_tile": latitude tile of the synthesis GEMM (0 without the
-        tensor-core path), "column_levels_per_warp": ...}."""
-        out = np.zeros(2, np.int32)
+        tensor-core path), "column_levels_per_warp": ..., "a_slots": A-operand
+        slots in tensor memory of the Legendre GEMMs (0 without them)}."""
+        out = np.zeros(3, np.int32)
         self._chk(load().gd_autotune(self.h, _p(out)))
-        return {"synth_tile": int(out[0]), "column_levels_per_warp": int(out[1])}
+        return {"synth_tile": int(out[0]), "column_levels_per_warp": int(out[1]), "a_slots": int(out[2])}
 
     def set_closure(self, net):
         """Attach a trained Mlp as the learned per-column closure (None detaches)."""

@@ -400,7 +400,7 @@ module gd_api
     integer(c_int) function gd_autotune(ctx, choices) bind(c, name='gd_autotune')
       import :: c_int, c_ptr
       type(c_ptr), value :: ctx
-      integer(c_int), intent(out) :: choices(2)
+      integer(c_int), intent(out) :: choices(3)
     end function
     ! ------------------------------------------- learned per-column closure --
     integer(c_int) function gd_mlp_init(nin, nhidden, nlayers, nout, seed, device, net) bind(c, name='gd_mlp_init')

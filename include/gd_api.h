@@ -429,10 +429,12 @@ const char* gd_sigio_last_error(void);
 
 /* Autotuner: times the candidate tile shapes of this context's kernels on
    its own buffers (a state must be set) and keeps the fastest for the later
-   steps: choices[0] = the synthesis Legendre GEMM's latitude tile (split
-   precision modes; 0 otherwise), choices[1] = the column kernel's levels per
-   warp.  Results do not depend on the tile; the levels per warp change the
-   order of the column sums (last-bit differences). */
+   steps.  choices must hold 3 ints: choices[0] = the synthesis Legendre
+   GEMM's latitude tile (split precision modes; 0 otherwise), choices[1] =
+   the column kernel's levels per warp, choices[2] = the A-operand slots in
+   tensor memory requested for both Legendre GEMMs (split modes; 0
+   otherwise).  Results do not depend on the tile or the slots; the levels
+   per warp change the order of the column sums (last-bit differences). */
 int gd_autotune(gd_ctx* ctx, int* choices);
 
 /* ---- Learned per-column closure -----------------------------------------

@@ -368,8 +368,13 @@ class Dycore : public DycoreBase {
       GD_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
       GD_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
       tcp.reset(new TcPlan());
+      // widest N tile at init (GD_TC_TILE_CAP: a tuning and measurement knob)
+      tcp->tile_cap = std::max(16, env_int("GD_TC_TILE_CAP", tcp->tile_cap));
       const int ncap = 2 * std::max(sc.ncol, ap.ncol);
       if constexpr (std::is_same<R, float>::value) {
+        // GD_TC_SEPX=1: the cross products in their own accumulator here too
+        // (a tuning and measurement knob; the FP64-state modes always do it)
+        tcp->sepx = c.precision == GD_PREC_TF32X3 && env_int("GD_TC_SEPX", 0) != 0;
         tc_init(*tcp, c.precision == GD_PREC_TF32X3 ? TC_TF32 : TC_BF16, T, nh, nlat, ncap, toff, P64keep, H64keep,
                 stream);
       } else {
@@ -1032,7 +1037,7 @@ class Dycore : public DycoreBase {
     col_lb = blb;
     if (tcp) {
       std::vector<int> tiles;
-      for (int cap : {48, 64, 80, 96}) {
+      for (int cap : {48, 64, 80, 96, 128, 144, 192}) {
         if (cap > tc_max_n(*tcp)) continue;  // beyond the GEMM kernel's TMEM budget
         const int n = tc_tile_n(nh, cap);
         if (std::find(tiles.begin(), tiles.end(), n) == tiles.end()) tiles.push_back(n);

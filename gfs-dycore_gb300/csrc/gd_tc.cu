@@ -301,6 +301,9 @@ struct TcArgs {
   // fused kernel only: A slots in tensor memory (the converters run up to na
   // chunks ahead of the MMAs)
   int na;
+  // fused kernel only: accumulator buffers in tensor memory, 2 (an item's
+  // epilogue overlaps the next item's MMAs) or 1 (wide N tiles)
+  int nbuf;
   // analysis only: the latitude (K) range split into nseg segments, item.w
   // the segment; segment q writes its FP32 partial sums at out + q * seg_stride
   int nseg;
@@ -688,6 +691,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
 constexpr int TCF_THREADS = 448;  // producer, MMA, 4 epilogue, 8 converter warps
 constexpr int TCF_MAXNS = 6;
 constexpr int TCF_MAXA = 4;  // A slots in tensor memory at most (64 columns each)
+constexpr int TCF_MAXN = 192;  // widest N tile (single-buffered E|O, 2N + 128 TMEM columns)
 
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* v) {
   asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};" ::"r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]) : "memory");
@@ -735,13 +739,14 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
   uint64_t* done = tempty + 2;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // TMEM: two accumulator buffers of bw columns, the running sums' E|O when
+  // TMEM: nbuf accumulator buffers of bw columns, the running sums' E|O when
   // K segments are folded, then the na A slots (hi 32, lo 32 columns each).
   // A buffer holds E|O of an item, or one parity's K segment when folding,
   // and with sepx the cross products' accumulator beside each
   const bool fold = a.cps > 0;
+  const bool dbuf = a.nbuf == 2;
   const uint32_t bw = (fold ? 1u : 2u) * (a.sepx ? 2u : 1u) * (uint32_t)N;
-  const uint32_t rcol = 2u * bw;
+  const uint32_t rcol = (dbuf ? 2u : 1u) * bw;
   const uint32_t acol = rcol + (fold ? 2u * (uint32_t)N : 0u);
 
   if (warp == 1) {
@@ -825,8 +830,8 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
         const bool slast = sc == cps - 1 || ip == (acc ? t.nk1 : t.nk0) - 1;
         sc = slast ? 0 : sc + 1;
         if (fold ? sfirst : i == 0) {  // wait until the epilogue drained the buffer
-          b = titem & 1;
-          const int u = titem >> 1;
+          b = dbuf ? (titem & 1) : 0;
+          const int u = dbuf ? (titem >> 1) : titem;
           if (u >= 1 && !mbar_wait(smem_u32(&tempty[b]), (uint32_t)((u - 1) & 1), a.err, 23)) {
             bad = true;
             break;
@@ -951,7 +956,7 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
         // of its parity (FP32, round to nearest)
         const int nsE = (t.nk0 + a.cps - 1) / a.cps, nsub = nsE + (t.nk1 + a.cps - 1) / a.cps;
         for (int j = 0; j < nsub; ++j, ++titem) {
-          const int b = titem & 1, u = titem >> 1;
+          const int b = dbuf ? (titem & 1) : 0, u = dbuf ? (titem >> 1) : titem;
           const bool ok = mbar_wait(smem_u32(&tfull[b]), (uint32_t)(u & 1), a.err, 28);
           if (!__all_sync(0xffffffffu, ok)) {
             bad = true;
@@ -988,8 +993,8 @@ __global__ void __launch_bounds__(TCF_THREADS, 1)
         if (bad) break;
         tw = lw + rcol;
       } else {
-        bt = titem & 1;
-        const bool ok = mbar_wait(smem_u32(&tfull[bt]), (uint32_t)((titem >> 1) & 1), a.err, 28);
+        bt = dbuf ? (titem & 1) : 0;
+        const bool ok = mbar_wait(smem_u32(&tfull[bt]), (uint32_t)((dbuf ? (titem >> 1) : titem) & 1), a.err, 28);
         if (!__all_sync(0xffffffffu, ok)) break;
         tc_fence_after();
         tw = lw + (uint32_t)bt * bw;
@@ -1122,18 +1127,23 @@ static void* tc_alloc(TcPlan& p, size_t bytes) {
   return d;
 }
 
-// TMEM columns of the fused kernel at N tile n: two accumulator buffers (E|O
-// of an item, or one parity's K segment when folding; doubled by the cross
-// products' accumulator), the running E|O sums when folding, na A slots
-static int tcf_tmem_cols(int n, bool sepx, bool fold, int na) {
+// TMEM columns of the fused kernel at N tile n: nbuf accumulator buffers
+// (E|O of an item, or one parity's K segment when folding; doubled by the
+// cross products' accumulator), the running E|O sums when folding, na A slots
+static int tcf_tmem_cols(int n, bool sepx, bool fold, int na, int nbuf) {
   const int bw = (fold ? 1 : 2) * (sepx ? 2 : 1) * n;
-  return 2 * bw + (fold ? 2 * n : 0) + 64 * na;
+  return nbuf * bw + (fold ? 2 * n : 0) + 64 * na;
 }
+// accumulator buffers of the fused kernel at N tile n: two where they fit
+// beside two A slots, else one (wide tiles: the epilogue no longer overlaps
+// the next item's MMAs, each chunk's MMAs cover more latitudes or degrees)
+static int tcf_nbuf(const TcPlan& p, int n) { return tcf_tmem_cols(n, p.sepx, p.cps > 0, 2, 2) <= 512 ? 2 : 1; }
 // A slots the fused kernel gets at N tile n: the plan's request, as far as
 // tensor memory holds them (at least two)
 static int tcf_slots(const TcPlan& p, int n) {
+  const int nb = tcf_nbuf(p, n);
   int na = std::max(2, std::min(p.aslots, TCF_MAXA));
-  while (na > 2 && tcf_tmem_cols(n, p.sepx, p.cps > 0, na) > 512) --na;
+  while (na > 2 && tcf_tmem_cols(n, p.sepx, p.cps > 0, na, nb) > 512) --na;
   return na;
 }
 
@@ -1142,8 +1152,8 @@ int tc_slots(const TcPlan& p, int n) { return tcf_slots(p, n); }
 int tc_max_n(const TcPlan& p) {
   if (!p.persistent) return 160;
   if (p.kind != TC_TF32) return 128;
-  int n = 96;
-  while (n > 16 && tcf_tmem_cols(n, p.sepx, p.cps > 0, 2) > 512) n -= 16;
+  int n = TCF_MAXN;
+  while (n > 16 && tcf_tmem_cols(n, p.sepx, p.cps > 0, 2, 1) > 512) n -= 16;
   return n;
 }
 
@@ -1167,8 +1177,9 @@ void tc_init(TcPlan& p, int kind, int T, int nh, int nlat, int ncap, const long*
   }
   // persistent: two E|O accumulator buffers (4N TMEM columns) -> N <= 128;
   // the fused TF32 path also keeps two A slots in TMEM and, as configured,
-  // cross-product accumulators and running sums
-  const int ncap_n = !p.persistent ? 160 : kind == TC_TF32 ? tc_max_n(p) : 128;
+  // cross-product accumulators and running sums (wider tiles, single-
+  // buffered, by the plan's tile cap or the autotuner)
+  const int ncap_n = !p.persistent ? 160 : kind == TC_TF32 ? std::min(tc_max_n(p), p.tile_cap) : 128;
   p.nsyn = tile_n(nh, ncap_n);
   p.nana = tile_n(kemax, ncap_n);
   p.kirows = round_up(kemax, p.nana);
@@ -1317,17 +1328,26 @@ static bool fused_ok(const TcPlan& p, const void* base, long ld) {
     const char* e = getenv("GD_TC_FUSED");
     return e && e[0] == '0';
   }();
-  return !off && p.kind == TC_TF32 && p.persistent && p.nsyn <= 96 && p.nana <= 96 && ((uintptr_t)base % 16) == 0 &&
-         ld % 4 == 0;
+  return !off && p.kind == TC_TF32 && p.persistent && p.nsyn <= tc_max_n(p) && p.nana <= tc_max_n(p) &&
+         ((uintptr_t)base % 16) == 0 && ld % 4 == 0;
 }
 
 static void launch_fused(const TcPlan& p, const CUtensorMap& raw, const CUtensorMap& bh, const CUtensorMap& bl,
                          TcArgs& args, int nitems, uint32_t raw_bytes, cudaStream_t s) {
   const uint32_t stage = (uint32_t)round_up(2 * args.N * 128 + (int)raw_bytes, 1024);
   const size_t avail = 227 * 1024 - 1024 - 256;
-  const int ns = (int)std::min<size_t>(TCF_MAXNS, avail / stage);
+  // TMA ring depth: as many stages as shared memory holds (at most
+  // TCF_MAXNS; GD_TC_STAGES lowers the cap, a tuning and measurement knob)
+  static const int cap = [] {
+    const char* e = getenv("GD_TC_STAGES");
+    const int v = (e && *e) ? atoi(e) : TCF_MAXNS;
+    return std::max(2, std::min(v, TCF_MAXNS));
+  }();
+  const int ns = (int)std::min<size_t>((size_t)cap, avail / stage);
+  args.nbuf = tcf_nbuf(p, args.N);
   args.na = tcf_slots(p, args.N);
-  if (ns < args.na || args.N > 96 || args.N % 16 || tcf_tmem_cols(args.N, p.sepx, p.cps > 0, args.na) > 512)
+  if (ns < args.na || args.N > TCF_MAXN || args.N % 16 ||
+      tcf_tmem_cols(args.N, p.sepx, p.cps > 0, args.na, args.nbuf) > 512)
     throw std::runtime_error("tc fused gemm: bad tile");
   const size_t sm = (size_t)ns * stage + 1024 + 256;
   args.tmem_cols = 512;

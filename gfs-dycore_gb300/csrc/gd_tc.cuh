@@ -35,6 +35,9 @@ struct TcPlan {
   // fused TF32x3 GEMM: A-operand slots in tensor memory requested (2..4; a
   // launch gets as many as fit beside its accumulators)
   int aslots = 2;
+  // widest N tile tc_init chooses for the fused TF32x3 GEMM (tiles above 96
+  // are single-buffered in TMEM); the autotuner may widen the synthesis tile
+  int tile_cap = 96;
   // fused TF32x3 analysis: the latitude sum in aseg segments, each written as
   // FP32 partial sums to its own copy of the output (nlm x ldA floats apart),
   // to be added in the caller's precision; set by the FP64-state modes

@@ -9,18 +9,22 @@
 // weights from a BF16 copy made after every update (biases stay FP32), so a
 // trained net is exactly the BF16 net it is evaluated as.
 //
-// The products are small (nh = 256) and the batch is the grid's columns, so
-// one tiled SIMT GEMM serves every product: 64 x 64 output tiles, K in steps
+// The products with the batch (the grid's columns) as rows, X W^T and dZ W,
+// run on the tensor cores (k_tc_mlp in gd_tc.cu) when every layer is at most
+// 256 wide: the weights are exact in TF32 and each activation or gradient is
+// split into TF32 hi + lo, so two MMAs per K step give the FP32 products of
+// the BF16 net.  That covers inference (gd_mlp_forward and the closure in
+// the step), the training forward pass (which also stores each hidden
+// layer's Z and A) and the backward product dZ_l W_l with the GELU
+// derivative fused.  The weight gradient dZ^T A, a reduction over the batch,
+// runs on a tiled SIMT GEMM with split K: 64 x 64 output tiles, K in steps
 // of 16 through shared memory, 4 x 4 outputs per thread, operands addressed
-// through (row, column) strides so the same kernel forms X W^T, dZ^T X and
-// dZ W, with the bias/GELU or GELU-derivative epilogue fused.  Inference
-// (gd_mlp_forward and the closure in the step) runs on the tensor cores
-// instead (k_tc_mlp in gd_tc.cu): the weights are exact in TF32 and each
-// activation is split into TF32 hi + lo, so two MMAs per K step give the
-// FP32 products of the BF16 net.
+// through (row, column) strides; the same kernel is the SIMT path of every
+// product for wider nets.
 #include <cuda_bf16.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdint>
 #include <memory>
 #include <random>
@@ -66,6 +70,18 @@ struct gd_mlp {
   uint32_t* hh[2] = {nullptr, nullptr};
   uint32_t* hl[2] = {nullptr, nullptr};
   std::vector<gd::TcMlpLayer> layers;
+  // tensor-core training: the forward pass that keeps Z and A (tlayers) and
+  // the backward products dZ_l W_l (blayers, l >= 1) against the weights
+  // transposed to [npt][kpt] (wtct); the output gradient and the hidden
+  // gradients split hi + lo (gyh/gyl, dzh/dzl ping-pong)
+  bool tcb = false;
+  std::vector<int> kpt, npt;
+  std::vector<long> tctoff;
+  float* wtct = nullptr;
+  uint32_t *gyh = nullptr, *gyl = nullptr;
+  uint32_t* dzh[2] = {nullptr, nullptr};
+  uint32_t* dzl[2] = {nullptr, nullptr};
+  std::vector<gd::TcMlpLayer> tlayers, blayers;
   int* terr = nullptr;
   cudaStream_t stream = nullptr;  // the stream the net's work runs on
   cudaStream_t own = nullptr;     // the net's own stream (destroyed with it)
@@ -294,6 +310,14 @@ __global__ void k_w_tc(const __nv_bfloat16* __restrict__ w, int fo, int fi, int 
     o[e] = (n < fo && k < fi) ? __bfloat162float(w[(long)n * fi + k]) : 0.f;
   }
 }
+// the same weights transposed, [Np][Kp] with Np >= fi and Kp >= fo: the B
+// operand of the backward product dZ W
+__global__ void k_w_tc_t(const __nv_bfloat16* __restrict__ w, int fo, int fi, int Np, int Kp, float* __restrict__ o) {
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < (long)Np * Kp; e += (long)gridDim.x * blockDim.x) {
+    const int n = (int)(e / Kp), k = (int)(e % Kp);
+    o[e] = (n < fi && k < fo) ? __bfloat162float(w[(long)k * fi + n]) : 0.f;
+  }
+}
 // inputs x [n][nin] split to TF32 hi + lo rows of pitch Kp (the padding
 // columns stay zero from allocation)
 __global__ void k_split_in(const float* __restrict__ x, long n, int nin, int Kp, uint32_t* __restrict__ xh,
@@ -399,6 +423,50 @@ void mlp_reserve(gd_mlp* p, int ncols) {
       }
       tc_mlp_maps(L, ah, al, p->wtc + p->tcoff[l]);
     }
+    if (p->tcb) {  // the training layers over the same buffers
+      const int L1 = p->nlayer - 1;
+      const int ldd = (p->nh + 31) / 32 * 32;  // pitch of a hidden gradient's split (= kpt of a hidden layer)
+      p->gyh = z((size_t)ncols * p->kpt[L1]);
+      p->gyl = z((size_t)ncols * p->kpt[L1]);
+      for (int i = 0; i < 2; ++i) {
+        p->dzh[i] = z((size_t)ncols * ldd);
+        p->dzl[i] = z((size_t)ncols * ldd);
+      }
+      GD_CUDA(cudaStreamSynchronize(p->stream));
+      p->tlayers = p->layers;
+      for (int l = 0; l < p->nl; ++l) {
+        TcMlpLayer& T = p->tlayers[l];
+        T.mode = 2;
+        T.z = p->zb + (size_t)l * ncols * p->nh;
+        T.act = p->ab + (size_t)l * ncols * p->nh;
+        T.ldz = p->nh;
+      }
+      p->tlayers[L1].y = p->yb;
+      p->tlayers[L1].ldy = p->nout;
+      // backward product of layer l: A = split dZ_l (the output gradient, or
+      // what layer l + 1 wrote), writes dZ_{l-1} to g0 / g1 and its split
+      p->blayers.assign(p->nlayer, TcMlpLayer{});
+      for (int l = 1; l < p->nlayer; ++l) {
+        TcMlpLayer& B = p->blayers[l];
+        const int out = (L1 - l) & 1;
+        B.M = ncols;
+        B.N = p->fin[l];
+        B.Np = p->npt[l];
+        B.Kp = p->kpt[l];
+        B.mode = 3;
+        B.err = p->terr;
+        B.zin = p->zb + (size_t)(l - 1) * ncols * p->nh;
+        B.ldz = p->nh;
+        B.y = out ? p->g1 : p->g0;
+        B.ldy = p->fin[l];
+        B.oh = p->dzh[out];
+        B.ol = p->dzl[out];
+        B.ldo = ldd;
+        const uint32_t* ah = l == L1 ? p->gyh : p->dzh[out ^ 1];
+        const uint32_t* al = l == L1 ? p->gyl : p->dzl[out ^ 1];
+        tc_mlp_maps(B, ah, al, p->wtct + p->tctoff[l]);
+      }
+    }
   }
 }
 
@@ -422,6 +490,33 @@ void forward_tc(gd_mlp* p, const float* x, int n, float* y, cudaStream_t s) {
       L.y = y;
       L.ldy = p->nout;
     }
+    tc_mlp_layer(L, s);
+  }
+}
+}  // namespace
+
+namespace {
+// the tensor-core forward of a training step: the hidden layers also keep
+// their pre-activations and activations (FP32) for the backward pass; the
+// transposed weights of the backward products are refreshed with the others
+void forward_tc_train(gd_mlp* p, const float* x, int n) {
+  cudaStream_t s = p->stream;
+  for (int l = 0; l < p->nlayer; ++l) {
+    const long cnt = (long)p->npd[l] * p->kp[l];
+    k_w_tc<<<std::min(ceil_div(cnt, 256), 1024), 256, 0, s>>>(p->w16 + p->offw[l], p->fout[l], p->fin[l], p->npd[l],
+                                                              p->kp[l], p->wtc + p->tcoff[l]);
+    if (l >= 1) {
+      const long ct = (long)p->npt[l] * p->kpt[l];
+      k_w_tc_t<<<std::min(ceil_div(ct, 256), 1024), 256, 0, s>>>(p->w16 + p->offw[l], p->fout[l], p->fin[l],
+                                                                  p->npt[l], p->kpt[l], p->wtct + p->tctoff[l]);
+    }
+  }
+  k_split_in<<<std::min(ceil_div((long)n * p->nin, 256), 8192), 256, 0, s>>>(x, n, p->nin, p->kp[0], p->xh, p->xl);
+  count_launch(2 * p->nlayer);
+  GD_LAUNCH_CHECK();
+  for (int l = 0; l < p->nlayer; ++l) {
+    TcMlpLayer L = p->tlayers[l];
+    L.M = n;
     tc_mlp_layer(L, s);
   }
 }
@@ -488,13 +583,22 @@ namespace {
 // loss and gradient of a batch into p->grad; the loss lands in p->lossd
 void loss_grad(gd_mlp* p, const float* x, const float* t, int n) {
   cudaStream_t s = p->stream;
-  forward_simt(p, x, n, p->yb, s);
+  if (p->tcb)
+    forward_tc_train(p, x, n);
+  else
+    forward_simt(p, x, n, p->yb, s);
   const long cnt = (long)n * p->nout;
   const int nb = std::min(KPART, ceil_div(cnt, 256));
   k_mse<<<nb, 256, 0, s>>>(p->yb, t, cnt, p->gy, p->partial);
   k_mse_final<<<1, KPART, 0, s>>>(p->partial, nb, cnt, p->lossd);
   count_launch(2);
   GD_LAUNCH_CHECK();
+  if (p->tcb) {  // the output gradient split, the A operand of the last layer's backward product
+    k_split_in<<<std::min(ceil_div(cnt, 256), 8192), 256, 0, s>>>(p->gy, n, p->nout, p->kpt[p->nlayer - 1], p->gyh,
+                                                                    p->gyl);
+    count_launch();
+    GD_LAUNCH_CHECK();
+  }
   // backward: dZ of layer l in cur; dW_l = dZ^T A_{l-1}, db_l = colsum dZ,
   // dZ_{l-1} = (dZ W_l) * GELU'(Z_{l-1})
   const float* cur = p->gy;
@@ -505,7 +609,12 @@ void loss_grad(gd_mlp* p, const float* x, const float* t, int n) {
     k_colsum<<<ceil_div(fo, 32), dim3(32, 8), 0, s>>>(cur, n, fo, p->grad + p->offb[l]);
     count_launch();
     GD_LAUNCH_CHECK();
-    if (l > 0) {
+    if (l > 0 && p->tcb) {  // dZ_{l-1} on the tensor cores, stored and split for layer l - 1
+      TcMlpLayer B = p->blayers[l];
+      B.M = n;
+      tc_mlp_layer(B, s);
+      cur = B.y;
+    } else if (l > 0) {
       float* nxt = (cur == p->g0) ? p->g1 : p->g0;
       const float* Zp = p->zb + (size_t)(l - 1) * p->bcap * p->nh;
       gemm(n, fi, fo, cur, (long)fo, 1L, p->w16 + p->offw[l], (long)fi, 1L, EpiGeluD{Zp, nxt, fi}, s);
@@ -556,6 +665,23 @@ int gd_mlp_init(int nin, int nhidden, int nlayers, int nout, unsigned long long 
     p->tcoff.push_back(toff);
     toff += (long)p->npd[l] * p->kp[l];
   }
+  // tensor-core training when the backward products dZ_l W_l fit as well
+  // (every layer's input at most 256 wide); GD_MLP_TRAIN_TC=0 keeps it on
+  // the SIMT kernels (a comparison knob)
+  {
+    const char* e = getenv("GD_MLP_TRAIN_TC");
+    p->tcb = p->tc && !(e && e[0] == '0');
+  }
+  long ttoff = 0;
+  for (int l = 0; l < p->nlayer; ++l) {
+    p->kpt.push_back((p->fout[l] + 31) / 32 * 32);
+    p->npt.push_back((p->fin[l] + 15) / 16 * 16);
+    p->tctoff.push_back(ttoff);
+    if (l >= 1) {
+      if (p->npt[l] > 256) p->tcb = false;
+      ttoff += (long)p->npt[l] * p->kpt[l];
+    }
+  }
   // He-normal hidden weights, the output layer scaled by 0.1 (the net starts
   // close to no correction), zero biases
   std::vector<float> h(off, 0.f);
@@ -582,6 +708,7 @@ int gd_mlp_init(int nin, int nhidden, int nlayers, int nout, unsigned long long 
     p->in_sd = (float*)p->alloc(sizeof(float) * nin);
     p->out_mu = (float*)p->alloc(sizeof(float) * nout);
     p->out_sd = (float*)p->alloc(sizeof(float) * nout);
+    if (p->tcb) p->wtct = (float*)p->alloc(sizeof(float) * std::max(ttoff, 1L));
     if (p->tc) {
       p->wtc = (float*)p->alloc(sizeof(float) * toff);
       p->terr = (int*)p->alloc(sizeof(int));
@@ -665,7 +792,7 @@ int gd_mlp_loss_grad(gd_mlp* p, const float* x, const float* t, int ncols, float
     need_device(p, t, "t");
     mlp_reserve(p, ncols);
     loss_grad(p, x, t, ncols);
-    GD_CUDA(cudaStreamSynchronize(p->stream));
+    mlp_check(p, p->stream);
     if (loss) GD_CUDA(cudaMemcpy(loss, p->lossd, sizeof(float), cudaMemcpyDeviceToHost));
     if (grad) GD_CUDA(cudaMemcpy(grad, p->grad, sizeof(float) * p->np, cudaMemcpyDeviceToHost));
   });
@@ -687,7 +814,7 @@ int gd_mlp_train_step(gd_mlp* p, const float* x, const float* t, int ncols, floa
     GD_LAUNCH_CHECK();
     if (loss) {
       GD_CUDA(cudaMemcpyAsync(loss, p->lossd, sizeof(float), cudaMemcpyDeviceToHost, p->stream));
-      GD_CUDA(cudaStreamSynchronize(p->stream));
+      mlp_check(p, p->stream);  // synchronises; raises a tensor-core wait that gave up
     }
   });
 }

@@ -1583,6 +1583,11 @@ struct TcMlpArgs {
   int M, N, Np, nk;
   const float* bias;
   int gelu;
+  int mode;
+  float* z;
+  float* act;
+  const float* zin;
+  int ldz;
   uint32_t* oh;
   uint32_t* ol;
   int ldo;
@@ -1593,6 +1598,9 @@ struct TcMlpArgs {
 };
 
 __device__ __forceinline__ float tc_gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float tc_gelu_d(float z) {
+  return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+}
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_tc_mlp(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
@@ -1664,7 +1672,55 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const bool ok = mbar_wait(smem_u32(done), 0, a.err, 34);
   tc_fence_after();
   const bool go = __all_sync(0xffffffffu, ok && *(volatile int*)a.err == 0);
-  if (go) {
+  if (go && a.mode >= 2) {
+    // training: each lane stages 64 accumulator columns of its row (plus the
+    // bias in the forward), then the warp finishes row after row with
+    // coalesced loads and stores: the forward stores z, gelu(z) and the split
+    // of gelu(z); the backward reads z of the layer below and stores
+    // dZ = acc * gelu'(z) and its split
+    constexpr int TP = 65;
+    uint32_t* th = reinterpret_cast<uint32_t*>(sm) + warp * (2 * 32 * TP);
+    const uint32_t tw = tbase + ((uint32_t)(warp * 32) << 16);
+    const int mw = m0 + warp * 32;
+    for (int g0 = 0; g0 < a.Np; g0 += 64) {
+      for (int g = g0; g < g0 + 64 && g < a.Np; g += 16) {
+        float v[16];
+        tmem_ld16(tw + g, v);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int n = g + q;
+          th[lane * TP + (n - g0)] = __float_as_uint(v[q] + (a.mode == 2 && n < a.N ? a.bias[n] : 0.f));
+        }
+      }
+      __syncwarp();
+      for (int r = 0; r < 32; ++r) {
+        const int m = mw + r;
+        if (m >= a.M) break;
+#pragma unroll
+        for (int c = 0; c < 64; c += 32) {
+          const int n = g0 + c + lane;
+          if (n < a.N) {
+            const float v = __uint_as_float(th[r * TP + c + lane]);
+            const long iz = (long)m * a.ldz + n;
+            float o;  // the value the next product takes, split hi + lo
+            if (a.mode == 2) {
+              o = tc_gelu(v);
+              a.z[iz] = v;
+              a.act[iz] = o;
+            } else {
+              o = v * tc_gelu_d(a.zin[iz]);
+              a.y[(long)m * a.ldy + n] = o;
+            }
+            uint32_t h, l;
+            Elem<TC_TF32>::splitf(o, h, l);
+            a.oh[(long)m * a.ldo + n] = h;
+            a.ol[(long)m * a.ldo + n] = l;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  } else if (go) {
     // each lane finishes 64 columns of its row into the warp's part of the
     // (now idle) ring, then the warp stores row after row: 128 contiguous
     // bytes per store instead of 32 rows' scattered words
@@ -1733,6 +1789,13 @@ void tc_mlp_layer(const TcMlpLayer& L, cudaStream_t s) {
   a.nk = L.Kp / 32;
   a.bias = L.bias;
   a.gelu = L.gelu;
+  a.mode = L.mode;
+  a.z = L.z;
+  a.act = L.act;
+  a.zin = L.zin;
+  a.ldz = L.ldz;
+  if (L.mode >= 2 && (!L.oh || !L.ol || L.ldz < L.N || (L.mode == 2 ? (!L.z || !L.act || !L.bias) : (!L.zin || !L.y))))
+    throw std::invalid_argument("tc_mlp_layer: training layer without its buffers");
   a.oh = L.oh;
   a.ol = L.ol;
   a.ldo = L.ldo;

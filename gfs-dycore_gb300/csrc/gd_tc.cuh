@@ -106,6 +106,16 @@ struct TcMlpLayer {
   float* y = nullptr;
   int ldy = 0;
   int* err = nullptr;  // device flag: nonzero when a bounded wait gave up
+  // training: mode 2, a hidden layer of the forward pass that also stores its
+  // pre-activation z = A W^T + b and activation gelu(z) in FP32 ([M][ldz]);
+  // mode 3, the backward product dZ_prev = (dZ W) * gelu'(zin) (no bias),
+  // stored in FP32 to y and split hi + lo to oh / ol.  Mode 0: inference
+  // (gelu selects a hidden layer or the output).
+  int mode = 0;
+  float* z = nullptr;
+  float* act = nullptr;
+  const float* zin = nullptr;
+  int ldz = 0;
 };
 // tensor maps of a layer over its operand buffers (rows M of A)
 void tc_mlp_maps(TcMlpLayer& L, const uint32_t* ah, const uint32_t* al, const float* w);

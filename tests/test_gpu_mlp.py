@@ -1,6 +1,8 @@
 """The learned closure on the GPU: the network's forward pass and gradients
-(gd_mlp, BF16 weights, FP32 accumulation) against the float64 numpy oracle
-with the same BF16-rounded weights; training; the closure inputs against the
+(gd_mlp, BF16 weights, FP32 accumulation; the products with the batch as
+rows on the tensor cores) against the float64 numpy oracle with the same
+BF16-rounded weights; tensor-core against SIMT training; training; the
+closure inputs against the
 library's transforms; a closure whose net is zero leaves the step bit for
 bit unchanged; and what a trained closure gains over the plain coarse step.
 
@@ -98,6 +100,28 @@ def test_closure_shape_gradient_matches_oracle():
             assert rel(g[o:o + sz], go[o:o + sz]) < 1e-4, (fo, fi, sz)
             o += sz
     assert o == net.nparams
+
+
+def test_tensor_core_training_matches_simt_training(monkeypatch):
+    # the configured closure net's loss and gradients with the forward and
+    # backward products dZ W on the tensor cores (the default) and with every
+    # product on the SIMT kernels (GD_MLP_TRAIN_TC=0, read when a net is made):
+    # both within FP32 accumulation of each other
+    from gdpy import core
+
+    nin, nh, nl, nout = 193, 256, 3, 192
+    rng = np.random.default_rng(21)
+    x = torch.from_numpy(rng.standard_normal((700, nin)).astype(np.float32)).cuda()
+    t = torch.from_numpy(rng.standard_normal((700, nout)).astype(np.float32)).cuda()
+    out = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("GD_MLP_TRAIN_TC", flag)
+        net = core.Mlp(nin, nh, nl, nout, seed=21)
+        out.append(net.loss_grad(x, t))
+    (l_tc, g_tc), (l_simt, g_simt) = out
+    assert abs(l_tc - l_simt) <= 1e-5 * l_simt
+    assert rel(g_tc, g_simt) < 1e-4
+    assert not np.array_equal(g_tc, g_simt)  # two different product paths ran
 
 
 def test_training_fits_a_smooth_map():

@@ -17,10 +17,12 @@
 // the step), the training forward pass (which also stores each hidden
 // layer's Z and A) and the backward product dZ_l W_l with the GELU
 // derivative fused.  The weight gradient dZ^T A, a reduction over the batch,
-// runs on a tiled SIMT GEMM with split K: 64 x 64 output tiles, K in steps
-// of 16 through shared memory, 4 x 4 outputs per thread, operands addressed
-// through (row, column) strides; the same kernel is the SIMT path of every
-// product for wider nets.
+// runs on the tensor cores too (k_tc_wgrad): both operands transposed with
+// the batch contiguous and split hi + lo (k_tsplit), the batch in K slices
+// whose partial tiles k_wsum adds in order.  Nets wider than 256 (and
+// GD_MLP_TRAIN_TC=0) train on a tiled SIMT GEMM: 64 x 64 output tiles, K in
+// steps of 16 through shared memory, 4 x 4 outputs per thread, operands
+// addressed through (row, column) strides, split K for the weight gradient.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -82,6 +84,14 @@ struct gd_mlp {
   uint32_t* dzh[2] = {nullptr, nullptr};
   uint32_t* dzl[2] = {nullptr, nullptr};
   std::vector<gd::TcMlpLayer> tlayers, blayers;
+  // the weight gradients dZ_l^T A_{l-1}: dZ and the layer inputs transposed
+  // (batch contiguous) and split, the slices' partial tiles
+  std::vector<gd::TcWgrad> wgl;
+  uint32_t *zth = nullptr, *ztl = nullptr, *ath = nullptr, *atl = nullptr;
+  float* wpart = nullptr;
+  int tcap = 0;        // batch capacity of the training buffers
+  int tbcap = 0;       // bcap the training layers were built over
+  int wsplit_max = 0;  // slices the partial buffer holds
   int* terr = nullptr;
   cudaStream_t stream = nullptr;  // the stream the net's work runs on
   cudaStream_t own = nullptr;     // the net's own stream (destroyed with it)
@@ -318,6 +328,38 @@ __global__ void k_w_tc_t(const __nv_bfloat16* __restrict__ w, int fo, int fi, in
     o[e] = (n < fi && k < fo) ? __bfloat162float(w[(long)k * fi + n]) : 0.f;
   }
 }
+// rows r < nbc of src [n][w] (rows r >= n read as zero) transposed and
+// split to TF32 hi + lo: dh / dl [c][r], row pitch kp -- the operands of a
+// weight gradient, with the batch contiguous
+__global__ void k_tsplit(const float* __restrict__ src, int n, int w, int nbc, int kp, uint32_t* __restrict__ dh,
+                         uint32_t* __restrict__ dl) {
+  __shared__ float t[32][33];
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int r = r0 + i, c = c0 + threadIdx.x;
+    t[i][threadIdx.x] = (r < n && c < w) ? src[(long)r * w + c] : 0.f;
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int c = c0 + i, r = r0 + threadIdx.x;
+    if (c < w && r < nbc) {
+      const float v = t[threadIdx.x][i];
+      const uint32_t h = (__float_as_uint(v) + 0x1000u) & 0xFFFFE000u;  // nearest TF32, ties away
+      dh[(long)c * kp + r] = h;
+      dl[(long)c * kp + r] = __float_as_uint(v - __uint_as_float(h));
+    }
+  }
+}
+// dW [fo][fi] = the sum of the slices' partial tiles [Mp][Np], in slice order
+__global__ void k_wsum(const float* __restrict__ part, int nsplit, int Mp, int Np, int fo, int fi,
+                       float* __restrict__ dw) {
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < (long)fo * fi; e += (long)gridDim.x * blockDim.x) {
+    const int m = (int)(e / fi), c = (int)(e % fi);
+    float s = 0.f;
+    for (int q = 0; q < nsplit; ++q) s += part[((long)q * Mp + m) * Np + c];
+    dw[e] = s;
+  }
+}
 // inputs x [n][nin] split to TF32 hi + lo rows of pitch Kp (the padding
 // columns stay zero from allocation)
 __global__ void k_split_in(const float* __restrict__ x, long n, int nin, int Kp, uint32_t* __restrict__ xh,
@@ -423,50 +465,6 @@ void mlp_reserve(gd_mlp* p, int ncols) {
       }
       tc_mlp_maps(L, ah, al, p->wtc + p->tcoff[l]);
     }
-    if (p->tcb) {  // the training layers over the same buffers
-      const int L1 = p->nlayer - 1;
-      const int ldd = (p->nh + 31) / 32 * 32;  // pitch of a hidden gradient's split (= kpt of a hidden layer)
-      p->gyh = z((size_t)ncols * p->kpt[L1]);
-      p->gyl = z((size_t)ncols * p->kpt[L1]);
-      for (int i = 0; i < 2; ++i) {
-        p->dzh[i] = z((size_t)ncols * ldd);
-        p->dzl[i] = z((size_t)ncols * ldd);
-      }
-      GD_CUDA(cudaStreamSynchronize(p->stream));
-      p->tlayers = p->layers;
-      for (int l = 0; l < p->nl; ++l) {
-        TcMlpLayer& T = p->tlayers[l];
-        T.mode = 2;
-        T.z = p->zb + (size_t)l * ncols * p->nh;
-        T.act = p->ab + (size_t)l * ncols * p->nh;
-        T.ldz = p->nh;
-      }
-      p->tlayers[L1].y = p->yb;
-      p->tlayers[L1].ldy = p->nout;
-      // backward product of layer l: A = split dZ_l (the output gradient, or
-      // what layer l + 1 wrote), writes dZ_{l-1} to g0 / g1 and its split
-      p->blayers.assign(p->nlayer, TcMlpLayer{});
-      for (int l = 1; l < p->nlayer; ++l) {
-        TcMlpLayer& B = p->blayers[l];
-        const int out = (L1 - l) & 1;
-        B.M = ncols;
-        B.N = p->fin[l];
-        B.Np = p->npt[l];
-        B.Kp = p->kpt[l];
-        B.mode = 3;
-        B.err = p->terr;
-        B.zin = p->zb + (size_t)(l - 1) * ncols * p->nh;
-        B.ldz = p->nh;
-        B.y = out ? p->g1 : p->g0;
-        B.ldy = p->fin[l];
-        B.oh = p->dzh[out];
-        B.ol = p->dzl[out];
-        B.ldo = ldd;
-        const uint32_t* ah = l == L1 ? p->gyh : p->dzh[out ^ 1];
-        const uint32_t* al = l == L1 ? p->gyl : p->dzl[out ^ 1];
-        tc_mlp_maps(B, ah, al, p->wtct + p->tctoff[l]);
-      }
-    }
   }
 }
 
@@ -494,6 +492,91 @@ void forward_tc(gd_mlp* p, const float* x, int n, float* y, cudaStream_t s) {
   }
 }
 }  // namespace
+
+// Training buffers (tensor-core path): the split gradients, the transposed
+// operands of the weight gradients and the slices' partial tiles for
+// batches of up to ncols, and the training layers over them and over the
+// activation buffers of mlp_reserve (rebuilt when those move).
+void train_reserve(gd_mlp* p, int ncols) {
+  if (!p->tcb || (ncols <= p->tcap && p->tbcap == p->bcap)) return;
+  GD_CUDA(cudaStreamSynchronize(p->stream));
+  auto z = [&](size_t words) {
+    uint32_t* b = (uint32_t*)p->alloc(sizeof(uint32_t) * words);
+    GD_CUDA(cudaMemsetAsync(b, 0, sizeof(uint32_t) * words, p->stream));
+    return b;
+  };
+  const int L1 = p->nlayer - 1;
+  const int ldd = (p->nh + 31) / 32 * 32;  // pitch of a hidden gradient's split (= kpt of a hidden layer)
+  if (ncols > p->tcap) {
+    const int cap = (ncols + 31) / 32 * 32;
+    int mp = 0, np = 0;
+    for (int l = 0; l < p->nlayer; ++l) {
+      mp = std::max(mp, (p->fout[l] + 127) / 128 * 128);
+      np = std::max(np, (p->fin[l] + 15) / 16 * 16);
+    }
+    int nsm = 0;
+    GD_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device));
+    p->wsplit_max = std::max(1, 2 * nsm);
+    p->gyh = z((size_t)cap * p->kpt[L1]);
+    p->gyl = z((size_t)cap * p->kpt[L1]);
+    for (int i = 0; i < 2; ++i) {
+      p->dzh[i] = z((size_t)cap * ldd);
+      p->dzl[i] = z((size_t)cap * ldd);
+    }
+    p->zth = z((size_t)mp * cap);
+    p->ztl = z((size_t)mp * cap);
+    p->ath = z((size_t)np * cap);
+    p->atl = z((size_t)np * cap);
+    p->wpart = (float*)p->alloc(sizeof(float) * (size_t)p->wsplit_max * mp * np);
+    p->tcap = cap;
+  }
+  GD_CUDA(cudaStreamSynchronize(p->stream));
+  const int ncb = p->bcap;
+  p->tlayers = p->layers;
+  for (int l = 0; l < p->nl; ++l) {
+    TcMlpLayer& T = p->tlayers[l];
+    T.mode = 2;
+    T.z = p->zb + (size_t)l * ncb * p->nh;
+    T.act = p->ab + (size_t)l * ncb * p->nh;
+    T.ldz = p->nh;
+  }
+  p->tlayers[L1].y = p->yb;
+  p->tlayers[L1].ldy = p->nout;
+  // backward product of layer l: A = split dZ_l (the output gradient, or
+  // what layer l + 1 wrote), writes dZ_{l-1} to g0 / g1 and its split
+  p->blayers.assign(p->nlayer, TcMlpLayer{});
+  for (int l = 1; l < p->nlayer; ++l) {
+    TcMlpLayer& B = p->blayers[l];
+    const int out = (L1 - l) & 1;
+    B.M = p->tcap;  // the A operand's rows: the split gradients hold tcap
+    B.N = p->fin[l];
+    B.Np = p->npt[l];
+    B.Kp = p->kpt[l];
+    B.mode = 3;
+    B.err = p->terr;
+    B.zin = p->zb + (size_t)(l - 1) * ncb * p->nh;
+    B.ldz = p->nh;
+    B.y = out ? p->g1 : p->g0;
+    B.ldy = p->fin[l];
+    B.oh = p->dzh[out];
+    B.ol = p->dzl[out];
+    B.ldo = ldd;
+    const uint32_t* ah = l == L1 ? p->gyh : p->dzh[out ^ 1];
+    const uint32_t* al = l == L1 ? p->gyl : p->dzl[out ^ 1];
+    tc_mlp_maps(B, ah, al, p->wtct + p->tctoff[l]);
+  }
+  // weight gradients: A = dZ_l transposed (fout rows), B = the layer's input transposed (fin rows)
+  p->wgl.assign(p->nlayer, TcWgrad{});
+  for (int l = 0; l < p->nlayer; ++l) {
+    TcWgrad& W = p->wgl[l];
+    W.Mp = (p->fout[l] + 127) / 128 * 128;
+    W.Np = (p->fin[l] + 15) / 16 * 16;
+    W.part = p->wpart;
+    W.err = p->terr;
+    tc_wgrad_maps(W, p->zth, p->ztl, p->ath, p->atl, p->tcap);
+  }
+  p->tbcap = p->bcap;
+}
 
 namespace {
 // the tensor-core forward of a training step: the hidden layers also keep
@@ -605,7 +688,24 @@ void loss_grad(gd_mlp* p, const float* x, const float* t, int n) {
   for (int l = p->nlayer - 1; l >= 0; --l) {
     const int fi = p->fin[l], fo = p->fout[l];
     const float* Ain = l == 0 ? x : p->ab + (size_t)(l - 1) * p->bcap * p->nh;
-    gemm_splitk(fo, fi, n, cur, 1L, (long)fo, Ain, (long)fi, 1L, p->kpart, p->grad + p->offw[l], s);
+    if (p->tcb) {  // dW_l on the tensor cores: dZ and the input transposed and split, K = the batch in slices
+      const int nbc = (n + 31) / 32 * 32, nk = nbc / 32;
+      const TcWgrad& W = p->wgl[l];
+      int ns = std::max(1, std::min(nk / 4, std::max(1, p->wsplit_max / (W.Mp / 128))));  // >= 4 chunks per slice
+      const int cps = (nk + ns - 1) / ns;
+      ns = (nk + cps - 1) / cps;  // every slice non-empty
+      k_tsplit<<<dim3(nbc / 32, ceil_div(fo, 32)), dim3(32, 8), 0, s>>>(cur, n, fo, nbc, p->tcap, p->zth, p->ztl);
+      k_tsplit<<<dim3(nbc / 32, ceil_div(fi, 32)), dim3(32, 8), 0, s>>>(Ain, n, fi, nbc, p->tcap, p->ath, p->atl);
+      count_launch(2);
+      GD_LAUNCH_CHECK();
+      tc_wgrad(W, nk, cps, ns, s);
+      k_wsum<<<std::min(ceil_div((long)fo * fi, 256), 1024), 256, 0, s>>>(p->wpart, ns, W.Mp, W.Np, fo, fi,
+                                                                        p->grad + p->offw[l]);
+      count_launch();
+      GD_LAUNCH_CHECK();
+    } else {
+      gemm_splitk(fo, fi, n, cur, 1L, (long)fo, Ain, (long)fi, 1L, p->kpart, p->grad + p->offw[l], s);
+    }
     k_colsum<<<ceil_div(fo, 32), dim3(32, 8), 0, s>>>(cur, n, fo, p->grad + p->offb[l]);
     count_launch();
     GD_LAUNCH_CHECK();
@@ -791,6 +891,7 @@ int gd_mlp_loss_grad(gd_mlp* p, const float* x, const float* t, int ncols, float
     need_device(p, x, "x");
     need_device(p, t, "t");
     mlp_reserve(p, ncols);
+    train_reserve(p, ncols);
     loss_grad(p, x, t, ncols);
     mlp_check(p, p->stream);
     if (loss) GD_CUDA(cudaMemcpy(loss, p->lossd, sizeof(float), cudaMemcpyDeviceToHost));
@@ -804,6 +905,7 @@ int gd_mlp_train_step(gd_mlp* p, const float* x, const float* t, int ncols, floa
     need_device(p, x, "x");
     need_device(p, t, "t");
     mlp_reserve(p, ncols);
+    train_reserve(p, ncols);
     loss_grad(p, x, t, ncols);
     ++p->adam_t;
     const float b1 = 0.9f, b2 = 0.999f;

@@ -1772,6 +1772,158 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(a.tmem_cols));
 }
 
+// Weight gradient of a closure layer (see TcWgrad): one CTA per 128 rows of
+// dZ^T and one slice of the batch; the producer loads A hi, A lo, B hi, B lo
+// per 32-deep K chunk into a 2-stage ring, the MMA thread issues three
+// products per K step into one accumulator, the four warps stage the
+// accumulator through the idle ring and store the slice's partial tile row
+// by row.  Every wait is bounded.
+constexpr int TCW_NS = 2;
+struct TcWgradArgs {
+  int Np, cps, nkt;  // chunks per slice, chunks in all
+  float* part;
+  long pstride;  // floats per slice
+  int* err;
+  uint32_t idesc, tmem_cols;
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_tc_wgrad(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+               const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, TcWgradArgs a) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t)1023);
+  const uint32_t bytesA = TC_M * 128, bytesB = (uint32_t)a.Np * 128;
+  const uint32_t stage_bytes = 2 * bytesA + 2 * bytesB;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + TCW_NS * stage_bytes);
+  uint64_t* empty = full + TCW_NS;
+  uint64_t* done = empty + TCW_NS;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * TC_M;
+  const int ks = blockIdx.y * a.cps;           // this slice's first K chunk
+  const int nk = max(0, min(a.cps, a.nkt - ks));  // its chunks (every slice has at least one)
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(a.tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < TCW_NS; ++s) {
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&empty[s]), 1);
+    }
+    mbar_init(smem_u32(done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+
+  if (tid == 0) {  // ---- TMA producer
+    int fills[TCW_NS] = {0, 0};
+    for (int i = 0; i < nk; ++i) {
+      const int s = i % TCW_NS, u = i / TCW_NS;
+      if (u >= 1 && !mbar_wait(smem_u32(&empty[s]), (u - 1) & 1, a.err, 41)) break;
+      unsigned char* st = sm + s * stage_bytes;
+      const uint32_t fb = smem_u32(&full[s]);
+      const int x = (ks + i) * 32;
+      mbar_expect_tx(fb, stage_bytes);
+      tma_2d(smem_u32(st), &mAh, x, m0, fb);
+      tma_2d(smem_u32(st + bytesA), &mAl, x, m0, fb);
+      tma_2d(smem_u32(st + 2 * bytesA), &mBh, x, 0, fb);
+      tma_2d(smem_u32(st + 2 * bytesA + bytesB), &mBl, x, 0, fb);
+      ++fills[s];
+    }
+    for (int s = 0; s < TCW_NS; ++s)  // never leave with copies in flight
+      if (fills[s] > 0) mbar_wait(smem_u32(&full[s]), (fills[s] - 1) & 1, a.err, 42);
+  } else if (tid == 32) {  // ---- MMA issuer
+    for (int i = 0; i < nk; ++i) {
+      const int s = i % TCW_NS, u = i / TCW_NS;
+      if (!mbar_wait(smem_u32(&full[s]), u & 1, a.err, 43)) break;
+      tc_fence_after();
+      unsigned char* st = sm + s * stage_bytes;
+      const uint64_t dah = smem_desc(smem_u32(st)), dal = smem_desc(smem_u32(st + bytesA));
+      const uint64_t dbh = smem_desc(smem_u32(st + 2 * bytesA)), dbl = smem_desc(smem_u32(st + 2 * bytesA + bytesB));
+#pragma unroll
+      for (int k4 = 0; k4 < 4; ++k4) {  // 4 K steps of 8 per 128-byte row
+        const uint64_t o = (uint64_t)(2 * k4);
+        mma<TC_TF32>(tbase, dah + o, dbh + o, a.idesc, (i > 0 || k4 > 0) ? 1u : 0u);
+        mma<TC_TF32>(tbase, dah + o, dbl + o, a.idesc, 1u);
+        mma<TC_TF32>(tbase, dal + o, dbh + o, a.idesc, 1u);
+      }
+      mma_commit(smem_u32(&empty[s]));
+    }
+    mma_commit(smem_u32(done));  // every issued MMA has completed at done
+  }
+  __syncwarp();
+  // ---- epilogue: the slice's partial tile, rows m0 + 32 w + r
+  const bool ok = mbar_wait(smem_u32(done), 0, a.err, 44);
+  tc_fence_after();
+  const bool go = __all_sync(0xffffffffu, ok && *(volatile int*)a.err == 0);
+  if (go) {
+    constexpr int TP = 65;
+    uint32_t* th = reinterpret_cast<uint32_t*>(sm) + warp * (32 * TP);
+    const uint32_t tw = tbase + ((uint32_t)(warp * 32) << 16);
+    float* out = a.part + (long)blockIdx.y * a.pstride + (long)(m0 + warp * 32) * a.Np;
+    for (int g0 = 0; g0 < a.Np; g0 += 64) {
+      for (int g = g0; g < g0 + 64 && g < a.Np; g += 16) {
+        float v[16];
+        tmem_ld16(tw + g, v);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) th[lane * TP + (g + q - g0)] = __float_as_uint(v[q]);
+      }
+      __syncwarp();
+      for (int r = 0; r < 32; ++r)
+#pragma unroll
+        for (int c = 0; c < 64; c += 32) {
+          const int n = g0 + c + lane;
+          if (n < a.Np) out[(long)r * a.Np + n] = __uint_as_float(th[r * TP + c + lane]);
+        }
+      __syncwarp();
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(a.tmem_cols));
+}
+
+void tc_wgrad_maps(TcWgrad& W, const uint32_t* ah, const uint32_t* al, const uint32_t* bh, const uint32_t* bl,
+                   int kpitch) {
+  if (W.Mp < TC_M || W.Mp % TC_M || W.Np < 16 || W.Np > 256 || W.Np % 16 || kpitch < 32 || kpitch % 32)
+    throw std::invalid_argument("tc_wgrad_maps: bad shape");
+  const uint64_t da[2] = {(uint64_t)kpitch, (uint64_t)W.Mp}, db[2] = {(uint64_t)kpitch, (uint64_t)W.Np};
+  make_map(&W.ah, const_cast<uint32_t*>(ah), TC_TF32, 2, da, 32, TC_M);
+  make_map(&W.al, const_cast<uint32_t*>(al), TC_TF32, 2, da, 32, TC_M);
+  make_map(&W.bh, const_cast<uint32_t*>(bh), TC_TF32, 2, db, 32, W.Np);
+  make_map(&W.bl, const_cast<uint32_t*>(bl), TC_TF32, 2, db, 32, W.Np);
+}
+
+void tc_wgrad(const TcWgrad& W, int nk, int cps, int nsplit, cudaStream_t s) {
+  if (nk < 1 || cps < 1 || nsplit < 1 || (long)(nsplit - 1) * cps >= nk || (long)nsplit * cps < nk || !W.part)
+    throw std::invalid_argument("tc_wgrad: bad K split");
+  TcWgradArgs a;
+  a.Np = W.Np;
+  a.cps = cps;
+  a.nkt = nk;
+  a.part = W.part;
+  a.pstride = (long)W.Mp * W.Np;
+  a.err = W.err;
+  a.idesc = make_idesc(TC_TF32, W.Np);
+  a.tmem_cols = tmem_cols_for(W.Np / 2);  // a power of two >= Np (and >= 32)
+  const size_t sm = (size_t)TCW_NS * (2 * TC_M * 128 + 2 * (size_t)W.Np * 128) + 1024 + 256;
+  static bool attr = false;
+  if (!attr) {
+    GD_CUDA(cudaFuncSetAttribute(k_tc_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    attr = true;
+  }
+  k_tc_wgrad<<<dim3(W.Mp / TC_M, nsplit), TC_THREADS, sm, s>>>(W.ah, W.al, W.bh, W.bl, a);
+  count_launch();
+  GD_LAUNCH_CHECK();
+}
+
 void tc_mlp_maps(TcMlpLayer& L, const uint32_t* ah, const uint32_t* al, const float* w) {
   if (L.Kp % 32 || L.Np % 16 || L.Np < 16 || L.Np > 256 || L.N > L.Np || L.M < 1)
     throw std::invalid_argument("tc_mlp_maps: bad layer shape");

@@ -121,4 +121,24 @@ struct TcMlpLayer {
 void tc_mlp_maps(TcMlpLayer& L, const uint32_t* ah, const uint32_t* al, const float* w);
 void tc_mlp_layer(const TcMlpLayer& L, cudaStream_t s);
 
+// Weight gradient of a closure layer: part[s][m][n] = sum over the K chunks
+// of slice s of A(m, k) B(n, k), both operands TF32 hi + lo rows with the
+// batch (K) contiguous: A = dZ^T (Mp rows, a multiple of 128), B = the
+// layer's input transposed (Np <= 256 rows).  Three products per K step
+// (hi hi, hi lo, lo hi), FP32 accumulation in TMEM; the slices' partial
+// tiles are summed afterwards in a fixed order.
+struct TcWgrad {
+  CUtensorMap ah, al, bh, bl;
+  int Mp = 0, Np = 0;
+  float* part = nullptr;  // [nsplit][Mp][Np]
+  int* err = nullptr;
+};
+// maps over the transposed operands; kpitch = their row length (batch
+// capacity, a multiple of 32)
+void tc_wgrad_maps(TcWgrad& W, const uint32_t* ah, const uint32_t* al, const uint32_t* bh, const uint32_t* bl,
+                   int kpitch);
+// nk = K chunks of 32 in use, split over nsplit slices of cps chunks each
+// (every slice non-empty)
+void tc_wgrad(const TcWgrad& W, int nk, int cps, int nsplit, cudaStream_t s);
+
 }  // namespace gd

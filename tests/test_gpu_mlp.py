@@ -103,10 +103,10 @@ def test_closure_shape_gradient_matches_oracle():
 
 
 def test_tensor_core_training_matches_simt_training(monkeypatch):
-    # the configured closure net's loss and gradients with the forward and
-    # backward products dZ W on the tensor cores (the default) and with every
-    # product on the SIMT kernels (GD_MLP_TRAIN_TC=0, read when a net is made):
-    # both within FP32 accumulation of each other
+    # the configured closure net's loss and gradients with the training
+    # products X W^T, dZ W and dZ^T A on the tensor cores (the default) and on
+    # the SIMT kernels (GD_MLP_TRAIN_TC=0, read when a net is made): both
+    # within FP32 accumulation of each other
     from gdpy import core
 
     nin, nh, nl, nout = 193, 256, 3, 192

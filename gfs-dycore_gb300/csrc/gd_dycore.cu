@@ -369,7 +369,7 @@ class Dycore : public DycoreBase {
       GD_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
       tcp.reset(new TcPlan());
       // widest N tile at init (GD_TC_TILE_CAP: a tuning and measurement knob)
-      tcp->tile_cap = std::max(16, env_int("GD_TC_TILE_CAP", tcp->tile_cap));
+      tcp->tile_cap = std::max(16, env_int("GD_TC_TILE_CAP", tcp->tile_cap) / 16 * 16);
       const int ncap = 2 * std::max(sc.ncol, ap.ncol);
       if constexpr (std::is_same<R, float>::value) {
         // GD_TC_SEPX=1: the cross products in their own accumulator here too

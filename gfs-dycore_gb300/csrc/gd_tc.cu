@@ -1580,7 +1580,7 @@ int tc_check(TcPlan& p, cudaStream_t s) {
 // lo W; W is exact in TF32), all four warps drain the accumulator (warp w
 // holds TMEM lanes 32w..32w+31 = rows).  Every wait is bounded.
 struct TcMlpArgs {
-  int M, N, Np, nk;
+  int M, N, Np, nk;  // Np: this launch's N tile (each CTA covers columns blockIdx.y * Np ...)
   const float* bias;
   int gelu;
   int mode;
@@ -1614,7 +1614,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint64_t* done = empty + TC_NS;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.x * TC_M;
+  const int m0 = blockIdx.x * TC_M, c0 = blockIdx.y * a.Np;  // rows, and the first of the CTA's Np columns
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
@@ -1644,7 +1644,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_expect_tx(fb, stage_bytes);
       tma_2d(smem_u32(st), &mAh, i * 32, m0, fb);
       tma_2d(smem_u32(st + bytesA), &mAl, i * 32, m0, fb);
-      tma_2d(smem_u32(st + 2 * bytesA), &mW, i * 32, 0, fb);
+      tma_2d(smem_u32(st + 2 * bytesA), &mW, i * 32, c0, fb);
       ++fills[s];
     }
     for (int s = 0; s < TC_NS; ++s)  // never leave with copies in flight
@@ -1688,8 +1688,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tmem_ld16(tw + g, v);
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-          const int n = g + q;
-          th[lane * TP + (n - g0)] = __float_as_uint(v[q] + (a.mode == 2 && n < a.N ? a.bias[n] : 0.f));
+          const int n = c0 + g + q;
+          th[lane * TP + (g + q - g0)] = __float_as_uint(v[q] + (a.mode == 2 && n < a.N ? a.bias[n] : 0.f));
         }
       }
       __syncwarp();
@@ -1698,8 +1698,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (m >= a.M) break;
 #pragma unroll
         for (int c = 0; c < 64; c += 32) {
-          const int n = g0 + c + lane;
-          if (n < a.N) {
+          const int n = c0 + g0 + c + lane;
+          if (g0 + c + lane < a.Np && n < a.N) {
             const float v = __uint_as_float(th[r * TP + c + lane]);
             const long iz = (long)m * a.ldz + n;
             float o;  // the value the next product takes, split hi + lo
@@ -1735,15 +1735,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tmem_ld16(tw + g, v);
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-          const int n = g + q;
+          const int n = c0 + g + q;
           const float z = v[q] + (n < a.N ? a.bias[n] : 0.f);
           uint32_t h, l = 0;
           if (a.gelu)
             Elem<TC_TF32>::splitf(tc_gelu(z), h, l);
           else
             h = __float_as_uint(z);
-          th[lane * TP + (n - g0)] = h;
-          tl[lane * TP + (n - g0)] = l;
+          th[lane * TP + (g + q - g0)] = h;
+          tl[lane * TP + (g + q - g0)] = l;
         }
       }
       __syncwarp();
@@ -1752,8 +1752,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (m >= a.M) break;
 #pragma unroll
         for (int c = 0; c < 64; c += 32) {
-          const int n = g0 + c + lane;
-          if (n < a.N) {
+          const int n = c0 + g0 + c + lane;
+          if (g0 + c + lane < a.Np && n < a.N) {
             if (a.gelu) {
               a.oh[(long)m * a.ldo + n] = th[r * TP + c + lane];
               a.ol[(long)m * a.ldo + n] = tl[r * TP + c + lane];
@@ -1931,13 +1931,34 @@ void tc_mlp_maps(TcMlpLayer& L, const uint32_t* ah, const uint32_t* al, const fl
   make_map(&L.ah, const_cast<uint32_t*>(ah), TC_TF32, 2, da, 32, TC_M);
   make_map(&L.al, const_cast<uint32_t*>(al), TC_TF32, 2, da, 32, TC_M);
   make_map(&L.w, const_cast<float*>(w), TC_TF32, 2, dw, 32, L.Np);
+  L.wbase = w;
+  L.wbox = L.Np;
 }
 
-void tc_mlp_layer(const TcMlpLayer& L, cudaStream_t s) {
+void tc_mlp_layer(const TcMlpLayer& Lin, cudaStream_t s) {
+  // N tile: the whole padded width, halved (down to 32 columns, a multiple
+  // of 16) while the row tiles alone leave SMs idle; the weights' map is
+  // made again for a narrower box
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    GD_CUDA(cudaGetDevice(&dev));
+    GD_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const int mt = (Lin.M + TC_M - 1) / TC_M;
+  int nt = Lin.Np;
+  while (nt >= 64 && (nt / 2) % 16 == 0 && (long)mt * ((Lin.Np + nt - 1) / nt) < nsm) nt /= 2;
+  TcMlpLayer L = Lin;
+  if (nt != L.wbox) {
+    if (!L.wbase) throw std::invalid_argument("tc_mlp_layer: layer without its weight map");
+    const uint64_t dw[2] = {(uint64_t)L.Kp, (uint64_t)L.Np};
+    make_map(&L.w, const_cast<float*>(L.wbase), TC_TF32, 2, dw, 32, nt);
+    L.wbox = nt;
+  }
   TcMlpArgs a;
   a.M = L.M;
   a.N = L.N;
-  a.Np = L.Np;
+  a.Np = nt;
   a.nk = L.Kp / 32;
   a.bias = L.bias;
   a.gelu = L.gelu;
@@ -1954,15 +1975,15 @@ void tc_mlp_layer(const TcMlpLayer& L, cudaStream_t s) {
   a.y = L.y;
   a.ldy = L.ldy;
   a.err = L.err;
-  a.idesc = make_idesc(TC_TF32, L.Np);
-  a.tmem_cols = tmem_cols_for(L.Np / 2);  // a power of two >= Np (and >= 32)
-  const size_t sm = (size_t)TC_NS * (2 * TC_M * 128 + (size_t)L.Np * 128) + 1024 + 256;
+  a.idesc = make_idesc(TC_TF32, nt);
+  a.tmem_cols = tmem_cols_for(nt / 2);  // a power of two >= nt (and >= 32)
+  const size_t sm = (size_t)TC_NS * (2 * TC_M * 128 + (size_t)nt * 128) + 1024 + 256;
   static bool attr = false;
   if (!attr) {
     GD_CUDA(cudaFuncSetAttribute(k_tc_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     attr = true;
   }
-  k_tc_mlp<<<ceil_div(L.M, TC_M), TC_THREADS, sm, s>>>(L.ah, L.al, L.w, a);
+  k_tc_mlp<<<dim3(mt, (L.Np + nt - 1) / nt), TC_THREADS, sm, s>>>(L.ah, L.al, L.w, a);
   count_launch();
   GD_LAUNCH_CHECK();
 }

@@ -98,6 +98,8 @@ int tc_check(TcPlan& p, cudaStream_t s);
 struct TcMlpLayer {
   CUtensorMap ah, al, w;
   int M = 0, N = 0, Np = 0, Kp = 0;
+  const float* wbase = nullptr;  // the weights the map w covers ([Np][Kp])
+  int wbox = 0;                  // N rows of the map's box (the N tile it was made for)
   const float* bias = nullptr;
   int gelu = 0;
   uint32_t* oh = nullptr;

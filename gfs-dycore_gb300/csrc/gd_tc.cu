@@ -678,16 +678,18 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
 // FP32 data instead.  Warp 0 loads, per K chunk, the raw tile in its natural
 // column-contiguous layout (synthesis: 32 degrees of one parity of the
 // spectral array; analysis: 32 northern latitude rows of the Fourier array
-// and their 32 mirrored southern rows) together with the table tiles.  Four
+// and their 32 mirrored southern rows) together with the table tiles.  Eight
 // converter warps (6-13) turn the raw tile into the A operand directly in
 // tensor memory: two threads on TMEM lane c (one per half of the chunk's 32
 // K entries, in warps w and w + 4) own batch column c, mask
 // degrees beyond the truncation and latitudes beyond the equator, forms
 // G_N +- G_S for the analysis, split to hi + lo and write their 16 columns of
-// each with one tcgen05.st.  The MMAs read A from TMEM (two slots
-// beside the double-buffered accumulators), so shared memory holds only
-// the TMA ring, which is 4-6 stages deep.  The split is the same as in
-// k_tc_split_x/g, so results match the unfused path bit for bit.
+// each with one tcgen05.st.  The MMAs read A from TMEM (a ring of 2-4 slots
+// beside one or two accumulator buffers, and in the FP64-state modes the
+// cross products' accumulators and the running sums of folded K segments),
+// so shared memory holds only the TMA ring, 2-6 stages deep.  The split is
+// the same as in k_tc_split_x/g, so results match the unfused path bit for
+// bit.
 constexpr int TCF_THREADS = 448;  // producer, MMA, 4 epilogue, 8 converter warps
 constexpr int TCF_MAXNS = 6;
 constexpr int TCF_MAXA = 4;  // A slots in tensor memory at most (64 columns each)

@@ -26,7 +26,8 @@ struct TcPlan {
   bool persistent = true;  // persistent warp-specialised GEMM (N <= 128)
   // fused TF32x3 GEMM: the hi*lo and lo*hi products in their own accumulator
   // (a third of the truncating accumulation steps in the main one); set by
-  // the FP64-state modes before tc_init (it bounds the N tile)
+  // the FP64-state modes (and GD_TC_SEPX) before tc_init (it bounds the N
+  // tile)
   bool sepx = false;
   // fused TF32x3 GEMM: K segments of cps chunks per parity, accumulated afresh
   // and folded in FP32 (round to nearest) by the epilogue; 0 = none; set

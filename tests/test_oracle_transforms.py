@@ -87,32 +87,41 @@ def test_legendre_tables_t574_vs_mpmath(oracle_mod, m):
     # three-term recurrence carried out in 60-digit arithmetic, at latitudes
     # from the pole row to the equator row; the oracle's FP64 values within
     # 1e-12 of each order's largest value (measured 2e-15 at m = 0, 1.3e-14
-    # at m = 574; a Condon-Shortley phase would miss odd orders by 2)
+    # at m = 574; a Condon-Shortley phase would miss odd orders by 2).  The
+    # derivative table dP/dphi against cos(phi) dP/dmu = ((n+1) eps_n P_{n-1}
+    # - n eps_{n+1} P_{n+1}) / cos(phi), eps_n = sqrt((n^2 - m^2) / (4 n^2 - 1))
+    # (measured at most 2.7e-13, at the row next to the pole for m = 0)
     mp = pytest.importorskip("mpmath")
     mp.mp.dps = 60
     T, nlat = 574, 576
     o = make(oracle_mod, T=T, nlon=1152, nlat=nlat)
     mus = np.sin(o.grid_info()["lats"][: nlat // 2])
-    P, _ = o.legendre(m)
+    P, H = o.legendre(m)
     rows = [0, 1, 2, 40, 144, 250, nlat // 2 - 1]
     ref = np.zeros((len(rows), T - m + 1))
+    refh = np.zeros_like(ref)
+    eps = lambda n: mp.sqrt(mp.mpf(n * n - m * m) / (4 * n * n - 1))
     for a, j in enumerate(rows):
         mu = mp.mpf(float(mus[j]))
         s2 = 1 - mu * mu
         # P_m^m = sqrt((2m+1) / (4 pi (2m)!)) (2m-1)!! (1 - mu^2)^(m/2)
         pmm = mp.sqrt((2 * m + 1) / (4 * mp.pi * mp.factorial(2 * m))) * mp.fac2(2 * m - 1) * s2 ** (mp.mpf(m) / 2)
+        pv = {m: pmm}
         p0, p1 = None, pmm
-        ref[a, 0] = float(pmm)
-        for n in range(m + 1, T + 1):
+        for n in range(m + 1, T + 2):  # one degree past T for the derivative identity
             an = mp.sqrt(mp.mpf(4 * n * n - 1) / (n * n - m * m))
             bn = mp.sqrt(mp.mpf((n - 1) ** 2 - m * m) / (4 * (n - 1) ** 2 - 1)) if n > m + 1 else mp.mpf(0)
             p2 = an * (mu * p1 - (bn * p0 if p0 is not None else 0))
             p0, p1 = p1, p2
-            ref[a, n - m] = float(p2)
-    got = P[rows, :]
-    scale = np.abs(ref).max()
-    assert scale > 0
-    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-12 * scale)
+            pv[n] = p2
+        for n in range(m, T + 1):
+            ref[a, n - m] = float(pv[n])
+            pm1 = pv[n - 1] if n - 1 >= m else 0
+            refh[a, n - m] = float(((n + 1) * eps(n) * pm1 - n * eps(n + 1) * pv[n + 1]) / mp.sqrt(s2))
+    for got, want in ((P[rows, :], ref), (H[rows, :], refh)):
+        scale = np.abs(want).max()
+        assert scale > 0
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 * scale)
 
 
 def test_orthonormality_under_gauss_quadrature(oracle_mod):

@@ -56,6 +56,26 @@ def test_isothermal_rest_is_steady_adiabatic(oracle_mod):
     assert np.abs(t["dlnps"]).max() < 1e-16
 
 
+@pytest.mark.parametrize("T,nlon,nlat", [(42, 128, 64), (62, 192, 94), (126, 384, 190)])
+def test_balanced_jet_is_steady_adiabatic(oracle_mod, T, nlon, nlat):
+    # a known answer for the whole of getdyntend: the barotropic jet u = 35
+    # sin^2(2 phi) on an isothermal atmosphere, ln ps in gradient-wind balance
+    # (the pressure-gradient force is -R T grad ln ps on every hybrid level), is
+    # a steady state of the adiabatic equations, and the discrete tendencies
+    # keep it to round-off (measured ddiv 2e-14 .. 2e-13 of f |vrt|, dvrt
+    # ~1e-17, dTv and dlnps zero)
+    L = 8
+    o = make(oracle_mod, T=T, nlon=nlon, nlat=nlat, nlev=L, adiabatic=True, heldsuarez=False)
+    st = inputs.balanced_jet_state(T, nlat, L, seed=0, tnoise=0.0)
+    o.set_state(st["vrt"], st["div"], st["tv"], st["lnps"])
+    t = o.getdyntend(1)
+    scale = 2 * inputs.OMEGA * np.abs(st["vrt"]).max()
+    assert np.abs(t["ddiv"]).max() < 1e-11 * scale
+    assert np.abs(t["dvrt"]).max() < 1e-14 * scale
+    assert np.abs(t["dtv"]).max() < 1e-14 * 300
+    assert np.abs(t["dlnps"]).max() < 1e-16
+
+
 def test_hs_step_mass_and_zonal_symmetry(oracle_mod):
     T, nlev = 21, 8
     o = make(oracle_mod, T=T, nlon=64, nlat=32, nlev=nlev, dt=1200.0)

@@ -345,6 +345,31 @@ def test_autotune_keeps_the_step(prec):
         assert rel(out[1][k], out[0][k]) < tol, k
 
 
+@pytest.mark.parametrize("prec", ["fp64", "f64_eddy", "f64_tf32x3", "tf32x3", "bf16x3", "fp32"])
+def test_balanced_jet_tendencies(prec):
+    # the known answer of the oracle's getdyntend (the barotropic jet on an
+    # isothermal atmosphere in gradient-wind balance is steady) through each
+    # precision mode at T126L8: the FP64-state modes keep it to round-off
+    # (measured divergence tendency 1.65e-13 of f max|vrt|); an FP32 state
+    # cannot hold the balance of the pressure-gradient and Coriolis terms
+    # better than its rounding (measured 1.31e-5)
+    T, L = 126, 8
+    nlon, nlat = GRIDS[T]
+    ak, bk = inputs.hybrid_coords(L)
+    st = inputs.balanced_jet_state(T, nlat, L, seed=0, tnoise=0.0)
+    g = core.Dycore(T, nlon, nlat, L, ak, bk, dt=600.0, precision=prec, adiabatic=True, heldsuarez=False)
+    g.set_state(st["vrt"], st["div"], st["tv"], st["lnps"])
+    t = g.getdyntend(1)
+    g.close()
+    scale = 2 * inputs.OMEGA * np.abs(st["vrt"]).max()
+    f64 = prec in ("fp64", "f64_eddy", "f64_tf32x3")
+    print(f"T126 balanced jet {prec}: ddiv {np.abs(t['ddiv']).max() / scale:.2e} of f max|vrt|")
+    assert np.abs(t["ddiv"]).max() < (1e-11 if f64 else 1e-4) * scale
+    assert np.abs(t["dvrt"]).max() < (1e-14 if f64 else 1e-8) * scale
+    assert np.abs(t["dtv"]).max() < (1e-10 if f64 else 1e-6)
+    assert np.abs(t["dlnps"]).max() < (1e-14 if f64 else 1e-8)
+
+
 # ---- FP64 state with the split-precision Legendre GEMM (f64_tf32x3) ----
 @pytest.mark.parametrize("prec", ["f64_tf32x3", "f64_eddy"])
 @pytest.mark.parametrize("T", [21, 42, 126])

@@ -76,6 +76,56 @@ def test_balanced_jet_is_steady_adiabatic(oracle_mod, T, nlon, nlat):
     assert np.abs(t["dlnps"]).max() < 1e-16
 
 
+def test_hs_forcing_vs_numpy_restatement(oracle_mod):
+    # the physics plugin of the Held-Suarez build (phy_run_hs.f90:42-77)
+    # restated in numpy on the oracle's own transforms: Phillips layer
+    # pressure from the interfaces p = ak + bk ps (top to bottom) for the
+    # fields stored bottom to top, Teq = max(200, (p/p0)^(2/7) (315 - 60
+    # sin^2 phi - 10 ln(p/p0) cos^2 phi)), blprof = max(0, (p/ps - 0.7) / 0.3),
+    # dTv = (ka + (ks - ka) blprof cos^4 phi)(Teq - Tv), dvrt, ddiv = -kf
+    # blprof (vrt, div), with the reference's single-precision constants
+    # (measured: the tendencies within 9.4e-15 of their largest value, the
+    # layer pressures within 3.6e-15)
+    T, nlon, nlat, L = 42, 128, 64, 20
+    ak, bk = inputs.hybrid_coords(L)
+    o = oracle_mod.Oracle(T, nlon, nlat, L, ak, bk, dt=1200.0)
+    st = inputs.hs_rest_state(T, L, seed=4, amp=2.0e-5)
+    rng = np.random.default_rng(4)
+    st["div"] = st["vrt"][::-1] * 0.3
+    st["tv"] = st["tv"] + 0.0
+    st["tv"][:, 1:30] += 0.5 * (rng.standard_normal((L, 29)) + 1j * rng.standard_normal((L, 29)))
+    o.set_state(st["vrt"], st["div"], st["tv"], st["lnps"])
+    o.getdyntend(3, inverse_only=True)  # the grid fields the plugin reads, as after getdyntend
+    t = o.getphytend()
+    prs_oracle = o.get_grid("prs")
+    f32 = np.float32
+    kappa = float(f32(287.05)) / float(f32(1004.6))
+    sigbot = float(f32(0.7))
+    kf = float(f32(1.0) / (f32(1.0) * f32(86400.0)))
+    ka = float(f32(1.0) / (f32(40.0) * f32(86400.0)))
+    ks = float(f32(1.0) / (f32(4.0) * f32(86400.0)))
+    expo = float(f32(2.0) / f32(7.0))
+    p0 = 1.0e5
+    lat = o.grid_info()["lats"][:, None]
+    sl, cl = np.sin(lat), np.cos(lat)
+    ps = np.exp(o.spectogrd(st["lnps"][None])[0])
+    vrtg, divg, tvg = o.spectogrd(st["vrt"]), o.spectogrd(st["div"]), o.spectogrd(st["tv"])
+    pk = [ak[i] + bk[i] * ps for i in range(L + 1)]  # interfaces, top to bottom
+    want = {k: np.zeros((L, o.nlm), np.complex128) for k in ("dtv", "dvrt", "ddiv")}
+    for b in range(L):  # field level b (bottom to top) is layer L - 1 - b
+        lo, up = pk[L - b], pk[L - 1 - b]
+        prs = ((lo ** kappa * lo - up ** kappa * up) / ((kappa + 1.0) * (lo - up))) ** (1.0 / kappa)
+        np.testing.assert_allclose(prs_oracle[b], prs, rtol=1e-13)  # calc_pressdata's Phillips pressure
+        bl = np.maximum(0.0, (prs / ps - sigbot) / (1.0 - sigbot))
+        teq = np.maximum(200.0, (prs / p0) ** expo * (315.0 - 60.0 * sl ** 2 - 10.0 * np.log(prs / p0) * cl ** 2))
+        want["dtv"][b] = o.grdtospec(((ka + (ks - ka) * bl * cl ** 4) * (teq - tvg[b]))[None])[0]
+        want["dvrt"][b] = o.grdtospec((-(bl * kf) * vrtg[b])[None])[0]
+        want["ddiv"][b] = o.grdtospec((-(bl * kf) * divg[b])[None])[0]
+    for k in ("dtv", "dvrt", "ddiv"):
+        np.testing.assert_allclose(t[k], want[k], rtol=0, atol=1e-12 * np.abs(want[k]).max())
+    assert np.abs(t["dlnps"]).max() == 0
+
+
 def test_hs_step_mass_and_zonal_symmetry(oracle_mod):
     T, nlev = 21, 8
     o = make(oracle_mod, T=T, nlon=64, nlat=32, nlev=nlev, dt=1200.0)

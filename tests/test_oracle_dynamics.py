@@ -126,6 +126,57 @@ def test_hs_forcing_vs_numpy_restatement(oracle_mod):
     assert np.abs(t["dlnps"]).max() == 0
 
 
+def test_getomega_vs_numpy_restatement(oracle_mod):
+    # getomega (dyn_run.f90:307-373) restated in numpy on the oracle's grid
+    # winds and divergence and its transforms: cg = V . grad ln ps, the
+    # top-down sums db (div dp) and cb (cg dbk), dlnps/dt = -db_N/ps - cb_N,
+    # etadot at the interior interfaces, and omega/p from the workb / workc
+    # terms with rlnp, alfa (pressure_data.f90:90-97; alfa at the top is the
+    # single-precision log 2), dbk and ck (dyn_init.f90:58-60)
+    # (measured 7.5e-16, 5.3e-16 and 2.3e-15 of the largest value)
+    T, nlon, nlat, L = 42, 128, 64, 20
+    ak, bk = inputs.hybrid_coords(L)
+    o = oracle_mod.Oracle(T, nlon, nlat, L, ak, bk, dt=1200.0)
+    st = inputs.hs_rest_state(T, L, seed=6, amp=2.0e-5)
+    st["div"] = 0.4 * st["vrt"][::-1]
+    st["lnps"] = st["lnps"].copy()
+    rng = np.random.default_rng(6)
+    st["lnps"][1:40] += 2e-3 * rng.standard_normal(39)
+    o.set_state(st["vrt"], st["div"], st["tv"], st["lnps"])
+    o.getdyntend(3, inverse_only=True)
+    ug, vg, divg = o.get_grid("ug"), o.get_grid("vg"), o.get_grid("divg")  # bottom to top
+    ps = np.exp(o.spectogrd(st["lnps"][None])[0])
+    gx, gy = o.getgrad(st["lnps"][None])
+    gx, gy = gx[0], gy[0]
+    pk = np.array([ak[i] + bk[i] * ps for i in range(L + 1)])  # interfaces, top to bottom
+    dpk = pk[1:] - pk[:-1]
+    dbk = bk[1:] - bk[:-1]
+    ck = ak[1:] * bk[:-1] - ak[:-1] * bk[1:]
+    rlnp = np.zeros_like(dpk)
+    alfa = np.zeros_like(dpk)
+    alfa[0] = float(np.log(np.float32(2.0)))
+    rlnp[1:] = np.log(pk[2:] / pk[1:-1])
+    alfa[1:] = 1.0 - (pk[1:-1] / dpk[1:]) * rlnp[1:]
+    cg = np.array([ug[L - 1 - k] * gx + vg[L - 1 - k] * gy for k in range(L)])  # top to bottom
+    db = np.cumsum(np.array([divg[L - 1 - k] * dpk[k] for k in range(L)]), axis=0)
+    cb = np.cumsum(np.array([cg[k] * dbk[k] for k in range(L)]), axis=0)
+    dlnpsdt = -db[L - 1] / ps - cb[L - 1]
+    etadot = np.zeros((L + 1,) + ps.shape)
+    for k in range(L - 1):
+        etadot[k + 1] = -ps * (bk[k + 1] * dlnpsdt + cb[k]) - db[k]
+    workb = np.zeros_like(dpk)
+    workc = np.zeros_like(dpk)
+    workb[0] = alfa[0] * (divg[L - 1] * dpk[0] + ps * cb[0] * dbk[0])
+    workc[0] = ps * cg[0] * dbk[0]
+    for k in range(1, L):
+        workb[k] = rlnp[k] * (db[k - 1] + ps * cb[k - 1]) + alfa[k] * (divg[L - 1 - k] * dpk[k] + ps * cg[k] * dbk[k])
+        workc[k] = ps * cg[k] * (dbk[k] + ck[k] * rlnp[k] / dpk[k])
+    dlnpdtg = np.array([(workc[L - 1 - b] - workb[L - 1 - b]) / dpk[L - 1 - b] for b in range(L)])  # bottom to top
+    for name, want in (("dlnpsdt", dlnpsdt), ("etadot", etadot), ("dlnpdtg", dlnpdtg)):
+        got = o.get_grid(name).reshape(want.shape)
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 * np.abs(want).max(), err_msg=name)
+
+
 def test_hs_step_mass_and_zonal_symmetry(oracle_mod):
     T, nlev = 21, 8
     o = make(oracle_mod, T=T, nlon=64, nlat=32, nlev=nlev, dt=1200.0)

@@ -206,3 +206,123 @@ def test_hs_noise_case_runs(oracle_mod):
     o.advance(2)
     d = o.diag()
     assert np.isfinite(d["spdmax"]) and 900 < d["psmin"] <= d["psmax"] < 1100
+
+
+# ---- getdyntend restated in numpy (dyn_run.f90:160-305, 375-603) ----------
+# Fields are numpy arrays [level][lat][lon]: 3-D grid fields bottom (0) to top,
+# interface quantities (pk, etadot) and layer coefficients (dpk, dbk, rlnp,
+# alfa) top (0) to bottom, as in the reference.
+def _np_getvadv(q, etadot, dpk):
+    L = q.shape[0]
+    v = np.zeros_like(q)
+    for t in range(L):  # layer t from the top is field level L - 1 - t
+        acc = 0.0
+        if t <= L - 2:
+            acc = acc + etadot[t + 1] * (q[L - 2 - t] - q[L - 1 - t])
+        if t >= 1:
+            acc = acc + etadot[t] * (q[L - 1 - t] - q[L - t])
+        v[L - 1 - t] = (0.5 / dpk[t]) * acc
+    return v
+
+
+def _np_getvadv_tracers(q, etadot, dpk):
+    L = q.shape[0]
+    half = np.zeros((L + 1,) + q.shape[1:])
+    d = np.zeros_like(half)
+    for k in range(1, L):
+        half[k] = 0.5 * (q[L - 1 - k] + q[L - k])
+        d[k] = q[L - 1 - k] - q[L - k]
+    half[0], half[L] = q[L - 1], q[0]
+    two_t = 2.0 * q[L - 1] - q[L - 2]
+    d[0] = np.where(q[L - 1] >= 0, q[L - 1] - np.maximum(0.0, two_t), q[L - 1] - np.minimum(0.0, two_t))
+    two_b = 2.0 * q[0] - q[1]
+    d[L] = np.where(q[0] >= 0, np.maximum(0.0, two_b) - q[0], np.minimum(0.0, two_b) - q[0])
+    tiny = np.finfo(np.float64).tiny
+    for k in range(1, L):
+        d[k] = np.where(np.abs(d[k]) < tiny, np.copysign(tiny, d[k]), d[k])
+    for k in range(1, L):  # Thuburn's limiter (phi + |phi|) / (1 + |phi|), upwind by etadot
+        up = etadot[k] > 0.0
+        phi = np.where(up, d[k - 1], d[k + 1]) / d[k]
+        qu = np.where(up, q[L - k], q[L - 1 - k])
+        half[k] = qu + (phi + np.abs(phi)) / (1.0 + np.abs(phi)) * (half[k] - qu)
+    v = np.zeros_like(q)
+    for t in range(L):
+        v[L - 1 - t] = (1.0 / dpk[t]) * ((half[t + 1] * etadot[t + 1] - half[t] * etadot[t]) +
+                                         q[L - 1 - t] * (etadot[t] - etadot[t + 1]))
+    return v
+
+
+def _np_getpresgrad(tv, tx, ty, phx, phy, lx, ly, ps, pk, dpk, bk, dbk, rlnp, alfa, rd):
+    L = tv.shape[0]
+    cofb1 = [-(1.0 / dpk[0]) * (alfa[0] * dbk[0])] + \
+        [-(1.0 / dpk[t]) * (bk[t] * rlnp[t] + alfa[t] * dbk[t]) for t in range(1, L)]
+    cofa = [-(1.0 / dpk[t]) * (bk[t + 1] * pk[t] / pk[t + 1] - bk[t] + rlnp[t] * (bk[t] - pk[t] * dbk[t] / dpk[t]))
+            for t in range(L)]
+    cofb2 = [None] * L
+    px3u, px3v = [None] * L, [None] * L
+    cofb2[L - 1] = 0.0 * ps
+    px3u[L - 1] = px3v[L - 1] = 0.0 * ps
+    for k in range(1, L):  # bottom-up sums over the layers below
+        cofb2[L - 1 - k] = cofb2[L - k] - rd * (bk[L + 1 - k] / pk[L + 1 - k] - bk[L - k] / pk[L - k]) * tv[k - 1]
+        px3u[L - 1 - k] = px3u[L - k] - rd * rlnp[L - k] * tx[k - 1]
+        px3v[L - 1 - k] = px3v[L - k] - rd * rlnp[L - k] * ty[k - 1]
+    gx, gy = np.zeros_like(tv), np.zeros_like(tv)
+    for t in range(L):
+        b = L - 1 - t
+        gx[b] = cofb1[t] * rd * tv[b] * ps * lx - phx + cofb2[t] * ps * lx + px3u[t] - rd * alfa[t] * tx[b] \
+            - cofa[t] * rd * tv[b] * ps * lx
+        gy[b] = cofb1[t] * rd * tv[b] * ps * ly - phy + cofb2[t] * ps * ly + px3v[t] - rd * alfa[t] * ty[b] \
+            - cofa[t] * rd * tv[b] * ps * ly
+    return gx, gy
+
+
+def test_getdyntend_vs_numpy_restatement(oracle_mod):
+    # the whole tendency computation of getdyntend (dyn_run.f90:160-305) in
+    # numpy on the oracle's grid fields and transforms: getpresgrad
+    # (:375-451), getvadv (:453-476), getvadv_tracers with Thuburn's limiter
+    # (:478-603), the energy conversion with the humidity factor, the flux
+    # form of the vorticity and divergence tendencies (getvrtdivspec of (Fu,
+    # Fv) gives (ddiv, -dvrt)), the kinetic-energy Laplacian and the tracer
+    # tendencies, with the reference's single-precision constants (measured
+    # within 5e-16 of each field's largest value; a limiter upwinded the wrong
+    # way misses the tracer tendencies by 46 %, R_d off by 1e-7 the divergence
+    # tendency by 1e-8)
+    T, nlon, nlat, L, nt = 42, 128, 64, 20, 2
+    ak, bk = inputs.hybrid_coords(L)
+    o = oracle_mod.Oracle(T, nlon, nlat, L, ak, bk, ntrac=nt, dt=1200.0)
+    st = inputs.smooth_random_state(T, L, ntrac=nt, seed=8)
+    o.set_state(st["vrt"], st["div"], st["tv"], st["lnps"], trc=st["trc"])
+    got = o.getdyntend(1)
+    f32 = np.float32
+    rd, cp, cvap = float(f32(287.05)), float(f32(1004.6)), float(f32(1846.0))
+    kappa, omega, a = rd / cp, float(f32(7.2921e-5)), float(f32(6.3712e6))
+    ug, vg, vrtg, tvg = o.get_grid("ug"), o.get_grid("vg"), o.get_grid("vrtg"), o.get_grid("tvg")
+    trcg = o.get_grid("trcg").reshape(nt, L, nlat, nlon)
+    dlnpdtg, dlnpsdt = o.get_grid("dlnpdtg"), o.get_grid("dlnpsdt")[0]
+    etadot = o.get_grid("etadot")  # top to bottom, checked against getomega above
+    phx, phy = o.get_grid("dphisdx")[0], o.get_grid("dphisdy")[0]
+    ps = np.exp(o.spectogrd(st["lnps"][None])[0])
+    lx, ly = (g[0] for g in o.getgrad(st["lnps"][None]))
+    tx, ty = o.getgrad(st["tv"])
+    pk = [ak[i] + bk[i] * ps for i in range(L + 1)]
+    dpk = [pk[t + 1] - pk[t] for t in range(L)]
+    dbk = bk[1:] - bk[:-1]
+    rlnp = [0.0 * ps + float(f32(99999.99))] + [np.log(pk[t + 1] / pk[t]) for t in range(1, L)]
+    alfa = [0.0 * ps + float(np.log(f32(2.0)))] + [1.0 - (pk[t] / dpk[t]) * rlnp[t] for t in range(1, L)]
+    gx, gy = _np_getpresgrad(tvg, tx, ty, phx, phy, lx, ly, ps, pk, dpk, bk, dbk, rlnp, alfa, rd)
+    vu, vv, vt = (_np_getvadv(f, etadot, dpk) for f in (ug, vg, tvg))
+    vq = kappa * dlnpdtg * tvg / (1.0 + (cvap / cp - 1.0) * trcg[0])
+    fcor = (2.0 * omega * np.sin(o.grid_info()["lats"]))[:, None]
+    vv, vu = vv - gy, vu - gx
+    dtv = o.grdtospec(-ug * tx - vg * ty - vt + vq)
+    ddiv, mdvrt = o.getvrtdivspec(ug * (vrtg + fcor) + vv, vg * (vrtg + fcor) - vu)
+    deg, _ = inputs.degree_order(T)
+    lap = -deg * (deg + 1.0)
+    ddiv = ddiv - (lap / a ** 2) * o.grdtospec(0.5 * (ug ** 2 + vg ** 2))
+    dtrc = []
+    for q in range(nt):
+        qx, qy = o.getgrad(st["trc"][q])
+        dtrc.append(o.grdtospec(-ug * qx - vg * qy - _np_getvadv_tracers(trcg[q], etadot, dpk)))
+    want = dict(dvrt=-mdvrt, ddiv=ddiv, dtv=dtv, dtrc=np.array(dtrc), dlnps=o.grdtospec(dlnpsdt[None])[0])
+    for k, w in want.items():
+        np.testing.assert_allclose(got[k], w, rtol=0, atol=1e-12 * np.abs(w).max(), err_msg=k)

@@ -413,3 +413,37 @@ def test_advance_vs_numpy_restatement(oracle_mod):
     want = _np_advance_dynamics(ev, st, dt, o.semimp(), o.damp(), T)
     for k in ("vrt", "div", "tv", "lnps", "trc"):
         np.testing.assert_allclose(got[k], want[k], rtol=0, atol=1e-12 * np.abs(want[k]).max(), err_msg=k)
+
+
+def test_advance_with_forcing_vs_numpy_restatement(oracle_mod):
+    # one Held-Suarez step: the dynamics as above, then the time-split physics
+    # (run.f90:509-538: the grid updated by an inverse-only pass, getphytend
+    # applied over dt) and the dry-mass fixer (dyn_run.f90:605-634: ps scaled
+    # by pcorr = pdryini / sum(areawts ps), its log analysed, the ln ps
+    # tendency (ws - lnps) / dt applied); measured within 2e-15 of each field's
+    # largest value
+    T, nlon, nlat, L, nt, dt = 42, 128, 64, 20, 1, 1200.0
+    ak, bk = inputs.hybrid_coords(L)
+    kw = dict(ntrac=nt, dt=dt)
+    o = oracle_mod.Oracle(T, nlon, nlat, L, ak, bk, **kw)
+    ev = oracle_mod.Oracle(T, nlon, nlat, L, ak, bk, **kw)
+    st = inputs.smooth_random_state(T, L, ntrac=nt, seed=12)
+    o.set_state(st["vrt"], st["div"], st["tv"], st["lnps"], trc=st["trc"])
+    o.advance(1)
+    got = o.get_state()
+    pdryini = o.diag()["pdryini"]
+    s = _np_advance_dynamics(ev, st, dt, o.semimp(), o.damp(), T)
+    ev.set_state(s["vrt"], s["div"], s["tv"], s["lnps"], trc=s["trc"])
+    ev.getdyntend(3, inverse_only=True)
+    ph = ev.getphytend()
+    s["vrt"] = s["vrt"] + dt * ph["dvrt"]
+    s["div"] = s["div"] + dt * ph["ddiv"]
+    s["tv"] = s["tv"] + dt * ph["dtv"]
+    s["trc"] = s["trc"] + dt * ph["dtrc"]
+    psg = ev.get_grid("psg")[0]
+    aw = ev.grid_info()["areawts"]
+    pcorr = pdryini / (aw[:, None] * psg).sum()
+    ws = ev.grdtospec(np.log(psg * pcorr)[None])[0]
+    s["lnps"] = s["lnps"] + dt * ((ws - s["lnps"]) / dt)
+    for k in ("vrt", "div", "tv", "lnps", "trc"):
+        np.testing.assert_allclose(got[k], s[k], rtol=0, atol=1e-12 * np.abs(s[k]).max(), err_msg=k)
